@@ -1,0 +1,175 @@
+/* mqi_gpu.h - C ABI of the GB300 proton transport engine (libmqigpu.so).
+ *
+ * This is the drop-in boundary for moqui's device path.  In moqui the device boundary is a pair of
+ * templated kernels plus the upload/download helpers that x_environment<R> calls:
+ *
+ *   upload_node / upload_materials / upload_vertices  (moqui/kernel_functions/mqi_upload_data.hpp:144-420)
+ *   transport_particles_patient[_stat]                 (moqui/kernel_functions/mqi_transport.hpp:113-389)
+ *   download_node                                      (moqui/kernel_functions/mqi_download_data.hpp:35-121)
+ *   calculate_standard_deviation / calculate_average   (moqui/kernel_functions/mqi_variables.hpp:19-66)
+ *
+ * Each entry point below names the reference interface it replaces.  Conventions:
+ *   - every function returns an int status: MQI_OK (0) or a negative MQI_ERR_* code; none exits;
+ *   - the caller owns every host array and the library copies what it keeps;
+ *   - the context owns its device buffers; outputs go to caller-allocated buffers;
+ *   - one context per host thread; a context is bound to one CUDA device;
+ *   - pointers are host pointers unless a function's `on_device` flag says otherwise.
+ * Device function pointers cannot cross a C ABI, so moqui's scorer and calibration plug-ins
+ * (fp_compute_hit, fp_compute_rsp/rl) are selected by enum here.
+ */
+#ifndef MQI_GPU_H
+#define MQI_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------------------------- */
+#define MQI_OK               0
+#define MQI_ERR_INVALID     -1 /* bad argument or size */
+#define MQI_ERR_CUDA        -2 /* a CUDA runtime call failed (see mqi_last_error) */
+#define MQI_ERR_NOMEM       -3 /* device allocation failed */
+#define MQI_ERR_STATE       -4 /* call order: e.g. transport before a grid was set */
+#define MQI_ERR_UNSUPPORTED -5 /* a plug-in that has no enum counterpart */
+#define MQI_ERR_OVERFLOW    -6 /* a device queue or buffer ran out of capacity */
+#define MQI_ERR_DEVICE      -7 /* a kernel reported a device-side error (bounded loop expired) */
+
+/* ---- scorer plug-ins: moqui's fp_compute_hit callbacks
+ *      (moqui/base/scorers/mqi_scorer_energy_deposit.hpp:12-177) ------------------------- */
+typedef enum {
+    MQI_SCORER_EDEP           = 1,  /* energy_deposit: dE + local_dE                           */
+    MQI_SCORER_DOSE_W         = 2,  /* dose_to_water (Dw_pointer)                              */
+    MQI_SCORER_DOSE_W2        = 3,  /* dose_to_water_square (Dw_square_pointer)                */
+    MQI_SCORER_DOSE_M         = 4,  /* dose_to_medium (Dm_pointer)                             */
+    MQI_SCORER_LETD_NUM       = 5,  /* LETd_weight1                                            */
+    MQI_SCORER_LETD_DEN       = 6,  /* LETd_weight2                                            */
+    MQI_SCORER_LETT_NUM       = 7,  /* LETt_weight1                                            */
+    MQI_SCORER_LETT_DEN       = 8,  /* LETt_weight2                                            */
+    MQI_SCORER_EDEP_PRIMARY   = 9,  /* energy_deposit_primary                                  */
+    MQI_SCORER_EDEP_SECONDARY = 10, /* energy_deposit_secondary                                */
+    MQI_SCORER_DIJ            = 11  /* dose_to_water keyed by (voxel, spot): the Dij scorer    */
+} mqi_scorer_type;
+
+/* ---- ROI mapping (moqui/base/mqi_roi.hpp:13-17) ------------------------------------------ */
+typedef enum {
+    MQI_ROI_DIRECT   = 0,
+    MQI_ROI_INDIRECT = 1,
+    MQI_ROI_CONTOUR  = 2
+} mqi_roi_method;
+
+/* ---- a source vertex, layout-identical to mqi::vertex_t<float> (moqui/base/mqi_vertex.hpp:16-29) */
+typedef struct {
+    float ke;     /* kinetic energy, MeV */
+    float pos[3]; /* mm, world frame */
+    float dir[3]; /* unit vector */
+} mqi_vertex;
+
+/* ---- run counters ------------------------------------------------------------------------- */
+typedef struct {
+    uint64_t histories;        /* primaries transported (moqui's tracked_particles)           */
+    uint64_t tracks;           /* tracks popped from the queue, primaries included             */
+    uint64_t steps;            /* voxel steps taken                                            */
+    uint64_t secondaries;      /* daughters pushed to the queue                                */
+    uint64_t local_daughters;  /* deposit-only daughters scored at creation (debug physics)    */
+    uint64_t dropped;          /* daughters dropped by the emulated stack limit                */
+    uint64_t waves;            /* queue generations processed                                  */
+    uint64_t device_errors;    /* bounded device loops that gave up                            */
+} mqi_stats;
+
+typedef struct mqi_ctx mqi_ctx;
+
+/* ---- context ------------------------------------------------------------------------------ */
+
+/* Create a context on CUDA device `device`.  Replaces cudaSetDevice(gpu_id) in
+ * phantom_env/tps_env (moqui/base/environments/mqi_phantom_env.hpp:44-46). */
+int mqi_create(int device, mqi_ctx** out);
+int mqi_destroy(mqi_ctx* ctx);
+
+/* Last error message of this context (or of the calling thread when ctx is NULL). */
+const char* mqi_last_error(const mqi_ctx* ctx);
+
+/* Run all subsequent work of this context on `cuda_stream` (a cudaStream_t; NULL = the
+ * context's own stream). */
+int mqi_set_stream(mqi_ctx* ctx, void* cuda_stream);
+
+/* Physics options.  physics_debug = 1 reproduces moqui built with -D__PHYSICS_DEBUG__ (the
+ * phantom example, tests/mc/phantom/CMakeLists.txt:10): delta cut 0.08511 MeV, 200-deep track
+ * stack, water shortcuts in the calibration, zero-energy local-deposit daughters.  0 is the
+ * release build (delta cut 0.0815 MeV, 10-deep stack).  score_local_deposit mirrors the
+ * kernel argument of the same name (mqi_transport.hpp:123). */
+int mqi_set_physics(mqi_ctx* ctx, int physics_debug, int score_local_deposit);
+
+/* Add a child geometry to the world: a rectilinear voxel grid with nx+1/ny+1/nz+1 edges (mm),
+ * an optional rotation (row-major 3x3, fwd = child->world; NULL = identity) and translation
+ * (NULL = 0).  Replaces the grid3d construction + upload_node/add_node_geometry
+ * (moqui/base/mqi_grid3d.hpp grid3d(...) ctors; mqi_upload_data.hpp:69-103, 144-398).
+ * Children are visited in the order they were added, as world->children[] is. */
+int mqi_add_child(mqi_ctx* ctx, int nx, int ny, int nz, const float* xe, const float* ye,
+                  const float* ze, const float* rot_fwd, const float* translation, int* child_id);
+
+/* Mass density per voxel in g/mm^3, x fastest ([nz][ny][nx]), as grid3d::set_data. */
+int mqi_set_density(mqi_ctx* ctx, int child_id, const float* rho, int on_device);
+
+/* HU per voxel converted on the device with patient_material_t::hu_to_density
+ * (moqui/base/materials/mqi_patient_materials.hpp:514-542), then multiplied by density_scale
+ * (tps_env's DensityScaling, moqui/base/environments/mqi_tps_env.hpp:766-769). */
+int mqi_set_hu(mqi_ctx* ctx, int child_id, const int16_t* hu, float density_scale, int on_device);
+
+/* Add a scorer to a child: scorer<R>(name, capacity, fp_compute_hit) + roi_t
+ * (moqui/base/mqi_scorer.hpp:39-79, moqui/base/mqi_roi.hpp:18-194).  For MQI_ROI_DIRECT the
+ * three arrays may be NULL.  The tally is a dense FP64 array of roi mask size. */
+int mqi_add_scorer(mqi_ctx* ctx, int child_id, int type, int roi_method, uint32_t roi_length,
+                   const uint32_t* roi_start, const uint32_t* roi_stride, const uint32_t* roi_acc,
+                   int* scorer_id);
+
+/* Source vertices for histories [0, n) and, optionally, their spot index (Dij column;
+ * scorer_offset_vector in mqi_transport.hpp:150-154).  Replaces upload_vertices
+ * (mqi_upload_data.hpp:413-420) and upload_scorer_offset_vector. */
+int mqi_set_vertices(mqi_ctx* ctx, const mqi_vertex* v, const uint32_t* spot_ids, uint64_t n,
+                     int on_device);
+
+/* Transport histories [h0, h1) of the current vertices with run seed `seed`, adding into the
+ * tallies.  Replaces transport_particles_patient<float><<<...>>> (mqi_transport.hpp:113-250).
+ * Blocks until the work is done. */
+int mqi_transport(mqi_ctx* ctx, uint64_t h0, uint64_t h1, uint64_t seed);
+
+/* Copy scorer `scorer_id`'s tally (FP64, roi mask size) to `out`.  Replaces download_node
+ * (mqi_download_data.hpp:35-121) followed by x_environment::reshape_data
+ * (moqui/base/environments/mqi_xenvironment.hpp:150-167).  `n_out` receives the element count;
+ * `out` may be NULL to query it. */
+int mqi_get_tally(mqi_ctx* ctx, int scorer_id, double* out, uint64_t* n_out, int on_device);
+
+/* Zero every tally and the run counters. */
+int mqi_reset_tallies(mqi_ctx* ctx);
+
+int mqi_get_stats(mqi_ctx* ctx, mqi_stats* out);
+
+/* Convert HU to density for n voxels (patient_material_t::hu_to_density, then * scale). */
+int mqi_hu_to_density(mqi_ctx* ctx, const int16_t* hu, float* rho, uint64_t n, float scale,
+                      int on_device);
+
+/* Walk rays through a child grid exactly as the transport's voxel loop does
+ * (mqi_transport.hpp:161-239) with the physics replaced by a boundary-only step.  rays: 6 floats
+ * each (pos, dir; world frame).  For ray r, entries [offsets[r], offsets[r+1]) of cnb/dist/cell
+ * hold the visited voxel, the exit distance grid3d::intersect returned there, and the cell.
+ * At most max_steps entries per ray; `capacity` bounds the total.  n_out receives the total. */
+int mqi_trace_rays(mqi_ctx* ctx, int child_id, const float* rays, uint64_t n_rays,
+                   uint32_t max_steps, int64_t* offsets, uint64_t* cnb, float* dist,
+                   int32_t* cells, uint64_t capacity, uint64_t* n_out);
+
+/* Evaluate the transport's tabulated physics functions on the device, for parity tests.
+ * For each energy E[i]: out[i*8 + {0..7}] = {cs_ion, cs_pp, cs_poe, cs_poi (per g/mm^3),
+ * dEdx (negative, MeV/mm in water), beta^2, Te_max, momentum}. */
+int mqi_eval_physics(mqi_ctx* ctx, const float* energies, uint64_t n, float* out);
+
+/* Library version string. */
+const char* mqi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MQI_GPU_H */

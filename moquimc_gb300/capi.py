@@ -1,0 +1,241 @@
+"""ctypes binding of libmqigpu.so (include/mqi_gpu.h).
+
+This is the thin Python layer over the C ABI; it adds no compute of its own.  The library must have
+been built (``moquimc_gb300.build.build_library``); loading fails loudly otherwise -- there is no
+CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from typing import Optional
+
+import numpy as np
+
+from . import build as _build
+
+MQI_OK = 0
+ERRORS = {
+    -1: "MQI_ERR_INVALID", -2: "MQI_ERR_CUDA", -3: "MQI_ERR_NOMEM", -4: "MQI_ERR_STATE",
+    -5: "MQI_ERR_UNSUPPORTED", -6: "MQI_ERR_OVERFLOW", -7: "MQI_ERR_DEVICE",
+}
+
+# scorer types (mqi_scorer_type)
+EDEP, DOSE_W, DOSE_W2, DOSE_M = 1, 2, 3, 4
+LETD_NUM, LETD_DEN, LETT_NUM, LETT_DEN = 5, 6, 7, 8
+EDEP_PRIMARY, EDEP_SECONDARY, DIJ = 9, 10, 11
+# roi methods
+ROI_DIRECT, ROI_INDIRECT, ROI_CONTOUR = 0, 1, 2
+
+# every exported symbol declared in include/mqi_gpu.h
+EXPORTS = (
+    "mqi_create", "mqi_destroy", "mqi_last_error", "mqi_set_stream", "mqi_set_physics",
+    "mqi_add_child", "mqi_set_density", "mqi_set_hu", "mqi_add_scorer", "mqi_set_vertices",
+    "mqi_transport", "mqi_get_tally", "mqi_reset_tallies", "mqi_get_stats", "mqi_hu_to_density",
+    "mqi_trace_rays", "mqi_eval_physics", "mqi_version",
+)
+
+VERTEX_DTYPE = np.dtype([("ke", "<f4"), ("pos", "<f4", (3,)), ("dir", "<f4", (3,))])
+
+
+class MqiStats(C.Structure):
+    _fields_ = [(n, C.c_uint64) for n in (
+        "histories", "tracks", "steps", "secondaries", "local_daughters", "dropped", "waves",
+        "device_errors")]
+
+    def as_dict(self) -> dict:
+        return {n: int(getattr(self, n)) for n, _ in self._fields_}
+
+
+class MqiError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+_lib: Optional[C.CDLL] = None
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load(path: Optional[str] = None) -> C.CDLL:
+    """Load libmqigpu.so and declare the signatures.  Raises if the library was not built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or library_path()
+    if not os.path.exists(path):
+        raise FileNotFoundError(f"{path} not built; run `python -c 'import __graft_entry__ as g; g.build()'`")
+    lib = C.CDLL(path)
+    vp, i32, u32, u64, f32 = C.c_void_p, C.c_int, C.c_uint32, C.c_uint64, C.c_float
+    P = C.POINTER
+    sig = {
+        "mqi_create": (i32, [i32, P(vp)]),
+        "mqi_destroy": (i32, [vp]),
+        "mqi_last_error": (C.c_char_p, [vp]),
+        "mqi_set_stream": (i32, [vp, vp]),
+        "mqi_set_physics": (i32, [vp, i32, i32]),
+        "mqi_add_child": (i32, [vp, i32, i32, i32, vp, vp, vp, vp, vp, P(i32)]),
+        "mqi_set_density": (i32, [vp, i32, vp, i32]),
+        "mqi_set_hu": (i32, [vp, i32, vp, f32, i32]),
+        "mqi_add_scorer": (i32, [vp, i32, i32, i32, u32, vp, vp, vp, P(i32)]),
+        "mqi_set_vertices": (i32, [vp, vp, vp, u64, i32]),
+        "mqi_transport": (i32, [vp, u64, u64, u64]),
+        "mqi_get_tally": (i32, [vp, i32, vp, P(u64), i32]),
+        "mqi_reset_tallies": (i32, [vp]),
+        "mqi_get_stats": (i32, [vp, P(MqiStats)]),
+        "mqi_hu_to_density": (i32, [vp, vp, vp, u64, f32, i32]),
+        "mqi_trace_rays": (i32, [vp, i32, vp, u64, u32, vp, vp, vp, vp, u64, P(u64)]),
+        "mqi_eval_physics": (i32, [vp, vp, u64, vp]),
+        "mqi_version": (C.c_char_p, []),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _ptr(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class Context:
+    """One engine context on one CUDA device (mqi_create ... mqi_destroy)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load()
+        h = C.c_void_p()
+        self._check(self.lib.mqi_create(device, C.byref(h)), None)
+        self.h = h
+        self.children: list[tuple[int, int, int]] = []
+        self.scorers: list[int] = []
+
+    def _check(self, rc: int, h) -> None:
+        if rc != MQI_OK:
+            msg = self.lib.mqi_last_error(h)
+            raise MqiError(rc, msg.decode() if msg else "")
+
+    def close(self) -> None:
+        if getattr(self, "h", None):
+            self.lib.mqi_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- setup ----
+    def set_physics(self, physics_debug: bool, score_local_deposit: bool = True) -> None:
+        self._check(self.lib.mqi_set_physics(self.h, int(physics_debug), int(score_local_deposit)), self.h)
+
+    def set_stream(self, stream_ptr: Optional[int]) -> None:
+        self._check(self.lib.mqi_set_stream(self.h, stream_ptr), self.h)
+
+    def add_child(self, xe, ye, ze, rot_fwd=None, translation=None) -> int:
+        xe = np.ascontiguousarray(xe, dtype=np.float32)
+        ye = np.ascontiguousarray(ye, dtype=np.float32)
+        ze = np.ascontiguousarray(ze, dtype=np.float32)
+        rf = None if rot_fwd is None else np.ascontiguousarray(rot_fwd, dtype=np.float32).reshape(9)
+        tr = None if translation is None else np.ascontiguousarray(translation, dtype=np.float32).reshape(3)
+        cid = C.c_int(-1)
+        self._check(self.lib.mqi_add_child(self.h, len(xe) - 1, len(ye) - 1, len(ze) - 1, _ptr(xe), _ptr(ye),
+                                           _ptr(ze), _ptr(rf), _ptr(tr), C.byref(cid)), self.h)
+        self.children.append((len(xe) - 1, len(ye) - 1, len(ze) - 1))
+        return cid.value
+
+    def set_density(self, child: int, rho: np.ndarray) -> None:
+        rho = np.ascontiguousarray(rho, dtype=np.float32)
+        self._check(self.lib.mqi_set_density(self.h, child, _ptr(rho), 0), self.h)
+
+    def set_density_device(self, child: int, dev_ptr: int) -> None:
+        self._check(self.lib.mqi_set_density(self.h, child, C.c_void_p(dev_ptr), 1), self.h)
+
+    def set_hu(self, child: int, hu: np.ndarray, density_scale: float = 1.0) -> None:
+        hu = np.ascontiguousarray(hu, dtype=np.int16)
+        self._check(self.lib.mqi_set_hu(self.h, child, _ptr(hu), C.c_float(density_scale), 0), self.h)
+
+    def add_scorer(self, child: int, stype: int, roi_method: int = ROI_DIRECT, start=None, stride=None,
+                   acc=None) -> int:
+        arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.uint32) for a in (start, stride, acc)]
+        length = 0 if arrs[1] is None else len(arrs[1])
+        sid = C.c_int(-1)
+        self._check(self.lib.mqi_add_scorer(self.h, child, stype, roi_method, length, _ptr(arrs[0]), _ptr(arrs[1]),
+                                            _ptr(arrs[2]), C.byref(sid)), self.h)
+        self.scorers.append(sid.value)
+        return sid.value
+
+    def set_vertices(self, vertices: np.ndarray, spot_ids: Optional[np.ndarray] = None) -> None:
+        v = np.ascontiguousarray(vertices)
+        if v.dtype != VERTEX_DTYPE:
+            v = np.ascontiguousarray(np.asarray(v, dtype=np.float32).reshape(-1, 7)).view(VERTEX_DTYPE).reshape(-1)
+        s = None if spot_ids is None else np.ascontiguousarray(spot_ids, dtype=np.uint32)
+        self._check(self.lib.mqi_set_vertices(self.h, _ptr(v), _ptr(s), len(v), 0), self.h)
+        self.n_vertices = len(v)
+
+    def set_vertices_device(self, dev_ptr: int, n: int, spot_dev_ptr: Optional[int] = None) -> None:
+        self._check(self.lib.mqi_set_vertices(self.h, C.c_void_p(dev_ptr),
+                                              None if spot_dev_ptr is None else C.c_void_p(spot_dev_ptr), n, 1),
+                    self.h)
+        self.n_vertices = n
+
+    # ---- run ----
+    def transport(self, h0: int, h1: int, seed: int) -> None:
+        self._check(self.lib.mqi_transport(self.h, h0, h1, seed & 0xFFFFFFFFFFFFFFFF), self.h)
+
+    def tally(self, scorer: int) -> np.ndarray:
+        n = C.c_uint64(0)
+        self._check(self.lib.mqi_get_tally(self.h, scorer, None, C.byref(n), 0), self.h)
+        out = np.empty(n.value, dtype=np.float64)
+        self._check(self.lib.mqi_get_tally(self.h, scorer, _ptr(out), C.byref(n), 0), self.h)
+        return out
+
+    def tally_to_device(self, scorer: int, dev_ptr: int) -> None:
+        n = C.c_uint64(0)
+        self._check(self.lib.mqi_get_tally(self.h, scorer, C.c_void_p(dev_ptr), C.byref(n), 1), self.h)
+
+    def reset(self) -> None:
+        self._check(self.lib.mqi_reset_tallies(self.h), self.h)
+
+    def stats(self) -> dict:
+        s = MqiStats()
+        self._check(self.lib.mqi_get_stats(self.h, C.byref(s)), self.h)
+        return s.as_dict()
+
+    # ---- probes ----
+    def hu_to_density(self, hu: np.ndarray, scale: float = 1.0) -> np.ndarray:
+        hu = np.ascontiguousarray(hu, dtype=np.int16)
+        out = np.empty(hu.shape, dtype=np.float32)
+        self._check(self.lib.mqi_hu_to_density(self.h, _ptr(hu), _ptr(out), hu.size, C.c_float(scale), 0), self.h)
+        return out
+
+    def trace_rays(self, child: int, rays: np.ndarray, max_steps: int):
+        rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 6)
+        n = len(rays)
+        cap = n * max_steps
+        off = np.zeros(n + 1, dtype=np.int64)
+        cnb = np.zeros(cap, dtype=np.uint64)
+        dist = np.zeros(cap, dtype=np.float32)
+        cells = np.zeros((cap, 3), dtype=np.int32)
+        tot = C.c_uint64(0)
+        self._check(self.lib.mqi_trace_rays(self.h, child, _ptr(rays), n, max_steps, _ptr(off), _ptr(cnb), _ptr(dist),
+                                            _ptr(cells), cap, C.byref(tot)), self.h)
+        t = tot.value
+        return off, cnb[:t], dist[:t], cells[:t]
+
+    def eval_physics(self, energies: np.ndarray) -> np.ndarray:
+        e = np.ascontiguousarray(energies, dtype=np.float32)
+        out = np.empty((len(e), 8), dtype=np.float32)
+        self._check(self.lib.mqi_eval_physics(self.h, _ptr(e), len(e), _ptr(out)), self.h)
+        return out

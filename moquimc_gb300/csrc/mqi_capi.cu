@@ -1,0 +1,663 @@
+// C ABI of the GB300 proton transport engine: context, buffers and the wave loop.
+//
+// The reference keeps its device state in globals (mc::mc_world, mc_materials, mc_vertices,
+// moqui/kernel_functions/mqi_variables.hpp:8-17) built by <<<1,1>>> kernels that call device-side
+// `new` (mqi_upload_data.hpp:69-142).  Here a context owns flat device buffers, and every kernel
+// receives what it reads by value.
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "mqi_device.cuh"
+#include "mqi_gpu.h"
+#include "mqi_internal.h"
+
+using namespace mqi_gpu;
+
+namespace
+{
+
+thread_local std::string g_thread_error;
+
+struct ChildHost {
+    int    nx = 0, ny = 0, nz = 0;
+    float* xe = nullptr;
+    float* ye = nullptr;
+    float* ze = nullptr;
+    float* rho = nullptr;
+    bool   has_rho = false;
+    float  rf[9], ri[9], tr[3];
+    int    identity = 1;
+};
+
+struct ScorerHost {
+    int       child = 0;
+    int       type = 0;
+    int       roi_method = 0;
+    int       stat_mode = 0;
+    uint32_t  roi_len = 0;
+    uint32_t* start = nullptr;
+    uint32_t* stride = nullptr;
+    uint32_t* acc = nullptr;
+    double*   tally = nullptr;
+    uint64_t  tally_len = 0;
+};
+
+struct QueueBuf {
+    Queue    q{};
+    void*    base = nullptr;
+};
+
+}   // namespace
+
+struct mqi_ctx {
+    int                     device = 0;
+    cudaStream_t            stream = nullptr;
+    bool                    own_stream = false;
+    std::string             err;
+    int                     physics_debug = 0;
+    int                     score_local = 1;
+    std::vector<ChildHost>  children;
+    std::vector<ScorerHost> scorers;
+    mqi_vertex*             vertices = nullptr;
+    uint64_t                n_vertices = 0;
+    uint64_t                vertex_cap = 0;
+    uint32_t*               spot_ids = nullptr;
+    uint64_t                spot_cap = 0;
+    bool                    has_spots = false;
+    QueueBuf                qa, qb;
+    uint32_t                queue_cap = 0;
+    uint32_t*               counters = nullptr;     // [0,1] queue sizes, [2] head, [3] error flag
+    unsigned long long*     stats = nullptr;        // 8 x u64
+    uint32_t*               host_counts = nullptr;  // pinned: 4 x u32
+    float*                  tables = nullptr;       // 6*600 physics + 3996 HU correction
+    int                     num_sms = 0;
+    int                     wave_block = 256;
+    int                     wave_grid = 0;
+    uint32_t                max_slice_steps = 0;
+    uint32_t                primary_chunk = 1u << 21;
+    uint64_t                waves = 0;
+};
+
+namespace
+{
+
+int
+fail(mqi_ctx* c, int code, const std::string& msg) {
+    if (c) c->err = msg;
+    g_thread_error = msg;
+    return code;
+}
+
+int
+cuda_fail(mqi_ctx* c, cudaError_t e, const char* what) {
+    return fail(c, e == cudaErrorMemoryAllocation ? MQI_ERR_NOMEM : MQI_ERR_CUDA,
+                std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define MQI_CUDA(c, expr, what)                           \
+    do {                                                  \
+        cudaError_t _e = (expr);                          \
+        if (_e != cudaSuccess) return cuda_fail(c, _e, what); \
+    } while (0)
+
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+        cudaGetDevice(&prev);
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard() {
+        int cur = -1;
+        cudaGetDevice(&cur);
+        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+void
+free_queue(QueueBuf& b) {
+    if (b.base) cudaFree(b.base);
+    b.base = nullptr;
+    b.q    = Queue{};
+}
+
+/// One allocation per queue, carved into the SoA columns (each 256-byte aligned).
+cudaError_t
+alloc_queue(QueueBuf& b, uint32_t cap) {
+    free_queue(b);
+    const size_t col   = ((size_t) cap * 4 + 255) & ~(size_t) 255;
+    const int    ncols = 14;
+    cudaError_t  e     = cudaMalloc(&b.base, col * ncols);
+    if (e != cudaSuccess) return e;
+    char* p = static_cast<char*>(b.base);
+    auto  f = [&](int k) { return reinterpret_cast<float*>(p + col * k); };
+    auto  u = [&](int k) { return reinterpret_cast<uint32_t*>(p + col * k); };
+    b.q.ke = f(0); b.q.px = f(1); b.q.py = f(2); b.q.pz = f(3);
+    b.q.dx = f(4); b.q.dy = f(5); b.q.dz = f(6); b.q.dE0 = f(7);
+    b.q.hist = u(8); b.q.uid_lo = u(9); b.q.uid_hi = u(10); b.q.ctr = u(11); b.q.meta = u(12);
+    b.q.cell = reinterpret_cast<int32_t*>(p + col * 13);
+    b.q.capacity = cap;
+    return cudaSuccess;
+}
+
+void
+identity3(float* m) {
+    for (int i = 0; i < 9; ++i) m[i] = (i % 4 == 0) ? 1.0f : 0.0f;
+}
+
+bool
+valid_ctx(mqi_ctx* c) {
+    return c != nullptr;
+}
+
+}   // namespace
+
+extern "C" {
+
+const char*
+mqi_version(void) {
+    return "mqi-gb300 0.1 (sm_103a)";
+}
+
+const char*
+mqi_last_error(const mqi_ctx* ctx) {
+    return ctx ? ctx->err.c_str() : g_thread_error.c_str();
+}
+
+int
+mqi_create(int device, mqi_ctx** out) {
+    if (!out) return fail(nullptr, MQI_ERR_INVALID, "mqi_create: out is NULL");
+    *out = nullptr;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess) return cuda_fail(nullptr, e, "mqi_create: cudaGetDeviceCount");
+    if (device < 0 || device >= n) return fail(nullptr, MQI_ERR_INVALID, "mqi_create: no such device");
+    auto* c   = new mqi_ctx();
+    c->device = device;
+    DeviceGuard g(device);
+    cudaDeviceProp prop{};
+    if ((e = cudaGetDeviceProperties(&prop, device)) != cudaSuccess) {
+        delete c;
+        return cuda_fail(nullptr, e, "mqi_create: cudaGetDeviceProperties");
+    }
+    c->num_sms = prop.multiProcessorCount;
+    if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess) {
+        delete c;
+        return cuda_fail(nullptr, e, "mqi_create: cudaStreamCreate");
+    }
+    c->own_stream = true;
+    const size_t tbytes = (6 * MQI_TABLE_N + MQI_DENSITY_CORRECTION_N) * sizeof(float);
+    std::vector<float> host(6 * MQI_TABLE_N + MQI_DENSITY_CORRECTION_N);
+    std::memcpy(&host[0 * MQI_TABLE_N], mqi_tab_cs_p_ion, sizeof(mqi_tab_cs_p_ion));
+    std::memcpy(&host[1 * MQI_TABLE_N], mqi_tab_dedx, sizeof(mqi_tab_dedx));
+    std::memcpy(&host[2 * MQI_TABLE_N], mqi_tab_range, sizeof(mqi_tab_range));
+    std::memcpy(&host[3 * MQI_TABLE_N], mqi_tab_cs_pp_e, sizeof(mqi_tab_cs_pp_e));
+    std::memcpy(&host[4 * MQI_TABLE_N], mqi_tab_cs_po_e, sizeof(mqi_tab_cs_po_e));
+    std::memcpy(&host[5 * MQI_TABLE_N], mqi_tab_cs_po_i, sizeof(mqi_tab_cs_po_i));
+    std::memcpy(&host[6 * MQI_TABLE_N], mqi_tab_density_correction, sizeof(mqi_tab_density_correction));
+    if ((e = cudaMalloc(&c->tables, tbytes)) != cudaSuccess ||
+        (e = cudaMemcpy(c->tables, host.data(), tbytes, cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMalloc(&c->counters, 8 * sizeof(uint32_t))) != cudaSuccess ||
+        (e = cudaMemset(c->counters, 0, 8 * sizeof(uint32_t))) != cudaSuccess ||
+        (e = cudaMalloc(&c->stats, 8 * sizeof(unsigned long long))) != cudaSuccess ||
+        (e = cudaMemset(c->stats, 0, 8 * sizeof(unsigned long long))) != cudaSuccess ||
+        (e = cudaMallocHost(&c->host_counts, 8 * sizeof(uint32_t))) != cudaSuccess) {
+        mqi_destroy(c);
+        return cuda_fail(nullptr, e, "mqi_create: allocation");
+    }
+    c->wave_grid = c->num_sms * 2;
+    *out = c;
+    return MQI_OK;
+}
+
+int
+mqi_destroy(mqi_ctx* c) {
+    if (!c) return MQI_OK;
+    DeviceGuard g(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    for (auto& ch : c->children) {
+        cudaFree(ch.xe); cudaFree(ch.ye); cudaFree(ch.ze); cudaFree(ch.rho);
+    }
+    for (auto& s : c->scorers) {
+        cudaFree(s.start); cudaFree(s.stride); cudaFree(s.acc); cudaFree(s.tally);
+    }
+    cudaFree(c->vertices);
+    cudaFree(c->spot_ids);
+    free_queue(c->qa);
+    free_queue(c->qb);
+    cudaFree(c->counters);
+    cudaFree(c->stats);
+    cudaFree(c->tables);
+    if (c->host_counts) cudaFreeHost(c->host_counts);
+    if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+    return MQI_OK;
+}
+
+int
+mqi_set_stream(mqi_ctx* c, void* s) {
+    if (!valid_ctx(c)) return fail(c, MQI_ERR_INVALID, "mqi_set_stream: ctx is NULL");
+    DeviceGuard g(c->device);
+    if (c->own_stream && c->stream) {
+        cudaStreamSynchronize(c->stream);
+        cudaStreamDestroy(c->stream);
+    }
+    if (s) {
+        c->stream     = static_cast<cudaStream_t>(s);
+        c->own_stream = false;
+    } else {
+        MQI_CUDA(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "mqi_set_stream");
+        c->own_stream = true;
+    }
+    return MQI_OK;
+}
+
+int
+mqi_set_physics(mqi_ctx* c, int physics_debug, int score_local_deposit) {
+    if (!valid_ctx(c)) return fail(c, MQI_ERR_INVALID, "mqi_set_physics: ctx is NULL");
+    c->physics_debug = physics_debug ? 1 : 0;
+    c->score_local   = score_local_deposit ? 1 : 0;
+    return MQI_OK;
+}
+
+int
+mqi_add_child(mqi_ctx* c, int nx, int ny, int nz, const float* xe, const float* ye, const float* ze,
+              const float* rot_fwd, const float* translation, int* child_id) {
+    if (!valid_ctx(c)) return fail(c, MQI_ERR_INVALID, "mqi_add_child: ctx is NULL");
+    if (nx <= 0 || ny <= 0 || nz <= 0 || nx > 2047 || ny > 2047 || nz > 2047 || !xe || !ye || !ze)
+        return fail(c, MQI_ERR_INVALID, "mqi_add_child: grid dimensions must be 1..2047 with edge arrays");
+    if ((int) c->children.size() >= kMaxChildren)
+        return fail(c, MQI_ERR_INVALID, "mqi_add_child: too many children");
+    if ((uint64_t) nx * ny * nz > 0xFFFFFFFEull)
+        return fail(c, MQI_ERR_INVALID, "mqi_add_child: more voxels than a 32-bit key can index");
+    for (int i = 0; i < nx; ++i) if (!(xe[i] < xe[i + 1])) return fail(c, MQI_ERR_INVALID, "mqi_add_child: x edges not increasing");
+    for (int i = 0; i < ny; ++i) if (!(ye[i] < ye[i + 1])) return fail(c, MQI_ERR_INVALID, "mqi_add_child: y edges not increasing");
+    for (int i = 0; i < nz; ++i) if (!(ze[i] < ze[i + 1])) return fail(c, MQI_ERR_INVALID, "mqi_add_child: z edges not increasing");
+    DeviceGuard g(c->device);
+    ChildHost ch;
+    ch.nx = nx; ch.ny = ny; ch.nz = nz;
+    MQI_CUDA(c, cudaMalloc(&ch.xe, (nx + 1) * sizeof(float)), "mqi_add_child");
+    MQI_CUDA(c, cudaMalloc(&ch.ye, (ny + 1) * sizeof(float)), "mqi_add_child");
+    MQI_CUDA(c, cudaMalloc(&ch.ze, (nz + 1) * sizeof(float)), "mqi_add_child");
+    MQI_CUDA(c, cudaMemcpy(ch.xe, xe, (nx + 1) * sizeof(float), cudaMemcpyHostToDevice), "mqi_add_child");
+    MQI_CUDA(c, cudaMemcpy(ch.ye, ye, (ny + 1) * sizeof(float), cudaMemcpyHostToDevice), "mqi_add_child");
+    MQI_CUDA(c, cudaMemcpy(ch.ze, ze, (nz + 1) * sizeof(float), cudaMemcpyHostToDevice), "mqi_add_child");
+    MQI_CUDA(c, cudaMalloc(&ch.rho, (size_t) nx * ny * nz * sizeof(float)), "mqi_add_child");
+    identity3(ch.rf);
+    ch.tr[0] = ch.tr[1] = ch.tr[2] = 0.0f;
+    if (rot_fwd) std::memcpy(ch.rf, rot_fwd, sizeof(ch.rf));
+    if (translation) std::memcpy(ch.tr, translation, sizeof(ch.tr));
+    // inverse = transpose (mat3x3::inverse, mqi_matrix.hpp)
+    const float* m = ch.rf;
+    float inv[9] = { m[0], m[3], m[6], m[1], m[4], m[7], m[2], m[5], m[8] };
+    std::memcpy(ch.ri, inv, sizeof(inv));
+    float id[9];
+    identity3(id);
+    ch.identity = (std::memcmp(ch.rf, id, sizeof(id)) == 0 && ch.tr[0] == 0.0f && ch.tr[1] == 0.0f && ch.tr[2] == 0.0f) ? 1 : 0;
+    c->children.push_back(ch);
+    if (child_id) *child_id = (int) c->children.size() - 1;
+    return MQI_OK;
+}
+
+int
+mqi_set_density(mqi_ctx* c, int id, const float* rho, int on_device) {
+    if (!valid_ctx(c) || !rho) return fail(c, MQI_ERR_INVALID, "mqi_set_density: bad argument");
+    if (id < 0 || id >= (int) c->children.size()) return fail(c, MQI_ERR_INVALID, "mqi_set_density: no such child");
+    DeviceGuard g(c->device);
+    ChildHost& ch = c->children[id];
+    const size_t bytes = (size_t) ch.nx * ch.ny * ch.nz * sizeof(float);
+    MQI_CUDA(c, cudaMemcpyAsync(ch.rho, rho, bytes, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->stream),
+             "mqi_set_density");
+    MQI_CUDA(c, cudaStreamSynchronize(c->stream), "mqi_set_density");
+    ch.has_rho = true;
+    return MQI_OK;
+}
+
+int
+mqi_hu_to_density(mqi_ctx* c, const int16_t* hu, float* rho, uint64_t n, float scale, int on_device) {
+    if (!valid_ctx(c) || (!hu && n) || (!rho && n)) return fail(c, MQI_ERR_INVALID, "mqi_hu_to_density: bad argument");
+    DeviceGuard g(c->device);
+    if (on_device) {
+        MQI_CUDA(c, launch_hu_to_density(c->tables + 6 * MQI_TABLE_N, hu, rho, n, scale, c->stream), "mqi_hu_to_density");
+        MQI_CUDA(c, cudaStreamSynchronize(c->stream), "mqi_hu_to_density");
+        return MQI_OK;
+    }
+    int16_t* dh = nullptr;
+    float*   dr = nullptr;
+    MQI_CUDA(c, cudaMalloc(&dh, n * sizeof(int16_t) + 16), "mqi_hu_to_density");
+    cudaError_t e = cudaMalloc(&dr, n * sizeof(float) + 16);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dh, hu, n * sizeof(int16_t), cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = launch_hu_to_density(c->tables + 6 * MQI_TABLE_N, dh, dr, n, scale, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(rho, dr, n * sizeof(float), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaFree(dh);
+    cudaFree(dr);
+    if (e != cudaSuccess) return cuda_fail(c, e, "mqi_hu_to_density");
+    return MQI_OK;
+}
+
+int
+mqi_set_hu(mqi_ctx* c, int id, const int16_t* hu, float scale, int on_device) {
+    if (!valid_ctx(c) || !hu) return fail(c, MQI_ERR_INVALID, "mqi_set_hu: bad argument");
+    if (id < 0 || id >= (int) c->children.size()) return fail(c, MQI_ERR_INVALID, "mqi_set_hu: no such child");
+    DeviceGuard g(c->device);
+    ChildHost&     ch = c->children[id];
+    const uint64_t n  = (uint64_t) ch.nx * ch.ny * ch.nz;
+    const int16_t* src = hu;
+    int16_t*       tmp = nullptr;
+    if (!on_device) {
+        MQI_CUDA(c, cudaMalloc(&tmp, n * sizeof(int16_t)), "mqi_set_hu");
+        cudaError_t e = cudaMemcpyAsync(tmp, hu, n * sizeof(int16_t), cudaMemcpyHostToDevice, c->stream);
+        if (e != cudaSuccess) { cudaFree(tmp); return cuda_fail(c, e, "mqi_set_hu"); }
+        src = tmp;
+    }
+    cudaError_t e = launch_hu_to_density(c->tables + 6 * MQI_TABLE_N, src, ch.rho, n, scale, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (tmp) cudaFree(tmp);
+    if (e != cudaSuccess) return cuda_fail(c, e, "mqi_set_hu");
+    ch.has_rho = true;
+    return MQI_OK;
+}
+
+int
+mqi_add_scorer(mqi_ctx* c, int child_id, int type, int roi_method, uint32_t roi_length, const uint32_t* roi_start,
+               const uint32_t* roi_stride, const uint32_t* roi_acc, int* scorer_id) {
+    if (!valid_ctx(c)) return fail(c, MQI_ERR_INVALID, "mqi_add_scorer: ctx is NULL");
+    if (child_id < 0 || child_id >= (int) c->children.size())
+        return fail(c, MQI_ERR_INVALID, "mqi_add_scorer: no such child");
+    if (type < MQI_SCORER_EDEP || type > MQI_SCORER_DIJ)
+        return fail(c, MQI_ERR_UNSUPPORTED, "mqi_add_scorer: unknown scorer type (custom fp_compute_hit callbacks have no C-ABI form)");
+    if (type == MQI_SCORER_DIJ)
+        return fail(c, MQI_ERR_UNSUPPORTED, "mqi_add_scorer: use the Dij entry points for MQI_SCORER_DIJ");
+    if ((int) c->scorers.size() >= kMaxScorers) return fail(c, MQI_ERR_INVALID, "mqi_add_scorer: too many scorers");
+    // scorers of one child are contiguous
+    if (!c->scorers.empty() && c->scorers.back().child != child_id) {
+        for (auto& s : c->scorers)
+            if (s.child == child_id) return fail(c, MQI_ERR_INVALID, "mqi_add_scorer: add a child's scorers together");
+    }
+    const ChildHost& ch = c->children[child_id];
+    const uint64_t nvox = (uint64_t) ch.nx * ch.ny * ch.nz;
+    DeviceGuard g(c->device);
+    ScorerHost s;
+    s.child      = child_id;
+    s.type       = type;
+    s.roi_method = roi_method;
+    s.stat_mode  = 0;
+    s.roi_len    = roi_length;
+    if (roi_method == MQI_ROI_DIRECT) {
+        s.tally_len = nvox;
+    } else if (roi_method == MQI_ROI_INDIRECT) {
+        if (!roi_start) return fail(c, MQI_ERR_INVALID, "mqi_add_scorer: INDIRECT needs roi_start (one entry per voxel)");
+        MQI_CUDA(c, cudaMalloc(&s.start, nvox * sizeof(uint32_t)), "mqi_add_scorer");
+        MQI_CUDA(c, cudaMemcpy(s.start, roi_start, nvox * sizeof(uint32_t), cudaMemcpyHostToDevice), "mqi_add_scorer");
+        s.tally_len = nvox;
+    } else if (roi_method == MQI_ROI_CONTOUR) {
+        if (!roi_start || !roi_stride || !roi_acc || roi_length == 0)
+            return fail(c, MQI_ERR_INVALID, "mqi_add_scorer: CONTOUR needs start/stride/acc arrays");
+        MQI_CUDA(c, cudaMalloc(&s.start, roi_length * sizeof(uint32_t)), "mqi_add_scorer");
+        MQI_CUDA(c, cudaMalloc(&s.stride, roi_length * sizeof(uint32_t)), "mqi_add_scorer");
+        MQI_CUDA(c, cudaMalloc(&s.acc, roi_length * sizeof(uint32_t)), "mqi_add_scorer");
+        MQI_CUDA(c, cudaMemcpy(s.start, roi_start, roi_length * sizeof(uint32_t), cudaMemcpyHostToDevice), "mqi_add_scorer");
+        MQI_CUDA(c, cudaMemcpy(s.stride, roi_stride, roi_length * sizeof(uint32_t), cudaMemcpyHostToDevice), "mqi_add_scorer");
+        MQI_CUDA(c, cudaMemcpy(s.acc, roi_acc, roi_length * sizeof(uint32_t), cudaMemcpyHostToDevice), "mqi_add_scorer");
+        s.tally_len = nvox;
+    } else {
+        return fail(c, MQI_ERR_INVALID, "mqi_add_scorer: unknown roi method");
+    }
+    MQI_CUDA(c, cudaMalloc(&s.tally, s.tally_len * sizeof(double)), "mqi_add_scorer");
+    MQI_CUDA(c, cudaMemset(s.tally, 0, s.tally_len * sizeof(double)), "mqi_add_scorer");
+    c->scorers.push_back(s);
+    if (scorer_id) *scorer_id = (int) c->scorers.size() - 1;
+    return MQI_OK;
+}
+
+int
+mqi_set_vertices(mqi_ctx* c, const mqi_vertex* v, const uint32_t* spot_ids, uint64_t n, int on_device) {
+    if (!valid_ctx(c) || (!v && n)) return fail(c, MQI_ERR_INVALID, "mqi_set_vertices: bad argument");
+    if (n > 0xFFFFFFFFull) return fail(c, MQI_ERR_INVALID, "mqi_set_vertices: at most 2^32-1 histories per call");
+    DeviceGuard g(c->device);
+    if (n > c->vertex_cap) {
+        cudaFree(c->vertices);
+        c->vertices = nullptr;
+        MQI_CUDA(c, cudaMalloc(&c->vertices, n * sizeof(mqi_vertex)), "mqi_set_vertices");
+        c->vertex_cap = n;
+    }
+    const cudaMemcpyKind k = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    if (n) MQI_CUDA(c, cudaMemcpyAsync(c->vertices, v, n * sizeof(mqi_vertex), k, c->stream), "mqi_set_vertices");
+    c->has_spots = spot_ids != nullptr;
+    if (spot_ids && n) {
+        if (n > c->spot_cap) {
+            cudaFree(c->spot_ids);
+            c->spot_ids = nullptr;
+            MQI_CUDA(c, cudaMalloc(&c->spot_ids, n * sizeof(uint32_t)), "mqi_set_vertices");
+            c->spot_cap = n;
+        }
+        MQI_CUDA(c, cudaMemcpyAsync(c->spot_ids, spot_ids, n * sizeof(uint32_t), k, c->stream), "mqi_set_vertices");
+    }
+    c->n_vertices = n;
+    return MQI_OK;
+}
+
+int
+mqi_transport(mqi_ctx* c, uint64_t h0, uint64_t h1, uint64_t seed) {
+    if (!valid_ctx(c)) return fail(c, MQI_ERR_INVALID, "mqi_transport: ctx is NULL");
+    if (c->children.empty()) return fail(c, MQI_ERR_STATE, "mqi_transport: no child geometry");
+    for (auto& ch : c->children)
+        if (!ch.has_rho) return fail(c, MQI_ERR_STATE, "mqi_transport: a child has no density");
+    if (h1 < h0 || h1 > c->n_vertices) return fail(c, MQI_ERR_INVALID, "mqi_transport: history range outside the vertices");
+    if (h0 == h1) return MQI_OK;
+    DeviceGuard g(c->device);
+    const uint32_t chunk = c->primary_chunk;
+    const uint32_t need  = chunk * 3u;
+    if (c->queue_cap < need) {
+        cudaError_t e = alloc_queue(c->qa, need);
+        if (e == cudaSuccess) e = alloc_queue(c->qb, need);
+        if (e != cudaSuccess) {
+            c->queue_cap = 0;
+            return cuda_fail(c, e, "mqi_transport: queue allocation");
+        }
+        c->queue_cap = need;
+    }
+    WaveParams P{};
+    P.n_children = (int) c->children.size();
+    for (int i = 0; i < P.n_children; ++i) {
+        const ChildHost& h = c->children[i];
+        ChildDev&        d = P.child[i];
+        d.nx = h.nx; d.ny = h.ny; d.nz = h.nz;
+        d.xe = h.xe; d.ye = h.ye; d.ze = h.ze; d.rho = h.rho;
+        std::memcpy(d.rf, h.rf, sizeof(d.rf));
+        std::memcpy(d.ri, h.ri, sizeof(d.ri));
+        std::memcpy(d.tr, h.tr, sizeof(d.tr));
+        d.identity = h.identity;
+        d.scorer_begin = 0;
+        d.n_scorers = 0;
+    }
+    for (int i = 0; i < (int) c->scorers.size(); ++i) {
+        const ScorerHost& s = c->scorers[i];
+        ScorerDev&        d = P.scorer[i];
+        d.type = s.type; d.roi_method = s.roi_method; d.stat_mode = s.stat_mode;
+        d.roi_len = s.roi_len; d.start = s.start; d.stride = s.stride; d.acc = s.acc;
+        d.tally = s.tally; d.tally_len = s.tally_len;
+        ChildDev& ch = P.child[s.child];
+        if (ch.n_scorers == 0) ch.scorer_begin = i;
+        ++ch.n_scorers;
+    }
+    // Non-stat kernel quirk (mqi_transport.hpp:204-225): with n >= 3 scorers on a node, scorers
+    // 0..n-3 are inserted twice per step.
+    for (int i = 0; i < P.n_children; ++i) {
+        const ChildDev& ch = P.child[i];
+        if (ch.n_scorers >= 3)
+            for (int k = 0; k < ch.n_scorers - 2; ++k) P.scorer[ch.scorer_begin + k].double_score = 1;
+    }
+    P.physics_debug   = c->physics_debug;
+    P.score_local     = c->score_local;
+    P.stack_limit     = c->physics_debug ? 200 : 10;
+    P.t_cut           = c->physics_debug ? kTcutDebug : kTcutRelease;
+    P.k0              = (uint32_t) seed;
+    P.k1              = (uint32_t) (seed >> 32);
+    P.max_slice_steps = c->max_slice_steps;
+    P.inline_local    = (P.n_children == 1) ? 1 : 0;
+    P.head            = c->counters + 2;
+    P.error_flag      = c->counters + 3;
+    P.stats           = c->stats;
+    P.spot_ids        = c->has_spots ? c->spot_ids : nullptr;
+    P.tables          = c->tables;
+    QueueBuf* A = &c->qa;
+    QueueBuf* B = &c->qb;
+    for (uint64_t h = h0; h < h1; h += chunk) {
+        const uint32_t n = (uint32_t) std::min<uint64_t>(chunk, h1 - h);
+        MQI_CUDA(c, launch_load_primaries(A->q, c->vertices, h, n, c->stream), "mqi_transport: load primaries");
+        c->host_counts[0] = n;
+        MQI_CUDA(c, cudaMemcpyAsync(c->counters + 0, c->host_counts, sizeof(uint32_t), cudaMemcpyHostToDevice, c->stream),
+                 "mqi_transport");
+        int cur = 0;
+        for (int wave = 0;; ++wave) {
+            if (wave > 100000) return fail(c, MQI_ERR_DEVICE, "mqi_transport: wave limit reached");
+            P.in    = A->q;
+            P.out   = B->q;
+            P.n_in  = c->counters + cur;
+            P.n_out = c->counters + (1 - cur);
+            MQI_CUDA(c, cudaMemsetAsync(c->counters + (1 - cur), 0, sizeof(uint32_t), c->stream), "mqi_transport");
+            MQI_CUDA(c, cudaMemsetAsync(c->counters + 2, 0, sizeof(uint32_t), c->stream), "mqi_transport");
+            MQI_CUDA(c, launch_wave(P, c->wave_grid, c->wave_block, c->stream), "mqi_transport: wave");
+            MQI_CUDA(c, cudaMemcpyAsync(c->host_counts, c->counters, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream),
+                     "mqi_transport");
+            MQI_CUDA(c, cudaStreamSynchronize(c->stream), "mqi_transport: wave");
+            ++c->waves;
+            if (c->host_counts[3] & 2u) return fail(c, MQI_ERR_OVERFLOW, "mqi_transport: particle queue overflow");
+            const uint32_t n_next = c->host_counts[1 - cur];
+            if (n_next == 0) break;
+            std::swap(A, B);
+            cur = 1 - cur;
+        }
+    }
+    if (c->host_counts[3] & 1u) return fail(c, MQI_ERR_DEVICE, "mqi_transport: a bounded device loop gave up");
+    return MQI_OK;
+}
+
+int
+mqi_get_tally(mqi_ctx* c, int id, double* out, uint64_t* n_out, int on_device) {
+    if (!valid_ctx(c)) return fail(c, MQI_ERR_INVALID, "mqi_get_tally: ctx is NULL");
+    if (id < 0 || id >= (int) c->scorers.size()) return fail(c, MQI_ERR_INVALID, "mqi_get_tally: no such scorer");
+    const ScorerHost& s = c->scorers[id];
+    if (n_out) *n_out = s.tally_len;
+    if (!out) return MQI_OK;
+    DeviceGuard g(c->device);
+    MQI_CUDA(c, cudaMemcpyAsync(out, s.tally, s.tally_len * sizeof(double), on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                                c->stream), "mqi_get_tally");
+    MQI_CUDA(c, cudaStreamSynchronize(c->stream), "mqi_get_tally");
+    return MQI_OK;
+}
+
+int
+mqi_reset_tallies(mqi_ctx* c) {
+    if (!valid_ctx(c)) return fail(c, MQI_ERR_INVALID, "mqi_reset_tallies: ctx is NULL");
+    DeviceGuard g(c->device);
+    for (auto& s : c->scorers)
+        MQI_CUDA(c, cudaMemsetAsync(s.tally, 0, s.tally_len * sizeof(double), c->stream), "mqi_reset_tallies");
+    MQI_CUDA(c, cudaMemsetAsync(c->stats, 0, 8 * sizeof(unsigned long long), c->stream), "mqi_reset_tallies");
+    MQI_CUDA(c, cudaMemsetAsync(c->counters + 3, 0, sizeof(uint32_t), c->stream), "mqi_reset_tallies");
+    MQI_CUDA(c, cudaStreamSynchronize(c->stream), "mqi_reset_tallies");
+    c->waves = 0;
+    return MQI_OK;
+}
+
+int
+mqi_get_stats(mqi_ctx* c, mqi_stats* out) {
+    if (!valid_ctx(c) || !out) return fail(c, MQI_ERR_INVALID, "mqi_get_stats: bad argument");
+    DeviceGuard g(c->device);
+    unsigned long long v[8];
+    MQI_CUDA(c, cudaMemcpyAsync(v, c->stats, sizeof(v), cudaMemcpyDeviceToHost, c->stream), "mqi_get_stats");
+    MQI_CUDA(c, cudaStreamSynchronize(c->stream), "mqi_get_stats");
+    out->histories       = v[0];
+    out->tracks          = v[1];
+    out->steps           = v[2];
+    out->secondaries     = v[3];
+    out->local_daughters = v[4];
+    out->dropped         = v[5];
+    out->waves           = c->waves;
+    out->device_errors   = v[7];
+    return MQI_OK;
+}
+
+int
+mqi_trace_rays(mqi_ctx* c, int id, const float* rays, uint64_t n_rays, uint32_t max_steps, int64_t* offsets,
+               uint64_t* cnb, float* dist, int32_t* cells, uint64_t capacity, uint64_t* n_out) {
+    if (!valid_ctx(c) || (!rays && n_rays) || !offsets || max_steps == 0)
+        return fail(c, MQI_ERR_INVALID, "mqi_trace_rays: bad argument");
+    if (id < 0 || id >= (int) c->children.size()) return fail(c, MQI_ERR_INVALID, "mqi_trace_rays: no such child");
+    if (n_rays * (uint64_t) max_steps > (1ull << 31)) return fail(c, MQI_ERR_INVALID, "mqi_trace_rays: n_rays * max_steps too large");
+    DeviceGuard g(c->device);
+    const ChildHost& h = c->children[id];
+    ChildDev d{};
+    d.nx = h.nx; d.ny = h.ny; d.nz = h.nz; d.xe = h.xe; d.ye = h.ye; d.ze = h.ze; d.rho = h.rho;
+    std::memcpy(d.rf, h.rf, sizeof(d.rf));
+    std::memcpy(d.ri, h.ri, sizeof(d.ri));
+    std::memcpy(d.tr, h.tr, sizeof(d.tr));
+    d.identity = h.identity;
+    const uint64_t slots = n_rays * (uint64_t) max_steps;
+    float*    d_rays = nullptr;
+    uint64_t* d_cnb = nullptr;
+    float*    d_dist = nullptr;
+    int32_t*  d_cells = nullptr;
+    uint32_t* d_counts = nullptr;
+    cudaError_t e = cudaMalloc(&d_rays, n_rays * 6 * sizeof(float) + 16);
+    if (e == cudaSuccess) e = cudaMalloc(&d_cnb, slots * sizeof(uint64_t) + 16);
+    if (e == cudaSuccess) e = cudaMalloc(&d_dist, slots * sizeof(float) + 16);
+    if (e == cudaSuccess) e = cudaMalloc(&d_cells, slots * 3 * sizeof(int32_t) + 16);
+    if (e == cudaSuccess) e = cudaMalloc(&d_counts, n_rays * sizeof(uint32_t) + 16);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(d_rays, rays, n_rays * 6 * sizeof(float), cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = launch_trace_rays(d, d_rays, n_rays, max_steps, d_cnb, d_dist, d_cells, d_counts, c->stream);
+    std::vector<uint32_t> counts(n_rays);
+    std::vector<uint64_t> hc(slots);
+    std::vector<float>    hd(slots);
+    std::vector<int32_t>  hcell(slots * 3);
+    if (e == cudaSuccess && n_rays) e = cudaMemcpyAsync(counts.data(), d_counts, n_rays * sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess && slots) e = cudaMemcpyAsync(hc.data(), d_cnb, slots * sizeof(uint64_t), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess && slots) e = cudaMemcpyAsync(hd.data(), d_dist, slots * sizeof(float), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess && slots) e = cudaMemcpyAsync(hcell.data(), d_cells, slots * 3 * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaFree(d_rays); cudaFree(d_cnb); cudaFree(d_dist); cudaFree(d_cells); cudaFree(d_counts);
+    if (e != cudaSuccess) return cuda_fail(c, e, "mqi_trace_rays");
+    uint64_t total = 0;
+    offsets[0] = 0;
+    for (uint64_t r = 0; r < n_rays; ++r) {
+        for (uint32_t k = 0; k < counts[r]; ++k) {
+            if (total < capacity) {
+                const uint64_t src = r * max_steps + k;
+                if (cnb) cnb[total] = hc[src];
+                if (dist) dist[total] = hd[src];
+                if (cells) { cells[3 * total] = hcell[3 * src]; cells[3 * total + 1] = hcell[3 * src + 1]; cells[3 * total + 2] = hcell[3 * src + 2]; }
+            }
+            ++total;
+        }
+        offsets[r + 1] = (int64_t) total;
+    }
+    if (n_out) *n_out = total;
+    if (total > capacity) return fail(c, MQI_ERR_OVERFLOW, "mqi_trace_rays: output capacity too small");
+    return MQI_OK;
+}
+
+int
+mqi_eval_physics(mqi_ctx* c, const float* energies, uint64_t n, float* out) {
+    if (!valid_ctx(c) || (!energies && n) || (!out && n)) return fail(c, MQI_ERR_INVALID, "mqi_eval_physics: bad argument");
+    DeviceGuard g(c->device);
+    float* de = nullptr;
+    float* dout = nullptr;
+    cudaError_t e = cudaMalloc(&de, n * sizeof(float) + 16);
+    if (e == cudaSuccess) e = cudaMalloc(&dout, n * 8 * sizeof(float) + 16);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(de, energies, n * sizeof(float), cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = launch_eval_physics(c->tables, de, n, dout, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, dout, n * 8 * sizeof(float), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaFree(de);
+    cudaFree(dout);
+    if (e != cudaSuccess) return cuda_fail(c, e, "mqi_eval_physics");
+    return MQI_OK;
+}
+
+}   // extern "C"

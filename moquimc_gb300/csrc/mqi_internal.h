@@ -1,0 +1,96 @@
+// Internal interface between the C ABI (mqi_capi.cu) and the kernels (mqi_kernels.cu).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "mqi_gpu.h"
+
+namespace mqi_gpu
+{
+
+constexpr int kMaxChildren = 4;
+constexpr int kMaxScorers  = 8;
+
+/// Flat device description of one scorer (scorer<R> + roi_t, mqi_scorer.hpp:39-79,
+/// mqi_roi.hpp:18-194).
+struct ScorerDev {
+    int             type;          // mqi_scorer_type
+    int             roi_method;    // mqi_roi_method
+    int             stat_mode;     // 1: gate/key by roi get_mask_idx (the _stat kernel's last scorers)
+    int             double_score;  // 1: scored twice per step (non-stat kernel quirk, mqi_transport.hpp:204-225)
+    uint32_t        roi_len;
+    const uint32_t* start;
+    const uint32_t* stride;
+    const uint32_t* acc;
+    double*         tally;         // dense, length = tally_len
+    uint64_t        tally_len;
+};
+
+/// One child geometry: grid + the contiguous range of its scorers.
+struct ChildDev {
+    int          nx, ny, nz;
+    const float* xe;
+    const float* ye;
+    const float* ze;
+    const float* rho;
+    float        rf[9], ri[9], tr[3];
+    int          identity;
+    int          scorer_begin, n_scorers;
+};
+
+/// Structure-of-arrays particle queue (replaces track_stack_t, mqi_track_stack.hpp:11-67).
+struct Queue {
+    float*    ke;      // vtx0.ke
+    float*    px;      // position (world frame for phase ENTER, child frame for phase STEP)
+    float*    py;
+    float*    pz;
+    float*    dx;
+    float*    dy;
+    float*    dz;
+    float*    dE0;     // deposit carried from creation (debug-physics daughters)
+    uint32_t* hist;    // history index
+    uint32_t* uid_lo;  // track uid within the history (0 = primary)
+    uint32_t* uid_hi;
+    uint32_t* ctr;     // next Philox block of this track
+    uint32_t* meta;    // below:16 | primary:1 | ke1_zero:1 | phase:1 | child:3 | npush:10 (bit layout in kernels)
+    int32_t*  cell;    // packed cell for phase STEP: x | y << 11 | z << 22 (each < 2048)
+    uint32_t  capacity;
+};
+
+/// Kernel parameters for one transport wave.
+struct WaveParams {
+    int       n_children;
+    ChildDev  child[kMaxChildren];
+    ScorerDev scorer[kMaxScorers];
+    int       physics_debug;
+    int       score_local;
+    int       stack_limit;
+    float     t_cut;
+    uint32_t  k0, k1;           // Philox key (run seed)
+    uint32_t  max_slice_steps;  // 0 = run each track to completion
+    int       inline_local;     // score deposit-only daughters at creation (single-child worlds)
+    Queue     in;
+    Queue     out;
+    const uint32_t* n_in;       // device: number of entries in `in`
+    uint32_t*       n_out;      // device: append cursor of `out`
+    uint32_t*       head;       // device: fetch cursor of `in`
+    unsigned long long* stats;  // device: mqi_stats fields (8 x u64)
+    const uint32_t* spot_ids;   // per history (may be null)
+    uint32_t*       error_flag; // device: set when a bounded loop gives up or a queue overflows
+    const float*    tables;     // device: the six physics tables, 6 x 600 floats in Tables order
+                                // (followed by the 3996 HU density-correction factors)
+};
+
+// ---- launchers (mqi_kernels.cu) ----
+cudaError_t launch_load_primaries(const Queue& q, const mqi_vertex* v, uint64_t h0, uint32_t n,
+                                  cudaStream_t s);
+cudaError_t launch_wave(const WaveParams& p, int grid, int block, cudaStream_t s);
+int         wave_smem_bytes();
+cudaError_t launch_hu_to_density(const float* corr, const int16_t* hu, float* rho, uint64_t n, float scale,
+                                 cudaStream_t s);
+cudaError_t launch_trace_rays(const ChildDev& c, const float* rays, uint64_t n_rays, uint32_t max_steps,
+                              uint64_t* cnb, float* dist, int32_t* cells, uint32_t* counts, cudaStream_t s);
+cudaError_t launch_eval_physics(const float* tables, const float* e, uint64_t n, float* out, cudaStream_t s);
+
+}   // namespace mqi_gpu

@@ -1,0 +1,958 @@
+// Transport kernels of the GB300 proton engine.
+//
+// The reference runs one thread per history with a per-thread LIFO stack of secondaries
+// (moqui/kernel_functions/mqi_transport.hpp:113-250, moqui/base/mqi_track_stack.hpp:11-67).
+// Here every track lives in a structure-of-arrays queue.  A wave kernel drains the queue: each
+// lane fetches a track (warp-aggregated cursor), steps it voxel by voxel in registers, scores
+// each step with warp-aggregated FP64 atomics, and appends its daughters -- and itself, when its
+// step budget for the wave runs out -- to the next queue.  The host (or a captured graph) swaps
+// queues until none is left.  Because each track's random stream is keyed by (seed, history,
+// track uid) and the 200/10-deep stack limit is emulated from each track's recorded stack depth,
+// the result does not depend on the order the queue is drained in.
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "mqi_device.cuh"
+#include "mqi_internal.h"
+
+namespace mqi_gpu
+{
+
+// meta word layout
+constexpr uint32_t kMetaBelowMask = 0xFFFFu;
+constexpr uint32_t kMetaPrimary   = 1u << 16;
+constexpr uint32_t kMetaKe1Zero   = 1u << 17;
+constexpr uint32_t kMetaPhaseStep = 1u << 18;
+constexpr int      kMetaChildShift = 19;   // 3 bits
+constexpr int      kMetaNpushShift = 22;   // 10 bits
+
+enum StatIdx { ST_HIST = 0, ST_TRACKS, ST_STEPS, ST_SEC, ST_LOCAL, ST_DROP, ST_WAVES, ST_ERR };
+
+constexpr uint32_t kMaxTrackSteps = 1u << 20;
+
+/// A track in registers: track_t<float> (mqi_track.hpp:48-205) reduced to what transport reads.
+struct Trk {
+    float    ke0, ke1;
+    float3   p0, d0, p1, d1;
+    float    dE, ldE;
+    int3     cell;
+    uint64_t uid;
+    uint32_t hist;
+    uint32_t below, npush;
+    int      child;
+    bool     primary, stopped;
+};
+
+/// Per-lane context of a wave.
+struct Ctx {
+    const WaveParams* P;
+    const Tables*     T;
+    Grid              g;          // current child grid
+    int               child;
+    uint32_t          spot;
+    bool              dbg;
+    float             tcut;
+    uint32_t          n_sec, n_local, n_drop, n_err;
+};
+
+__device__ inline Grid
+make_grid(const ChildDev& c, const float* sxe, const float* sye, const float* sze) {
+    Grid g;
+    g.nx = c.nx; g.ny = c.ny; g.nz = c.nz;
+    g.xe = sxe ? sxe : c.xe;
+    g.ye = sye ? sye : c.ye;
+    g.ze = sze ? sze : c.ze;
+    g.rho = c.rho;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) { g.rf[i] = c.rf[i]; g.ri[i] = c.ri[i]; }
+    g.tr[0] = c.tr[0]; g.tr[1] = c.tr[1]; g.tr[2] = c.tr[2];
+    g.identity = c.identity;
+    return g;
+}
+
+// ------------------------------------------------------------------------------------------
+// Scoring (mqi_transport.hpp:204-225 and :342-364; scorer callbacks in
+// moqui/base/scorers/mqi_scorer_energy_deposit.hpp:12-177; insert_hashtable :68-111).
+// ------------------------------------------------------------------------------------------
+
+/// Add v to tally[key]; lanes of the warp that hit the same key are combined first so that
+/// one FP64 atomic is issued per distinct voxel.
+__device__ inline void
+tally_add(double* tally, uint32_t key, double v, bool valid) {
+    const unsigned mask  = __activemask();
+    const uint32_t k     = valid ? key : 0xFFFFFFFFu;
+    const unsigned peers = __match_any_sync(mask, k);
+    if (!valid) return;
+    if (__popc(peers) == 1) {
+        atomicAdd(&tally[key], v);
+        return;
+    }
+    double   s = 0.0;
+    unsigned m = peers;
+    while (m) {
+        const int src = __ffs(m) - 1;
+        s += __shfl_sync(peers, v, src);
+        m &= m - 1;
+    }
+    if ((int) (threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&tally[key], s);
+}
+
+/// roi_t::idx / get_mask_idx for the three mapping methods (mqi_roi.hpp:47-71, 87-160).
+__device__ inline int32_t
+roi_lower_bound(const ScorerDev& s, uint32_t v) {
+    int32_t first = 0, count = (int32_t) s.roi_len;
+    while (count > 0) {
+        const int32_t step = count / 2;
+        const int32_t it   = first + step;
+        if (s.start[it] <= v) { first = it + 1; count -= step + 1; }
+        else count = step;
+    }
+    return first;
+}
+
+__device__ inline int32_t
+roi_idx(const ScorerDev& s, uint32_t v) {
+    if (s.roi_method == MQI_ROI_INDIRECT) return (int32_t) s.start[v];
+    if (s.roi_method == MQI_ROI_CONTOUR) {
+        const int32_t c = roi_lower_bound(s, v) - 1;
+        if (c < 0) return -1;
+        return (v - s.start[c] < s.stride[c]) ? 1 : -1;
+    }
+    return (int32_t) v;
+}
+
+__device__ inline int32_t
+roi_mask_idx(const ScorerDev& s, uint32_t v) {
+    if (s.roi_method == MQI_ROI_INDIRECT) return (int32_t) s.start[v];
+    if (s.roi_method == MQI_ROI_CONTOUR) {
+        const int32_t c = roi_lower_bound(s, v) - 1;
+        if (c < 0) return -1;
+        uint32_t d = v - s.start[c];
+        if (d < s.stride[c]) {
+            if (c > 0) d += s.acc[c - 1];
+            return (int32_t) d;
+        }
+        return -1;
+    }
+    return (int32_t) v;
+}
+
+/// fp_compute_hit for the enum'd scorers.
+__device__ inline double
+compute_hit(int type, const Trk& t, float rho, float vol, float spr_ke0) {
+    const float edep = t.dE + t.ldE;
+    switch (type) {
+    case MQI_SCORER_EDEP: return (double) edep;
+    case MQI_SCORER_EDEP_PRIMARY: return t.primary ? (double) t.dE : 0.0;
+    case MQI_SCORER_EDEP_SECONDARY: return t.primary ? 0.0 : (double) t.dE;
+    case MQI_SCORER_DOSE_W:
+    case MQI_SCORER_DIJ: {
+        if (rho < 1.0e-7f) return 0.0;
+        return (double) edep * 1.60218e-10 / (double) (vol * rho * spr_ke0);
+    }
+    case MQI_SCORER_DOSE_W2: {
+        if (rho < 1.0e-7f) return 0.0;
+        const double d = (double) edep * 1.60218e-10 / (double) (vol * rho * spr_ke0);
+        return d * d;
+    }
+    case MQI_SCORER_DOSE_M:
+        return t.primary ? (double) t.dE * 1.60218e-13 * 1000.0 / (double) (vol * rho) : 0.0;
+    default: break;
+    }
+    // LET scorers (mqi_scorer_energy_deposit.hpp:91-177)
+    const float  density = rho * 1000.0f;
+    const double lx = (double) (t.p1.x - t.p0.x), ly = (double) (t.p1.y - t.p0.y), lz = (double) (t.p1.z - t.p0.z);
+    const double length = sqrt(lx * lx + ly * ly + lz * lz);
+    if (!(length > 0.0)) return 0.0;
+    const double let = (double) t.dE / length / (double) density;
+    switch (type) {
+    case MQI_SCORER_LETD_NUM: return (let >= 25.0) ? 0.0 : (double) t.dE * let;
+    case MQI_SCORER_LETD_DEN: return (let >= 25.0) ? 0.0 : (double) t.dE;
+    case MQI_SCORER_LETT_NUM: return length * let;
+    case MQI_SCORER_LETT_DEN: return length;
+    default: return 0.0;
+    }
+}
+
+/// Score one step of track t in voxel cnb with every scorer of the current child.
+__device__ inline void
+score_step(Ctx& C, const Trk& t, uint32_t cnb, float rho, float vol) {
+    const WaveParams& P   = *C.P;
+    const ChildDev&   ch  = P.child[C.child];
+    const float       spr = spr_default(rho, t.ke0, C.dbg);
+    for (int si = 0; si < ch.n_scorers; ++si) {
+        const ScorerDev& s = P.scorer[ch.scorer_begin + si];
+        bool     ok;
+        uint32_t key;
+        if (s.stat_mode) {
+            const int32_t m = roi_mask_idx(s, cnb);
+            ok              = m >= 0;
+            key             = (uint32_t) m;
+        } else {
+            ok  = roi_idx(s, cnb) > 0;
+            key = cnb;
+        }
+        double v = 0.0;
+        if (ok) v = compute_hit(s.type, t, rho, vol, spr);
+        const bool valid = ok && v > 0.0 && key < s.tally_len;
+        if (s.double_score) tally_add(s.tally, key, v + v, valid);
+        else tally_add(s.tally, key, v, valid);
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// Daughters
+// ------------------------------------------------------------------------------------------
+
+/// Child-frame -> world-frame transform the reference applies to a daughter's vertex before
+/// pushing it (e.g. mqi_pp_elastic.hpp:188-195): R_fwd * (p - T) + T and R_fwd * d.
+__device__ inline void
+daughter_to_world(const Grid& g, float3& p, float3& d) {
+    if (g.identity) return;
+    const float3 q = make_float3(p.x - g.tr[0], p.y - g.tr[1], p.z - g.tr[2]);
+    const float3 r = matvec(g.rf, q);
+    p              = make_float3(r.x + g.tr[0], r.y + g.tr[1], r.z + g.tr[2]);
+    d              = matvec(g.rf, d);
+}
+
+/// World -> child frame on entry (mqi_transport.hpp:165-168).
+__device__ inline void
+to_child(const Grid& g, float3& p, float3& d) {
+    if (!g.identity) {
+        p = matvec(g.ri, make_float3(fsub(p.x, g.tr[0]), fsub(p.y, g.tr[1]), fsub(p.z, g.tr[2])));
+        d = matvec(g.ri, d);
+    }
+    d = normalize3(d);
+}
+
+/// Child -> world frame on exit (mqi_transport.hpp:234-237).
+__device__ inline void
+to_world(const Grid& g, float3& p, float3& d) {
+    if (g.identity) return;
+    const float3 r = matvec(g.rf, p);
+    p              = make_float3(fadd(r.x, g.tr[0]), fadd(r.y, g.tr[1]), fadd(r.z, g.tr[2]));
+    d              = matvec(g.rf, d);
+}
+
+/// track_t::update_post_vertex_position with the last_step length
+/// (p_ionization_tabulated::last_step, mqi_p_ionization.hpp:481-490).
+__device__ inline float3
+last_step_pos(const Ctx& C, float3 p0, float3 d0, float ke0, float dE, float rho) {
+    float lw = 0.0f;
+    if (dE > 0.0f) lw = -dE / dedx_lookup(*C.T, ke0);
+    const float sl = lw * kWaterDensity / (spr_default(rho, ke0, C.dbg) * rho);
+    return make_float3(p0.x + d0.x * sl, p0.y + d0.y * sl, p0.z + d0.z * sl);
+}
+
+/// What the reference does when it pops a deposit-only daughter (kinetic energy at or below
+/// the 0.5 MeV tracking cut) in a single-child world: enter the grid, take the stepping()
+/// cut branch (mqi_fippel_physics.hpp:86-94) and score once.  Returns false when the daughter
+/// needs the general path (outside the grid or in a vacuum voxel).
+__device__ inline bool
+score_local_daughter(Ctx& C, float3 pw, float3 dw, float ke0, float dE0) {
+    float3 p = pw, d = dw;
+    to_child(C.g, p, d);
+    Trk t;
+    t.cell = grid_index(C.g, p, d);
+    if (!grid_valid(C.g, t.cell)) return false;
+    const uint32_t cnb = grid_cnb(C.g, t.cell);
+    const float    rho = C.g.rho[cnb];
+    if (rho < 1.0e-7f) return false;
+    const float d2b = grid_exit(C.g, p, d, t.cell);
+    if (d2b < 0.0f) return true;   // the voxel loop breaks before scoring
+    t.p0 = p; t.d0 = d; t.p1 = p; t.d1 = d;
+    t.ke0 = ke0 < 0.0f ? 0.0f : ke0;
+    t.dE = dE0; t.ldE = 0.0f;
+    t.primary = false;
+    if (rho <= 99.9f) {
+        t.dE += t.ke0;
+        t.p1 = last_step_pos(C, p, d, t.ke0, t.dE, rho);
+    }
+    score_step(C, t, cnb, rho, grid_volume(C.g, t.cell));
+    return true;
+}
+
+/// track_stack_t::push_secondary (mqi_track_stack.hpp:36-41) with the stack depth emulated:
+/// a track popped with `below` entries under it pushes its i-th daughter at depth below + i,
+/// and the push is dropped when that reaches the limit (200 with debug physics, else 10).
+__device__ inline void
+push_daughter(Ctx& C, Trk& t, float ke0, bool ke1_zero, float3 p, float3 d, float dE0) {
+    if (t.below + t.npush >= (uint32_t) C.P->stack_limit) {
+        ++C.n_drop;
+        return;
+    }
+    const uint32_t below = t.below + t.npush;
+    const uint64_t uid   = daughter_uid(t.uid, t.npush);
+    ++t.npush;
+    daughter_to_world(C.g, p, d);
+    if (C.P->inline_local && ke0 <= kTpCut && score_local_daughter(C, p, d, ke0, dE0)) {
+        ++C.n_local;
+        return;
+    }
+    const Queue& q   = C.P->out;
+    const uint32_t i = atomicAdd(C.P->n_out, 1u);
+    if (i >= q.capacity) {
+        atomicOr(C.P->error_flag, 2u);
+        ++C.n_err;
+        return;
+    }
+    q.ke[i] = ke0;
+    q.px[i] = p.x; q.py[i] = p.y; q.pz[i] = p.z;
+    q.dx[i] = d.x; q.dy[i] = d.y; q.dz[i] = d.z;
+    q.dE0[i] = dE0;
+    q.hist[i] = t.hist;
+    q.uid_lo[i] = (uint32_t) uid;
+    q.uid_hi[i] = (uint32_t) (uid >> 32);
+    q.ctr[i] = 0;
+    q.meta[i] = (below & kMetaBelowMask) | (ke1_zero ? kMetaKe1Zero : 0u);
+    q.cell[i] = 0;
+    ++C.n_sec;
+}
+
+// ------------------------------------------------------------------------------------------
+// Physics: p_ionization_tabulated (mqi_p_ionization.hpp:297-490), pp/po elastic, po inelastic
+// ------------------------------------------------------------------------------------------
+
+/// energy_loss (mqi_p_ionization.hpp:297-331) with the straggling variance (:334-345).  The
+/// range-table walk is guarded at index 0 (the reference's uint16 index wraps there).
+__device__ inline float
+energy_loss(const Tables& T, const Rel& rel, float rho, float len, float spr, float z) {
+    const float lw = len * spr * rho / kWaterDensity;
+    int n = (int) ((rel.Ek - 0.1f) / 0.5f);
+    if (n > MQI_TABLE_N - 2) n = MQI_TABLE_N - 2;
+    if (n < 0) n = 0;
+    float x0 = 0.1f + (float) n * 0.5f;
+    float x1 = x0 + 0.5f;
+    if (x0 > rel.Ek && n > 0) n -= 1;
+    if (x1 < rel.Ek && n < MQI_TABLE_N - 2) n += 1;
+    float r = intpl1d(rel.Ek, x0, x1, T.range[n], T.range[n + 1]);
+    if (r < lw) return rel.Ek;
+    r -= lw;
+    while (n > 0 && r < T.range[n]) --n;
+    x0 = 0.1f + (float) n * 0.5f;
+    x1 = x0 + 0.5f;
+    const float dE_mean = rel.Ek - intpl1d(r, T.range[n], T.range[n + 1], x0, x1);
+    const float Te      = (rel.Te_max >= kTeStragCap) ? kTeStragCap : rel.Te_max;
+    float       var     = dedx_term0() * rho / kWaterDensity * lw;
+    var *= Te / rel.beta_sq * (1.0f - 0.5f * rel.beta_sq);
+    float ret = z * sqrtf(var) + dE_mean;
+    if (ret < 0.0f) ret = -ret;
+    return ret;
+}
+
+/// p_ionization_tabulated::along_step (mqi_p_ionization.hpp:349-420): CSDA loss with Gaussian
+/// straggling, Highland-style multiple scattering, position/energy update.  The step's first
+/// block of random words is laid out as: [0] free path, [1,2] Box-Muller pair (straggling,
+/// scattering angle), [3] azimuth.
+__device__ inline void
+along_step(Ctx& C, Trk& t, float len, float rho, float spr, float z_strag, float z_mcs, float u_phi) {
+    const Rel   rel(t.ke0);
+    const float dE = energy_loss(*C.T, rel, rho, len, spr, z_strag);
+    float       r  = 1.0f;
+    if (dE >= t.ke0) {
+        r         = t.ke0 / dE;
+        t.stopped = true;
+    }
+    const float P     = rel.momentum();
+    const float X0    = radiation_length_default(rho, C.dbg);
+    const float th_sq = ((kEs / P) * (kEs / P) / rel.beta_sq) * len / X0;
+    float       th    = sqrtf(th_sq);
+    th                = z_mcs * (sqrtf(2.0f) * th);
+    if (th < 0.0f) th = -th;
+    const float phi = 2.0f * kPi * u_phi;
+    t.d1            = rotate_dir(t.d1, th, phi);
+    t.dE += dE * r;
+    t.p1 = advance(t.p0, t.d0, r * len);
+    t.ke1 -= dE * r;
+}
+
+/// Delta-ray production (p_ionization_tabulated::post_step, mqi_p_ionization.hpp:425-477).
+__device__ inline void
+post_delta(Ctx& C, Trk& t, Rng& rng) {
+    const Rel rel(t.ke1);
+    float     Te = 0.0f;
+    for (int it = 0;; ++it) {
+        const float n = rng.uniform();
+        Te            = C.tcut * rel.Te_max;
+        Te /= ((1.0f - n) * rel.Te_max + n * C.tcut);
+        if (rng.uniform() < 1.0f - rel.beta_sq * Te / rel.Te_max + Te * Te / (2.0f * rel.Et_sq)) break;
+        if (it >= 63) {   // acceptance >= 1 - beta^2 > 0: unreachable in practice, bounded anyway
+            ++C.n_err;
+            break;
+        }
+    }
+    if (C.dbg) push_daughter(C, t, 0.0f, true, t.p0, t.d0, Te);
+    else t.dE += Te;
+    t.ke1 -= Te;
+}
+
+/// p-p elastic (pp_elastic_tabulated::post_step, mqi_pp_elastic.hpp:119-219).
+__device__ inline void
+post_pp(Ctx& C, Trk& t, Rng& rng) {
+    const Rel   rel(t.ke1);
+    const float Mp_sq = kMp * kMp;
+    const float minv  = kTpCut / rel.Ek;
+    const float u     = rng.uniform() * (1.0f - 2.0f * minv) + minv;
+    const float E1    = rel.Et;
+    const float dE    = rel.Ek * u;
+    const float E3    = (rel.Ek - dE) + kMp;
+    const float E4    = dE + kMp;
+    const float P1    = rel.momentum();
+    const float P3    = sqrtf(E3 * E3 - Mp_sq);
+    const float P4    = sqrtf(E4 * E4 - Mp_sq);
+    float c3  = E1 * E3 - Mp_sq - kMp * (E1 - E3);
+    c3 /= (P1 * P3);
+    float c34 = E3 * E4 - E1 * kMp;
+    c34 /= (P3 * P4);
+    c3  = fminf(fmaxf(c3, -1.0f), 1.0f);
+    c34 = fminf(fmaxf(c34, -1.0f), 1.0f);
+    const float th3 = acosf(c3);
+    const float th4 = th3 - acosf(c34);
+    const float phi = 2.0f * kPi * rng.uniform();
+    t.ke1 -= dE;
+    t.d1 = rotate_dir(t.d1, th3, phi);
+    const float3 dd = rotate_dir(t.d1, th4, phi);
+    push_daughter(C, t, dE, false, t.p1, dd, 0.0f);
+}
+
+/// p-O elastic (po_elastic::post_step, mqi_po_elastic.hpp:96-217).  The energy given to the
+/// oxygen is a truncated exponential of mean Tp_avg on [0, Tp_max]; it is drawn by inverting
+/// its CDF, which has the same law as the reference's redraw-until-below-Tp_max loop
+/// (mqi_math.hpp:298-307) without the loop.
+__device__ inline void
+post_poe(Ctx& C, Trk& t, Rng& rng) {
+    const Rel rel(t.ke1);
+    if (rel.Ek <= 5.5f) {
+        const float dE = rel.Ek;
+        if (C.dbg) push_daughter(C, t, dE, true, t.p1, t.d1, dE);
+        else t.ldE += dE;
+        t.ke1 -= dE;
+        t.stopped = true;
+        return;
+    }
+    const float MoMp    = kMo / kMp;
+    const float MoMp_sq = MoMp * MoMp;
+    const float Tp_avg  = 0.65f * expf(-0.0013f * rel.Ek) - 0.71f * expf(-0.0177f * rel.Ek);
+    const float Tp_max  = (2.0f * kMo * rel.beta_sq * rel.gamma_sq) / (1.0f + 2.0f * rel.gamma * MoMp + MoMp_sq);
+    const float u       = rng.uniform();
+    float       dE      = -Tp_avg * log1pf(u * expm1f(-Tp_max / Tp_avg));
+    if (!(dE >= 0.0f)) dE = 0.0f;
+    if (dE > Tp_max) dE = Tp_max;
+    const float E1 = rel.Ek * (rel.Ek + 2.0f * kMp);
+    const float E3 = (rel.Ek - dE) * (rel.Ek - dE + 2.0f * kMp);
+    float c3 = (E1 + E3 - dE * (dE + 2.0f * kMo)) / 2.0f / sqrtf(E1 * E3);
+    c3              = fminf(fmaxf(c3, -1.0f), 1.0f);
+    const float th3 = acosf(c3);
+    const float phi = 2.0f * kPi * rng.uniform();
+    if (C.dbg) push_daughter(C, t, dE, true, t.p0, t.d0, dE);
+    else t.ldE += dE;
+    t.ke1 -= dE;
+    t.d1 = rotate_dir(t.d1, th3, phi);
+}
+
+/// p-O inelastic cascade (po_inelastic_tabulated::post_step, mqi_po_inelastic.hpp:158-288).
+__device__ inline void
+post_poi(Ctx& C, Trk& t, Rng& rng) {
+    const float Ek = t.ke1;
+    float       Eb = 5.0f, Er = Ek;
+    float       P2, PL, pw;
+    if (Ek <= 215.0f && Ek > 200.0f) { P2 = 0.78f; PL = P2 + (1.0f - P2) * 0.9f; pw = 0.4f; }
+    else if (Ek > 215.0f)            { P2 = 0.78f; PL = P2 + (1.0f - P2) * 1.0f; pw = 0.4f; }
+    else if (Ek > 150.0f)            { P2 = 0.72f; PL = P2 + (1.0f - P2) * 0.83f; pw = 0.45f; }
+    else                             { P2 = 0.7f;  PL = P2 + (1.0f - P2) * 0.83f; pw = 0.52f; }
+    for (int round = 0; (Er - Eb) > 2.0f; ++round) {
+        if (round >= 64) { ++C.n_err; break; }   // Eb shrinks by 0.65 and Er by >= 2 MeV per round
+        Er -= Eb;
+        float dE = powf(rng.uniform(), pw) * (Er - 2.0f) + 2.0f;
+        if (dE >= Er) dE = Er;
+        Er -= dE;
+        t.ke1 -= (dE + Eb);
+        const float zeta = rng.uniform();
+        if (zeta < P2) {
+            float c = (2.0f * dE / Ek - 1.0f) + 2.0f * (1.0f - dE / Ek) * rng.uniform();
+            c               = fminf(fmaxf(c, -1.0f), 1.0f);
+            const float th  = acosf(c);
+            const float phi = 2.0f * kPi * rng.uniform();
+            const float3 dd = rotate_dir(t.d1, th, phi);
+            push_daughter(C, t, dE, false, t.p1, dd, 0.0f);
+        } else if (zeta < PL) {
+            // long-range energy (neutrons, photons) leaves the system
+        } else if (C.dbg) {
+            push_daughter(C, t, dE, true, t.p0, t.d0, dE);
+        }
+        Eb *= 0.65f;
+    }
+    t.dE += Er;
+    t.ke1 -= Er;
+    t.stopped = true;
+}
+
+/// fippel_physics::stepping (mqi_fippel_physics.hpp:67-216).
+__device__ inline void
+stepping(Ctx& C, Trk& t, Rng& rng, float rho, float d2b) {
+    if (rho < 1.0e-7f) {
+        t.p1 = advance(t.p0, t.d0, d2b);
+        return;
+    }
+    if (rho > 99.9f) {
+        t.stopped = true;
+        return;
+    }
+    if (t.ke0 <= kTpCut) {
+        if (t.ke0 < 0.0f) t.ke0 = 0.0f;
+        t.dE += t.ke0;
+        t.ke1 -= t.ke0;
+        t.p1      = last_step_pos(C, t.p0, t.d0, t.ke0, t.dE, rho);
+        t.stopped = true;
+        return;
+    }
+    const Tables& T = *C.T;
+    rng.begin_step();
+    const Rel   rel(t.ke0);
+    const float spr      = spr_default(rho, t.ke0, C.dbg);
+    const float dedx     = dedx_lookup(T, rel.Ek);
+    const float cur_min  = kMaxStep * spr * rho / kWaterDensity;
+    const float max_loss = -1.0f * cur_min * dedx;
+    float cs1[4] = { cs_lookup(T.cs_ion, rel.Ek, 0.1f, 299.6f, rho), cs_lookup(T.cs_pp, rel.Ek, 0.5f, 300.0f, rho),
+                     cs_lookup(T.cs_poe, rel.Ek, 0.5f, 300.0f, rho), cs_lookup(T.cs_poi, rel.Ek, 0.5f, 300.0f, rho) };
+    const float e2 = t.ke0 - max_loss;
+    float cs2[4] = { cs_lookup(T.cs_ion, e2, 0.1f, 299.6f, rho), cs_lookup(T.cs_pp, e2, 0.5f, 300.0f, rho),
+                     cs_lookup(T.cs_poe, e2, 0.5f, 300.0f, rho), cs_lookup(T.cs_poi, e2, 0.5f, 300.0f, rho) };
+    const float sum1 = cs1[0] + cs1[1] + cs1[2] + cs1[3];
+    const float sum2 = cs2[0] + cs2[1] + cs2[2] + cs2[3];
+    const bool  pick1 = sum1 >= sum2;
+    const float cs_sum = pick1 ? sum1 : sum2;
+    const float c0 = pick1 ? cs1[0] : cs2[0];
+    const float c1 = pick1 ? cs1[1] : cs2[1];
+    const float c2 = pick1 ? cs1[2] : cs2[2];
+    const float c3 = pick1 ? cs1[3] : cs2[3];
+    const float u_mfp      = rng.uniform();
+    const float mfp        = -1.0f * logf(u_mfp) / cs_sum;
+    const float step_limit = cur_min * kWaterDensity / (spr * rho);
+    // Box-Muller pair and azimuth for along_step (words 1..3 of the step's first block)
+    const float bm_u1 = rng.uniform();
+    const float bm_u2 = rng.uniform();
+    const float u_phi = rng.uniform();
+    float       s_bm, c_bm;
+    sincospif(2.0f * bm_u2, &s_bm, &c_bm);
+    const float bm_r  = sqrtf(-2.0f * logf(bm_u1));
+    const float z1    = bm_r * c_bm;
+    const float z2    = bm_r * s_bm;
+    if (d2b < mfp && d2b < step_limit) {
+        along_step(C, t, d2b, rho, spr, z1, z2, u_phi);
+    } else if ((mfp < d2b || fabsf(mfp - d2b) < kGeoTol) &&
+               (mfp < step_limit || fabsf(mfp - step_limit) < kGeoTol)) {
+        along_step(C, t, mfp, rho, spr, z1, z2, u_phi);
+        if (t.ke1 <= kTpCut) return;
+        const float u = cs_sum * rng.uniform();
+        t.d1          = t.d0;
+        if (u < c0) post_delta(C, t, rng);
+        else if (u < c0 + c1) post_pp(C, t, rng);
+        else if (u < c0 + c1 + c2) post_poe(C, t, rng);
+        else if (u < c0 + c1 + c2 + c3) post_poi(C, t, rng);
+    } else {
+        along_step(C, t, step_limit, rho, spr, z1, z2, u_phi);
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// The wave kernel
+// ------------------------------------------------------------------------------------------
+
+__device__ inline void
+load_track(const Queue& q, uint32_t i, Trk& t, Rng& rng, bool& step_phase) {
+    t.ke0  = q.ke[i];
+    const uint32_t meta = q.meta[i];
+    t.ke1  = (meta & kMetaKe1Zero) ? 0.0f : t.ke0;
+    t.p0   = make_float3(q.px[i], q.py[i], q.pz[i]);
+    t.d0   = make_float3(q.dx[i], q.dy[i], q.dz[i]);
+    t.p1   = t.p0;
+    t.d1   = t.d0;
+    t.dE   = q.dE0[i];
+    t.ldE  = 0.0f;
+    t.hist = q.hist[i];
+    t.uid  = (uint64_t) q.uid_lo[i] | ((uint64_t) q.uid_hi[i] << 32);
+    t.below   = meta & kMetaBelowMask;
+    t.primary = (meta & kMetaPrimary) != 0;
+    t.child   = (int) ((meta >> kMetaChildShift) & 7u);
+    t.npush   = (meta >> kMetaNpushShift) & 1023u;
+    t.stopped = false;
+    step_phase = (meta & kMetaPhaseStep) != 0;
+    const int32_t c = q.cell[i];
+    t.cell = make_int3(c & 2047, (c >> 11) & 2047, (c >> 22) & 2047);
+    rng.hist   = t.hist;
+    rng.uid_lo = (uint32_t) t.uid;
+    rng.uid_hi = (uint32_t) (t.uid >> 32);
+    rng.ctr    = q.ctr[i];
+    rng.pos    = 4;
+}
+
+/// Write a track that used up its step budget back to the next queue, mid-grid.
+__device__ inline void
+requeue_track(Ctx& C, const Trk& t, const Rng& rng) {
+    const Queue& q   = C.P->out;
+    const uint32_t i = atomicAdd(C.P->n_out, 1u);
+    if (i >= q.capacity) {
+        atomicOr(C.P->error_flag, 2u);
+        ++C.n_err;
+        return;
+    }
+    q.ke[i] = t.ke0;
+    q.px[i] = t.p0.x; q.py[i] = t.p0.y; q.pz[i] = t.p0.z;
+    q.dx[i] = t.d0.x; q.dy[i] = t.d0.y; q.dz[i] = t.d0.z;
+    q.dE0[i] = 0.0f;
+    q.hist[i] = t.hist;
+    q.uid_lo[i] = (uint32_t) t.uid;
+    q.uid_hi[i] = (uint32_t) (t.uid >> 32);
+    q.ctr[i] = rng.ctr;
+    q.meta[i] = (t.below & kMetaBelowMask) | (t.primary ? kMetaPrimary : 0u) |
+                (t.ke1 != t.ke0 ? kMetaKe1Zero : 0u) | kMetaPhaseStep |
+                ((uint32_t) t.child << kMetaChildShift) | ((t.npush & 1023u) << kMetaNpushShift);
+    q.cell[i] = t.cell.x | (t.cell.y << 11) | (t.cell.z << 22);
+}
+
+__global__ void __launch_bounds__(256)
+k_wave(const WaveParams P) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    Tables* T = reinterpret_cast<Tables*>(smem);
+    {
+        const float4* src = reinterpret_cast<const float4*>(P.tables);
+        float4*       dst = reinterpret_cast<float4*>(smem);
+        for (int i = threadIdx.x; i < 6 * MQI_TABLE_N / 4; i += blockDim.x) dst[i] = src[i];
+    }
+    // Edges of the children staged after the tables when they fit.
+    float* sedges     = reinterpret_cast<float*>(smem + sizeof(Tables));
+    const float* sxe[kMaxChildren] = { nullptr, nullptr, nullptr, nullptr };
+    const float* sye[kMaxChildren] = { nullptr, nullptr, nullptr, nullptr };
+    const float* sze[kMaxChildren] = { nullptr, nullptr, nullptr, nullptr };
+    {
+        int off = 0;
+        for (int c = 0; c < P.n_children; ++c) {
+            const ChildDev& ch = P.child[c];
+            const int need     = ch.nx + ch.ny + ch.nz + 3;
+            if (off + need > 3 * 2048 + 12) break;
+            float* e = sedges + off;
+            for (int i = threadIdx.x; i <= ch.nx; i += blockDim.x) e[i] = ch.xe[i];
+            for (int i = threadIdx.x; i <= ch.ny; i += blockDim.x) e[ch.nx + 1 + i] = ch.ye[i];
+            for (int i = threadIdx.x; i <= ch.nz; i += blockDim.x) e[ch.nx + ch.ny + 2 + i] = ch.ze[i];
+            sxe[c] = e;
+            sye[c] = e + ch.nx + 1;
+            sze[c] = e + ch.nx + ch.ny + 2;
+            off += need;
+        }
+    }
+    __syncthreads();
+
+    Ctx C;
+    C.P      = &P;
+    C.T      = T;
+    C.dbg    = P.physics_debug != 0;
+    C.tcut   = P.t_cut;
+    C.n_sec = C.n_local = C.n_drop = C.n_err = 0;
+    uint32_t n_tracks = 0, n_steps = 0, n_hist = 0;
+
+    Rng rng;
+    rng.k0 = P.k0;
+    rng.k1 = P.k1;
+    Trk  t;
+    bool have  = false;
+    bool in_grid = false;
+    uint32_t slice = 0;
+    uint32_t track_steps = 0;   // per-track guard: a track is abandoned after kMaxTrackSteps
+    const uint32_t n_in = *P.n_in;
+    const int lane = threadIdx.x & 31;
+
+    for (;;) {
+        // ---- fetch (one atomic per warp) ----
+        const unsigned act   = __activemask();
+        const unsigned needm = __ballot_sync(act, !have);
+        if (needm) {
+            uint32_t base = 0;
+            const int leader = __ffs(needm) - 1;
+            if (lane == leader) base = atomicAdd(P.head, (uint32_t) __popc(needm));
+            base = __shfl_sync(act, base, leader);
+            if (!have) {
+                const uint32_t idx = base + (uint32_t) __popc(needm & ((1u << lane) - 1u));
+                if (idx >= n_in) break;
+                bool step_phase;
+                load_track(P.in, idx, t, rng, step_phase);
+                have    = true;
+                in_grid = step_phase;
+                slice   = 0;
+                track_steps = 0;
+                ++n_tracks;
+                if (step_phase) {
+                    C.child = t.child;
+                    C.g     = make_grid(P.child[t.child], sxe[t.child], sye[t.child], sze[t.child]);
+                }
+            }
+        }
+        if (!in_grid) {
+            // ---- child entry (mqi_transport.hpp:161-190) ----
+            if (t.stopped || t.child >= P.n_children) {
+                if (t.primary) ++n_hist;
+                have = false;
+                continue;
+            }
+            C.child = t.child;
+            C.g     = make_grid(P.child[t.child], sxe[t.child], sye[t.child], sze[t.child]);
+            C.spot  = P.spot_ids ? P.spot_ids[t.hist] : 0xFFFFFFFFu;
+            to_child(C.g, t.p0, t.d0);
+            t.p1 = t.p0;
+            t.d1 = t.d0;
+            int3 c = grid_index(C.g, t.p0, t.d0);
+            if (!grid_valid(C.g, c)) {
+                const float dist = grid_entry(C.g, t.p0, t.d0);
+                if (dist < 0.0f) {
+                    to_world(C.g, t.p0, t.d0);
+                    t.p1 = t.p0;
+                    t.d1 = t.d0;
+                    ++t.child;
+                    continue;
+                }
+                t.p1 = advance(t.p0, t.d0, dist);
+                // move(): vtx0 = vtx1 (including ke), deposits reset
+                t.p0  = t.p1;
+                t.d0  = t.d1;
+                t.ke0 = t.ke1;
+                t.dE = t.ldE = 0.0f;
+                c = grid_index(C.g, t.p0, t.d0);
+            }
+            t.cell = c;
+            if (!grid_valid(C.g, c)) {
+                to_world(C.g, t.p0, t.d0);
+                t.p1 = t.p0;
+                t.d1 = t.d0;
+                ++t.child;
+                continue;
+            }
+            in_grid = true;
+            continue;
+        }
+        // ---- one voxel step (mqi_transport.hpp:192-233) ----
+        C.spot = P.spot_ids ? P.spot_ids[t.hist] : 0xFFFFFFFFu;
+        const uint32_t cnb = grid_cnb(C.g, t.cell);
+        const float    rho = C.g.rho[cnb];
+        const float    d2b = grid_exit(C.g, t.p0, t.d0, t.cell);
+        stepping(C, t, rng, rho, d2b);
+        ++n_steps;
+        if (++track_steps > kMaxTrackSteps) {   // no physical track comes near this; never hang
+            t.stopped = true;
+            ++C.n_err;
+        }
+        bool leave = false;
+        if (d2b < 0.0f) {
+            leave = true;
+        } else {
+            score_step(C, t, cnb, rho, grid_volume(C.g, t.cell));
+            if (!t.stopped) {
+                grid_step_index(C.g, t.p1, t.d1, t.cell);
+                t.p0  = t.p1;
+                t.d0  = t.d1;
+                t.ke0 = t.ke1;
+                t.dE = t.ldE = 0.0f;
+            }
+            leave = t.stopped || !grid_valid(C.g, t.cell);
+        }
+        if (leave) {
+            to_world(C.g, t.p0, t.d0);
+            t.p1 = t.p0;
+            t.d1 = t.d0;
+            ++t.child;
+            in_grid = false;
+            continue;
+        }
+        if (P.max_slice_steps && ++slice >= P.max_slice_steps) {
+            requeue_track(C, t, rng);
+            have    = false;
+            in_grid = false;
+        }
+    }
+
+    // ---- counters: shared-memory reduction, one global atomic per block and field ----
+    __syncthreads();
+    __shared__ unsigned long long sstat[8];
+    if (threadIdx.x < 8) sstat[threadIdx.x] = 0ull;
+    __syncthreads();
+    const unsigned long long v[8] = { n_hist, n_tracks, n_steps, C.n_sec, C.n_local, C.n_drop, 0ull, C.n_err };
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+        if (v[k]) atomicAdd(&sstat[k], v[k]);
+    __syncthreads();
+    if (threadIdx.x < 8 && sstat[threadIdx.x]) atomicAdd(&P.stats[threadIdx.x], sstat[threadIdx.x]);
+    if (C.n_err) atomicOr(P.error_flag, 1u);
+}
+
+}   // namespace mqi_gpu
+namespace mqi_gpu
+{
+
+// ------------------------------------------------------------------------------------------
+// Primaries: vertex_t<float> AoS (mqi_vertex.hpp:16-29) -> queue entries
+// (track_t::set + push_primary, mqi_track.hpp:124-133, mqi_track_stack.hpp:44-48).
+// ------------------------------------------------------------------------------------------
+__global__ void
+k_load_primaries(Queue q, const mqi_vertex* __restrict__ v, uint64_t h0, uint32_t n) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const mqi_vertex x = v[h0 + i];
+    q.ke[i]     = x.ke;
+    q.px[i]     = x.pos[0];
+    q.py[i]     = x.pos[1];
+    q.pz[i]     = x.pos[2];
+    q.dx[i]     = x.dir[0];
+    q.dy[i]     = x.dir[1];
+    q.dz[i]     = x.dir[2];
+    q.dE0[i]    = 0.0f;
+    q.hist[i]   = (uint32_t) (h0 + i);
+    q.uid_lo[i] = 0u;
+    q.uid_hi[i] = 0u;
+    q.ctr[i]    = 0u;
+    q.meta[i]   = kMetaPrimary;
+    q.cell[i]   = 0;
+}
+
+cudaError_t
+launch_load_primaries(const Queue& q, const mqi_vertex* v, uint64_t h0, uint32_t n, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_load_primaries<<<(n + 255) / 256, 256, 0, s>>>(q, v, h0, n);
+    return cudaGetLastError();
+}
+
+int
+wave_smem_bytes() {
+    return (int) sizeof(Tables) + (3 * 2048 + 12) * (int) sizeof(float);
+}
+
+cudaError_t
+launch_wave(const WaveParams& p, int grid, int block, cudaStream_t s) {
+    const int   smem = wave_smem_bytes();
+    cudaError_t e    = cudaFuncSetAttribute(k_wave, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    k_wave<<<grid, block, smem, s>>>(p);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------------------------------
+// HU -> density (patient_material_t::hu_to_density, mqi_patient_materials.hpp:514-542), then
+// the DensityScaling factor (mqi_tps_env.hpp:766-769).  The piecewise line is evaluated in
+// double with explicit round-to-nearest operations, as the reference's host code does, so the
+// result is bit-identical.
+// ------------------------------------------------------------------------------------------
+__global__ void
+k_hu_to_density(const float* __restrict__ corr, const int16_t* __restrict__ hu, float* __restrict__ rho,
+                uint64_t n, float scale) {
+    for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n; i += (uint64_t) gridDim.x * blockDim.x) {
+        int h = hu[i];
+        if (h < -1000) h = -1000;
+        else if (h > 2995) h = 2995;
+        double r;
+        const double hd = (double) h;
+        if (h < -98) r = __dadd_rn(0.00121, __dmul_rn(0.001029700665188, __dadd_rn(1000.0, hd)));
+        else if (h < 15) r = __dadd_rn(1.018, __dmul_rn(0.000893, hd));
+        else if (h < 23) r = 1.03;
+        else if (h < 101) r = __dadd_rn(1.003, __dmul_rn(0.001169, hd));
+        else if (h < 2001) r = __dadd_rn(1.017, __dmul_rn(0.000592, hd));
+        else if (h < 2995) r = __dadd_rn(2.201, __dmul_rn(0.0005, __dadd_rn(-2000.0, hd)));
+        else r = 4.54;
+        float f = (float) r;
+        f       = __fmul_rn(f, corr[h + 1000]);
+        f       = (float) __ddiv_rn((double) f, 1000.0);
+        rho[i]  = __fmul_rn(f, scale);
+    }
+}
+
+cudaError_t
+launch_hu_to_density(const float* corr, const int16_t* hu, float* rho, uint64_t n, float scale, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    const uint64_t blocks = (n + 255) / 256;
+    k_hu_to_density<<<(unsigned) (blocks < 152 * 64 ? blocks : 152 * 64), 256, 0, s>>>(corr, hu, rho, n, scale);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------------------------------
+// Ray walk: the transport's child entry and voxel loop (mqi_transport.hpp:161-233) with the
+// physics step replaced by "advance to the voxel exit".  One thread per ray; ray r writes its
+// entries at [r * max_steps, ...) and its count to counts[r].
+// ------------------------------------------------------------------------------------------
+__global__ void
+k_trace_rays(ChildDev c, const float* __restrict__ rays, uint64_t n_rays, uint32_t max_steps,
+             uint64_t* __restrict__ cnb, float* __restrict__ dist, int32_t* __restrict__ cells,
+             uint32_t* __restrict__ counts) {
+    const uint64_t r = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x;
+    if (r >= n_rays) return;
+    const Grid g = make_grid(c, nullptr, nullptr, nullptr);
+    float3 p0 = make_float3(rays[6 * r + 0], rays[6 * r + 1], rays[6 * r + 2]);
+    float3 d0 = make_float3(rays[6 * r + 3], rays[6 * r + 4], rays[6 * r + 5]);
+    to_child(g, p0, d0);
+    float3 d1 = d0;
+    int3   cell = grid_index(g, p0, d0);
+    uint32_t k = 0;
+    bool entered = true;
+    if (!grid_valid(g, cell)) {
+        const float e = grid_entry(g, p0, d0);
+        if (e < 0.0f) {
+            entered = false;
+        } else {
+            p0   = advance(p0, d0, e);
+            d0   = d1;
+            cell = grid_index(g, p0, d0);
+        }
+    }
+    const uint64_t base = r * (uint64_t) max_steps;
+    while (entered && grid_valid(g, cell) && k < max_steps) {
+        const uint32_t id  = grid_cnb(g, cell);
+        const float    d2b = grid_exit(g, p0, d0, cell);
+        cnb[base + k]           = id;
+        dist[base + k]          = d2b;
+        cells[3 * (base + k)]     = cell.x;
+        cells[3 * (base + k) + 1] = cell.y;
+        cells[3 * (base + k) + 2] = cell.z;
+        ++k;
+        if (d2b < 0.0f) break;
+        const float3 p1 = advance(p0, d0, d2b);
+        grid_step_index(g, p1, d1, cell);
+        p0 = p1;
+        d0 = d1;
+    }
+    counts[r] = k;
+}
+
+cudaError_t
+launch_trace_rays(const ChildDev& c, const float* rays, uint64_t n_rays, uint32_t max_steps, uint64_t* cnb,
+                  float* dist, int32_t* cells, uint32_t* counts, cudaStream_t s) {
+    if (n_rays == 0) return cudaSuccess;
+    k_trace_rays<<<(unsigned) ((n_rays + 127) / 128), 128, 0, s>>>(c, rays, n_rays, max_steps, cnb, dist, cells, counts);
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------------------------------
+// Physics probe for parity tests: the same device functions the transport calls.
+// ------------------------------------------------------------------------------------------
+__global__ void
+k_eval_physics(const float* __restrict__ tables, const float* __restrict__ e, uint64_t n, float* __restrict__ out) {
+    __shared__ __align__(16) Tables T;
+    for (int i = threadIdx.x; i < 6 * MQI_TABLE_N; i += blockDim.x) reinterpret_cast<float*>(&T)[i] = tables[i];
+    __syncthreads();
+    for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n; i += (uint64_t) gridDim.x * blockDim.x) {
+        const Rel rel(e[i]);
+        float*    o = out + 8 * i;
+        o[0] = cs_lookup(T.cs_ion, rel.Ek, 0.1f, 299.6f, 1.0f);
+        o[1] = cs_lookup(T.cs_pp, rel.Ek, 0.5f, 300.0f, 1.0f);
+        o[2] = cs_lookup(T.cs_poe, rel.Ek, 0.5f, 300.0f, 1.0f);
+        o[3] = cs_lookup(T.cs_poi, rel.Ek, 0.5f, 300.0f, 1.0f);
+        o[4] = dedx_lookup(T, rel.Ek);
+        o[5] = rel.beta_sq;
+        o[6] = rel.Te_max;
+        o[7] = rel.momentum();
+    }
+}
+
+cudaError_t
+launch_eval_physics(const float* t, const float* e, uint64_t n, float* out, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_eval_physics<<<(unsigned) ((n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024), 256, 0, s>>>(t, e, n, out);
+    return cudaGetLastError();
+}
+
+}   // namespace mqi_gpu

@@ -1,0 +1,92 @@
+"""Build recipe for the CPU oracles (test infrastructure, never part of the product path).
+
+* ``oracle/_ref/bin/ref_oracle_{dbg,rel}``: the reference's own CPU code path, compiled with g++ from
+  the staged, patched copy of its headers (``oracle/stage_ref.py``) and ``oracle/ref_driver.cpp``.
+  ``dbg`` is built with ``-D__PHYSICS_DEBUG__`` (moqui's phantom example build), ``rel`` without.
+  When the reference checkout is present the copy is re-staged first; elsewhere the copy that
+  travelled with the repository is compiled as is.
+* ``oracle/_build/libmqi_oracle.so``: the C restatement ``oracle/mqi_oracle.c``.
+
+All builds use ``-ffp-contract=off`` so the x86 and Arm builds round identically.
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF_SRC = os.path.join(HERE, "_ref", "src")
+REF_BIN = os.path.join(HERE, "_ref", "bin")
+BUILD = os.path.join(HERE, "_build")
+REFERENCE_ROOT = "/root/reference"
+
+
+def _run(cmd):
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError(f"command failed: {' '.join(cmd)}\n{res.stdout[-4000:]}\n{res.stderr[-4000:]}")
+
+
+def _stale(target, deps):
+    if not os.path.exists(target):
+        return True
+    t = os.path.getmtime(target)
+    return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
+
+
+def ref_binary(debug: bool) -> str:
+    return os.path.join(REF_BIN, "ref_oracle_dbg" if debug else "ref_oracle_rel")
+
+
+def build_reference(force: bool = False) -> bool:
+    """Stage (when possible) and compile the reference CPU oracle.  Returns False when no staged
+    copy exists (the reference was never available to this checkout)."""
+    if os.path.isdir(os.path.join(REFERENCE_ROOT, "moqui")):
+        sys.path.insert(0, HERE)
+        import stage_ref  # noqa: E402
+
+        if force or not os.path.isdir(os.path.join(REF_SRC, "moqui")):
+            stage_ref.stage(REFERENCE_ROOT)
+    if not os.path.isdir(os.path.join(REF_SRC, "moqui")):
+        return False
+    os.makedirs(REF_BIN, exist_ok=True)
+    drv = os.path.join(HERE, "ref_driver.cpp")
+    jobs = []
+    for debug in (True, False):
+        out = ref_binary(debug)
+        if force or _stale(out, [drv, os.path.join(REF_SRC, "moqui", "base", "mqi_p_ionization.hpp")]):
+            cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-w", f"-I{REF_SRC}", drv, "-o", out, "-lz"]
+            if debug:
+                cmd.insert(4, "-D__PHYSICS_DEBUG__")
+            jobs.append(subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True))
+    for j in jobs:
+        out, err = j.communicate()
+        if j.returncode != 0:
+            raise RuntimeError(f"reference oracle build failed:\n{err[-4000:]}")
+    return True
+
+
+def oracle_lib() -> str:
+    return os.path.join(BUILD, "libmqi_oracle.so")
+
+
+def build_restatement(force: bool = False) -> str:
+    src = os.path.join(HERE, "mqi_oracle.c")
+    hdr = os.path.join(HERE, "mqi_oracle.h")
+    out = oracle_lib()
+    if not os.path.exists(src):
+        return ""
+    os.makedirs(BUILD, exist_ok=True)
+    if force or _stale(out, [src, hdr]):
+        _run(["gcc", "-std=c11", "-O2", "-ffp-contract=off", "-fPIC", "-shared", src, "-o", out, "-lm"])
+    return out
+
+
+def build_all(force: bool = False) -> None:
+    build_restatement(force)
+    build_reference(force)
+
+
+if __name__ == "__main__":
+    build_all(force="--force" in sys.argv)

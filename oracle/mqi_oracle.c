@@ -1,0 +1,710 @@
+/* mqi_oracle.c - CPU restatement of moqui's proton transport (TEST INFRASTRUCTURE ONLY).
+ *
+ * See mqi_oracle.h.  Each function cites the reference file:line it restates.  Floating point is
+ * FP32 throughout the stepping, as in moqui's float instantiation; build with -ffp-contract=off so
+ * x86 and Arm builds agree.
+ */
+#include "mqi_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "../moquimc_gb300/csrc/mqi_tables.h"
+
+/* ---- constants (mqi_physics_constants.hpp:14-38, mqi_interaction.hpp:24-30) ---------------- */
+#define MP 938.272046f
+#define ME 0.510998928f
+#define MO 14903.3460795634f
+#define WATER_DENSITY 0.001f
+#define X0_WATER 360.863f
+#define TP_CUT 0.5f
+#define ES 13.9f
+#define NEAR_ZERO 1e-7f
+#define GEO_TOL 1e-3f
+#define PI_F 3.14159265358979323846f
+
+typedef struct { float x, y, z; } v3;
+
+static v3 mk(float x, float y, float z) { v3 r = { x, y, z }; return r; }
+
+/* ---- Philox4x32-10 (Salmon et al., SC'11) and the per-track stream ------------------------- */
+typedef struct { uint32_t x, y, z, w; } u4;
+
+static u4 philox(u4 c, uint32_t k0, uint32_t k1) {
+    for (int r = 0; r < 10; ++r) {
+        uint64_t p0 = (uint64_t) 0xD2511F53u * c.x;
+        uint64_t p1 = (uint64_t) 0xCD9E8D57u * c.z;
+        u4 n = { (uint32_t) (p1 >> 32) ^ c.y ^ k0, (uint32_t) p1, (uint32_t) (p0 >> 32) ^ c.w ^ k1, (uint32_t) p0 };
+        c = n;
+        k0 += 0x9E3779B9u;
+        k1 += 0xBB67AE85u;
+    }
+    return c;
+}
+
+static uint64_t mix64(uint64_t z) {
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+static uint64_t daughter_uid(uint64_t parent, uint32_t k) {
+    return mix64(parent * 0x9E3779B97F4A7C15ull + (uint64_t) (k + 1u));
+}
+
+typedef struct {
+    uint32_t k0, k1, hist, lo, hi, ctr, pos;
+    u4       blk;
+} rng_t;
+
+static void rng_begin_step(rng_t* r) { r->pos = 4; }
+
+static uint32_t rng_next(rng_t* r) {
+    if (r->pos >= 4) {
+        u4 c = { r->ctr, r->hist, r->lo, r->hi };
+        r->blk = philox(c, r->k0, r->k1);
+        r->ctr++;
+        r->pos = 0;
+    }
+    uint32_t w = r->pos == 0 ? r->blk.x : r->pos == 1 ? r->blk.y : r->pos == 2 ? r->blk.z : r->blk.w;
+    r->pos++;
+    return w;
+}
+
+static float rng_u(rng_t* r) { return ((float) (rng_next(r) >> 8) + 0.5f) * (1.0f / 16777216.0f); }
+
+/* ---- helpers (mqi_math.hpp:26-30, mqi_relativistic_quantities.hpp:24-40) ------------------ */
+static float intpl1d(float x, float x0, float x1, float y0, float y1) {
+    return (x1 == x0) ? y0 : y0 + (x - x0) * (y1 - y0) / (x1 - x0);
+}
+
+typedef struct { float Ek, Et, Et_sq, gamma, gamma_sq, beta_sq, Te_max; } rel_t;
+
+static rel_t rel_of(float ek) {
+    rel_t r;
+    const float MeMp = ME / MP, MeMp_sq = MeMp * MeMp;
+    r.Ek = ek;
+    r.Et = ek + MP;
+    r.Et_sq = r.Et * r.Et;
+    r.gamma = r.Et / MP;
+    r.gamma_sq = r.gamma * r.gamma;
+    r.beta_sq = 1.0f - 1.0f / r.gamma_sq;
+    r.Te_max = (2.0f * ME * r.beta_sq * r.gamma_sq) / (1.0f + 2.0f * r.gamma * MeMp + MeMp_sq);
+    return r;
+}
+
+static float momentum(const rel_t* r) { return sqrtf(r->Et * r->Et - MP * MP); }
+
+/* ---- cross sections and stopping power (mqi_p_ionization.hpp:254-286, mqi_pp_elastic.hpp:221-235,
+ *      mqi_po_elastic.hpp:243-256, mqi_po_inelastic.hpp:141-155) ---------------------------- */
+static float cs_tab(const float* t, float Ek, float lo, float hi, float rho) {
+    float cs = 0.0f;
+    if (Ek >= lo && Ek <= hi) {
+        int i0 = (int) ((Ek - lo) / 0.5f);
+        int i1 = i0 + 1 < MQI_TABLE_N ? i0 + 1 : MQI_TABLE_N - 1;
+        float x0 = lo + (float) i0 * 0.5f;
+        float x1 = x0 + 0.5f;
+        cs = intpl1d(Ek, x0, x1, t[i0], t[i1]);
+    }
+    return cs * rho;
+}
+
+static float dedx(float Ek) {
+    float pw = 0.0f;
+    if (Ek >= 0.1f && Ek <= 299.6f) {
+        int i0 = (int) ((Ek - 0.1f) / 0.5f);
+        int i1 = i0 + 1 < MQI_TABLE_N ? i0 + 1 : MQI_TABLE_N - 1;
+        float x0 = 0.1f + (float) i0 * 0.5f;
+        float x1 = x0 + 0.5f;
+        pw = intpl1d(Ek, x0, x1, mqi_tab_dedx[i0], mqi_tab_dedx[i1]);
+    } else if (Ek < 0.1f && Ek > 0.0f) {
+        pw = mqi_tab_dedx[0];
+    }
+    return -1.0f * pw;
+}
+
+/* ---- calibration (materials/mqi_patient_materials.hpp:414-473, 514-542) -------------------- */
+float mqo_spr(float rho, float Ek, int dbg) {
+    const float d = rho * 1000.0f;
+    if (dbg && fabsf(d - 1.0f) < 1e-3f) return 1.0f;
+    if (d <= 0.26f) {
+        if (d < 0.0012f) return 0.0f;
+        return intpl1d(d, 0.0012f, 0.26f, 0.8815f, 0.9925f);
+    }
+    float rsp = 1.0123f - 3.386e-5f * Ek;
+    rsp += 0.291f * (1.0f + powf(Ek, -0.3421f)) * (powf(d, -0.7f) - 1.0f);
+    if (d >= 0.9f) return rsp;
+    return intpl1d(d, 0.26f, 0.9f, 0.9925f, rsp);
+}
+
+float mqo_x0(float rho, int dbg) {
+    const float d = rho * 1000.0f;
+    float f;
+    if (dbg && fabsf(d - 1.0f) < 1e-3f) return X0_WATER;
+    if (d <= 0.26f) f = 0.9857f + 0.0085f * d;
+    else if (d <= 0.9f) f = 1.0446f - 0.2180f * d;
+    else f = 1.19f + 0.44f * logf(d - 0.44f);
+    return (WATER_DENSITY * X0_WATER) / (d * 0.001f * f);
+}
+
+float mqo_hu_to_density(int hu) {
+    double r;
+    float  f;
+    if (hu < -1000) hu = -1000;
+    else if (hu > 2995) hu = 2995;
+    if (hu < -98) r = 0.00121 + 0.001029700665188 * (1000.0 + hu);
+    else if (hu < 15) r = 1.018 + 0.000893 * hu;
+    else if (hu < 23) r = 1.03;
+    else if (hu < 101) r = 1.003 + 0.001169 * hu;
+    else if (hu < 2001) r = 1.017 + 0.000592 * hu;
+    else if (hu < 2995) r = 2.201 + 0.0005 * (-2000.0 + hu);
+    else r = 4.54;
+    f = (float) r;
+    f = f * mqi_tab_density_correction[hu + 1000];
+    f = (float) ((double) f / 1000.0);
+    return f;
+}
+
+void mqo_eval_physics(const float* e, uint64_t n, float* out) {
+    for (uint64_t i = 0; i < n; ++i) {
+        rel_t r = rel_of(e[i]);
+        float* o = out + 8 * i;
+        o[0] = cs_tab(mqi_tab_cs_p_ion, r.Ek, 0.1f, 299.6f, 1.0f);
+        o[1] = cs_tab(mqi_tab_cs_pp_e, r.Ek, 0.5f, 300.0f, 1.0f);
+        o[2] = cs_tab(mqi_tab_cs_po_e, r.Ek, 0.5f, 300.0f, 1.0f);
+        o[3] = cs_tab(mqi_tab_cs_po_i, r.Ek, 0.5f, 300.0f, 1.0f);
+        o[4] = dedx(r.Ek);
+        o[5] = r.beta_sq;
+        o[6] = r.Te_max;
+        o[7] = momentum(&r);
+    }
+}
+
+/* ---- geometry (moqui/base/mqi_grid3d.hpp:488-889) ------------------------------------------ */
+
+/* grid3d::index(p, dir) for one axis: the reference's linear scan, restated literally
+ * (mqi_grid3d.hpp:751-780). */
+static int index_scan(const float* e, int n, float p, float dir) {
+    int idx = -1;
+    for (int ind = 0; ind < n; ind++) {
+        if (fabsf(e[ind] - p) < GEO_TOL) {
+            if (dir > 0) return ind;
+            if (dir < 0) return ind - 1;
+            return ind;
+        } else if (fabsf(e[ind + 1] - p) < GEO_TOL) {
+            if (dir > 0) return ind + 1;
+            if (dir < 0) return ind;
+            return ind;
+        } else if (e[ind] - p < 0 && e[ind + 1] - p > 0) {
+            return ind;
+        } else {
+            idx = -1;
+        }
+    }
+    return idx;
+}
+
+static int valid(const mqo_grid* g, int x, int y, int z) {
+    return !(x < 0 || y < 0 || z < 0 || x >= g->nx || y >= g->ny || z >= g->nz);
+}
+
+/* intersect(p, d, idx) per axis (mqi_grid3d.hpp:528-605) */
+static float exit_axis(float p, float* d, float v1, float v2, int idx, int dim) {
+    if ((*d) * (*d) > NEAR_ZERO) {
+        if (*d < 0) {
+            float t = -(p - v1) / *d;
+            if (fabsf(t) < GEO_TOL && idx > 0) return 1.0f / GEO_TOL;
+            return t;
+        } else {
+            float t = (v2 - p) / *d;
+            if (fabsf(t) < GEO_TOL && idx < dim) return 1.0f / GEO_TOL;
+            return t;
+        }
+    }
+    *d = 0.0f;
+    return HUGE_VALF;
+}
+
+static float intersect_voxel(const mqo_grid* g, v3 p, v3* d, int cx, int cy, int cz) {
+    float tx = exit_axis(p.x, &d->x, g->xe[cx], g->xe[cx + 1], cx, g->nx);
+    float ty = exit_axis(p.y, &d->y, g->ye[cy], g->ye[cy + 1], cy, g->ny);
+    float tz = exit_axis(p.z, &d->z, g->ze[cz], g->ze[cz + 1], cz, g->nz);
+    float u;
+    if (tx < ty) u = (tx < tz) ? tx : tz;
+    else u = (ty < tz) ? ty : tz;
+    return (u > 0) ? u : -1.0f;
+}
+
+/* intersect(p, d) from outside (mqi_grid3d.hpp:628-743); returns entry distance or -1 */
+static float intersect_box(const mqo_grid* g, v3 p, v3* d) {
+    float x0 = g->xe[0], x1 = g->xe[g->nx], y0 = g->ye[0], y1 = g->ye[g->ny], z0 = g->ze[0], z1 = g->ze[g->nz];
+    float tminx, tmaxx, tminy, tmaxy, tminz, tmaxz, umin, umax;
+    if (p.x >= x0 && p.x <= x1 && p.y >= y0 && p.y <= y1 && p.z >= z0 && p.z <= z1) return 0.0f;
+    if (d->x * d->x > NEAR_ZERO) {
+        if (d->x > 0) { tminx = (x0 - p.x) / d->x; tmaxx = (x1 - p.x) / d->x; }
+        else { tmaxx = (x0 - p.x) / d->x; tminx = (x1 - p.x) / d->x; }
+    } else { d->x = 0; tminx = -HUGE_VALF; tmaxx = HUGE_VALF; }
+    if (d->y * d->y > NEAR_ZERO) {
+        if (d->y > 0) { tminy = (y0 - p.y) / d->y; tmaxy = (y1 - p.y) / d->y; }
+        else { tmaxy = (y0 - p.y) / d->y; tminy = (y1 - p.y) / d->y; }
+    } else { d->y = 0; tminy = -HUGE_VALF; tmaxy = HUGE_VALF; }
+    if (d->z * d->z > NEAR_ZERO) {
+        if (d->z > 0) { tminz = (z0 - p.z) / d->z; tmaxz = (z1 - p.z) / d->z; }
+        else { tmaxz = (z0 - p.z) / d->z; tminz = (z1 - p.z) / d->z; }
+    } else { d->z = 0; tminz = -HUGE_VALF; tmaxz = HUGE_VALF; }
+    if (tminx > tminy) umin = (tminx > tminz) ? tminx : tminz;
+    else umin = (tminy > tminz) ? tminy : tminz;
+    if (tmaxx < tmaxy) umax = (tmaxx < tmaxz) ? tmaxx : tmaxz;
+    else umax = (tmaxy < tmaxz) ? tmaxy : tmaxz;
+    if ((umin < umax || fabsf(umin - umax) < GEO_TOL) && umin >= 0 && umax >= 0) return umin;
+    return -1.0f;
+}
+
+/* index(vtx1, dir1, idx) (mqi_grid3d.hpp:846-877) */
+static void index_update(const mqo_grid* g, v3 p, v3 d, int* cx, int* cy, int* cz) {
+    if (d.x < 0 && (fabsf(p.x - g->xe[*cx]) < GEO_TOL || p.x < g->xe[*cx])) *cx -= 1;
+    else if (d.x > 0 && (fabsf(p.x - g->xe[*cx + 1]) < GEO_TOL || p.x > g->xe[*cx + 1])) *cx += 1;
+    if (d.y < 0 && (fabsf(p.y - g->ye[*cy]) < GEO_TOL || p.y < g->ye[*cy])) *cy -= 1;
+    else if (d.y > 0 && (fabsf(p.y - g->ye[*cy + 1]) < GEO_TOL || p.y > g->ye[*cy + 1])) *cy += 1;
+    if (d.z < 0 && (fabsf(p.z - g->ze[*cz]) < GEO_TOL || p.z < g->ze[*cz])) *cz -= 1;
+    else if (d.z > 0 && (fabsf(p.z - g->ze[*cz + 1]) < GEO_TOL || p.z > g->ze[*cz + 1])) *cz += 1;
+}
+
+static v3 normalize(v3 v) {
+    float n = sqrtf(v.x * v.x + v.y * v.y + v.z * v.z);
+    return mk(v.x / n, v.y / n, v.z / n);
+}
+
+static v3 advance(v3 p, v3 d, float len) { return mk(p.x + d.x * len, p.y + d.y * len, p.z + d.z * len); }
+
+int mqo_trace_ray(const mqo_grid* g, const float ray[6], int max_steps, uint64_t* cnb, float* dist, int32_t* cells) {
+    v3 p0 = mk(ray[0], ray[1], ray[2]);
+    v3 d0 = normalize(mk(ray[3], ray[4], ray[5]));
+    v3 d1 = d0;
+    int cx = index_scan(g->xe, g->nx, p0.x, d0.x);
+    int cy = index_scan(g->ye, g->ny, p0.y, d0.y);
+    int cz = index_scan(g->ze, g->nz, p0.z, d0.z);
+    int k = 0;
+    if (!valid(g, cx, cy, cz)) {
+        float e = intersect_box(g, p0, &d0);
+        if (e < 0) return 0;
+        p0 = advance(p0, d0, e);
+        d0 = d1;
+        cx = index_scan(g->xe, g->nx, p0.x, d0.x);
+        cy = index_scan(g->ye, g->ny, p0.y, d0.y);
+        cz = index_scan(g->ze, g->nz, p0.z, d0.z);
+    }
+    while (valid(g, cx, cy, cz) && k < max_steps) {
+        float d2b = intersect_voxel(g, p0, &d0, cx, cy, cz);
+        cnb[k] = (uint64_t) cz * g->nx * g->ny + (uint64_t) cy * g->nx + cx;
+        dist[k] = d2b;
+        cells[3 * k] = cx; cells[3 * k + 1] = cy; cells[3 * k + 2] = cz;
+        ++k;
+        if (d2b < 0) break;
+        v3 p1 = advance(p0, d0, d2b);
+        index_update(g, p1, d1, &cx, &cy, &cz);
+        p0 = p1;
+        d0 = d1;
+    }
+    return k;
+}
+
+/* ---- tracks and the LIFO stack (mqi_track.hpp:48-205, mqi_track_stack.hpp:11-67) ----------- */
+typedef struct {
+    float    ke0, ke1;
+    v3       p0, d0, p1, d1;
+    float    dE, ldE;
+    int      primary, stopped;
+    uint64_t uid;
+    uint32_t npush;
+} trk_t;
+
+typedef struct {
+    trk_t*  t;
+    int     idx, limit;
+    uint64_t pushed, dropped;
+} stack_t_;
+
+typedef struct {
+    const mqo_grid*  g;
+    int              dbg;
+    float            tcut;
+    stack_t_*        stk;
+    rng_t            rng;
+} env_t;
+
+static void push(env_t* E, trk_t* parent, float ke0, float ke1, v3 p, v3 d, float dE0) {
+    stack_t_* s = E->stk;
+    if (s->idx >= s->limit) {   /* push_secondary silently drops (mqi_track_stack.hpp:36-41) */
+        s->dropped++;
+        return;
+    }
+    trk_t* n = &s->t[s->idx++];
+    memset(n, 0, sizeof(*n));
+    n->ke0 = ke0;
+    n->ke1 = ke1;
+    n->p0 = p; n->p1 = p; n->d0 = d; n->d1 = d;
+    n->dE = dE0;
+    n->primary = 0;
+    n->uid = daughter_uid(parent->uid, parent->npush);
+    parent->npush++;
+    s->pushed++;
+}
+
+/* Möller-Hughes alignment + track_t::update_post_vertex_direction (mqi_track.hpp:163-172,
+ * mqi_matrix.hpp:88-150) */
+static v3 rotate_dir(v3 t, float th, float ph) {
+    float s1 = sinf(th), c1 = cosf(th), s2 = sinf(ph), c2 = cosf(ph);
+    v3 dl = normalize(mk(c2 * s1, s2 * s1, c1));
+    float tn = sqrtf(t.x * t.x + t.y * t.y + t.z * t.z);
+    float c = t.z / tn;
+    float m[9];
+    if (fabsf(c - 1.0f) < GEO_TOL || fabsf(c + 1.0f) < GEO_TOL) {
+        float r2 = 1.0f / sqrtf(2.0f);
+        float ux = r2, uy = 0.0f, uz = -r2;
+        float vx = 1.0f - t.x, vy = -t.y, vz = -t.z;
+        float vn = sqrtf(vx * vx + vy * vy + vz * vz);
+        vx /= vn; vy /= vn; vz /= vn;
+        float du = ux * ux + uy * uy + uz * uz, dv = vx * vx + vy * vy + vz * vz, duv = vx * ux + vy * uy + vz * uz;
+        float a = 2.0f / du, b = 2.0f / dv, k = 4.0f * duv / (du * dv);
+        m[0] = 1.0f - a * ux * ux - b * vx * vx + k * vx * ux;
+        m[1] = 0.0f - a * ux * uy - b * vx * vy + k * vx * uy;
+        m[2] = 0.0f - a * ux * uz - b * vx * vz + k * vx * uz;
+        m[3] = 0.0f - a * uy * ux - b * vy * vx + k * vy * ux;
+        m[4] = 1.0f - a * uy * uy - b * vy * vy + k * vy * uy;
+        m[5] = 0.0f - a * uy * uz - b * vy * vz + k * vy * uz;
+        m[6] = 0.0f - a * uz * ux - b * vz * vx + k * vz * ux;
+        m[7] = 0.0f - a * uz * uy - b * vz * vy + k * vz * uy;
+        m[8] = 1.0f - a * uz * uz - b * vz * vz + k * vz * uz;
+    } else {
+        float vx = -t.y, vy = t.x, vz = 0.0f;
+        float h = (1.0f - c) / (1.0f - c * c);
+        m[0] = c + h * vx * vx; m[1] = h * vx * vy - vz; m[2] = h * vx * vz + vy;
+        m[3] = h * vx * vy + vz; m[4] = c + h * vy * vy; m[5] = h * vy * vz - vx;
+        m[6] = h * vx * vz - vy; m[7] = h * vy * vz + vx; m[8] = c + h * vz * vz;
+    }
+    return normalize(mk(m[0] * dl.x + m[1] * dl.y + m[2] * dl.z, m[3] * dl.x + m[4] * dl.y + m[5] * dl.z,
+                        m[6] * dl.x + m[7] * dl.y + m[8] * dl.z));
+}
+
+/* energy_loss + energy_straggling (mqi_p_ionization.hpp:297-345), range walk guarded at 0 */
+static float energy_loss(rel_t* rel, float rho, float len, float spr, float z) {
+    float lw = len * spr * rho / WATER_DENSITY;
+    int n = (int) ((rel->Ek - 0.1f) / 0.5f);
+    float x0, x1, r, dE_mean, Te, var, ret;
+    if (n > MQI_TABLE_N - 2) n = MQI_TABLE_N - 2;
+    if (n < 0) n = 0;
+    x0 = 0.1f + (float) n * 0.5f;
+    x1 = x0 + 0.5f;
+    if (x0 > rel->Ek && n > 0) n -= 1;
+    if (x1 < rel->Ek && n < MQI_TABLE_N - 2) n += 1;
+    r = intpl1d(rel->Ek, x0, x1, mqi_tab_range[n], mqi_tab_range[n + 1]);
+    if (r < lw) return rel->Ek;
+    r -= lw;
+    while (n > 0 && r < mqi_tab_range[n]) --n;
+    x0 = 0.1f + (float) n * 0.5f;
+    x1 = x0 + 0.5f;
+    dE_mean = rel->Ek - intpl1d(r, mqi_tab_range[n], mqi_tab_range[n + 1], x0, x1);
+    Te = (rel->Te_max >= 0.08511f) ? 0.08511f : rel->Te_max;
+    {
+        /* dedx_term0 (mqi_physics_constants.hpp:29-30) in float */
+        const float re = 2.8179403262e-12f, re_sq = re * re;
+        const float two_pi = (float) (2.0 * 3.14159265358979323846);
+        const float t = (float) ((double) two_pi * (double) re_sq);
+        const float t2 = t * ME;
+        const float term0 = (float) ((double) t2 * 3.3428e+23 / 1000.0);
+        var = term0 * rho / WATER_DENSITY * lw;
+    }
+    var *= Te / rel->beta_sq * (1.0f - 0.5f * rel->beta_sq);
+    ret = z * sqrtf(var) + dE_mean;
+    if (ret < 0) ret = -ret;
+    return ret;
+}
+
+/* last_step (mqi_p_ionization.hpp:481-490) */
+static void last_step(env_t* E, trk_t* t, float rho) {
+    float lw = 0.0f, sl;
+    if (t->dE > 0) lw = -t->dE / dedx(t->ke0);
+    sl = lw * WATER_DENSITY / (mqo_spr(rho, t->ke0, E->dbg) * rho);
+    t->p1 = advance(t->p0, t->d0, sl);
+}
+
+/* along_step (mqi_p_ionization.hpp:349-420) */
+static void along_step(env_t* E, trk_t* t, float len, float rho, float spr, float z1, float z2, float u_phi) {
+    rel_t rel = rel_of(t->ke0);
+    float dE = energy_loss(&rel, rho, len, spr, z1);
+    float r = 1.0f, P, X0, th_sq, th, phi;
+    if (dE >= t->ke0) {
+        r = t->ke0 / dE;
+        t->stopped = 1;
+    }
+    P = momentum(&rel);
+    X0 = mqo_x0(rho, E->dbg);
+    th_sq = ((ES / P) * (ES / P) / rel.beta_sq) * len / X0;
+    th = sqrtf(th_sq);
+    th = z2 * (sqrtf(2.0f) * th);
+    if (th < 0) th = -th;
+    phi = 2.0f * PI_F * u_phi;
+    t->d1 = rotate_dir(t->d1, th, phi);
+    t->dE += dE * r;
+    t->p1 = advance(t->p0, t->d0, r * len);
+    t->ke1 -= dE * r;
+}
+
+/* p_ionization post_step (mqi_p_ionization.hpp:425-477) */
+static void post_delta(env_t* E, trk_t* t) {
+    rel_t rel = rel_of(t->ke1);
+    float Te = 0.0f;
+    for (int it = 0; it < 64; ++it) {
+        float n = rng_u(&E->rng);
+        Te = E->tcut * rel.Te_max;
+        Te /= ((1.0f - n) * rel.Te_max + n * E->tcut);
+        if (rng_u(&E->rng) < 1.0f - rel.beta_sq * Te / rel.Te_max + Te * Te / (2.0f * rel.Et_sq)) break;
+    }
+    if (E->dbg) push(E, t, 0.0f, 0.0f, t->p0, t->d0, Te);
+    else t->dE += Te;
+    t->ke1 -= Te;
+}
+
+/* pp_elastic post_step (mqi_pp_elastic.hpp:119-219) */
+static void post_pp(env_t* E, trk_t* t) {
+    rel_t rel = rel_of(t->ke1);
+    const float Mp_sq = MP * MP;
+    float minv = TP_CUT / rel.Ek;
+    float u = rng_u(&E->rng) * (1.0f - 2.0f * minv) + minv;
+    float E1 = rel.Et, dE = rel.Ek * u, E3 = (rel.Ek - dE) + MP, E4 = dE + MP;
+    float P1 = momentum(&rel), P3 = sqrtf(E3 * E3 - Mp_sq), P4 = sqrtf(E4 * E4 - Mp_sq);
+    float c3 = E1 * E3 - Mp_sq - MP * (E1 - E3), c34 = E3 * E4 - E1 * MP, th3, th4, phi;
+    v3 dd;
+    c3 /= (P1 * P3);
+    c34 /= (P3 * P4);
+    c3 = fminf(fmaxf(c3, -1.0f), 1.0f);
+    c34 = fminf(fmaxf(c34, -1.0f), 1.0f);
+    th3 = acosf(c3);
+    th4 = th3 - acosf(c34);
+    phi = 2.0f * PI_F * rng_u(&E->rng);
+    t->ke1 -= dE;
+    t->d1 = rotate_dir(t->d1, th3, phi);
+    dd = rotate_dir(t->d1, th4, phi);
+    push(E, t, dE, dE, t->p1, dd, 0.0f);
+}
+
+/* po_elastic post_step (mqi_po_elastic.hpp:96-217); truncated exponential by inverse CDF */
+static void post_poe(env_t* E, trk_t* t) {
+    rel_t rel = rel_of(t->ke1);
+    if (rel.Ek <= 5.5f) {
+        float dE = rel.Ek;
+        if (E->dbg) push(E, t, dE, 0.0f, t->p1, t->d1, dE);
+        else t->ldE += dE;
+        t->ke1 -= dE;
+        t->stopped = 1;
+        return;
+    }
+    {
+        const float MoMp = MO / MP, MoMp_sq = MoMp * MoMp;
+        float Tp_avg = 0.65f * expf(-0.0013f * rel.Ek) - 0.71f * expf(-0.0177f * rel.Ek);
+        float Tp_max = (2.0f * MO * rel.beta_sq * rel.gamma_sq) / (1.0f + 2.0f * rel.gamma * MoMp + MoMp_sq);
+        float u = rng_u(&E->rng);
+        float dE = -Tp_avg * log1pf(u * expm1f(-Tp_max / Tp_avg));
+        float E1, E3, c3, th3, phi;
+        if (!(dE >= 0.0f)) dE = 0.0f;
+        if (dE > Tp_max) dE = Tp_max;
+        E1 = rel.Ek * (rel.Ek + 2.0f * MP);
+        E3 = (rel.Ek - dE) * (rel.Ek - dE + 2.0f * MP);
+        c3 = (E1 + E3 - dE * (dE + 2.0f * MO)) / 2.0f / sqrtf(E1 * E3);
+        c3 = fminf(fmaxf(c3, -1.0f), 1.0f);
+        th3 = acosf(c3);
+        phi = 2.0f * PI_F * rng_u(&E->rng);
+        if (E->dbg) push(E, t, dE, 0.0f, t->p0, t->d0, dE);
+        else t->ldE += dE;
+        t->ke1 -= dE;
+        t->d1 = rotate_dir(t->d1, th3, phi);
+    }
+}
+
+/* po_inelastic post_step (mqi_po_inelastic.hpp:158-288) */
+static void post_poi(env_t* E, trk_t* t) {
+    const float Ek = t->ke1;
+    float Eb = 5.0f, Er = Ek, P2, PL, pw;
+    if (Ek <= 215.0f && Ek > 200.0f) { P2 = 0.78f; PL = P2 + (1.0f - P2) * 0.9f; pw = 0.4f; }
+    else if (Ek > 215.0f) { P2 = 0.78f; PL = P2 + (1.0f - P2) * 1.0f; pw = 0.4f; }
+    else if (Ek > 150.0f) { P2 = 0.72f; PL = P2 + (1.0f - P2) * 0.83f; pw = 0.45f; }
+    else { P2 = 0.7f; PL = P2 + (1.0f - P2) * 0.83f; pw = 0.52f; }
+    while ((Er - Eb) > 2.0f) {
+        float dE, zeta;
+        Er -= Eb;
+        dE = powf(rng_u(&E->rng), pw) * (Er - 2.0f) + 2.0f;
+        if (dE >= Er) dE = Er;
+        Er -= dE;
+        t->ke1 -= (dE + Eb);
+        zeta = rng_u(&E->rng);
+        if (zeta < P2) {
+            float c = (2.0f * dE / Ek - 1.0f) + 2.0f * (1.0f - dE / Ek) * rng_u(&E->rng);
+            float th, phi;
+            c = fminf(fmaxf(c, -1.0f), 1.0f);
+            th = acosf(c);
+            phi = 2.0f * PI_F * rng_u(&E->rng);
+            push(E, t, dE, dE, t->p1, rotate_dir(t->d1, th, phi), 0.0f);
+        } else if (zeta < PL) {
+        } else if (E->dbg) {
+            push(E, t, dE, 0.0f, t->p0, t->d0, dE);
+        }
+        Eb *= 0.65f;
+    }
+    t->dE += Er;
+    t->ke1 -= Er;
+    t->stopped = 1;
+}
+
+/* fippel_physics::stepping (mqi_fippel_physics.hpp:67-216) */
+static void stepping(env_t* E, trk_t* t, float rho, float d2b) {
+    rel_t rel, rel2;
+    float spr, dd, cur_min, max_loss, cs1[4], cs2[4], sum1, sum2, cs_sum, c[4], u_mfp, mfp, step_limit;
+    float bm_u1, bm_u2, u_phi, bm_r, z1, z2;
+    if (rho < 1.0e-7f) { t->p1 = advance(t->p0, t->d0, d2b); return; }
+    if (rho > 99.9f) { t->stopped = 1; return; }
+    if (t->ke0 <= TP_CUT) {
+        if (t->ke0 < 0) t->ke0 = 0;
+        t->dE += t->ke0;
+        t->ke1 -= t->ke0;
+        last_step(E, t, rho);
+        t->stopped = 1;
+        return;
+    }
+    rng_begin_step(&E->rng);
+    rel = rel_of(t->ke0);
+    spr = mqo_spr(rho, t->ke0, E->dbg);
+    dd = dedx(rel.Ek);
+    cur_min = 1.0f * spr * rho / WATER_DENSITY;
+    max_loss = -1.0f * cur_min * dd;
+    cs1[0] = cs_tab(mqi_tab_cs_p_ion, rel.Ek, 0.1f, 299.6f, rho);
+    cs1[1] = cs_tab(mqi_tab_cs_pp_e, rel.Ek, 0.5f, 300.0f, rho);
+    cs1[2] = cs_tab(mqi_tab_cs_po_e, rel.Ek, 0.5f, 300.0f, rho);
+    cs1[3] = cs_tab(mqi_tab_cs_po_i, rel.Ek, 0.5f, 300.0f, rho);
+    rel2 = rel_of(t->ke0 - max_loss);
+    cs2[0] = cs_tab(mqi_tab_cs_p_ion, rel2.Ek, 0.1f, 299.6f, rho);
+    cs2[1] = cs_tab(mqi_tab_cs_pp_e, rel2.Ek, 0.5f, 300.0f, rho);
+    cs2[2] = cs_tab(mqi_tab_cs_po_e, rel2.Ek, 0.5f, 300.0f, rho);
+    cs2[3] = cs_tab(mqi_tab_cs_po_i, rel2.Ek, 0.5f, 300.0f, rho);
+    sum1 = cs1[0] + cs1[1] + cs1[2] + cs1[3];
+    sum2 = cs2[0] + cs2[1] + cs2[2] + cs2[3];
+    cs_sum = (sum1 >= sum2) ? sum1 : sum2;
+    for (int k = 0; k < 4; ++k) c[k] = (sum1 >= sum2) ? cs1[k] : cs2[k];
+    u_mfp = rng_u(&E->rng);
+    mfp = -1.0f * logf(u_mfp) / cs_sum;
+    step_limit = cur_min * WATER_DENSITY / (spr * rho);
+    bm_u1 = rng_u(&E->rng);
+    bm_u2 = rng_u(&E->rng);
+    u_phi = rng_u(&E->rng);
+    bm_r = sqrtf(-2.0f * logf(bm_u1));
+    z1 = bm_r * cosf(2.0f * PI_F * bm_u2);
+    z2 = bm_r * sinf(2.0f * PI_F * bm_u2);
+    if (d2b < mfp && d2b < step_limit) {
+        along_step(E, t, d2b, rho, spr, z1, z2, u_phi);
+    } else if ((mfp < d2b || fabsf(mfp - d2b) < GEO_TOL) && (mfp < step_limit || fabsf(mfp - step_limit) < GEO_TOL)) {
+        float u;
+        along_step(E, t, mfp, rho, spr, z1, z2, u_phi);
+        if (t->ke1 <= TP_CUT) return;
+        u = cs_sum * rng_u(&E->rng);
+        t->d1 = t->d0;
+        if (u < c[0]) post_delta(E, t);
+        else if (u < c[0] + c[1]) post_pp(E, t);
+        else if (u < c[0] + c[1] + c[2]) post_poe(E, t);
+        else if (u < c[0] + c[1] + c[2] + c[3]) post_poi(E, t);
+    } else {
+        along_step(E, t, step_limit, rho, spr, z1, z2, u_phi);
+    }
+}
+
+/* scorer callbacks (scorers/mqi_scorer_energy_deposit.hpp:12-77) */
+static double hit(const mqo_config* cfg, const trk_t* t, float rho, float vol, int dbg) {
+    float edep = t->dE + t->ldE;
+    if (cfg->scorer == 1) return (double) edep;
+    if (rho < 1.0e-7f) return 0.0;
+    {
+        double d = (double) edep * 1.60218e-10 / (double) (vol * rho * mqo_spr(rho, t->ke0, dbg));
+        return cfg->scorer == 3 ? d * d : d;
+    }
+}
+
+/* The history loop (mqi_transport.hpp:146-249), one child, DIRECT ROI. */
+int mqo_transport(const mqo_grid* g, const mqo_config* cfg, const float* V, uint64_t h0, uint64_t h1, uint64_t seed,
+                  double* tally, double* per_hist, mqo_stats* st) {
+    env_t    E;
+    stack_t_ S;
+    memset(&E, 0, sizeof(E));
+    memset(&S, 0, sizeof(S));
+    S.limit = cfg->physics_debug ? 200 : 10;
+    S.t = (trk_t*) calloc((size_t) S.limit, sizeof(trk_t));
+    if (!S.t) return -3;
+    E.g = g;
+    E.dbg = cfg->physics_debug;
+    E.tcut = cfg->physics_debug ? 0.08511f : 0.0815f;
+    E.stk = &S;
+    E.rng.k0 = (uint32_t) seed;
+    E.rng.k1 = (uint32_t) (seed >> 32);
+    for (uint64_t h = h0; h < h1; ++h) {
+        const float* v = V + 7 * h;
+        double hsum = 0.0;
+        trk_t* p = &S.t[0];
+        memset(p, 0, sizeof(*p));
+        p->ke0 = p->ke1 = v[0];
+        p->p0 = p->p1 = mk(v[1], v[2], v[3]);
+        p->d0 = p->d1 = mk(v[4], v[5], v[6]);
+        p->primary = 1;
+        p->uid = 0;
+        S.idx = 1;
+        while (S.idx > 0) {
+            trk_t t = S.t[--S.idx];
+            int cx, cy, cz;
+            if (st) st->tracks++;
+            E.rng.hist = (uint32_t) h;
+            E.rng.lo = (uint32_t) t.uid;
+            E.rng.hi = (uint32_t) (t.uid >> 32);
+            E.rng.ctr = 0;
+            E.rng.pos = 4;
+            /* child entry (mqi_transport.hpp:165-190), identity transform */
+            t.d0 = normalize(t.d0);
+            t.p1 = t.p0;
+            t.d1 = t.d0;
+            cx = index_scan(g->xe, g->nx, t.p0.x, t.d0.x);
+            cy = index_scan(g->ye, g->ny, t.p0.y, t.d0.y);
+            cz = index_scan(g->ze, g->nz, t.p0.z, t.d0.z);
+            if (!valid(g, cx, cy, cz)) {
+                float e = intersect_box(g, t.p0, &t.d0);
+                if (e < 0) continue;
+                t.p1 = advance(t.p0, t.d0, e);
+                t.p0 = t.p1; t.d0 = t.d1; t.ke0 = t.ke1; t.dE = t.ldE = 0.0f;
+                cx = index_scan(g->xe, g->nx, t.p0.x, t.d0.x);
+                cy = index_scan(g->ye, g->ny, t.p0.y, t.d0.y);
+                cz = index_scan(g->ze, g->nz, t.p0.z, t.d0.z);
+            }
+            while (valid(g, cx, cy, cz) && !t.stopped) {
+                uint64_t cnb = (uint64_t) cz * g->nx * g->ny + (uint64_t) cy * g->nx + cx;
+                float rho = g->rho[cnb];
+                float d2b = intersect_voxel(g, t.p0, &t.d0, cx, cy, cz);
+                stepping(&E, &t, rho, d2b);
+                if (st) st->steps++;
+                if (d2b < 0) break;
+                if (cnb > 0) {   /* DIRECT ROI: roi_->idx(cnb) > 0 */
+                    float vol = (g->xe[cx + 1] - g->xe[cx]) * (g->ye[cy + 1] - g->ye[cy]) * (g->ze[cz + 1] - g->ze[cz]);
+                    double val = hit(cfg, &t, rho, vol, E.dbg);
+                    if (val > 0) {
+                        tally[cnb] += val;
+                        hsum += val;
+                    }
+                }
+                if (!t.stopped) {
+                    index_update(g, t.p1, t.d1, &cx, &cy, &cz);
+                    t.p0 = t.p1; t.d0 = t.d1; t.ke0 = t.ke1; t.dE = t.ldE = 0.0f;
+                }
+            }
+        }
+        if (per_hist) per_hist[h - h0] = hsum;
+        if (st) st->histories++;
+    }
+    if (st) { st->pushed += S.pushed; st->dropped += S.dropped; }
+    free(S.t);
+    return 0;
+}

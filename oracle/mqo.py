@@ -1,0 +1,209 @@
+"""ctypes binding of the C restatement (oracle/mqi_oracle.c) and runners for the reference's own
+CPU build (oracle/_ref/bin).  TEST INFRASTRUCTURE: only tests, the smoke check and the bench's
+CPU-baseline leg use this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import json
+import os
+import struct
+import subprocess
+import tempfile
+from typing import Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys_path_added = False
+
+
+def _build():
+    import sys
+
+    sys.path.insert(0, HERE)
+    import build_oracle  # noqa: E402
+
+    return build_oracle
+
+
+class _Grid(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("xe", C.c_void_p), ("ye", C.c_void_p),
+                ("ze", C.c_void_p), ("rho", C.c_void_p)]
+
+
+class _Cfg(C.Structure):
+    _fields_ = [("physics_debug", C.c_int), ("scorer", C.c_int)]
+
+
+class _Stats(C.Structure):
+    _fields_ = [(n, C.c_uint64) for n in ("histories", "tracks", "steps", "pushed", "dropped")]
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build().build_restatement()
+        _lib = C.CDLL(path)
+        _lib.mqo_transport.restype = C.c_int
+        _lib.mqo_transport.argtypes = [C.POINTER(_Grid), C.POINTER(_Cfg), C.c_void_p, C.c_uint64, C.c_uint64,
+                                       C.c_uint64, C.c_void_p, C.c_void_p, C.POINTER(_Stats)]
+        _lib.mqo_eval_physics.restype = None
+        _lib.mqo_eval_physics.argtypes = [C.c_void_p, C.c_uint64, C.c_void_p]
+        _lib.mqo_spr.restype = C.c_float
+        _lib.mqo_spr.argtypes = [C.c_float, C.c_float, C.c_int]
+        _lib.mqo_x0.restype = C.c_float
+        _lib.mqo_x0.argtypes = [C.c_float, C.c_int]
+        _lib.mqo_hu_to_density.restype = C.c_float
+        _lib.mqo_hu_to_density.argtypes = [C.c_int]
+        _lib.mqo_trace_ray.restype = C.c_int
+        _lib.mqo_trace_ray.argtypes = [C.POINTER(_Grid), C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class Grid:
+    def __init__(self, xe, ye, ze, rho):
+        self.xe = np.ascontiguousarray(xe, np.float32)
+        self.ye = np.ascontiguousarray(ye, np.float32)
+        self.ze = np.ascontiguousarray(ze, np.float32)
+        self.rho = np.ascontiguousarray(rho, np.float32).reshape(-1)
+        self.c = _Grid(len(self.xe) - 1, len(self.ye) - 1, len(self.ze) - 1, _p(self.xe).value, _p(self.ye).value,
+                       _p(self.ze).value, _p(self.rho).value)
+
+
+def transport(grid: Grid, vertices: np.ndarray, h0: int, h1: int, seed: int, physics_debug: bool, scorer: int = 2,
+              per_history: bool = False):
+    """Run the C restatement; returns (tally, per_history_sums or None, stats dict)."""
+    v = np.ascontiguousarray(vertices).view(np.float32).reshape(-1, 7)
+    tally = np.zeros(grid.rho.size, np.float64)
+    ph = np.zeros(h1 - h0, np.float64) if per_history else None
+    st = _Stats()
+    cfg = _Cfg(int(physics_debug), scorer)
+    rc = lib().mqo_transport(C.byref(grid.c), C.byref(cfg), _p(v), h0, h1, seed, _p(tally),
+                             None if ph is None else _p(ph), C.byref(st))
+    if rc != 0:
+        raise RuntimeError(f"mqo_transport failed: {rc}")
+    return tally, ph, {n: int(getattr(st, n)) for n, _ in st._fields_}
+
+
+def eval_physics(energies: np.ndarray) -> np.ndarray:
+    e = np.ascontiguousarray(energies, np.float32)
+    out = np.empty((len(e), 8), np.float32)
+    lib().mqo_eval_physics(_p(e), len(e), _p(out))
+    return out
+
+
+def spr(rho: float, ke: float, dbg: bool) -> float:
+    return lib().mqo_spr(rho, ke, int(dbg))
+
+
+def x0(rho: float, dbg: bool) -> float:
+    return lib().mqo_x0(rho, int(dbg))
+
+
+def hu_to_density(hu: int) -> float:
+    return lib().mqo_hu_to_density(int(hu))
+
+
+def trace_rays(grid: Grid, rays: np.ndarray, max_steps: int):
+    rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 6)
+    offs = [0]
+    cnbs, dists, cells = [], [], []
+    cnb = np.zeros(max_steps, np.uint64)
+    dist = np.zeros(max_steps, np.float32)
+    cell = np.zeros((max_steps, 3), np.int32)
+    for r in rays:
+        r = np.ascontiguousarray(r)
+        k = lib().mqo_trace_ray(C.byref(grid.c), _p(r), max_steps, _p(cnb), _p(dist), _p(cell))
+        cnbs.append(cnb[:k].copy())
+        dists.append(dist[:k].copy())
+        cells.append(cell[:k].copy())
+        offs.append(offs[-1] + k)
+    cat = lambda xs, dt, shp: np.concatenate(xs) if xs else np.zeros(shp, dt)  # noqa: E731
+    return (np.asarray(offs, np.int64), cat(cnbs, np.uint64, (0,)), cat(dists, np.float32, (0,)),
+            cat(cells, np.int32, (0, 3)))
+
+
+# ---- the reference's own CPU build ------------------------------------------------------------
+
+def ref_available() -> bool:
+    b = _build()
+    return os.path.exists(b.ref_binary(True)) or b.build_reference()
+
+
+def ref_binary(debug: bool) -> str:
+    b = _build()
+    path = b.ref_binary(debug)
+    if not os.path.exists(path):
+        b.build_reference()
+    return path
+
+
+def write_rays(path, grid_bounds, nxyz, max_steps, rays):
+    with open(path, "wb") as f:
+        f.write(np.asarray(grid_bounds, np.float32).tobytes())
+        f.write(np.asarray(nxyz, np.int32).tobytes())
+        f.write(struct.pack("<I", max_steps))
+        r = np.ascontiguousarray(rays, np.float32).reshape(-1)
+        f.write(struct.pack("<Q", r.size))
+        f.write(r.tobytes())
+
+
+def read_vecs(path, dtypes):
+    out = []
+    with open(path, "rb") as f:
+        for dt in dtypes:
+            n = struct.unpack("<Q", f.read(8))[0]
+            out.append(np.frombuffer(f.read(n * np.dtype(dt).itemsize), dtype=dt).copy())
+    return out
+
+
+def ref_trace_rays(grid_bounds, nxyz, rays, max_steps):
+    with tempfile.TemporaryDirectory() as td:
+        i, o = os.path.join(td, "rays.bin"), os.path.join(td, "out.bin")
+        write_rays(i, grid_bounds, nxyz, max_steps, rays)
+        subprocess.run([ref_binary(True), "raywalk", i, o], check=True, capture_output=True)
+        off, cnb, dist, cells = read_vecs(o, [np.int64, np.uint64, np.float32, np.int32])
+    return off, cnb, dist, cells.reshape(-1, 3)
+
+
+def ref_phantom_cmd(debug: bool, lxyz, pxyz, nxyz, energy, position, size, histories, phantom_path, out_dir, seed,
+                    beam="uniform"):
+    return [ref_binary(debug), "phantom", "--lxyz", *map(str, lxyz), "--pxyz", *map(str, pxyz), "--nxyz",
+            *map(str, nxyz), "--spot_energy", str(energy), "0", "--spot_position", *map(str, position),
+            "--spot_size", *map(str, size), "--histories", str(histories), "--phantom_path", phantom_path,
+            "--output_prefix", out_dir, "--random_seed", str(seed), "--beam", beam, "--json",
+            os.path.join(out_dir, "run.json")]
+
+
+def ref_phantom_parallel(debug: bool, lxyz, pxyz, nxyz, energy, position, size, histories_each, n_proc, hu,
+                         seed0, beam="uniform", workdir: Optional[str] = None):
+    """Run n_proc reference CPU processes (distinct seeds) in parallel; returns (summed dose, list of
+    per-process run records, per-process doses)."""
+    td = workdir or tempfile.mkdtemp(prefix="mqi_ref_")
+    ph = os.path.join(td, "phantom.raw")
+    np.ascontiguousarray(hu, np.int16).tofile(ph)
+    procs, dirs = [], []
+    for p in range(n_proc):
+        od = os.path.join(td, f"p{p}")
+        os.makedirs(od, exist_ok=True)
+        dirs.append(od)
+        cmd = ref_phantom_cmd(debug, lxyz, pxyz, nxyz, energy, position, size, histories_each, ph, od, seed0 + p, beam)
+        procs.append(subprocess.Popen(cmd, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL))
+    rcs = [q.wait() for q in procs]
+    if any(rcs):
+        raise RuntimeError(f"reference oracle failed: {rcs}")
+    n = int(np.prod(nxyz))
+    doses, recs = [], []
+    for od in dirs:
+        doses.append(np.fromfile(os.path.join(od, "0_water_dE_total.raw"), dtype=np.float64, count=n))
+        with open(os.path.join(od, "run.json")) as f:
+            recs.append(json.load(f))
+    return np.sum(doses, axis=0), recs, doses

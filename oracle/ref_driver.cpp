@@ -1,0 +1,415 @@
+// Reference CPU oracle driver: test infrastructure only.
+//
+// This translation unit is compiled against the staged, patched copy of the reference headers
+// (oracle/stage_ref.py) and runs the reference's OWN CPU code path.  It is the checker that pins
+// the C restatement (oracle/mqi_oracle.c) and the CUDA path; nothing in the product links it.
+//
+// Modes (argv[1]):
+//   phantom <phantom_env CLI> [--beam uniform|gaussian] [--json <file>]
+//       Runs mqi::phantom_env<float> (moqui/base/environments/mqi_phantom_env.hpp:37-428) on the CPU:
+//       initialize -> run -> save_reshaped_files.  run() is overridden only to (a) seed the CPU
+//       transport RNG from --random_seed (the stock CPU branch default-constructs it, so every
+//       process would share one stream, mqi_transport.hpp:147-149 / mqi_phantom_env.hpp:420-422)
+//       and (b) time the transport call alone.  --beam gaussian swaps phsp_6d_uniform for the
+//       Gaussian phsp_6d (moqui/base/distributions/mqi_phsp6d.hpp) with sigma = --spot_size.
+//   raywalk <rays.bin> <out.bin>
+//       Walks rays through a grid3d exactly as the transport kernel's voxel loop does
+//       (mqi_transport.hpp:161-239) with the physics replaced by a pure boundary step.
+//   physics <out.bin>
+//       Tabulates the deterministic physics functions on fixed input grids.
+//   sample <out.bin> <n> <seed>
+//       Draws n samples from each sampling routine at fixed inputs (along_step, the four
+//       post_step processes) for distribution tests.
+#include <moqui/base/environments/mqi_phantom_env.hpp>
+#include <moqui/kernel_functions/mqi_transport.hpp>
+
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <string>
+#include <vector>
+
+// Shim: the reference's print_materials reads members that no longer exist
+// (moqui/kernel_functions/mqi_print_data.hpp:20-24).  An empty specialisation lets
+// x_environment<float>::initialize instantiate; it only printed diagnostics.
+template<>
+void
+mc::print_materials<float>(mqi::material_t<float>*, uint16_t) {}
+
+namespace
+{
+
+template<typename T>
+void
+write_vec(std::ofstream& f, const std::vector<T>& v) {
+    uint64_t n = v.size();
+    f.write(reinterpret_cast<const char*>(&n), sizeof(n));
+    if (n) f.write(reinterpret_cast<const char*>(v.data()), n * sizeof(T));
+}
+
+template<typename T>
+std::vector<T>
+read_vec(std::ifstream& f) {
+    uint64_t n = 0;
+    f.read(reinterpret_cast<char*>(&n), sizeof(n));
+    std::vector<T> v(n);
+    if (n) f.read(reinterpret_cast<char*>(v.data()), n * sizeof(T));
+    return v;
+}
+
+/// phantom_env with a seeded CPU transport RNG, a timed transport phase and an optional
+/// Gaussian spot.  Everything else is the stock reference class.
+class oracle_phantom_env : public mqi::phantom_env<float>
+{
+public:
+    bool        gaussian = false;
+    double      transport_seconds = 0.0;
+    uint32_t    tracked = 0;
+
+    oracle_phantom_env(mqi::cli& c, bool g) : mqi::phantom_env<float>(c), gaussian(g) {}
+
+    void
+    setup_beamsource() override {
+        if (!gaussian) {
+            mqi::phantom_env<float>::setup_beamsource();
+            return;
+        }
+        // Same construction as phantom_env::setup_beamsource (mqi_phantom_env.hpp:204-232)
+        // with the Gaussian 6-D phase space.
+        mqi::coordinate_transform<float> p_coord(this->spot_angles, { 0, 0, 0 });
+        mqi::vec3<float>                 dir(0, 0, -1);
+        std::array<float, 6> beamlet_mean = { this->spot_position[0], this->spot_position[1],
+                                              this->spot_position[2], dir.x, dir.y, dir.z };
+        std::array<float, 6> beamlet_sigm = { this->spot_size[0], this->spot_size[1], 0, 0, 0, 0 };
+        std::array<float, 2> corr         = { 0.0, 0.0 };
+        auto phsp   = new mqi::phsp_6d<float>(beamlet_mean, beamlet_sigm, corr);
+        auto energy = new mqi::const_1d<float>({ this->spot_energy[0] }, { this->spot_energy[1] });
+        this->beamsource.append_beamlet(mqi::beamlet<float>(energy, phsp), this->n_histories, p_coord);
+        uint32_t h1    = this->beamsource.total_histories();
+        this->vertices = new mqi::vertex_t<float>[h1];
+        for (size_t i = 0; i < h1; ++i) {
+            auto bl           = this->beamsource(i);
+            this->vertices[i] = bl(&this->beam_rng);
+        }
+    }
+
+    void
+    run() override {
+        // CPU branch of phantom_env::run (mqi_phantom_env.hpp:302-323, 416-423).
+        uint32_t h1     = this->beamsource.total_histories();
+        this->num_spots = this->beamsource.total_beamlets();
+        uint32_t tp[1]  = { 0 };
+        std::vector<int32_t> transport_seed(h1);
+        std::default_random_engine tmp_rng;
+        tmp_rng.seed(this->random_seed);
+        for (uint32_t i = 0; i < h1; ++i)
+            transport_seed[i] = tmp_rng();
+        mc::mc_world     = this->world;
+        mc::mc_vertices  = this->vertices;
+        mc::mc_materials = this->materials;
+        mqi::thrd_t* worker_threads = new mqi::thrd_t[1];
+        worker_threads[0].rnd_generator.seed(static_cast<unsigned long>(this->random_seed) * 2654435761UL + 12345UL);
+        auto t0 = std::chrono::steady_clock::now();
+        mc::transport_particles_patient<float>(
+          worker_threads, mc::mc_world, mc::mc_vertices, mc::mc_materials, h1, tp, transport_seed.data());
+        auto t1 = std::chrono::steady_clock::now();
+        transport_seconds = std::chrono::duration<double>(t1 - t0).count();
+        tracked           = tp[0];
+        delete[] worker_threads;
+    }
+};
+
+int
+run_phantom(int argc, char** argv) {
+    bool        gaussian = false;
+    std::string json;
+    std::vector<char*> rest;
+    rest.push_back(argv[0]);
+    for (int i = 2; i < argc; ++i) {
+        if (!std::strcmp(argv[i], "--beam") && i + 1 < argc) {
+            gaussian = !std::strcmp(argv[++i], "gaussian");
+        } else if (!std::strcmp(argv[i], "--json") && i + 1 < argc) {
+            json = argv[++i];
+        } else {
+            rest.push_back(argv[i]);
+        }
+    }
+    mqi::cli cl;
+    cl.read(static_cast<int>(rest.size()), rest.data());
+    oracle_phantom_env env(cl, gaussian);
+    env.initialize();
+    env.run();
+    env.finalize();
+    env.save_reshaped_files();
+    if (!json.empty()) {
+        std::ofstream f(json);
+        f << "{\"transport_seconds\": " << env.transport_seconds << ", \"histories\": "
+          << env.beamsource.total_histories() << ", \"tracked\": " << env.tracked
+#ifdef __PHYSICS_DEBUG__
+          << ", \"physics_debug\": 1"
+#else
+          << ", \"physics_debug\": 0"
+#endif
+          << "}\n";
+    }
+    return 0;
+}
+
+/// Ray walk through a grid built with the reference's uniform-edge constructor
+/// (mqi_grid3d.hpp grid3d(xmin,xmax,nx+1,...)).  Input layout (all little-endian):
+///   f32[9] grid: xmin xmax ymin ymax zmin zmax, i32[3] n, u32 max_steps, then vec<f32> rays
+///   (6 floats per ray: pos, dir).  Output: vec<i64> offsets (n_rays+1), vec<u64> cnb,
+///   vec<f32> dist, vec<i32> cell (3 per entry).
+int
+run_raywalk(const char* in_path, const char* out_path) {
+    std::ifstream fin(in_path, std::ios::binary);
+    float  g[6];
+    int32_t n[3];
+    uint32_t max_steps;
+    fin.read(reinterpret_cast<char*>(g), sizeof(g));
+    fin.read(reinterpret_cast<char*>(n), sizeof(n));
+    fin.read(reinterpret_cast<char*>(&max_steps), sizeof(max_steps));
+    std::vector<float> rays = read_vec<float>(fin);
+    mqi::grid3d<mqi::density_t, float> geo(
+      g[0], g[1], n[0] + 1, g[2], g[3], n[1] + 1, g[4], g[5], n[2] + 1);
+    std::vector<int64_t>  off(1, 0);
+    std::vector<uint64_t> cnbs;
+    std::vector<float>    dists;
+    std::vector<int32_t>  cells;
+    const size_t n_rays = rays.size() / 6;
+    for (size_t r = 0; r < n_rays; ++r) {
+        mqi::track_t<float> track;
+        mqi::vertex_t<float> v;
+        v.ke  = 100.0f;
+        v.pos = mqi::vec3<float>(rays[6 * r + 0], rays[6 * r + 1], rays[6 * r + 2]);
+        v.dir = mqi::vec3<float>(rays[6 * r + 3], rays[6 * r + 4], rays[6 * r + 5]);
+        track.set(v);
+        // Child entry (mqi_transport.hpp:165-190).
+        track.vtx0.pos = geo.rotation_matrix_inv * (track.vtx0.pos - geo.translation_vector);
+        track.vtx0.dir = geo.rotation_matrix_inv * (track.vtx0.dir);
+        track.vtx0.dir.normalize();
+        track.vtx1.pos = track.vtx0.pos;
+        track.vtx1.dir = track.vtx0.dir;
+        mqi::vec3<mqi::ijk_t> chk = geo.index(track.vtx0.pos, track.vtx0.dir);
+        bool entered = true;
+        if (!geo.is_valid(chk)) {
+            track.its = geo.intersect(track.vtx0.pos, track.vtx0.dir);
+            if (track.its.dist < 0) {
+                entered = false;
+            } else {
+                track.update_post_vertex_position(track.its.dist);
+                track.move();
+                track.its.cell = geo.index(track.vtx0.pos, track.vtx0.dir);
+            }
+        } else {
+            track.its.dist = 0.0;
+            track.its.cell = chk;
+        }
+        uint32_t steps = 0;
+        // Voxel loop (mqi_transport.hpp:192-233) with a boundary-only step.
+        while (entered && geo.is_valid(track.its.cell) && steps < max_steps) {
+            mqi::cnb_t cnb = geo.ijk2cnb(track.its.cell);
+            track.its      = geo.intersect(track.vtx0.pos, track.vtx0.dir, track.its.cell);
+            cnbs.push_back(cnb);
+            dists.push_back(track.its.dist);
+            cells.push_back(track.its.cell.x);
+            cells.push_back(track.its.cell.y);
+            cells.push_back(track.its.cell.z);
+            ++steps;
+            if (track.its.dist < 0) break;
+            track.update_post_vertex_position(track.its.dist);
+            geo.index(track.vtx1.pos, track.vtx1.dir, track.its.cell);
+            track.move();
+        }
+        off.push_back(static_cast<int64_t>(cnbs.size()));
+    }
+    std::ofstream fout(out_path, std::ios::binary);
+    write_vec(fout, off);
+    write_vec(fout, cnbs);
+    write_vec(fout, dists);
+    write_vec(fout, cells);
+    return 0;
+}
+
+/// Deterministic physics tables.  Output: a sequence of named f32 vectors.
+int
+run_physics(const char* out_path) {
+    mqi::fippel_physics<float>       fp;
+    mqi::patient_material_t<float>   pm;
+    mqi::material_t<float>*          mat = &pm;
+    std::ofstream                    fout(out_path, std::ios::binary);
+    // Energy grid: dense regular grid plus the table nodes themselves and values just around them.
+    std::vector<float> E;
+    for (int i = 0; i <= 6100; ++i)
+        E.push_back(0.02f + 0.05f * i);   // 0.02 .. 305.02 MeV
+    for (int i = 0; i < 600; ++i) {
+        E.push_back(0.1f + 0.5f * i);
+        E.push_back(0.5f + 0.5f * i);
+        E.push_back(std::nextafter(0.5f + 0.5f * i, 0.0f));
+    }
+    const float rhos[] = { 0.0000012f, 0.00026f, 0.0003068f, 0.0009f, 0.00098822f, 0.001f,
+                           0.0010005f, 0.00103f, 0.0017939f, 0.0025f };
+    std::vector<float> rho_v(std::begin(rhos), std::end(rhos));
+    write_vec(fout, E);
+    write_vec(fout, rho_v);
+    std::vector<float> beta_sq, gamma, te_max, et, mom;
+    std::vector<float> cs_ion, cs_pp, cs_poe, cs_poi, dedx;
+    for (float e : E) {
+        mqi::relativistic_quantities<float> rel(e, 938.272046f);
+        beta_sq.push_back(rel.beta_sq);
+        gamma.push_back(rel.gamma);
+        te_max.push_back(rel.Te_max);
+        et.push_back(rel.Et);
+        mom.push_back(rel.momentum());
+        cs_ion.push_back(fp.p_ion.cross_section(rel, mat, 1.0f));
+        cs_pp.push_back(fp.pp_e.cross_section(rel, mat, 1.0f));
+        cs_poe.push_back(fp.po_e.cross_section(rel, mat, 1.0f));
+        cs_poi.push_back(fp.po_i.cross_section(rel, mat, 1.0f));
+        dedx.push_back(fp.p_ion.dEdx(rel, mat));
+    }
+    write_vec(fout, beta_sq);
+    write_vec(fout, gamma);
+    write_vec(fout, te_max);
+    write_vec(fout, et);
+    write_vec(fout, mom);
+    write_vec(fout, cs_ion);
+    write_vec(fout, cs_pp);
+    write_vec(fout, cs_poe);
+    write_vec(fout, cs_poi);
+    write_vec(fout, dedx);
+    // SPR(rho, E) and X0(rho) on the rho set x energy grid (every 10th energy).
+    std::vector<float> spr, x0, strag;
+    for (float r : rho_v) {
+        for (size_t i = 0; i < E.size(); i += 10) {
+            spr.push_back(mat->compute_rsp_(r, E[i]));
+        }
+        x0.push_back(mat->compute_rl_(r, 0.001f, 360.863f));
+        for (size_t i = 0; i < E.size(); i += 10) {
+            mqi::relativistic_quantities<float> rel(E[i], 938.272046f);
+            strag.push_back(fp.p_ion.energy_straggling(rel, mat, 1.0f, r));
+        }
+    }
+    write_vec(fout, spr);
+    write_vec(fout, x0);
+    write_vec(fout, strag);
+    // HU -> density for every HU in [-1100, 3100].
+    std::vector<float> hu_rho;
+    for (int hu = -1100; hu <= 3100; ++hu)
+        hu_rho.push_back(pm.hu_to_density(static_cast<int16_t>(hu)));
+    write_vec(fout, hu_rho);
+    return 0;
+}
+
+/// Sampling probes.  A small water grid hosts the track so that the daughters' coordinate
+/// transforms have a node.  Output: named f32 vectors (see the list at the end).
+int
+run_sample(const char* out_path, long n, unsigned seed) {
+    mqi::fippel_physics<float>     fp;
+    mqi::patient_material_t<float> pm;
+    mqi::material_t<float>*        mat = &pm;
+    mqi::grid3d<mqi::density_t, float> geo(-50.f, 50.f, 101, -50.f, 50.f, 101, -50.f, 50.f, 101);
+    mqi::node_t<float> node;
+    node.geo = &geo;
+    mqi::mqi_rng rng;
+    rng.seed(seed);
+    const float rho = 0.001f;
+    std::ofstream fout(out_path, std::ios::binary);
+    auto make_track = [&](float ke) {
+        mqi::vertex_t<float> v;
+        v.ke  = ke;
+        v.pos = mqi::vec3<float>(0.f, 0.f, 0.f);
+        v.dir = mqi::vec3<float>(0.f, 0.f, -1.f);
+        mqi::track_t<float> t(v);
+        t.c_node = &node;
+        return t;
+    };
+    const float energies[] = { 10.0f, 50.0f, 150.0f };
+    for (float ke : energies) {
+        // along_step over 1 mm: energy loss and polar deflection.
+        std::vector<float> dE, cth;
+        for (long i = 0; i < n; ++i) {
+            mqi::track_t<float>       t = make_track(ke);
+            mqi::track_stack_t<float> stk;
+            fp.p_ion.along_step(t, stk, &rng, 1.0f, mat, rho);
+            dE.push_back(t.vtx0.ke - t.vtx1.ke);
+            cth.push_back(-t.vtx1.dir.z);
+        }
+        write_vec(fout, dE);
+        write_vec(fout, cth);
+        // Delta-ray energy (p_ion post_step).
+        std::vector<float> te;
+        for (long i = 0; i < n; ++i) {
+            mqi::track_t<float>       t = make_track(ke);
+            mqi::track_stack_t<float> stk;
+            fp.p_ion.post_step(t, stk, &rng, 1.0f, mat, true);
+            te.push_back(t.vtx0.ke - t.vtx1.ke);
+        }
+        write_vec(fout, te);
+        // p-p elastic: energy transfer, primary polar cosine, daughter polar cosine.
+        std::vector<float> pp_de, pp_c3, pp_c4;
+        for (long i = 0; i < n; ++i) {
+            mqi::track_t<float>       t = make_track(ke);
+            mqi::track_stack_t<float> stk;
+            fp.pp_e.post_step(t, stk, &rng, 1.0f, mat, true);
+            pp_de.push_back(t.vtx0.ke - t.vtx1.ke);
+            pp_c3.push_back(-t.vtx1.dir.z);
+            pp_c4.push_back(stk.idx > 0 ? -stk.tracks[stk.idx - 1].vtx1.dir.z : 2.0f);
+        }
+        write_vec(fout, pp_de);
+        write_vec(fout, pp_c3);
+        write_vec(fout, pp_c4);
+        // p-O elastic: energy transfer and primary polar cosine.
+        std::vector<float> poe_de, poe_c3;
+        for (long i = 0; i < n; ++i) {
+            mqi::track_t<float>       t = make_track(ke);
+            mqi::track_stack_t<float> stk;
+            fp.po_e.post_step(t, stk, &rng, 1.0f, mat, true);
+            poe_de.push_back(t.vtx0.ke - t.vtx1.ke);
+            poe_c3.push_back(-t.vtx1.dir.z);
+        }
+        write_vec(fout, poe_de);
+        write_vec(fout, poe_c3);
+        // p-O inelastic: number of proton secondaries, their summed energy, energy deposited
+        // by the primary (Er).
+        std::vector<float> poi_n, poi_e2, poi_dep;
+        for (long i = 0; i < n; ++i) {
+            mqi::track_t<float>       t = make_track(ke);
+            mqi::track_stack_t<float> stk;
+            fp.po_i.post_step(t, stk, &rng, 1.0f, mat, true);
+            int   np = 0;
+            float e2 = 0.f;
+            for (int k = 0; k < stk.idx; ++k) {
+                if (stk.tracks[k].vtx1.ke > 0.f) {   // proton secondaries carry ke in vtx1
+                    ++np;
+                    e2 += stk.tracks[k].vtx1.ke;
+                }
+            }
+            poi_n.push_back(static_cast<float>(np));
+            poi_e2.push_back(e2);
+            poi_dep.push_back(t.dE);
+        }
+        write_vec(fout, poi_n);
+        write_vec(fout, poi_e2);
+        write_vec(fout, poi_dep);
+    }
+    return 0;
+}
+
+}   // namespace
+
+int
+main(int argc, char** argv) {
+    if (argc < 2) {
+        std::fprintf(stderr, "usage: %s phantom|raywalk|physics|sample ...\n", argv[0]);
+        return 2;
+    }
+    const std::string mode = argv[1];
+    if (mode == "phantom") return run_phantom(argc, argv);
+    if (mode == "raywalk" && argc >= 4) return run_raywalk(argv[2], argv[3]);
+    if (mode == "physics" && argc >= 3) return run_physics(argv[2]);
+    if (mode == "sample" && argc >= 5)
+        return run_sample(argv[2], std::atol(argv[3]), static_cast<unsigned>(std::atol(argv[4])));
+    std::fprintf(stderr, "bad arguments\n");
+    return 2;
+}
