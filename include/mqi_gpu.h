@@ -77,6 +77,9 @@ typedef struct {
     uint64_t dropped;          /* daughters dropped by the emulated stack limit                */
     uint64_t waves;            /* queue generations processed                                  */
     uint64_t device_errors;    /* bounded device loops that gave up                            */
+    uint64_t kernel_launches;  /* engine kernels launched by mqi_transport                     */
+    uint64_t wave_launches;    /* launches of the transport wave kernel                        */
+    double   wave_ms;          /* summed CUDA-event time of the wave kernel launches           */
 } mqi_stats;
 
 typedef struct mqi_ctx mqi_ctx;
@@ -164,6 +167,14 @@ int mqi_trace_rays(mqi_ctx* ctx, int child_id, const float* rays, uint64_t n_ray
  * For each energy E[i]: out[i*8 + {0..7}] = {cs_ion, cs_pp, cs_poe, cs_poi (per g/mm^3),
  * dEdx (negative, MeV/mm in water), beta^2, Te_max, momentum}. */
 int mqi_eval_physics(mqi_ctx* ctx, const float* energies, uint64_t n, float* out);
+
+/* Launch shape of the transport (no counterpart in moqui, whose launch is fixed at 512 threads per
+ * block).  block: threads per block (multiple of 32, <= 256); blocks_per_sm: resident blocks per
+ * SM the wave kernel is launched with; slice_steps: voxel steps a track takes before it is
+ * re-queued (0 = run each track to completion); primary_chunk: primaries loaded per queue
+ * generation.  block, blocks_per_sm and primary_chunk keep their values when <= 0, slice_steps
+ * when < 0.  Results do not depend on any of these. */
+int mqi_set_tuning(mqi_ctx* ctx, int block, int blocks_per_sm, int slice_steps, int primary_chunk);
 
 /* Library version string. */
 const char* mqi_version(void);

@@ -32,7 +32,7 @@ EXPORTS = (
     "mqi_create", "mqi_destroy", "mqi_last_error", "mqi_set_stream", "mqi_set_physics",
     "mqi_add_child", "mqi_set_density", "mqi_set_hu", "mqi_add_scorer", "mqi_set_vertices",
     "mqi_transport", "mqi_get_tally", "mqi_reset_tallies", "mqi_get_stats", "mqi_hu_to_density",
-    "mqi_trace_rays", "mqi_eval_physics", "mqi_version",
+    "mqi_trace_rays", "mqi_eval_physics", "mqi_set_tuning", "mqi_version",
 )
 
 VERTEX_DTYPE = np.dtype([("ke", "<f4"), ("pos", "<f4", (3,)), ("dir", "<f4", (3,))])
@@ -41,10 +41,10 @@ VERTEX_DTYPE = np.dtype([("ke", "<f4"), ("pos", "<f4", (3,)), ("dir", "<f4", (3,
 class MqiStats(C.Structure):
     _fields_ = [(n, C.c_uint64) for n in (
         "histories", "tracks", "steps", "secondaries", "local_daughters", "dropped", "waves",
-        "device_errors")]
+        "device_errors", "kernel_launches", "wave_launches")] + [("wave_ms", C.c_double)]
 
     def as_dict(self) -> dict:
-        return {n: int(getattr(self, n)) for n, _ in self._fields_}
+        return {n: (float if n == "wave_ms" else int)(getattr(self, n)) for n, _ in self._fields_}
 
 
 class MqiError(RuntimeError):
@@ -89,6 +89,7 @@ def load(path: Optional[str] = None) -> C.CDLL:
         "mqi_hu_to_density": (i32, [vp, vp, vp, u64, f32, i32]),
         "mqi_trace_rays": (i32, [vp, i32, vp, u64, u32, vp, vp, vp, vp, u64, P(u64)]),
         "mqi_eval_physics": (i32, [vp, vp, u64, vp]),
+        "mqi_set_tuning": (i32, [vp, i32, i32, i32, i32]),
         "mqi_version": (C.c_char_p, []),
     }
     for name, (res, args) in sig.items():
@@ -139,6 +140,9 @@ class Context:
     # ---- setup ----
     def set_physics(self, physics_debug: bool, score_local_deposit: bool = True) -> None:
         self._check(self.lib.mqi_set_physics(self.h, int(physics_debug), int(score_local_deposit)), self.h)
+
+    def set_tuning(self, block: int = 0, blocks_per_sm: int = 0, slice_steps: int = -1, primary_chunk: int = 0) -> None:
+        self._check(self.lib.mqi_set_tuning(self.h, block, blocks_per_sm, slice_steps, primary_chunk), self.h)
 
     def set_stream(self, stream_ptr: Optional[int]) -> None:
         self._check(self.lib.mqi_set_stream(self.h, stream_ptr), self.h)
@@ -239,3 +243,12 @@ class Context:
         out = np.empty((len(e), 8), dtype=np.float32)
         self._check(self.lib.mqi_eval_physics(self.h, _ptr(e), len(e), _ptr(out)), self.h)
         return out
+
+    # ---- raw-pointer variants (pinned host or device buffers owned by the caller) ----
+    def set_vertices_ptr(self, ptr: int, n: int, on_device: bool) -> None:
+        self._check(self.lib.mqi_set_vertices(self.h, C.c_void_p(ptr), None, n, int(on_device)), self.h)
+        self.n_vertices = n
+
+    def tally_to_ptr(self, scorer: int, ptr: int, on_device: bool) -> None:
+        n = C.c_uint64(0)
+        self._check(self.lib.mqi_get_tally(self.h, scorer, C.c_void_p(ptr), C.byref(n), int(on_device)), self.h)

@@ -81,6 +81,10 @@ struct mqi_ctx {
     uint32_t                max_slice_steps = 0;
     uint32_t                primary_chunk = 1u << 21;
     uint64_t                waves = 0;
+    uint64_t                kernel_launches = 0;
+    uint64_t                wave_launches = 0;
+    double                  wave_ms = 0.0;
+    cudaEvent_t             ev0 = nullptr, ev1 = nullptr;
 };
 
 namespace
@@ -205,7 +209,8 @@ mqi_create(int device, mqi_ctx** out) {
         (e = cudaMemset(c->counters, 0, 8 * sizeof(uint32_t))) != cudaSuccess ||
         (e = cudaMalloc(&c->stats, 8 * sizeof(unsigned long long))) != cudaSuccess ||
         (e = cudaMemset(c->stats, 0, 8 * sizeof(unsigned long long))) != cudaSuccess ||
-        (e = cudaMallocHost(&c->host_counts, 8 * sizeof(uint32_t))) != cudaSuccess) {
+        (e = cudaMallocHost(&c->host_counts, 8 * sizeof(uint32_t))) != cudaSuccess ||
+        (e = cudaEventCreate(&c->ev0)) != cudaSuccess || (e = cudaEventCreate(&c->ev1)) != cudaSuccess) {
         mqi_destroy(c);
         return cuda_fail(nullptr, e, "mqi_create: allocation");
     }
@@ -233,6 +238,8 @@ mqi_destroy(mqi_ctx* c) {
     cudaFree(c->stats);
     cudaFree(c->tables);
     if (c->host_counts) cudaFreeHost(c->host_counts);
+    if (c->ev0) cudaEventDestroy(c->ev0);
+    if (c->ev1) cudaEventDestroy(c->ev1);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
     delete c;
     return MQI_OK;
@@ -252,6 +259,25 @@ mqi_set_stream(mqi_ctx* c, void* s) {
     } else {
         MQI_CUDA(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking), "mqi_set_stream");
         c->own_stream = true;
+    }
+    return MQI_OK;
+}
+
+int
+mqi_set_tuning(mqi_ctx* c, int block, int blocks_per_sm, int slice_steps, int primary_chunk) {
+    if (!valid_ctx(c)) return fail(c, MQI_ERR_INVALID, "mqi_set_tuning: ctx is NULL");
+    if (block > 0) {
+        if (block % 32 != 0 || block > 256) return fail(c, MQI_ERR_INVALID, "mqi_set_tuning: block must be a multiple of 32, <= 256");
+        c->wave_block = block;
+    }
+    if (blocks_per_sm > 0) {
+        if (blocks_per_sm > 64) return fail(c, MQI_ERR_INVALID, "mqi_set_tuning: blocks_per_sm must be <= 64");
+        c->wave_grid = c->num_sms * blocks_per_sm;
+    }
+    if (slice_steps >= 0) c->max_slice_steps = (uint32_t) slice_steps;
+    if (primary_chunk > 0) {
+        if (primary_chunk > (1 << 24)) return fail(c, MQI_ERR_INVALID, "mqi_set_tuning: primary_chunk must be <= 2^24");
+        c->primary_chunk = (uint32_t) primary_chunk;
     }
     return MQI_OK;
 }
@@ -506,11 +532,13 @@ mqi_transport(mqi_ctx* c, uint64_t h0, uint64_t h1, uint64_t seed) {
     P.stats           = c->stats;
     P.spot_ids        = c->has_spots ? c->spot_ids : nullptr;
     P.tables          = c->tables;
+    MQI_CUDA(c, cudaMemsetAsync(c->counters + 3, 0, sizeof(uint32_t), c->stream), "mqi_transport");
     QueueBuf* A = &c->qa;
     QueueBuf* B = &c->qb;
     for (uint64_t h = h0; h < h1; h += chunk) {
         const uint32_t n = (uint32_t) std::min<uint64_t>(chunk, h1 - h);
         MQI_CUDA(c, launch_load_primaries(A->q, c->vertices, h, n, c->stream), "mqi_transport: load primaries");
+        ++c->kernel_launches;
         c->host_counts[0] = n;
         MQI_CUDA(c, cudaMemcpyAsync(c->counters + 0, c->host_counts, sizeof(uint32_t), cudaMemcpyHostToDevice, c->stream),
                  "mqi_transport");
@@ -523,11 +551,17 @@ mqi_transport(mqi_ctx* c, uint64_t h0, uint64_t h1, uint64_t seed) {
             P.n_out = c->counters + (1 - cur);
             MQI_CUDA(c, cudaMemsetAsync(c->counters + (1 - cur), 0, sizeof(uint32_t), c->stream), "mqi_transport");
             MQI_CUDA(c, cudaMemsetAsync(c->counters + 2, 0, sizeof(uint32_t), c->stream), "mqi_transport");
+            MQI_CUDA(c, cudaEventRecord(c->ev0, c->stream), "mqi_transport");
             MQI_CUDA(c, launch_wave(P, c->wave_grid, c->wave_block, c->stream), "mqi_transport: wave");
+            MQI_CUDA(c, cudaEventRecord(c->ev1, c->stream), "mqi_transport");
             MQI_CUDA(c, cudaMemcpyAsync(c->host_counts, c->counters, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream),
                      "mqi_transport");
             MQI_CUDA(c, cudaStreamSynchronize(c->stream), "mqi_transport: wave");
             ++c->waves;
+            ++c->kernel_launches;
+            ++c->wave_launches;
+            float ms = 0.0f;
+            if (cudaEventElapsedTime(&ms, c->ev0, c->ev1) == cudaSuccess) c->wave_ms += ms;
             if (c->host_counts[3] & 2u) return fail(c, MQI_ERR_OVERFLOW, "mqi_transport: particle queue overflow");
             const uint32_t n_next = c->host_counts[1 - cur];
             if (n_next == 0) break;
@@ -563,6 +597,9 @@ mqi_reset_tallies(mqi_ctx* c) {
     MQI_CUDA(c, cudaMemsetAsync(c->counters + 3, 0, sizeof(uint32_t), c->stream), "mqi_reset_tallies");
     MQI_CUDA(c, cudaStreamSynchronize(c->stream), "mqi_reset_tallies");
     c->waves = 0;
+    c->kernel_launches = 0;
+    c->wave_launches = 0;
+    c->wave_ms = 0.0;
     return MQI_OK;
 }
 
@@ -581,6 +618,9 @@ mqi_get_stats(mqi_ctx* c, mqi_stats* out) {
     out->dropped         = v[5];
     out->waves           = c->waves;
     out->device_errors   = v[7];
+    out->kernel_launches = c->kernel_launches;
+    out->wave_launches   = c->wave_launches;
+    out->wave_ms         = c->wave_ms;
     return MQI_OK;
 }
 

@@ -165,7 +165,12 @@ struct Rel {
         Et_sq               = Et * Et;
         gamma               = Et / kMp;
         gamma_sq            = gamma * gamma;
-        beta_sq             = 1.0f - 1.0f / gamma_sq;
+        // The reference evaluates 1 - 1/gamma^2 in double (1.0 is a double literal); a float
+        // quotient would lose ~1e-3 relative at 0.02 MeV.  r + e*r recovers the quotient to about
+        // 2^-46 (e is the exact residual of the rounded reciprocal), and 1 - r is exact.
+        const float r       = 1.0f / gamma_sq;
+        const float e       = fmaf(-r, gamma_sq, 1.0f);
+        beta_sq             = (1.0f - r) - e * r;
         Te_max              = (2.0f * kMe * beta_sq * gamma_sq) / (1.0f + 2.0f * gamma * MeMp + MeMp_sq);
     }
     __host__ __device__ inline float

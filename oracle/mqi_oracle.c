@@ -89,7 +89,7 @@ static rel_t rel_of(float ek) {
     r.Et_sq = r.Et * r.Et;
     r.gamma = r.Et / MP;
     r.gamma_sq = r.gamma * r.gamma;
-    r.beta_sq = 1.0f - 1.0f / r.gamma_sq;
+    r.beta_sq = (float) (1.0 - 1.0 / (double) r.gamma_sq);   /* double intermediate, as the reference */
     r.Te_max = (2.0f * ME * r.beta_sq * r.gamma_sq) / (1.0f + 2.0f * r.gamma * MeMp + MeMp_sq);
     return r;
 }

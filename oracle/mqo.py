@@ -196,10 +196,15 @@ def ref_phantom_parallel(debug: bool, lxyz, pxyz, nxyz, energy, position, size, 
         os.makedirs(od, exist_ok=True)
         dirs.append(od)
         cmd = ref_phantom_cmd(debug, lxyz, pxyz, nxyz, energy, position, size, histories_each, ph, od, seed0 + p, beam)
-        procs.append(subprocess.Popen(cmd, stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL))
+        log = open(os.path.join(od, "log.txt"), "w")
+        procs.append(subprocess.Popen(cmd, stdout=log, stderr=subprocess.STDOUT))
+        log.close()
     rcs = [q.wait() for q in procs]
     if any(rcs):
-        raise RuntimeError(f"reference oracle failed: {rcs}")
+        bad = [i for i, r in enumerate(rcs) if r]
+        with open(os.path.join(dirs[bad[0]], "log.txt"), errors="replace") as f:
+            tail = f.read()[-3000:]
+        raise RuntimeError(f"reference oracle failed: {rcs}\n{tail}")
     n = int(np.prod(nxyz))
     doses, recs = [], []
     for od in dirs:

@@ -24,7 +24,10 @@
 #include <moqui/kernel_functions/mqi_transport.hpp>
 
 #include <chrono>
+#include <csignal>
 #include <cstdio>
+#include <execinfo.h>
+#include <unistd.h>
 #include <cstring>
 #include <fstream>
 #include <string>
@@ -398,8 +401,21 @@ run_sample(const char* out_path, long n, unsigned seed) {
 
 }   // namespace
 
+void
+on_fatal_signal(int sig) {
+    void* frames[64];
+    const int n = backtrace(frames, 64);
+    const char msg[] = "ref_driver: fatal signal, backtrace:\n";
+    (void) !write(2, msg, sizeof(msg) - 1);
+    backtrace_symbols_fd(frames, n, 2);
+    std::signal(sig, SIG_DFL);
+    std::raise(sig);
+}
+
 int
 main(int argc, char** argv) {
+    std::signal(SIGSEGV, on_fatal_signal);
+    std::signal(SIGABRT, on_fatal_signal);
     if (argc < 2) {
         std::fprintf(stderr, "usage: %s phantom|raywalk|physics|sample ...\n", argv[0]);
         return 2;

@@ -1,0 +1,57 @@
+"""The C ABI library loads and exports every entry point include/mqi_gpu.h declares (no GPU work)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    with open(os.path.join(ROOT, "include", "mqi_gpu.h")) as f:
+        text = f.read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(mqi_[a-z_0-9]+)\s*\(", text)))
+
+
+def test_header_declares_expected_entry_points():
+    names = declared_functions()
+    for must in ("mqi_create", "mqi_transport", "mqi_get_tally", "mqi_set_vertices", "mqi_trace_rays"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol(built_lib):
+    missing = [n for n in declared_functions() if not hasattr(built_lib, n)]
+    assert not missing, missing
+
+
+def test_binding_covers_every_declared_symbol(built_lib):
+    from moquimc_gb300 import capi
+
+    assert set(declared_functions()) <= set(capi.EXPORTS)
+
+
+def test_version_string(built_lib):
+    assert b"sm_103a" in built_lib.mqi_version()
+
+
+def test_errors_are_status_codes_not_exits(built_lib):
+    """Bad arguments come back as negative codes with a message (moqui calls exit() instead)."""
+    lib = built_lib
+    assert lib.mqi_create(0, None) == -1
+    assert b"NULL" in lib.mqi_last_error(None)
+    assert lib.mqi_transport(None, 0, 1, 0) == -1
+    assert lib.mqi_set_physics(None, 1, 1) == -1
+
+
+def test_create_without_device_fails_cleanly(built_lib):
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    h = ctypes.c_void_p()
+    rc = built_lib.mqi_create(0, ctypes.byref(h))
+    assert rc in (-1, -2)
+    assert h.value is None
+    assert built_lib.mqi_last_error(None)

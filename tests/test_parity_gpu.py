@@ -1,0 +1,237 @@
+"""GPU parity tests: the CUDA path, called through the C ABI, against the golden vectors of the
+reference's own CPU build and against the C restatement run on the same random streams.
+
+Tolerances:
+* integer/index work (voxel walks, HU -> density): bit-exact;
+* tabulated physics: identical table lookups, <= 2e-6 relative where the reference uses double
+  intermediates;
+* dose (FP32 stepping, FP64 tally) vs the reference: per depth bin within 2% or 3 sigma of the
+  combined statistical uncertainty in bins above 10% of the maximum (>= 95% of bins), R80 within
+  0.2 mm;
+* GPU vs the C restatement on identical Philox streams: total energy within 1e-4, and at least 99%
+  of the dose in voxels that agree to 1e-3 (rare FP32 ulp differences in libm functions can flip
+  a branch of a single history).
+"""
+import numpy as np
+import pytest
+
+from moquimc_gb300 import capi
+from moquimc_gb300 import phantom as ph
+from moquimc_gb300 import workloads
+
+pytestmark = pytest.mark.gpu
+
+
+def _ctx_for(wl, make, scorer=capi.DOSE_W):
+    c = make()
+    c.set_physics(wl.physics_debug)
+    cid = c.add_child(*wl.edges())
+    c.set_hu(cid, wl.hu)
+    sid = c.add_scorer(cid, scorer)
+    return c, cid, sid
+
+
+@pytest.mark.parametrize("name", ["phantom", "ct"])
+def test_raywalk_gpu_bit_exact(golden, gpu_ctx_factory, name):
+    g = golden("raywalk.npz")
+    b, n = g[f"{name}_bounds"], g[f"{name}_n"]
+    edges = [ph.uniform_edges(float(b[2 * a]), float(b[2 * a + 1]), int(n[a])) for a in range(3)]
+    c = gpu_ctx_factory()
+    cid = c.add_child(*edges)
+    off, cnb, dist, cells = c.trace_rays(cid, g[f"{name}_rays"], int(g[f"{name}_max_steps"]))
+    np.testing.assert_array_equal(off, g[f"{name}_offsets"])
+    np.testing.assert_array_equal(cnb.astype(np.uint32), g[f"{name}_cnb"])
+    np.testing.assert_array_equal(dist.view(np.uint32), g[f"{name}_dist_bits"])
+    nx, ny = int(n[0]), int(n[1])
+    np.testing.assert_array_equal(cells[:, 0] + nx * (cells[:, 1] + ny * cells[:, 2]), cnb.astype(np.int64))
+
+
+def test_physics_probe_gpu(golden, gpu_ctx_factory):
+    p = golden("physics.npz")
+    c = gpu_ctx_factory()
+    out = c.eval_physics(p["energies"])
+    for k, name in enumerate(["cs_ion", "cs_pp", "cs_poe", "cs_poi", "dedx"]):
+        np.testing.assert_allclose(out[:, k], p[name], rtol=1e-6, atol=0, err_msg=name)
+        assert np.mean(out[:, k] == p[name]) > 0.99, name
+    np.testing.assert_allclose(out[:, 5], p["beta_sq"], rtol=2e-6, atol=1e-9)
+    np.testing.assert_allclose(out[:, 6], p["te_max"], rtol=2e-6, atol=1e-12)
+    np.testing.assert_allclose(out[:, 7], p["momentum"], rtol=1e-6)
+
+
+def test_hu_to_density_gpu_bit_exact(golden, gpu_ctx_factory):
+    p = golden("physics.npz")
+    c = gpu_ctx_factory()
+    rho = c.hu_to_density(p["hu"].astype(np.int16))
+    np.testing.assert_array_equal(rho.view(np.uint32), p["hu_rho"].view(np.uint32))
+    rho2 = c.hu_to_density(p["hu"].astype(np.int16), scale=1.035)
+    np.testing.assert_array_equal(rho2, (p["hu_rho"] * np.float32(1.035)).astype(np.float32))
+
+
+def _oracle_grid(oracle, wl):
+    lut = {int(h): oracle.hu_to_density(int(h)) for h in np.unique(wl.hu)}
+    rho = np.vectorize(lut.get)(wl.hu).astype(np.float32).reshape(-1)
+    return oracle.Grid(*wl.edges(), rho)
+
+
+@pytest.mark.parametrize("wname", ["c1", "c2"])
+def test_gpu_matches_oracle_on_same_streams(oracle, gpu_ctx_factory, wname):
+    wl = workloads.WORKLOADS[wname](histories=400)
+    n, seed = 400, 0xC0FFEE
+    v = wl.vertices(n, 11)
+    c, cid, sid = _ctx_for(wl, gpu_ctx_factory, capi.EDEP)
+    c.set_vertices(v)
+    c.transport(0, n, seed)
+    gpu = c.tally(sid)
+    st = c.stats()
+    ora, _, ost = oracle.transport(_oracle_grid(oracle, wl), v, 0, n, seed, wl.physics_debug, scorer=1)
+    assert st["histories"] == n == ost["histories"]
+    assert abs(gpu.sum() - ora.sum()) <= 1e-4 * ora.sum()
+    close = np.abs(gpu - ora) <= 1e-3 * np.maximum(np.abs(ora), 1e-30)
+    assert ora[close].sum() >= 0.99 * ora.sum()
+    assert abs(st["steps"] - ost["steps"]) <= 0.005 * ost["steps"]
+    assert st["dropped"] == ost["dropped"]
+
+
+def _gpu_idd_batches(wl, make, batches, each, seed0):
+    c, cid, sid = _ctx_for(wl, make)
+    out, coarse = [], []
+    for b in range(batches):
+        c.reset()
+        c.set_vertices(wl.vertices(each, seed0 + b))
+        c.transport(0, each, seed0 * 7919 + b)
+        d = c.tally(sid)
+        out.append(ph.depth_dose(d, wl.nxyz) / each)
+        coarse.append(d)
+    return np.array(out), coarse
+
+
+def _coarse(d, nxyz, b):
+    nx, ny, nz = nxyz
+    return d.reshape(nz, ny, nx).reshape(nz // b[2], b[2], ny // b[1], b[1], nx // b[0], b[0]).sum(axis=(1, 3, 5))
+
+
+@pytest.mark.parametrize("wname,fixture", [("c1", "dose_c1.npz"), ("c2", "dose_c2.npz")])
+def test_gpu_dose_matches_reference(golden, gpu_ctx_factory, wname, fixture):
+    gd = golden(fixture)
+    wl = workloads.WORKLOADS[wname]()
+    each = int(gd["histories_per_batch"])
+    idd, doses = _gpu_idd_batches(wl, gpu_ctx_factory, 8, each, 2024)
+    ref = gd["idd"]
+    rm, rs = ref.mean(0), ref.std(0, ddof=1) / np.sqrt(len(ref))
+    tm, ts = idd.mean(0), idd.std(0, ddof=1) / np.sqrt(len(idd))
+    sel = rm > 0.1 * rm.max()
+    ok = (np.abs(tm - rm) <= 0.02 * rm) | (np.abs(tm - rm) <= 3 * np.sqrt(rs ** 2 + ts ** 2))
+    assert ok[sel].mean() >= 0.95, ok[sel].mean()
+    dz = wl.lxyz[2] / wl.nxyz[2]
+    assert abs(ph.r80(tm, dz) - ph.r80(rm, dz)) <= 0.2, (ph.r80(tm, dz), ph.r80(rm, dz))
+    # per-voxel (coarse bins) dose
+    b = tuple(int(x) for x in gd["coarse_bins"])
+    gc = np.array([_coarse(d, wl.nxyz, b) / each for d in doses])
+    rc = gd["coarse"]
+    gm, gs = gc.mean(0), gc.std(0, ddof=1) / np.sqrt(len(gc))
+    cm, cs = rc.mean(0), rc.std(0, ddof=1) / np.sqrt(len(rc))
+    sel = cm > 0.1 * cm.max()
+    ok = (np.abs(gm - cm) <= 0.02 * cm) | (np.abs(gm - cm) <= 3 * np.sqrt(gs ** 2 + cs ** 2))
+    assert ok[sel].mean() >= 0.95, ok[sel].mean()
+
+
+def test_slicing_and_launch_shape_do_not_change_results(gpu_ctx_factory):
+    wl = workloads.c1()
+    n = 3000
+    v = wl.vertices(n, 5)
+    res = []
+    for tune in ({}, {"slice_steps": 37}, {"block": 128, "blocks_per_sm": 4, "slice_steps": 5}):
+        c, cid, sid = _ctx_for(wl, gpu_ctx_factory)
+        if tune:
+            c.set_tuning(**tune)
+        c.set_vertices(v)
+        c.transport(0, n, 99)
+        res.append((c.tally(sid), c.stats()))
+    base, st0 = res[0]
+    for d, st in res[1:]:
+        np.testing.assert_allclose(d, base, rtol=1e-9, atol=1e-300)
+        assert st["steps"] == st0["steps"] and st["histories"] == n
+
+
+def test_chunked_primaries_match_single_chunk(gpu_ctx_factory):
+    wl = workloads.c2(histories=5000)
+    n = 5000
+    v = wl.vertices(n, 6)
+    out = []
+    for chunk in (0, 777):
+        c, cid, sid = _ctx_for(wl, gpu_ctx_factory)
+        if chunk:
+            c.set_tuning(primary_chunk=chunk)
+        c.set_vertices(v)
+        c.transport(0, n, 4242)
+        out.append(c.tally(sid))
+    np.testing.assert_allclose(out[1], out[0], rtol=1e-9, atol=1e-300)
+
+
+def test_history_ranges_add_up(gpu_ctx_factory):
+    """transport(0, n) equals transport(0, k) + transport(k, n): histories are independent."""
+    wl = workloads.c1()
+    n = 2000
+    v = wl.vertices(n, 8)
+    c, cid, sid = _ctx_for(wl, gpu_ctx_factory)
+    c.set_vertices(v)
+    c.transport(0, n, 5)
+    whole = c.tally(sid)
+    c.reset()
+    c.transport(0, 700, 5)
+    c.transport(700, n, 5)
+    np.testing.assert_allclose(c.tally(sid), whole, rtol=1e-9, atol=1e-300)
+
+
+def test_edge_cases(gpu_ctx_factory):
+    wl = workloads.c1()
+    c, cid, sid = _ctx_for(wl, gpu_ctx_factory)
+    v = wl.vertices(64, 1)
+    c.set_vertices(v)
+    c.transport(5, 5, 1)                      # empty range is a no-op
+    assert c.tally(sid).sum() == 0.0
+    miss = v.copy()
+    miss["pos"][:, 0] = 500.0                 # beam line outside the phantom: no dose
+    c.set_vertices(miss)
+    c.transport(0, 64, 1)
+    assert c.tally(sid).sum() == 0.0
+    assert c.stats()["histories"] == 64
+    inside = v.copy()
+    inside["pos"][:, 2] = -100.0              # starts inside the grid
+    c.set_vertices(inside)
+    c.transport(0, 64, 1)
+    idd = ph.depth_dose(c.tally(sid), wl.nxyz)
+    assert idd[:99].sum() == 0.0 and idd[100:].sum() > 0.0
+    with pytest.raises(capi.MqiError):
+        c.transport(0, 65, 1)                 # beyond the vertices
+    with pytest.raises(capi.MqiError):
+        c.add_scorer(7, capi.DOSE_W)          # no such child
+    with pytest.raises(capi.MqiError):
+        c.add_scorer(cid, 99)                 # unknown plug-in
+    c.reset()
+    assert c.tally(sid).sum() == 0.0 and c.stats()["histories"] == 0
+
+
+def test_queue_overflow_is_reported(gpu_ctx_factory):
+    """A queue sized below what a generation needs is detected on the device (bounds-checked
+    append) and reported as MQI_ERR_OVERFLOW; nothing is written out of bounds."""
+    wl = workloads.c1()
+    c, cid, sid = _ctx_for(wl, gpu_ctx_factory)
+    c.set_physics(False)
+    c.set_tuning(primary_chunk=1)             # queue capacity 3 tracks
+    v = wl.vertices(2000, 2)
+    c.set_vertices(v)
+    with pytest.raises(capi.MqiError) as e:
+        c.transport(0, 2000, 3)
+    assert e.value.code == -6
+    c.set_tuning(primary_chunk=4096)          # the context stays usable
+    c.reset()
+    c.transport(0, 2000, 3)
+    assert c.stats()["histories"] == 2000
+
+
+def test_transport_before_setup_is_a_state_error(gpu_ctx_factory):
+    c = gpu_ctx_factory()
+    with pytest.raises(capi.MqiError) as e:
+        c.transport(0, 0, 1)
+    assert e.value.code == -4
