@@ -255,8 +255,10 @@ struct Grid {
     const float* ye;
     const float* ze;
     const float* rho;  // g/mm^3, x fastest
-    float        rf[9], ri[9], tr[3];   // rotation fwd / inv (row-major), translation
-    int          identity;              // rf == I and tr == 0
+    const float* rf;   // rotation fwd (row-major 3x3), kernel-parameter space
+    const float* ri;   // rotation inverse
+    const float* tr;   // translation
+    int          identity;   // rf == I and tr == 0
 };
 
 __device__ inline float fadd(float a, float b) { return __fadd_rn(a, b); }

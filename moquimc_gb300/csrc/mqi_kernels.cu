@@ -63,9 +63,9 @@ make_grid(const ChildDev& c, const float* sxe, const float* sye, const float* sz
     g.ye = sye ? sye : c.ye;
     g.ze = sze ? sze : c.ze;
     g.rho = c.rho;
-#pragma unroll
-    for (int i = 0; i < 9; ++i) { g.rf[i] = c.rf[i]; g.ri[i] = c.ri[i]; }
-    g.tr[0] = c.tr[0]; g.tr[1] = c.tr[1]; g.tr[2] = c.tr[2];
+    g.rf  = c.rf;
+    g.ri  = c.ri;
+    g.tr  = c.tr;
     g.identity = c.identity;
     return g;
 }
@@ -538,20 +538,21 @@ stepping(Ctx& C, Trk& t, Rng& rng, float rho, float d2b) {
     const float bm_r  = sqrtf(-2.0f * logf(bm_u1));
     const float z1    = bm_r * c_bm;
     const float z2    = bm_r * s_bm;
-    if (d2b < mfp && d2b < step_limit) {
-        along_step(C, t, d2b, rho, spr, z1, z2, u_phi);
-    } else if ((mfp < d2b || fabsf(mfp - d2b) < kGeoTol) &&
-               (mfp < step_limit || fabsf(mfp - step_limit) < kGeoTol)) {
-        along_step(C, t, mfp, rho, spr, z1, z2, u_phi);
-        if (t.ke1 <= kTpCut) return;
+    // The three branches of the reference (boundary, interaction, maximum step) differ only in the
+    // step length given to along_step and in the post-step process of the interaction branch, so
+    // the length is selected first and along_step runs once for every lane of the warp.
+    const bool to_boundary = d2b < mfp && d2b < step_limit;
+    const bool interaction = !to_boundary && (mfp < d2b || fabsf(mfp - d2b) < kGeoTol) &&
+                             (mfp < step_limit || fabsf(mfp - step_limit) < kGeoTol);
+    const float len = to_boundary ? d2b : (interaction ? mfp : step_limit);
+    along_step(C, t, len, rho, spr, z1, z2, u_phi);
+    if (interaction && t.ke1 > kTpCut) {
         const float u = cs_sum * rng.uniform();
         t.d1          = t.d0;
         if (u < c0) post_delta(C, t, rng);
         else if (u < c0 + c1) post_pp(C, t, rng);
         else if (u < c0 + c1 + c2) post_poe(C, t, rng);
         else if (u < c0 + c1 + c2 + c3) post_poi(C, t, rng);
-    } else {
-        along_step(C, t, step_limit, rho, spr, z1, z2, u_phi);
     }
 }
 
@@ -612,7 +613,7 @@ requeue_track(Ctx& C, const Trk& t, const Rng& rng) {
 }
 
 __global__ void __launch_bounds__(256)
-k_wave(const WaveParams P) {
+k_wave(const __grid_constant__ WaveParams P) {
     extern __shared__ __align__(16) unsigned char smem[];
     Tables* T = reinterpret_cast<Tables*>(smem);
     {
@@ -622,9 +623,9 @@ k_wave(const WaveParams P) {
     }
     // Edges of the children staged after the tables when they fit.
     float* sedges     = reinterpret_cast<float*>(smem + sizeof(Tables));
-    const float* sxe[kMaxChildren] = { nullptr, nullptr, nullptr, nullptr };
-    const float* sye[kMaxChildren] = { nullptr, nullptr, nullptr, nullptr };
-    const float* sze[kMaxChildren] = { nullptr, nullptr, nullptr, nullptr };
+    __shared__ const float* s_edges[kMaxChildren][3];   // staged edge arrays per child (null: global)
+    if (threadIdx.x < kMaxChildren * 3) s_edges[threadIdx.x / 3][threadIdx.x % 3] = nullptr;
+    __syncthreads();
     {
         int off = 0;
         for (int c = 0; c < P.n_children; ++c) {
@@ -635,9 +636,11 @@ k_wave(const WaveParams P) {
             for (int i = threadIdx.x; i <= ch.nx; i += blockDim.x) e[i] = ch.xe[i];
             for (int i = threadIdx.x; i <= ch.ny; i += blockDim.x) e[ch.nx + 1 + i] = ch.ye[i];
             for (int i = threadIdx.x; i <= ch.nz; i += blockDim.x) e[ch.nx + ch.ny + 2 + i] = ch.ze[i];
-            sxe[c] = e;
-            sye[c] = e + ch.nx + 1;
-            sze[c] = e + ch.nx + ch.ny + 2;
+            if (threadIdx.x == 0) {
+                s_edges[c][0] = e;
+                s_edges[c][1] = e + ch.nx + 1;
+                s_edges[c][2] = e + ch.nx + ch.ny + 2;
+            }
             off += need;
         }
     }
@@ -683,7 +686,7 @@ k_wave(const WaveParams P) {
                 ++n_tracks;
                 if (step_phase) {
                     C.child = t.child;
-                    C.g     = make_grid(P.child[t.child], sxe[t.child], sye[t.child], sze[t.child]);
+                    C.g     = make_grid(P.child[t.child], s_edges[t.child][0], s_edges[t.child][1], s_edges[t.child][2]);
                 }
             }
         }
@@ -695,7 +698,7 @@ k_wave(const WaveParams P) {
                 continue;
             }
             C.child = t.child;
-            C.g     = make_grid(P.child[t.child], sxe[t.child], sye[t.child], sze[t.child]);
+            C.g     = make_grid(P.child[t.child], s_edges[t.child][0], s_edges[t.child][1], s_edges[t.child][2]);
             C.spot  = P.spot_ids ? P.spot_ids[t.hist] : 0xFFFFFFFFu;
             to_child(C.g, t.p0, t.d0);
             t.p1 = t.p0;
@@ -876,7 +879,7 @@ launch_hu_to_density(const float* corr, const int16_t* hu, float* rho, uint64_t 
 // entries at [r * max_steps, ...) and its count to counts[r].
 // ------------------------------------------------------------------------------------------
 __global__ void
-k_trace_rays(ChildDev c, const float* __restrict__ rays, uint64_t n_rays, uint32_t max_steps,
+k_trace_rays(const __grid_constant__ ChildDev c, const float* __restrict__ rays, uint64_t n_rays, uint32_t max_steps,
              uint64_t* __restrict__ cnb, float* __restrict__ dist, int32_t* __restrict__ cells,
              uint32_t* __restrict__ counts) {
     const uint64_t r = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x;
