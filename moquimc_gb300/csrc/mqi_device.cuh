@@ -196,6 +196,34 @@ cs_lookup(const float* tab, float Ek, float e_min, float e_max, float rho) {
     return cs * rho;
 }
 
+/// The four macroscopic cross sections at one energy.  p-p, p-O elastic and p-O inelastic share
+/// one energy grid (0.5 MeV .. 300 MeV in 0.5 MeV steps), so their node index and interpolation
+/// weights are computed once; the arithmetic per table is that of cs_lookup, so the values are
+/// identical.
+struct CrossSections {
+    float ion, pp, poe, poi;
+};
+
+__device__ inline CrossSections
+cross_sections(const Tables& T, float Ek, float rho) {
+    CrossSections c;
+    c.ion = cs_lookup(T.cs_ion, Ek, 0.1f, 299.6f, rho);
+    c.pp = c.poe = c.poi = 0.0f;
+    if (Ek >= 0.5f && Ek <= 300.0f) {
+        const int   i0 = (int) ((Ek - 0.5f) / 0.5f);
+        const int   i1 = min(i0 + 1, MQI_TABLE_N - 1);
+        const float x0 = 0.5f + (float) i0 * 0.5f;
+        const float x1 = x0 + 0.5f;
+        c.pp  = intpl1d(Ek, x0, x1, T.cs_pp[i0], T.cs_pp[i1]);
+        c.poe = intpl1d(Ek, x0, x1, T.cs_poe[i0], T.cs_poe[i1]);
+        c.poi = intpl1d(Ek, x0, x1, T.cs_poi[i0], T.cs_poi[i1]);
+    }
+    c.pp *= rho;
+    c.poe *= rho;
+    c.poi *= rho;
+    return c;
+}
+
 /// p_ionization_tabulated::dEdx (mqi_p_ionization.hpp:271-286); returns a negative number.
 __device__ inline float
 dedx_lookup(const Tables& T, float Ek) {

@@ -40,6 +40,7 @@ struct Trk {
     uint32_t hist;
     uint32_t below, npush;
     int      child;
+    float    spr0;   // SPR at (voxel density, ke0) when the step computed it, else < 0
     bool     primary, stopped;
 };
 
@@ -179,7 +180,7 @@ __device__ inline void
 score_step(Ctx& C, const Trk& t, uint32_t cnb, float rho, float vol) {
     const WaveParams& P   = *C.P;
     const ChildDev&   ch  = P.child[C.child];
-    const float       spr = spr_default(rho, t.ke0, C.dbg);
+    const float       spr = t.spr0 >= 0.0f ? t.spr0 : spr_default(rho, t.ke0, C.dbg);
     for (int si = 0; si < ch.n_scorers; ++si) {
         const ScorerDev& s = P.scorer[ch.scorer_begin + si];
         bool     ok;
@@ -263,6 +264,7 @@ score_local_daughter(Ctx& C, float3 pw, float3 dw, float ke0, float dE0) {
     t.p0 = p; t.d0 = d; t.p1 = p; t.d1 = d;
     t.ke0 = ke0 < 0.0f ? 0.0f : ke0;
     t.dE = dE0; t.ldE = 0.0f;
+    t.spr0 = -1.0f;
     t.primary = false;
     if (rho <= 99.9f) {
         t.dE += t.ke0;
@@ -345,8 +347,8 @@ energy_loss(const Tables& T, const Rel& rel, float rho, float len, float spr, fl
 /// block of random words is laid out as: [0] free path, [1,2] Box-Muller pair (straggling,
 /// scattering angle), [3] azimuth.
 __device__ inline void
-along_step(Ctx& C, Trk& t, float len, float rho, float spr, float z_strag, float z_mcs, float u_phi) {
-    const Rel   rel(t.ke0);
+along_step(Ctx& C, Trk& t, const Rel& rel, float len, float rho, float spr, float z_strag, float z_mcs,
+           float u_phi) {
     const float dE = energy_loss(*C.T, rel, rho, len, spr, z_strag);
     float       r  = 1.0f;
     if (dE >= t.ke0) {
@@ -490,6 +492,7 @@ post_poi(Ctx& C, Trk& t, Rng& rng) {
 /// fippel_physics::stepping (mqi_fippel_physics.hpp:67-216).
 __device__ inline void
 stepping(Ctx& C, Trk& t, Rng& rng, float rho, float d2b) {
+    t.spr0 = -1.0f;
     if (rho < 1.0e-7f) {
         t.p1 = advance(t.p0, t.d0, d2b);
         return;
@@ -513,19 +516,16 @@ stepping(Ctx& C, Trk& t, Rng& rng, float rho, float d2b) {
     const float dedx     = dedx_lookup(T, rel.Ek);
     const float cur_min  = kMaxStep * spr * rho / kWaterDensity;
     const float max_loss = -1.0f * cur_min * dedx;
-    float cs1[4] = { cs_lookup(T.cs_ion, rel.Ek, 0.1f, 299.6f, rho), cs_lookup(T.cs_pp, rel.Ek, 0.5f, 300.0f, rho),
-                     cs_lookup(T.cs_poe, rel.Ek, 0.5f, 300.0f, rho), cs_lookup(T.cs_poi, rel.Ek, 0.5f, 300.0f, rho) };
-    const float e2 = t.ke0 - max_loss;
-    float cs2[4] = { cs_lookup(T.cs_ion, e2, 0.1f, 299.6f, rho), cs_lookup(T.cs_pp, e2, 0.5f, 300.0f, rho),
-                     cs_lookup(T.cs_poe, e2, 0.5f, 300.0f, rho), cs_lookup(T.cs_poi, e2, 0.5f, 300.0f, rho) };
-    const float sum1 = cs1[0] + cs1[1] + cs1[2] + cs1[3];
-    const float sum2 = cs2[0] + cs2[1] + cs2[2] + cs2[3];
+    const CrossSections k1 = cross_sections(T, rel.Ek, rho);
+    const CrossSections k2 = cross_sections(T, t.ke0 - max_loss, rho);
+    const float sum1 = k1.ion + k1.pp + k1.poe + k1.poi;
+    const float sum2 = k2.ion + k2.pp + k2.poe + k2.poi;
     const bool  pick1 = sum1 >= sum2;
     const float cs_sum = pick1 ? sum1 : sum2;
-    const float c0 = pick1 ? cs1[0] : cs2[0];
-    const float c1 = pick1 ? cs1[1] : cs2[1];
-    const float c2 = pick1 ? cs1[2] : cs2[2];
-    const float c3 = pick1 ? cs1[3] : cs2[3];
+    const float c0 = pick1 ? k1.ion : k2.ion;
+    const float c1 = pick1 ? k1.pp : k2.pp;
+    const float c2 = pick1 ? k1.poe : k2.poe;
+    const float c3 = pick1 ? k1.poi : k2.poi;
     const float u_mfp      = rng.uniform();
     const float mfp        = -1.0f * logf(u_mfp) / cs_sum;
     const float step_limit = cur_min * kWaterDensity / (spr * rho);
@@ -545,7 +545,8 @@ stepping(Ctx& C, Trk& t, Rng& rng, float rho, float d2b) {
     const bool interaction = !to_boundary && (mfp < d2b || fabsf(mfp - d2b) < kGeoTol) &&
                              (mfp < step_limit || fabsf(mfp - step_limit) < kGeoTol);
     const float len = to_boundary ? d2b : (interaction ? mfp : step_limit);
-    along_step(C, t, len, rho, spr, z1, z2, u_phi);
+    along_step(C, t, rel, len, rho, spr, z1, z2, u_phi);
+    t.spr0 = spr;
     if (interaction && t.ke1 > kTpCut) {
         const float u = cs_sum * rng.uniform();
         t.d1          = t.d0;

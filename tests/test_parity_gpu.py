@@ -97,7 +97,10 @@ def test_gpu_matches_oracle_history_by_history(oracle, gpu_ctx_factory, wname):
         c.reset()
         c.transport(h, h + 1, seed)
         e_gpu[h] = c.tally(sid).sum()
-        steps += c.stats()["steps"]
+        st = c.stats()
+        # the oracle pops each deposit-only daughter and counts its one step; the GPU scores
+        # them where they are created
+        steps += st["steps"] + st["local_daughters"]
     _, e_ora, ost = oracle.transport(_oracle_grid(oracle, wl), v, 0, n, seed, wl.physics_debug, scorer=1,
                                      per_history=True)
     same = np.abs(e_gpu - e_ora) <= 1e-4 * np.maximum(e_ora, 1e-9)
