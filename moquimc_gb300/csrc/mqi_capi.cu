@@ -532,6 +532,7 @@ mqi_transport(mqi_ctx* c, uint64_t h0, uint64_t h1, uint64_t seed) {
     P.stats           = c->stats;
     P.spot_ids        = c->has_spots ? c->spot_ids : nullptr;
     P.tables          = c->tables;
+    P.smem_edge_floats = wave_edge_floats(P.child, P.n_children);
     MQI_CUDA(c, cudaMemsetAsync(c->counters + 3, 0, sizeof(uint32_t), c->stream), "mqi_transport");
     QueueBuf* A = &c->qa;
     QueueBuf* B = &c->qb;
@@ -552,7 +553,7 @@ mqi_transport(mqi_ctx* c, uint64_t h0, uint64_t h1, uint64_t seed) {
             MQI_CUDA(c, cudaMemsetAsync(c->counters + (1 - cur), 0, sizeof(uint32_t), c->stream), "mqi_transport");
             MQI_CUDA(c, cudaMemsetAsync(c->counters + 2, 0, sizeof(uint32_t), c->stream), "mqi_transport");
             MQI_CUDA(c, cudaEventRecord(c->ev0, c->stream), "mqi_transport");
-            MQI_CUDA(c, launch_wave(P, c->wave_grid, c->wave_block, c->stream), "mqi_transport: wave");
+            MQI_CUDA(c, launch_wave(P, c->wave_grid, c->wave_block, c->wave_grid / c->num_sms, c->stream), "mqi_transport: wave");
             MQI_CUDA(c, cudaEventRecord(c->ev1, c->stream), "mqi_transport");
             MQI_CUDA(c, cudaMemcpyAsync(c->host_counts, c->counters, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream),
                      "mqi_transport");

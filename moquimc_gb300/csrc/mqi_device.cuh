@@ -102,6 +102,14 @@ daughter_uid(uint64_t parent_uid, uint32_t push_index) {
     return mix64(parent_uid * 0x9E3779B97F4A7C15ull + (uint64_t) (push_index + 1u));
 }
 
+/// One Philox block, out of line: the hot step draws its first block inline (begin_step) and
+/// only the rare post-step processes need more, so one shared copy of the ten rounds keeps the
+/// kernel's instruction footprint small.
+static __device__ __noinline__ u32x4
+philox_block(uint32_t ctr, uint32_t hist, uint32_t lo, uint32_t hi, uint32_t k0, uint32_t k1) {
+    return philox4x32_10(u32x4{ ctr, hist, lo, hi }, k0, k1);
+}
+
 /// The random stream of one track.  Each physics step starts on a fresh 4-word block
 /// (`begin_step`), so the words a step consumes never depend on where a queue slice ended.
 struct Rng {
@@ -112,14 +120,17 @@ struct Rng {
     u32x4    blk;
     int      pos;        // next word of blk (4 = exhausted)
 
-    __host__ __device__ inline void
+    /// Start a step on a fresh block (generated here, inline).
+    __device__ inline void
     begin_step() {
-        pos = 4;
+        blk = philox4x32_10(u32x4{ ctr, hist, uid_lo, uid_hi }, k0, k1);
+        ++ctr;
+        pos = 0;
     }
-    __host__ __device__ inline uint32_t
+    __device__ inline uint32_t
     next() {
         if (pos >= 4) {
-            blk = philox4x32_10(u32x4{ ctr, hist, uid_lo, uid_hi }, k0, k1);
+            blk = philox_block(ctr, hist, uid_lo, uid_hi, k0, k1);
             ++ctr;
             pos = 0;
         }
@@ -127,7 +138,7 @@ struct Rng {
         ++pos;
         return w;
     }
-    __host__ __device__ inline float
+    __device__ inline float
     uniform() {
         return u01(next());
     }
@@ -444,7 +455,7 @@ grid_volume(const Grid& g, int3 c) {
 // Direction update: track_t::update_post_vertex_direction (mqi_track.hpp:163-172) with the
 // Moller-Hughes alignment of mat3x3(f, t) (mqi_matrix.hpp:88-150), ref vector f = (0,0,1).
 // ------------------------------------------------------------------------------------------
-__device__ inline float3
+static __device__ __noinline__ float3
 rotate_dir(float3 t, float th, float ph) {
     float s1, c1, s2, c2;
     sincosf(th, &s1, &c1);

@@ -78,6 +78,7 @@ struct WaveParams {
     unsigned long long* stats;  // device: mqi_stats fields (8 x u64)
     const uint32_t* spot_ids;   // per history (may be null)
     uint32_t*       error_flag; // device: set when a bounded loop gives up or a queue overflows
+    int             smem_edge_floats; // shared-memory floats for staged child edges
     const float*    tables;     // device: the six physics tables, 6 x 600 floats in Tables order
                                 // (followed by the 3996 HU density-correction factors)
 };
@@ -85,8 +86,9 @@ struct WaveParams {
 // ---- launchers (mqi_kernels.cu) ----
 cudaError_t launch_load_primaries(const Queue& q, const mqi_vertex* v, uint64_t h0, uint32_t n,
                                   cudaStream_t s);
-cudaError_t launch_wave(const WaveParams& p, int grid, int block, cudaStream_t s);
-int         wave_smem_bytes();
+cudaError_t launch_wave(const WaveParams& p, int grid, int block, int blocks_per_sm, cudaStream_t s);
+int         wave_smem_bytes(const WaveParams& p);
+int         wave_edge_floats(const ChildDev* c, int n);
 cudaError_t launch_hu_to_density(const float* corr, const int16_t* hu, float* rho, uint64_t n, float scale,
                                  cudaStream_t s);
 cudaError_t launch_trace_rays(const ChildDev& c, const float* rays, uint64_t n_rays, uint32_t max_steps,

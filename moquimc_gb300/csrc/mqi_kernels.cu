@@ -237,11 +237,11 @@ to_world(const Grid& g, float3& p, float3& d) {
 
 /// track_t::update_post_vertex_position with the last_step length
 /// (p_ionization_tabulated::last_step, mqi_p_ionization.hpp:481-490).
-__device__ inline float3
-last_step_pos(const Ctx& C, float3 p0, float3 d0, float ke0, float dE, float rho) {
+__device__ __noinline__ float3
+last_step_pos(const Tables* T, bool dbg, float3 p0, float3 d0, float ke0, float dE, float rho) {
     float lw = 0.0f;
-    if (dE > 0.0f) lw = -dE / dedx_lookup(*C.T, ke0);
-    const float sl = lw * kWaterDensity / (spr_default(rho, ke0, C.dbg) * rho);
+    if (dE > 0.0f) lw = -dE / dedx_lookup(*T, ke0);
+    const float sl = lw * kWaterDensity / (spr_default(rho, ke0, dbg) * rho);
     return make_float3(p0.x + d0.x * sl, p0.y + d0.y * sl, p0.z + d0.z * sl);
 }
 
@@ -268,7 +268,7 @@ score_local_daughter(Ctx& C, float3 pw, float3 dw, float ke0, float dE0) {
     t.primary = false;
     if (rho <= 99.9f) {
         t.dE += t.ke0;
-        t.p1 = last_step_pos(C, p, d, t.ke0, t.dE, rho);
+        t.p1 = last_step_pos(C.T, C.dbg, p, d, t.ke0, t.dE, rho);
     }
     score_step(C, t, cnb, rho, grid_volume(C.g, t.cell));
     return true;
@@ -489,6 +489,32 @@ post_poi(Ctx& C, Trk& t, Rng& rng) {
     t.stopped = true;
 }
 
+/// What a discrete interaction reads and changes, passed by value to the out-of-line handler so
+/// the stepping loop's track stays in registers.
+struct PostState {
+    Trk      t;
+    Rng      rng;
+    uint32_t n_sec, n_local, n_drop, n_err;
+};
+
+/// The post-step process of an interaction step (mqi_fippel_physics.hpp:178-196), out of line:
+/// it runs on a few percent of the steps, and one copy of the four processes keeps the hot
+/// loop's instruction footprint and register pressure down.
+__device__ __noinline__ PostState
+post_interaction(const WaveParams* P, const Tables* T, Grid g, int child, bool dbg, float tcut, int proc,
+                 PostState s) {
+    Ctx C;
+    C.P = P; C.T = T; C.g = g; C.child = child; C.dbg = dbg; C.tcut = tcut;
+    C.spot = 0xFFFFFFFFu;
+    C.n_sec = C.n_local = C.n_drop = C.n_err = 0;
+    if (proc == 0) post_delta(C, s.t, s.rng);
+    else if (proc == 1) post_pp(C, s.t, s.rng);
+    else if (proc == 2) post_poe(C, s.t, s.rng);
+    else post_poi(C, s.t, s.rng);
+    s.n_sec = C.n_sec; s.n_local = C.n_local; s.n_drop = C.n_drop; s.n_err = C.n_err;
+    return s;
+}
+
 /// fippel_physics::stepping (mqi_fippel_physics.hpp:67-216).
 __device__ inline void
 stepping(Ctx& C, Trk& t, Rng& rng, float rho, float d2b) {
@@ -505,7 +531,7 @@ stepping(Ctx& C, Trk& t, Rng& rng, float rho, float d2b) {
         if (t.ke0 < 0.0f) t.ke0 = 0.0f;
         t.dE += t.ke0;
         t.ke1 -= t.ke0;
-        t.p1      = last_step_pos(C, t.p0, t.d0, t.ke0, t.dE, rho);
+        t.p1      = last_step_pos(C.T, C.dbg, t.p0, t.d0, t.ke0, t.dE, rho);
         t.stopped = true;
         return;
     }
@@ -550,10 +576,19 @@ stepping(Ctx& C, Trk& t, Rng& rng, float rho, float d2b) {
     if (interaction && t.ke1 > kTpCut) {
         const float u = cs_sum * rng.uniform();
         t.d1          = t.d0;
-        if (u < c0) post_delta(C, t, rng);
-        else if (u < c0 + c1) post_pp(C, t, rng);
-        else if (u < c0 + c1 + c2) post_poe(C, t, rng);
-        else if (u < c0 + c1 + c2 + c3) post_poi(C, t, rng);
+        const int proc = (u < c0) ? 0 : (u < c0 + c1) ? 1 : (u < c0 + c1 + c2) ? 2 : (u < c0 + c1 + c2 + c3) ? 3 : -1;
+        if (proc >= 0) {
+            PostState ps;
+            ps.t   = t;
+            ps.rng = rng;
+            ps     = post_interaction(C.P, C.T, C.g, C.child, C.dbg, C.tcut, proc, ps);
+            t      = ps.t;
+            rng    = ps.rng;
+            C.n_sec += ps.n_sec;
+            C.n_local += ps.n_local;
+            C.n_drop += ps.n_drop;
+            C.n_err += ps.n_err;
+        }
     }
 }
 
@@ -613,8 +648,8 @@ requeue_track(Ctx& C, const Trk& t, const Rng& rng) {
     q.cell[i] = t.cell.x | (t.cell.y << 11) | (t.cell.z << 22);
 }
 
-__global__ void __launch_bounds__(256)
-k_wave(const __grid_constant__ WaveParams P) {
+__device__ __forceinline__ void
+wave_body(const WaveParams& P) {
     extern __shared__ __align__(16) unsigned char smem[];
     Tables* T = reinterpret_cast<Tables*>(smem);
     {
@@ -632,7 +667,7 @@ k_wave(const __grid_constant__ WaveParams P) {
         for (int c = 0; c < P.n_children; ++c) {
             const ChildDev& ch = P.child[c];
             const int need     = ch.nx + ch.ny + ch.nz + 3;
-            if (off + need > 3 * 2048 + 12) break;
+            if (off + need > P.smem_edge_floats) break;
             float* e = sedges + off;
             for (int i = threadIdx.x; i <= ch.nx; i += blockDim.x) e[i] = ch.xe[i];
             for (int i = threadIdx.x; i <= ch.ny; i += blockDim.x) e[ch.nx + 1 + i] = ch.ye[i];
@@ -823,18 +858,48 @@ launch_load_primaries(const Queue& q, const mqi_vertex* v, uint64_t h0, uint32_t
     return cudaGetLastError();
 }
 
+/// The wave kernel in the launch shapes the tuner chooses from: (threads per block, minimum
+/// resident blocks per SM).  The register budget each shape implies is what differs.
+template<int kBlock, int kMinBlocks>
+__global__ void __launch_bounds__(kBlock, kMinBlocks)
+k_wave(const __grid_constant__ WaveParams P) {
+    wave_body(P);
+}
+
 int
-wave_smem_bytes() {
-    return (int) sizeof(Tables) + (3 * 2048 + 12) * (int) sizeof(float);
+wave_smem_bytes(const WaveParams& p) {
+    return (int) sizeof(Tables) + p.smem_edge_floats * (int) sizeof(float);
+}
+
+int
+wave_edge_floats(const ChildDev* c, int n) {
+    int f = 0;
+    for (int i = 0; i < n; ++i) {
+        const int need = c[i].nx + c[i].ny + c[i].nz + 3;
+        if (f + need > 3 * 2048 + 12) break;
+        f += need;
+    }
+    return (f + 3) & ~3;
+}
+
+template<int B, int M>
+static cudaError_t
+launch_variant(const WaveParams& p, int grid, cudaStream_t s) {
+    const int   smem = wave_smem_bytes(p);
+    cudaError_t e    = cudaFuncSetAttribute(k_wave<B, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    k_wave<B, M><<<grid, B, smem, s>>>(p);
+    return cudaGetLastError();
 }
 
 cudaError_t
-launch_wave(const WaveParams& p, int grid, int block, cudaStream_t s) {
-    const int   smem = wave_smem_bytes();
-    cudaError_t e    = cudaFuncSetAttribute(k_wave, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e != cudaSuccess) return e;
-    k_wave<<<grid, block, smem, s>>>(p);
-    return cudaGetLastError();
+launch_wave(const WaveParams& p, int grid, int block, int blocks_per_sm, cudaStream_t s) {
+    if (block == 128) {
+        if (blocks_per_sm >= 6) return launch_variant<128, 6>(p, grid, s);
+        if (blocks_per_sm == 5) return launch_variant<128, 5>(p, grid, s);
+        return launch_variant<128, 4>(p, grid, s);
+    }
+    return launch_variant<256, 2>(p, grid, s);
 }
 
 // ------------------------------------------------------------------------------------------
