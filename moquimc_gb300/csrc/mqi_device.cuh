@@ -455,8 +455,8 @@ grid_volume(const Grid& g, int3 c) {
 // Direction update: track_t::update_post_vertex_direction (mqi_track.hpp:163-172) with the
 // Moller-Hughes alignment of mat3x3(f, t) (mqi_matrix.hpp:88-150), ref vector f = (0,0,1).
 // ------------------------------------------------------------------------------------------
-static __device__ __noinline__ float3
-rotate_dir(float3 t, float th, float ph) {
+__device__ __forceinline__ float3
+rotate_dir_inline(float3 t, float th, float ph) {
     float s1, c1, s2, c2;
     sincosf(th, &s1, &c1);
     sincosf(ph, &s2, &c2);
@@ -507,6 +507,12 @@ rotate_dir(float3 t, float th, float ph) {
                            m[6] * dl.x + m[7] * dl.y + m[8] * dl.z);
     const float on = sqrtf(o.x * o.x + o.y * o.y + o.z * o.z);
     return make_float3(o.x / on, o.y / on, o.z / on);
+}
+
+/// Out-of-line copy for the rare post-step processes (one copy instead of one per call site).
+static __device__ __noinline__ float3
+rotate_dir(float3 t, float th, float ph) {
+    return rotate_dir_inline(t, th, ph);
 }
 
 }   // namespace mqi_gpu

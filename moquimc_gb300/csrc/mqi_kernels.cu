@@ -146,14 +146,17 @@ compute_hit(int type, const Trk& t, float rho, float vol, float spr_ke0) {
     case MQI_SCORER_EDEP: return (double) edep;
     case MQI_SCORER_EDEP_PRIMARY: return t.primary ? (double) t.dE : 0.0;
     case MQI_SCORER_EDEP_SECONDARY: return t.primary ? 0.0 : (double) t.dE;
+    // dose_to_water in Gy per history: formed in FP32 (one rounding per step; the reference forms
+    // it in double) and accumulated in FP64.  GB300's FP64 pipe is narrow, so the per-step
+    // division stays in FP32.
     case MQI_SCORER_DOSE_W:
     case MQI_SCORER_DIJ: {
         if (rho < 1.0e-7f) return 0.0;
-        return (double) edep * 1.60218e-10 / (double) (vol * rho * spr_ke0);
+        return (double) (edep * 1.60218e-10f / (vol * rho * spr_ke0));
     }
     case MQI_SCORER_DOSE_W2: {
         if (rho < 1.0e-7f) return 0.0;
-        const double d = (double) edep * 1.60218e-10 / (double) (vol * rho * spr_ke0);
+        const double d = (double) (edep * 1.60218e-10f / (vol * rho * spr_ke0));
         return d * d;
     }
     case MQI_SCORER_DOSE_M:
@@ -362,7 +365,7 @@ along_step(Ctx& C, Trk& t, const Rel& rel, float len, float rho, float spr, floa
     th                = z_mcs * (sqrtf(2.0f) * th);
     if (th < 0.0f) th = -th;
     const float phi = 2.0f * kPi * u_phi;
-    t.d1            = rotate_dir(t.d1, th, phi);
+    t.d1            = rotate_dir_inline(t.d1, th, phi);
     t.dE += dE * r;
     t.p1 = advance(t.p0, t.d0, r * len);
     t.ke1 -= dE * r;

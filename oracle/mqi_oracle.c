@@ -623,7 +623,7 @@ static double hit(const mqo_config* cfg, const trk_t* t, float rho, float vol, i
     if (cfg->scorer == 1) return (double) edep;
     if (rho < 1.0e-7f) return 0.0;
     {
-        double d = (double) edep * 1.60218e-10 / (double) (vol * rho * mqo_spr(rho, t->ke0, dbg));
+        double d = (double) (edep * 1.60218e-10f / (vol * rho * mqo_spr(rho, t->ke0, dbg)));
         return cfg->scorer == 3 ? d * d : d;
     }
 }
