@@ -76,7 +76,7 @@ struct mqi_ctx {
     uint32_t*               host_counts = nullptr;  // pinned: 4 x u32
     float*                  tables = nullptr;       // 6*600 physics + 3996 HU correction
     int                     num_sms = 0;
-    int                     wave_block = 256;
+    int                     wave_block = 128;
     int                     wave_grid = 0;
     uint32_t                max_slice_steps = 0;
     uint32_t                primary_chunk = 1u << 21;
@@ -214,7 +214,7 @@ mqi_create(int device, mqi_ctx** out) {
         mqi_destroy(c);
         return cuda_fail(nullptr, e, "mqi_create: allocation");
     }
-    c->wave_grid = c->num_sms * 2;
+    c->wave_grid = c->num_sms * 5;   // 128-thread blocks, 5 per SM (96 registers): fastest measured shape
     *out = c;
     return MQI_OK;
 }

@@ -492,18 +492,17 @@ post_poi(Ctx& C, Trk& t, Rng& rng) {
     t.stopped = true;
 }
 
-/// What a discrete interaction reads and changes, passed by value to the out-of-line handler so
-/// the stepping loop's track stays in registers.
+/// What a discrete interaction reads and changes.
 struct PostState {
     Trk      t;
     Rng      rng;
     uint32_t n_sec, n_local, n_drop, n_err;
 };
 
-/// The post-step process of an interaction step (mqi_fippel_physics.hpp:178-196), out of line:
-/// it runs on a few percent of the steps, and one copy of the four processes keeps the hot
-/// loop's instruction footprint and register pressure down.
-__device__ __noinline__ PostState
+/// The post-step process of an interaction step (mqi_fippel_physics.hpp:178-196).  It stays
+/// inline (an out-of-line call passing the track by value measured 25% slower); what it calls
+/// that is large and rare -- extra Philox blocks, the post-step rotations -- is out of line.
+__device__ __forceinline__ PostState
 post_interaction(const WaveParams* P, const Tables* T, Grid g, int child, bool dbg, float tcut, int proc,
                  PostState s) {
     Ctx C;
