@@ -176,6 +176,29 @@ int mqi_eval_physics(mqi_ctx* ctx, const float* energies, uint64_t n, float* out
  * when < 0.  Results do not depend on any of these. */
 int mqi_set_tuning(mqi_ctx* ctx, int block, int blocks_per_sm, int slice_steps, int primary_chunk);
 
+/* Transport without any device allocation, for callers that cannot call cudaMalloc once running
+ * (device memory owned by a pre-sized pool or another framework's allocator, plug-in hosts that
+ * forbid allocation after start-up, loops that cannot afford cudaMalloc's device synchronisation).
+ * No counterpart in the reference, whose upload/run path allocates on every call.
+ *
+ * The caller supplies every buffer as device memory on the current device: the grid edges
+ * (nx+1, ny+1, nz+1 floats), the density (g/mm^3, x fastest), `n_histories` vertices, and the FP64
+ * tally (nx*ny*nz doubles, DIRECT ROI, accumulated into, not cleared).  scorer_type is one of
+ * EDEP, DOSE_W, DOSE_W2, DOSE_M.  Work is issued on `cuda_stream` (NULL = the legacy default
+ * stream) and the call returns when it is done.
+ *
+ * The transport's own scratch (its particle queues) is a 24 MiB static device array in the
+ * library, held by every GPU that loads it until the process exits.  At most 16777216 histories
+ * per call (larger requests return MQI_ERR_INVALID); a queue generation that outgrows the
+ * scratch returns MQI_ERR_OVERFLOW.  All calls share the array: calls whose GPU work overlaps
+ * race and must be serialised.  The first call on a device resolves the array's address and
+ * uploads the physics tables (synchronous copies); make it before any stream capture begins.
+ * Messages: mqi_last_error(NULL). */
+int mqi_transport_noalloc(int nx, int ny, int nz, const float* d_xe, const float* d_ye,
+                          const float* d_ze, const float* d_rho, const mqi_vertex* d_vertices,
+                          uint64_t n_histories, int scorer_type, int physics_debug, uint64_t seed,
+                          double* d_tally, void* cuda_stream);
+
 /* Library version string. */
 const char* mqi_version(void);
 

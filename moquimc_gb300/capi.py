@@ -32,7 +32,7 @@ EXPORTS = (
     "mqi_create", "mqi_destroy", "mqi_last_error", "mqi_set_stream", "mqi_set_physics",
     "mqi_add_child", "mqi_set_density", "mqi_set_hu", "mqi_add_scorer", "mqi_set_vertices",
     "mqi_transport", "mqi_get_tally", "mqi_reset_tallies", "mqi_get_stats", "mqi_hu_to_density",
-    "mqi_trace_rays", "mqi_eval_physics", "mqi_set_tuning", "mqi_version",
+    "mqi_trace_rays", "mqi_eval_physics", "mqi_set_tuning", "mqi_transport_noalloc", "mqi_version",
 )
 
 VERTEX_DTYPE = np.dtype([("ke", "<f4"), ("pos", "<f4", (3,)), ("dir", "<f4", (3,))])
@@ -90,6 +90,7 @@ def load(path: Optional[str] = None) -> C.CDLL:
         "mqi_trace_rays": (i32, [vp, i32, vp, u64, u32, vp, vp, vp, vp, u64, P(u64)]),
         "mqi_eval_physics": (i32, [vp, vp, u64, vp]),
         "mqi_set_tuning": (i32, [vp, i32, i32, i32, i32]),
+        "mqi_transport_noalloc": (i32, [i32, i32, i32, vp, vp, vp, vp, vp, u64, i32, i32, u64, vp, vp]),
         "mqi_version": (C.c_char_p, []),
     }
     for name, (res, args) in sig.items():

@@ -160,6 +160,11 @@ valid_ctx(mqi_ctx* c) {
 
 }   // namespace
 
+void
+mqi_gpu::set_thread_error(const char* msg) {
+    g_thread_error = msg ? msg : "";
+}
+
 extern "C" {
 
 const char*

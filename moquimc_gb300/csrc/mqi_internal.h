@@ -83,6 +83,9 @@ struct WaveParams {
                                 // (followed by the 3996 HU density-correction factors)
 };
 
+/// Record the calling thread's last error message (returned by mqi_last_error(NULL)).
+void set_thread_error(const char* msg);
+
 // ---- launchers (mqi_kernels.cu) ----
 cudaError_t launch_load_primaries(const Queue& q, const mqi_vertex* v, uint64_t h0, uint32_t n,
                                   cudaStream_t s);
