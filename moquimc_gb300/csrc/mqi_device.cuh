@@ -225,9 +225,13 @@ cross_sections(const Tables& T, float Ek, float rho) {
         const int   i1 = min(i0 + 1, MQI_TABLE_N - 1);
         const float x0 = 0.5f + (float) i0 * 0.5f;
         const float x1 = x0 + 0.5f;
-        c.pp  = intpl1d(Ek, x0, x1, T.cs_pp[i0], T.cs_pp[i1]);
-        c.poe = intpl1d(Ek, x0, x1, T.cs_poe[i0], T.cs_poe[i1]);
-        c.poi = intpl1d(Ek, x0, x1, T.cs_poi[i0], T.cs_poi[i1]);
+        // On this grid x1 - x0 is exactly 0.5 for every node (checked exhaustively in FP32), so
+        // intpl1d's division by it is the exact scaling by 2 written here: identical results.
+        (void) x1;
+        const float dx = Ek - x0;
+        c.pp  = T.cs_pp[i0] + dx * (T.cs_pp[i1] - T.cs_pp[i0]) * 2.0f;
+        c.poe = T.cs_poe[i0] + dx * (T.cs_poe[i1] - T.cs_poe[i0]) * 2.0f;
+        c.poi = T.cs_poi[i0] + dx * (T.cs_poi[i1] - T.cs_poi[i0]) * 2.0f;
     }
     c.pp *= rho;
     c.poe *= rho;
@@ -457,56 +461,41 @@ grid_volume(const Grid& g, int3 c) {
 // ------------------------------------------------------------------------------------------
 __device__ __forceinline__ float3
 rotate_dir_inline(float3 t, float th, float ph) {
+    // dl = mat3x3(0, th, ph) * (0,0,1): the new direction in the frame whose z axis is t.
     float s1, c1, s2, c2;
     sincosf(th, &s1, &c1);
     sincosf(ph, &s2, &c2);
-    float3 dl = make_float3(c2 * s1, s2 * s1, c1);
-    {
-        const float n = sqrtf(dl.x * dl.x + dl.y * dl.y + dl.z * dl.z);
-        dl            = make_float3(dl.x / n, dl.y / n, dl.z / n);
-    }
-    const float tn = sqrtf(t.x * t.x + t.y * t.y + t.z * t.z);
-    const float c  = t.z / tn;
-    float m[9];
-    if (fabsf(c - 1.0f) < kGeoTol || fabsf(c + 1.0f) < kGeoTol) {
-        // reflection form with x = (1,0,0): uu = x - f, vv = x - t, both normalised
-        const float r2 = 0.70710677f;   // (1,0,-1)/|(1,0,-1)| in float
-        const float ux = r2, uy = 0.0f, uz = -r2;
-        float vx = 1.0f - t.x, vy = -t.y, vz = -t.z;
-        const float vn = sqrtf(vx * vx + vy * vy + vz * vz);
-        vx /= vn; vy /= vn; vz /= vn;
-        const float du = ux * ux + uy * uy + uz * uz;
-        const float dv = vx * vx + vy * vy + vz * vz;
-        const float duv = vx * ux + vy * uy + vz * uz;
-        const float a = 2.0f / du, b = 2.0f / dv, k = 4.0f * duv / (du * dv);
-        m[0] = 1.0f - a * ux * ux - b * vx * vx + k * vx * ux;
-        m[1] = 0.0f - a * ux * uy - b * vx * vy + k * vx * uy;
-        m[2] = 0.0f - a * ux * uz - b * vx * vz + k * vx * uz;
-        m[3] = 0.0f - a * uy * ux - b * vy * vx + k * vy * ux;
-        m[4] = 1.0f - a * uy * uy - b * vy * vy + k * vy * uy;
-        m[5] = 0.0f - a * uy * uz - b * vy * vz + k * vy * uz;
-        m[6] = 0.0f - a * uz * ux - b * vz * vx + k * vz * ux;
-        m[7] = 0.0f - a * uz * uy - b * vz * vy + k * vz * uy;
-        m[8] = 1.0f - a * uz * uz - b * vz * vz + k * vz * uz;
-    } else {
-        // v = f x t = (-t.y, t.x, 0), h = (1-c)/(1-c^2)
-        const float vx = -t.y, vy = t.x, vz = 0.0f;
-        const float h = (1.0f - c) / (1.0f - c * c);
-        m[0] = c + h * vx * vx;
-        m[1] = h * vx * vy - vz;
-        m[2] = h * vx * vz + vy;
-        m[3] = h * vx * vy + vz;
-        m[4] = c + h * vy * vy;
-        m[5] = h * vy * vz - vx;
-        m[6] = h * vx * vz - vy;
-        m[7] = h * vy * vz + vx;
-        m[8] = c + h * vz * vz;
-    }
-    float3 o = make_float3(m[0] * dl.x + m[1] * dl.y + m[2] * dl.z,
-                           m[3] * dl.x + m[4] * dl.y + m[5] * dl.z,
-                           m[6] * dl.x + m[7] * dl.y + m[8] * dl.z);
-    const float on = sqrtf(o.x * o.x + o.y * o.y + o.z * o.z);
-    return make_float3(o.x / on, o.y / on, o.z / on);
+    const float dx = c2 * s1, dy = s2 * s1, dz = c1;
+    const float it = rsqrtf(t.x * t.x + t.y * t.y + t.z * t.z);
+    const float tx = t.x * it, ty = t.y * it, c = t.z * it;
+    // Moller-Hughes, general case: R = c I + [v]x + h v v^T with v = z x t = (-ty, tx, 0) and
+    // h = (1 - c) / (1 - c^2) = 1 / (1 + c):  R dl = c dl + v x dl + h (v . dl) v.
+    const float vx = -ty, vy = tx;
+    const float h  = 1.0f / (1.0f + c);
+    const float vd = vx * dx + vy * dy;
+    const float gx = c * dx - vy * dz + h * vd * vx;
+    const float gy = c * dy + vx * dz + h * vd * vy;
+    const float gz = c * dz + (vx * dy - vy * dx);
+    // Moller-Hughes near +-z (|c -+ 1| < 1e-3): the product of the reflections about
+    // u = (x - z)/|x - z| and w = (x - t)/|x - t|, x = (1,0,0):
+    // R dl = dl - 2 (u.dl) u - 2 (w.dl) w + 4 (u.w)(u.dl) w.
+    const float r2 = 0.70710678f;
+    float       wx = 1.0f - tx, wy = -ty, wz = -c;
+    const float iw = rsqrtf(wx * wx + wy * wy + wz * wz);
+    wx *= iw; wy *= iw; wz *= iw;
+    const float ud = r2 * (dx - dz);
+    const float wd = wx * dx + wy * dy + wz * dz;
+    const float uw = r2 * (wx - wz);
+    const float k  = 4.0f * uw * ud - 2.0f * wd;
+    const float rx = dx - 2.0f * ud * r2 + k * wx;
+    const float ry = dy + k * wy;
+    const float rz = dz + 2.0f * ud * r2 + k * wz;
+    // both forms are evaluated and one selected: lanes of a warp near and away from the beam
+    // axis then run one instruction stream
+    const bool  refl = fabsf(c - 1.0f) < kGeoTol || fabsf(c + 1.0f) < kGeoTol;
+    const float ox = refl ? rx : gx, oy = refl ? ry : gy, oz = refl ? rz : gz;
+    const float io = rsqrtf(ox * ox + oy * oy + oz * oz);
+    return make_float3(ox * io, oy * io, oz * io);
 }
 
 /// Out-of-line copy for the rare post-step processes (one copy instead of one per call site).

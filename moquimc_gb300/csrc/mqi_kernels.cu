@@ -277,6 +277,40 @@ score_local_daughter(Ctx& C, float3 pw, float3 dw, float ke0, float dE0) {
     return true;
 }
 
+/// Emit one daughter that survived the stack-limit check: move it to the world frame, score it
+/// where it stands when it is a deposit-only daughter of a single-child world, else append it to
+/// the next queue.  Out of line and by value: it runs on a few percent of the steps and its
+/// body would otherwise be inlined at every push site of the four processes.
+/// Returns 0 queued, 1 scored locally, 2 queue overflow.
+static __device__ __noinline__ int
+emit_daughter(const WaveParams* P, const Tables* T, int child, const float* xe, const float* ye, const float* ze,
+              bool dbg, uint32_t below, uint64_t uid, uint32_t hist, float ke0, bool ke1_zero, float3 p, float3 d,
+              float dE0) {
+    Ctx C;
+    C.P = P; C.T = T; C.child = child; C.dbg = dbg; C.tcut = 0.0f; C.spot = 0xFFFFFFFFu;
+    C.g = make_grid(P->child[child], xe, ye, ze);
+    C.n_sec = C.n_local = C.n_drop = C.n_err = 0;
+    daughter_to_world(C.g, p, d);
+    if (P->inline_local && ke0 <= kTpCut && score_local_daughter(C, p, d, ke0, dE0)) return 1;
+    const Queue&   q = P->out;
+    const uint32_t i = atomicAdd(P->n_out, 1u);
+    if (i >= q.capacity) {
+        atomicOr(P->error_flag, 2u);
+        return 2;
+    }
+    q.ke[i] = ke0;
+    q.px[i] = p.x; q.py[i] = p.y; q.pz[i] = p.z;
+    q.dx[i] = d.x; q.dy[i] = d.y; q.dz[i] = d.z;
+    q.dE0[i] = dE0;
+    q.hist[i] = hist;
+    q.uid_lo[i] = (uint32_t) uid;
+    q.uid_hi[i] = (uint32_t) (uid >> 32);
+    q.ctr[i] = 0;
+    q.meta[i] = (below & kMetaBelowMask) | (ke1_zero ? kMetaKe1Zero : 0u);
+    q.cell[i] = 0;
+    return 0;
+}
+
 /// track_stack_t::push_secondary (mqi_track_stack.hpp:36-41) with the stack depth emulated:
 /// a track popped with `below` entries under it pushes its i-th daughter at depth below + i,
 /// and the push is dropped when that reaches the limit (200 with debug physics, else 10).
@@ -289,29 +323,11 @@ push_daughter(Ctx& C, Trk& t, float ke0, bool ke1_zero, float3 p, float3 d, floa
     const uint32_t below = t.below + t.npush;
     const uint64_t uid   = daughter_uid(t.uid, t.npush);
     ++t.npush;
-    daughter_to_world(C.g, p, d);
-    if (C.P->inline_local && ke0 <= kTpCut && score_local_daughter(C, p, d, ke0, dE0)) {
-        ++C.n_local;
-        return;
-    }
-    const Queue& q   = C.P->out;
-    const uint32_t i = atomicAdd(C.P->n_out, 1u);
-    if (i >= q.capacity) {
-        atomicOr(C.P->error_flag, 2u);
-        ++C.n_err;
-        return;
-    }
-    q.ke[i] = ke0;
-    q.px[i] = p.x; q.py[i] = p.y; q.pz[i] = p.z;
-    q.dx[i] = d.x; q.dy[i] = d.y; q.dz[i] = d.z;
-    q.dE0[i] = dE0;
-    q.hist[i] = t.hist;
-    q.uid_lo[i] = (uint32_t) uid;
-    q.uid_hi[i] = (uint32_t) (uid >> 32);
-    q.ctr[i] = 0;
-    q.meta[i] = (below & kMetaBelowMask) | (ke1_zero ? kMetaKe1Zero : 0u);
-    q.cell[i] = 0;
-    ++C.n_sec;
+    const int r = emit_daughter(C.P, C.T, C.child, C.g.xe, C.g.ye, C.g.ze, C.dbg, below, uid, t.hist, ke0, ke1_zero, p, d,
+                                dE0);
+    if (r == 0) ++C.n_sec;
+    else if (r == 1) ++C.n_local;
+    else ++C.n_err;
 }
 
 // ------------------------------------------------------------------------------------------
