@@ -473,8 +473,8 @@ rotate_dir_inline(float3 t, float th, float ph) {
     const float vx = -ty, vy = tx;
     const float h  = 1.0f / (1.0f + c);
     const float vd = vx * dx + vy * dy;
-    const float gx = c * dx - vy * dz + h * vd * vx;
-    const float gy = c * dy + vx * dz + h * vd * vy;
+    const float gx = c * dx + vy * dz + h * vd * vx;
+    const float gy = c * dy - vx * dz + h * vd * vy;
     const float gz = c * dz + (vx * dy - vy * dx);
     // Moller-Hughes near +-z (|c -+ 1| < 1e-3): the product of the reflections about
     // u = (x - z)/|x - z| and w = (x - t)/|x - t|, x = (1,0,0):
