@@ -168,6 +168,53 @@ int mqi_trace_rays(mqi_ctx* ctx, int child_id, const float* rays, uint64_t n_ray
  * dEdx (negative, MeV/mm in water), beta^2, Te_max, momentum}. */
 int mqi_eval_physics(mqi_ctx* ctx, const float* energies, uint64_t n, float* out);
 
+/* ---- statistics --------------------------------------------------------------------------- */
+
+/* Add tps_env's statistics pair to a child (Dose_stat and DoseSquare_stat,
+ * moqui/base/environments/mqi_tps_env.hpp:936-960): per-step dose_to_water and its square, keyed by
+ * the stat ROI's mask index (roi_t::get_mask_idx, moqui/base/mqi_roi.hpp:58-69) as the _stat
+ * kernel's last two scorers are (mqi_transport.hpp:353-364).  DIRECT: every voxel (voxel 0
+ * included); INDIRECT: roi_start holds one mask index per voxel (0xFFFFFFFF = outside) and
+ * roi_length is the mask size; CONTOUR: start/stride/acc as roi_t.  A child carrying the pair is
+ * scored like the _stat kernel: its other scorers are inserted once per step. */
+int mqi_add_stat_scorers(mqi_ctx* ctx, int child_id, int roi_method, uint32_t roi_length,
+                         const uint32_t* roi_start, const uint32_t* roi_stride,
+                         const uint32_t* roi_acc, int* dose_id, int* dose2_id);
+
+/* The reference's uncertainty estimate (calculate_standard_deviation,
+ * moqui/kernel_functions/mqi_variables.hpp:19-48, and tps_env::calculate_stat,
+ * moqui/base/environments/mqi_tps_env.hpp:1338-1426): with n histories, sigma_i =
+ * sqrt((S2_i/n - (S1_i/n)^2)/(n-1)) and mean_i = S1_i/n per scored voxel; returns the average of
+ * sigma_i/mean_i over voxels with mean_i > threshold * max_i mean_i, as a fraction (the reference
+ * prints it x100), and the number of such voxels. */
+int mqi_stat_uncertainty(mqi_ctx* ctx, int dose_id, int dose2_id, uint64_t n_histories,
+                         float threshold, double* mean_rel_sigma, uint64_t* n_voxels);
+
+/* Batch estimator (no counterpart in moqui, whose estimator squares per-step deposits): fold the
+ * scorer's tally -- one batch of histories -- into running per-voxel sums of batch tallies and of
+ * their squares, and zero the tally. */
+int mqi_batch_accumulate(mqi_ctx* ctx, int scorer_id);
+
+/* Relative standard error of the batch mean, averaged over voxels whose batch mean exceeds
+ * threshold * max (>= 2 batches). */
+int mqi_batch_uncertainty(mqi_ctx* ctx, int scorer_id, float threshold, double* mean_rel_sigma,
+                          uint64_t* n_voxels, uint64_t* n_batches);
+
+/* The batch-mean tally (sum of batches / number of batches). */
+int mqi_get_batch_mean(mqi_ctx* ctx, int scorer_id, double* out, uint64_t* n_out, int on_device);
+
+/* calculate_average (moqui/kernel_functions/mqi_variables.hpp:50-66): multiply a tally by weight. */
+int mqi_scale_tally(mqi_ctx* ctx, int scorer_id, double weight);
+
+/* tps_env::run_by_beam_stat (moqui/base/environments/mqi_tps_env.hpp:1241-1336): transport
+ * histories [0, histories_per_run) again with a new seed until the reference estimate over the
+ * stat pair is <= criteria (a fraction, e.g. 0.01) or max_runs runs are done, then scale the
+ * child's other scorers by histories_per_run / histories_done (calculate_average_results,
+ * :1428-1476).  The vertices are re-used each run (moqui re-samples them). */
+int mqi_run_until_stat(mqi_ctx* ctx, int dose_id, int dose2_id, uint64_t histories_per_run,
+                       float criteria, float threshold, uint64_t max_runs, uint64_t seed,
+                       uint64_t* histories_done, double* achieved);
+
 /* Launch shape of the transport (no counterpart in moqui, whose launch is fixed at 512 threads per
  * block).  block: threads per block (multiple of 32, <= 256); blocks_per_sm: resident blocks per
  * SM the wave kernel is launched with; slice_steps: voxel steps a track takes before it is

@@ -33,6 +33,8 @@ EXPORTS = (
     "mqi_add_child", "mqi_set_density", "mqi_set_hu", "mqi_add_scorer", "mqi_set_vertices",
     "mqi_transport", "mqi_get_tally", "mqi_reset_tallies", "mqi_get_stats", "mqi_hu_to_density",
     "mqi_trace_rays", "mqi_eval_physics", "mqi_set_tuning", "mqi_transport_noalloc", "mqi_version",
+    "mqi_add_stat_scorers", "mqi_stat_uncertainty", "mqi_batch_accumulate", "mqi_batch_uncertainty",
+    "mqi_get_batch_mean", "mqi_scale_tally", "mqi_run_until_stat",
 )
 
 VERTEX_DTYPE = np.dtype([("ke", "<f4"), ("pos", "<f4", (3,)), ("dir", "<f4", (3,))])
@@ -92,6 +94,13 @@ def load(path: Optional[str] = None) -> C.CDLL:
         "mqi_set_tuning": (i32, [vp, i32, i32, i32, i32]),
         "mqi_transport_noalloc": (i32, [i32, i32, i32, vp, vp, vp, vp, vp, u64, i32, i32, u64, vp, vp]),
         "mqi_version": (C.c_char_p, []),
+        "mqi_add_stat_scorers": (i32, [vp, i32, i32, u32, vp, vp, vp, P(i32), P(i32)]),
+        "mqi_stat_uncertainty": (i32, [vp, i32, i32, u64, f32, P(C.c_double), P(u64)]),
+        "mqi_batch_accumulate": (i32, [vp, i32]),
+        "mqi_batch_uncertainty": (i32, [vp, i32, f32, P(C.c_double), P(u64), P(u64)]),
+        "mqi_get_batch_mean": (i32, [vp, i32, vp, P(u64), i32]),
+        "mqi_scale_tally": (i32, [vp, i32, C.c_double]),
+        "mqi_run_until_stat": (i32, [vp, i32, i32, u64, f32, f32, u64, u64, P(u64), P(C.c_double)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -253,3 +262,47 @@ class Context:
     def tally_to_ptr(self, scorer: int, ptr: int, on_device: bool) -> None:
         n = C.c_uint64(0)
         self._check(self.lib.mqi_get_tally(self.h, scorer, C.c_void_p(ptr), C.byref(n), int(on_device)), self.h)
+
+    # ---- statistics ----
+    def add_stat_scorers(self, child: int, roi_method: int = ROI_DIRECT, start=None, stride=None, acc=None,
+                         mask_size: int = 0) -> tuple[int, int]:
+        arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.uint32) for a in (start, stride, acc)]
+        length = mask_size if roi_method == ROI_INDIRECT else (0 if arrs[1] is None else len(arrs[1]))
+        a, b = C.c_int(-1), C.c_int(-1)
+        self._check(self.lib.mqi_add_stat_scorers(self.h, child, roi_method, length, _ptr(arrs[0]), _ptr(arrs[1]),
+                                                  _ptr(arrs[2]), C.byref(a), C.byref(b)), self.h)
+        self.scorers += [a.value, b.value]
+        return a.value, b.value
+
+    def stat_uncertainty(self, dose_id: int, dose2_id: int, n_histories: int, threshold: float) -> tuple[float, int]:
+        v, n = C.c_double(0), C.c_uint64(0)
+        self._check(self.lib.mqi_stat_uncertainty(self.h, dose_id, dose2_id, n_histories, C.c_float(threshold),
+                                                  C.byref(v), C.byref(n)), self.h)
+        return v.value, n.value
+
+    def batch_accumulate(self, scorer: int) -> None:
+        self._check(self.lib.mqi_batch_accumulate(self.h, scorer), self.h)
+
+    def batch_uncertainty(self, scorer: int, threshold: float) -> tuple[float, int, int]:
+        v, n, b = C.c_double(0), C.c_uint64(0), C.c_uint64(0)
+        self._check(self.lib.mqi_batch_uncertainty(self.h, scorer, C.c_float(threshold), C.byref(v), C.byref(n),
+                                                   C.byref(b)), self.h)
+        return v.value, n.value, b.value
+
+    def batch_mean(self, scorer: int) -> np.ndarray:
+        n = C.c_uint64(0)
+        self._check(self.lib.mqi_get_batch_mean(self.h, scorer, None, C.byref(n), 0), self.h)
+        out = np.empty(n.value, np.float64)
+        self._check(self.lib.mqi_get_batch_mean(self.h, scorer, _ptr(out), C.byref(n), 0), self.h)
+        return out
+
+    def scale_tally(self, scorer: int, weight: float) -> None:
+        self._check(self.lib.mqi_scale_tally(self.h, scorer, C.c_double(weight)), self.h)
+
+    def run_until_stat(self, dose_id: int, dose2_id: int, histories_per_run: int, criteria: float, threshold: float,
+                       max_runs: int, seed: int) -> tuple[int, float]:
+        done, got = C.c_uint64(0), C.c_double(0)
+        self._check(self.lib.mqi_run_until_stat(self.h, dose_id, dose2_id, histories_per_run, C.c_float(criteria),
+                                                C.c_float(threshold), max_runs, seed, C.byref(done), C.byref(got)),
+                    self.h)
+        return done.value, got.value

@@ -45,6 +45,9 @@ struct ScorerHost {
     uint32_t* acc = nullptr;
     double*   tally = nullptr;
     uint64_t  tally_len = 0;
+    double*   batch_s1 = nullptr;   // batch estimator: running sums of batch tallies and squares
+    double*   batch_s2 = nullptr;
+    uint64_t  n_batches = 0;
 };
 
 struct QueueBuf {
@@ -85,6 +88,7 @@ struct mqi_ctx {
     uint64_t                wave_launches = 0;
     double                  wave_ms = 0.0;
     cudaEvent_t             ev0 = nullptr, ev1 = nullptr;
+    unsigned long long*     stat_scratch = nullptr;   // 3 x u64 for the statistics reductions
 };
 
 namespace
@@ -234,7 +238,9 @@ mqi_destroy(mqi_ctx* c) {
     }
     for (auto& s : c->scorers) {
         cudaFree(s.start); cudaFree(s.stride); cudaFree(s.acc); cudaFree(s.tally);
+        cudaFree(s.batch_s1); cudaFree(s.batch_s2);
     }
+    cudaFree(c->stat_scratch);
     cudaFree(c->vertices);
     cudaFree(c->spot_ids);
     free_queue(c->qa);
@@ -518,10 +524,13 @@ mqi_transport(mqi_ctx* c, uint64_t h0, uint64_t h1, uint64_t seed) {
         ++ch.n_scorers;
     }
     // Non-stat kernel quirk (mqi_transport.hpp:204-225): with n >= 3 scorers on a node, scorers
-    // 0..n-3 are inserted twice per step.
+    // 0..n-3 are inserted twice per step.  A node that carries the statistics pair runs the _stat
+    // kernel instead (mqi_transport.hpp:342-364), which scores each scorer once.
     for (int i = 0; i < P.n_children; ++i) {
         const ChildDev& ch = P.child[i];
-        if (ch.n_scorers >= 3)
+        bool has_stat = false;
+        for (int k = 0; k < ch.n_scorers; ++k) has_stat = has_stat || P.scorer[ch.scorer_begin + k].stat_mode;
+        if (ch.n_scorers >= 3 && !has_stat)
             for (int k = 0; k < ch.n_scorers - 2; ++k) P.scorer[ch.scorer_begin + k].double_score = 1;
     }
     P.physics_debug   = c->physics_debug;
@@ -703,6 +712,208 @@ mqi_eval_physics(mqi_ctx* c, const float* energies, uint64_t n, float* out) {
     cudaFree(de);
     cudaFree(dout);
     if (e != cudaSuccess) return cuda_fail(c, e, "mqi_eval_physics");
+    return MQI_OK;
+}
+
+}   // extern "C"
+
+// ------------------------------------------------------------------------------------------
+// Statistics: the stat scorer pair, the reference estimator, the batch estimator, averaging
+// ------------------------------------------------------------------------------------------
+namespace
+{
+
+int
+ensure_stat_scratch(mqi_ctx* c) {
+    if (!c->stat_scratch) MQI_CUDA(c, cudaMalloc(&c->stat_scratch, 4 * sizeof(unsigned long long)), "statistics scratch");
+    return MQI_OK;
+}
+
+int
+read_stat(mqi_ctx* c, double* mean_rel, uint64_t* n_vox) {
+    unsigned long long h[3] = { 0, 0, 0 };
+    MQI_CUDA(c, cudaMemcpyAsync(h, c->stat_scratch, sizeof(h), cudaMemcpyDeviceToHost, c->stream), "statistics");
+    MQI_CUDA(c, cudaStreamSynchronize(c->stream), "statistics");
+    double sum = 0.0;
+    std::memcpy(&sum, &h[2], sizeof(sum));
+    if (n_vox) *n_vox = h[1];
+    if (mean_rel) *mean_rel = h[1] ? sum / (double) h[1] : 0.0;
+    return MQI_OK;
+}
+
+}   // namespace
+
+extern "C" {
+
+int
+mqi_add_stat_scorers(mqi_ctx* c, int child_id, int roi_method, uint32_t roi_length, const uint32_t* roi_start,
+                     const uint32_t* roi_stride, const uint32_t* roi_acc, int* dose_id, int* dose2_id) {
+    if (!valid_ctx(c)) return fail(c, MQI_ERR_INVALID, "mqi_add_stat_scorers: ctx is NULL");
+    if (child_id < 0 || child_id >= (int) c->children.size())
+        return fail(c, MQI_ERR_INVALID, "mqi_add_stat_scorers: no such child");
+    if ((int) c->scorers.size() + 2 > kMaxScorers) return fail(c, MQI_ERR_INVALID, "mqi_add_stat_scorers: too many scorers");
+    if (!c->scorers.empty() && c->scorers.back().child != child_id)
+        for (auto& s : c->scorers)
+            if (s.child == child_id) return fail(c, MQI_ERR_INVALID, "mqi_add_stat_scorers: add a child's scorers together");
+    const ChildHost& ch   = c->children[child_id];
+    const uint64_t   nvox = (uint64_t) ch.nx * ch.ny * ch.nz;
+    DeviceGuard g(c->device);
+    ScorerHost proto;
+    proto.child      = child_id;
+    proto.roi_method = roi_method;
+    proto.stat_mode  = 1;
+    proto.roi_len    = roi_length;
+    if (roi_method == MQI_ROI_DIRECT) {
+        proto.tally_len = nvox;
+    } else if (roi_method == MQI_ROI_INDIRECT) {
+        if (!roi_start || roi_length == 0)
+            return fail(c, MQI_ERR_INVALID, "mqi_add_stat_scorers: INDIRECT needs roi_start (mask index per voxel) and the mask size");
+        proto.tally_len = roi_length;
+    } else if (roi_method == MQI_ROI_CONTOUR) {
+        if (!roi_start || !roi_stride || !roi_acc || roi_length == 0)
+            return fail(c, MQI_ERR_INVALID, "mqi_add_stat_scorers: CONTOUR needs start/stride/acc arrays");
+        proto.tally_len = roi_acc[roi_length - 1];
+    } else {
+        return fail(c, MQI_ERR_INVALID, "mqi_add_stat_scorers: unknown roi method");
+    }
+    int ids[2];
+    const int types[2] = { MQI_SCORER_DOSE_W, MQI_SCORER_DOSE_W2 };
+    for (int k = 0; k < 2; ++k) {
+        ScorerHost s = proto;
+        s.type       = types[k];
+        const uint64_t n_start = (roi_method == MQI_ROI_INDIRECT) ? nvox : roi_length;
+        if (roi_method != MQI_ROI_DIRECT) {
+            MQI_CUDA(c, cudaMalloc(&s.start, n_start * sizeof(uint32_t)), "mqi_add_stat_scorers");
+            MQI_CUDA(c, cudaMemcpy(s.start, roi_start, n_start * sizeof(uint32_t), cudaMemcpyHostToDevice), "mqi_add_stat_scorers");
+        }
+        if (roi_method == MQI_ROI_CONTOUR) {
+            MQI_CUDA(c, cudaMalloc(&s.stride, roi_length * sizeof(uint32_t)), "mqi_add_stat_scorers");
+            MQI_CUDA(c, cudaMalloc(&s.acc, roi_length * sizeof(uint32_t)), "mqi_add_stat_scorers");
+            MQI_CUDA(c, cudaMemcpy(s.stride, roi_stride, roi_length * sizeof(uint32_t), cudaMemcpyHostToDevice), "mqi_add_stat_scorers");
+            MQI_CUDA(c, cudaMemcpy(s.acc, roi_acc, roi_length * sizeof(uint32_t), cudaMemcpyHostToDevice), "mqi_add_stat_scorers");
+        }
+        MQI_CUDA(c, cudaMalloc(&s.tally, s.tally_len * sizeof(double)), "mqi_add_stat_scorers");
+        MQI_CUDA(c, cudaMemset(s.tally, 0, s.tally_len * sizeof(double)), "mqi_add_stat_scorers");
+        c->scorers.push_back(s);
+        ids[k] = (int) c->scorers.size() - 1;
+    }
+    if (dose_id) *dose_id = ids[0];
+    if (dose2_id) *dose2_id = ids[1];
+    return MQI_OK;
+}
+
+int
+mqi_stat_uncertainty(mqi_ctx* c, int dose_id, int dose2_id, uint64_t n_histories, float threshold, double* mean_rel_sigma,
+                     uint64_t* n_voxels) {
+    if (!valid_ctx(c)) return fail(c, MQI_ERR_INVALID, "mqi_stat_uncertainty: ctx is NULL");
+    if (dose_id < 0 || dose_id >= (int) c->scorers.size() || dose2_id < 0 || dose2_id >= (int) c->scorers.size())
+        return fail(c, MQI_ERR_INVALID, "mqi_stat_uncertainty: no such scorer");
+    const ScorerHost& a = c->scorers[dose_id];
+    const ScorerHost& b = c->scorers[dose2_id];
+    if (a.tally_len != b.tally_len) return fail(c, MQI_ERR_INVALID, "mqi_stat_uncertainty: tallies differ in size");
+    if (n_histories < 2) return fail(c, MQI_ERR_INVALID, "mqi_stat_uncertainty: needs at least 2 histories");
+    DeviceGuard g(c->device);
+    if (ensure_stat_scratch(c) != MQI_OK) return MQI_ERR_NOMEM;
+    MQI_CUDA(c, launch_stat(a.tally, b.tally, a.tally_len, (double) n_histories, 0, threshold, c->num_sms, c->stat_scratch,
+                            c->stream), "mqi_stat_uncertainty");
+    return read_stat(c, mean_rel_sigma, n_voxels);
+}
+
+int
+mqi_batch_accumulate(mqi_ctx* c, int scorer_id) {
+    if (!valid_ctx(c)) return fail(c, MQI_ERR_INVALID, "mqi_batch_accumulate: ctx is NULL");
+    if (scorer_id < 0 || scorer_id >= (int) c->scorers.size()) return fail(c, MQI_ERR_INVALID, "mqi_batch_accumulate: no such scorer");
+    ScorerHost& s = c->scorers[scorer_id];
+    DeviceGuard g(c->device);
+    if (!s.batch_s1) {
+        MQI_CUDA(c, cudaMalloc(&s.batch_s1, s.tally_len * sizeof(double)), "mqi_batch_accumulate");
+        MQI_CUDA(c, cudaMalloc(&s.batch_s2, s.tally_len * sizeof(double)), "mqi_batch_accumulate");
+        MQI_CUDA(c, cudaMemsetAsync(s.batch_s1, 0, s.tally_len * sizeof(double), c->stream), "mqi_batch_accumulate");
+        MQI_CUDA(c, cudaMemsetAsync(s.batch_s2, 0, s.tally_len * sizeof(double), c->stream), "mqi_batch_accumulate");
+        s.n_batches = 0;
+    }
+    MQI_CUDA(c, launch_batch_fold(s.tally, s.batch_s1, s.batch_s2, s.tally_len, c->num_sms, c->stream), "mqi_batch_accumulate");
+    MQI_CUDA(c, cudaStreamSynchronize(c->stream), "mqi_batch_accumulate");
+    ++s.n_batches;
+    return MQI_OK;
+}
+
+int
+mqi_batch_uncertainty(mqi_ctx* c, int scorer_id, float threshold, double* mean_rel_sigma, uint64_t* n_voxels,
+                      uint64_t* n_batches) {
+    if (!valid_ctx(c)) return fail(c, MQI_ERR_INVALID, "mqi_batch_uncertainty: ctx is NULL");
+    if (scorer_id < 0 || scorer_id >= (int) c->scorers.size()) return fail(c, MQI_ERR_INVALID, "mqi_batch_uncertainty: no such scorer");
+    const ScorerHost& s = c->scorers[scorer_id];
+    if (n_batches) *n_batches = s.n_batches;
+    if (s.n_batches < 2) return fail(c, MQI_ERR_STATE, "mqi_batch_uncertainty: needs at least 2 accumulated batches");
+    DeviceGuard g(c->device);
+    if (ensure_stat_scratch(c) != MQI_OK) return MQI_ERR_NOMEM;
+    MQI_CUDA(c, launch_stat(s.batch_s1, s.batch_s2, s.tally_len, (double) s.n_batches, 1, threshold, c->num_sms,
+                            c->stat_scratch, c->stream), "mqi_batch_uncertainty");
+    return read_stat(c, mean_rel_sigma, n_voxels);
+}
+
+int
+mqi_get_batch_mean(mqi_ctx* c, int scorer_id, double* out, uint64_t* n_out, int on_device) {
+    if (!valid_ctx(c)) return fail(c, MQI_ERR_INVALID, "mqi_get_batch_mean: ctx is NULL");
+    if (scorer_id < 0 || scorer_id >= (int) c->scorers.size()) return fail(c, MQI_ERR_INVALID, "mqi_get_batch_mean: no such scorer");
+    const ScorerHost& s = c->scorers[scorer_id];
+    if (n_out) *n_out = s.tally_len;
+    if (!out) return MQI_OK;
+    if (s.n_batches == 0) return fail(c, MQI_ERR_STATE, "mqi_get_batch_mean: no accumulated batch");
+    DeviceGuard g(c->device);
+    double* dst = out;
+    if (!on_device) MQI_CUDA(c, cudaMalloc(&dst, s.tally_len * sizeof(double)), "mqi_get_batch_mean");
+    cudaError_t e = launch_copy_scaled(s.batch_s1, dst, s.tally_len, 1.0 / (double) s.n_batches, c->num_sms, c->stream);
+    if (e == cudaSuccess && !on_device)
+        e = cudaMemcpyAsync(out, dst, s.tally_len * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (!on_device) cudaFree(dst);
+    if (e != cudaSuccess) return cuda_fail(c, e, "mqi_get_batch_mean");
+    return MQI_OK;
+}
+
+int
+mqi_scale_tally(mqi_ctx* c, int scorer_id, double weight) {
+    if (!valid_ctx(c)) return fail(c, MQI_ERR_INVALID, "mqi_scale_tally: ctx is NULL");
+    if (scorer_id < 0 || scorer_id >= (int) c->scorers.size()) return fail(c, MQI_ERR_INVALID, "mqi_scale_tally: no such scorer");
+    const ScorerHost& s = c->scorers[scorer_id];
+    DeviceGuard g(c->device);
+    MQI_CUDA(c, launch_scale(s.tally, s.tally_len, weight, c->num_sms, c->stream), "mqi_scale_tally");
+    MQI_CUDA(c, cudaStreamSynchronize(c->stream), "mqi_scale_tally");
+    return MQI_OK;
+}
+
+int
+mqi_run_until_stat(mqi_ctx* c, int dose_id, int dose2_id, uint64_t histories_per_run, float criteria, float threshold,
+                   uint64_t max_runs, uint64_t seed, uint64_t* histories_done, double* achieved) {
+    if (!valid_ctx(c)) return fail(c, MQI_ERR_INVALID, "mqi_run_until_stat: ctx is NULL");
+    if (histories_per_run == 0 || histories_per_run > c->n_vertices)
+        return fail(c, MQI_ERR_INVALID, "mqi_run_until_stat: histories_per_run must be 1..number of vertices");
+    if (dose_id < 0 || dose_id >= (int) c->scorers.size() || !c->scorers[dose_id].stat_mode)
+        return fail(c, MQI_ERR_INVALID, "mqi_run_until_stat: dose_id must be a stat scorer");
+    uint64_t done = 0;
+    double   stat = 1.0;   // current_stat = 100% before the first run (mqi_tps_env.hpp:1244)
+    for (uint64_t run = 0; run < max_runs && stat > (double) criteria; ++run) {
+        const int rc = mqi_transport(c, 0, histories_per_run, seed + 0x9E3779B97F4A7C15ull * run);
+        if (rc != MQI_OK) return rc;
+        done += histories_per_run;
+        const int rs = mqi_stat_uncertainty(c, dose_id, dose2_id, done, threshold, &stat, nullptr);
+        if (rs != MQI_OK) return rs;
+    }
+    // calculate_average_results (mqi_tps_env.hpp:1428-1476): the child's other scorers are scaled
+    // to the planned number of histories
+    const int child = c->scorers[dose_id].child;
+    const double w  = (double) histories_per_run / (double) done;
+    for (int i = 0; i < (int) c->scorers.size(); ++i) {
+        const ScorerHost& s = c->scorers[i];
+        if (s.child == child && !s.stat_mode) {
+            const int rc = mqi_scale_tally(c, i, w);
+            if (rc != MQI_OK) return rc;
+        }
+    }
+    if (histories_done) *histories_done = done;
+    if (achieved) *achieved = stat;
     return MQI_OK;
 }
 

@@ -96,6 +96,11 @@ cudaError_t launch_hu_to_density(const float* corr, const int16_t* hu, float* rh
                                  cudaStream_t s);
 cudaError_t launch_trace_rays(const ChildDev& c, const float* rays, uint64_t n_rays, uint32_t max_steps,
                               uint64_t* cnb, float* dist, int32_t* cells, uint32_t* counts, cudaStream_t s);
+cudaError_t launch_stat(const double* s1, const double* s2, uint64_t n, double nh, int mode, float threshold, int sms,
+                        unsigned long long* scratch, cudaStream_t s);
+cudaError_t launch_batch_fold(double* tally, double* s1, double* s2, uint64_t n, int sms, cudaStream_t s);
+cudaError_t launch_scale(double* a, uint64_t n, double w, int sms, cudaStream_t s);
+cudaError_t launch_copy_scaled(const double* a, double* out, uint64_t n, double w, int sms, cudaStream_t s);
 cudaError_t launch_eval_physics(const float* tables, const float* e, uint64_t n, float* out, cudaStream_t s);
 
 }   // namespace mqi_gpu
