@@ -80,9 +80,12 @@ make_grid(const ChildDev& c, const float* sxe, const float* sye, const float* sz
 /// one FP64 atomic is issued per distinct voxel.
 __device__ inline void
 tally_add(double* tally, uint32_t key, double v, bool valid) {
-    const unsigned mask  = __activemask();
-    const uint32_t k     = valid ? key : 0xFFFFFFFFu;
-    const unsigned peers = __match_any_sync(mask, k);
+    // Lanes are grouped by the target address, not by the voxel alone: under independent thread
+    // scheduling lanes of one warp can reach this instruction from different iterations of the
+    // scorer loop (different tallies) with the same voxel index.
+    const unsigned           mask  = __activemask();
+    const unsigned long long k     = valid ? (unsigned long long) (tally + key) : 0ull;
+    const unsigned           peers = __match_any_sync(mask, k);
     if (!valid) return;
     if (__popc(peers) == 1) {
         atomicAdd(&tally[key], v);
