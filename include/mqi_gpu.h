@@ -67,6 +67,20 @@ typedef struct {
     float dir[3]; /* unit vector */
 } mqi_vertex;
 
+/* ---- a pencil-beam spot of a plan: moqui's beamlet = energy pdf x 6-D phase-space pdf x coordinate
+ *      transform (moqui/base/mqi_beamlet.hpp:40-90) with the Gaussian phsp_6d
+ *      (moqui/base/distributions/mqi_phsp6d.hpp) and norm_1d/const_1d energy ------------------- */
+typedef struct {
+    float    energy;        /* mean kinetic energy, MeV */
+    float    energy_sigma;  /* Gaussian energy spread, MeV (0: mono-energetic, const_1d) */
+    float    mean[5];       /* beam frame: x, y, z (mm) and x', y' (direction cosines) */
+    float    sigma[5];      /* Gaussian sigmas of the five variables above */
+    float    corr[2];       /* x-x' and y-y' correlation */
+    float    rot[9];        /* beam frame -> world rotation, row-major (coordinate_transform) */
+    float    trans[3];      /* beam frame -> world translation, mm */
+    uint64_t histories;     /* histories of this spot */
+} mqi_spot;
+
 /* ---- run counters ------------------------------------------------------------------------- */
 typedef struct {
     uint64_t histories;        /* primaries transported (moqui's tracked_particles)           */
@@ -138,6 +152,23 @@ int mqi_set_vertices(mqi_ctx* ctx, const mqi_vertex* v, const uint32_t* spot_ids
  * tallies.  Replaces transport_particles_patient<float><<<...>>> (mqi_transport.hpp:113-250).
  * Blocks until the work is done. */
 int mqi_transport(mqi_ctx* ctx, uint64_t h0, uint64_t h1, uint64_t seed);
+
+/* A plan of spots whose histories are sampled on the device: history h belongs to spot s when
+ * sum(histories of spots < s) <= h < sum(histories of spots <= s), and spot s is its Dij column.
+ * Replaces beamsource::append_beamlet + the host vertex loop + upload_vertices
+ * (moqui/base/mqi_beamsource.hpp:48-112, moqui/base/environments/mqi_tps_env.hpp:1182-1236).
+ * `total_histories` receives the plan's history count. */
+int mqi_set_spot_plan(mqi_ctx* ctx, const mqi_spot* spots, uint32_t n_spots, uint64_t* total_histories);
+
+/* Transport histories [h0, h1) of the spot plan with run seed `seed`: one queue drain for any
+ * number of spots (one spot per call gives moqui's per-spot runs, tps_env::run_by_spot,
+ * mqi_tps_env.hpp:1477-1603). */
+int mqi_transport_plan(mqi_ctx* ctx, uint64_t h0, uint64_t h1, uint64_t seed);
+
+/* Write the source vertices (and spot ids, when spot_out is not NULL) that mqi_transport_plan
+ * with run seed `seed` starts for histories [h0, h1) of the plan: the sampled beamlet vertices
+ * beamsource produces (mqi_beamlet.hpp:80-90).  Host buffers of h1-h0 entries. */
+int mqi_sample_plan(mqi_ctx* ctx, uint64_t h0, uint64_t h1, uint64_t seed, mqi_vertex* out, uint32_t* spot_out);
 
 /* Copy scorer `scorer_id`'s tally (FP64, roi mask size) to `out`.  Replaces download_node
  * (mqi_download_data.hpp:35-121) followed by x_environment::reshape_data

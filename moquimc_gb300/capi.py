@@ -34,10 +34,16 @@ EXPORTS = (
     "mqi_transport", "mqi_get_tally", "mqi_reset_tallies", "mqi_get_stats", "mqi_hu_to_density",
     "mqi_trace_rays", "mqi_eval_physics", "mqi_set_tuning", "mqi_transport_noalloc", "mqi_version",
     "mqi_add_stat_scorers", "mqi_stat_uncertainty", "mqi_batch_accumulate", "mqi_batch_uncertainty",
-    "mqi_get_batch_mean", "mqi_scale_tally", "mqi_run_until_stat",
+    "mqi_get_batch_mean", "mqi_scale_tally", "mqi_run_until_stat", "mqi_set_spot_plan", "mqi_transport_plan",
+    "mqi_sample_plan",
 )
 
 VERTEX_DTYPE = np.dtype([("ke", "<f4"), ("pos", "<f4", (3,)), ("dir", "<f4", (3,))])
+# mqi_spot (include/mqi_gpu.h): 26 floats, then the 64-bit history count at byte 104
+SPOT_DTYPE = np.dtype({"names": ["energy", "energy_sigma", "mean", "sigma", "corr", "rot", "trans", "histories"],
+                       "formats": ["<f4", "<f4", ("<f4", (5,)), ("<f4", (5,)), ("<f4", (2,)), ("<f4", (9,)),
+                                   ("<f4", (3,)), "<u8"],
+                       "offsets": [0, 4, 8, 28, 48, 56, 92, 104], "itemsize": 112})
 
 
 class MqiStats(C.Structure):
@@ -101,6 +107,9 @@ def load(path: Optional[str] = None) -> C.CDLL:
         "mqi_get_batch_mean": (i32, [vp, i32, vp, P(u64), i32]),
         "mqi_scale_tally": (i32, [vp, i32, C.c_double]),
         "mqi_run_until_stat": (i32, [vp, i32, i32, u64, f32, f32, u64, u64, P(u64), P(C.c_double)]),
+        "mqi_set_spot_plan": (i32, [vp, vp, u32, P(u64)]),
+        "mqi_transport_plan": (i32, [vp, u64, u64, u64]),
+        "mqi_sample_plan": (i32, [vp, u64, u64, u64, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -306,3 +315,22 @@ class Context:
                                                 C.c_float(threshold), max_runs, seed, C.byref(done), C.byref(got)),
                     self.h)
         return done.value, got.value
+
+    # ---- spot plans ----
+    def set_spot_plan(self, spots: np.ndarray) -> int:
+        sp = np.ascontiguousarray(spots, dtype=SPOT_DTYPE)
+        tot = C.c_uint64(0)
+        self._check(self.lib.mqi_set_spot_plan(self.h, _ptr(sp), len(sp), C.byref(tot)), self.h)
+        self.plan_histories = tot.value
+        self.plan_cum = np.concatenate([[0], np.cumsum(sp["histories"].astype(np.uint64))])
+        return tot.value
+
+    def transport_plan(self, h0: int, h1: int, seed: int) -> None:
+        self._check(self.lib.mqi_transport_plan(self.h, h0, h1, seed & 0xFFFFFFFFFFFFFFFF), self.h)
+
+    def sample_plan(self, h0: int, h1: int, seed: int):
+        """Vertices and spot ids mqi_transport_plan starts for histories [h0, h1)."""
+        v = np.empty(h1 - h0, dtype=VERTEX_DTYPE)
+        sid = np.empty(h1 - h0, dtype=np.uint32)
+        self._check(self.lib.mqi_sample_plan(self.h, h0, h1, seed & 0xFFFFFFFFFFFFFFFF, _ptr(v), _ptr(sid)), self.h)
+        return v, sid

@@ -89,6 +89,11 @@ struct mqi_ctx {
     double                  wave_ms = 0.0;
     cudaEvent_t             ev0 = nullptr, ev1 = nullptr;
     unsigned long long*     stat_scratch = nullptr;   // 3 x u64 for the statistics reductions
+    mqi_spot*               plan_spots = nullptr;     // spot plan (device)
+    uint64_t*               plan_cum = nullptr;       // cumulative histories, n_plan_spots + 1 (device)
+    uint32_t                n_plan_spots = 0;
+    uint64_t                plan_histories = 0;
+    std::vector<uint64_t>   plan_cum_host;
 };
 
 namespace
@@ -138,7 +143,7 @@ cudaError_t
 alloc_queue(QueueBuf& b, uint32_t cap) {
     free_queue(b);
     const size_t col   = ((size_t) cap * 4 + 255) & ~(size_t) 255;
-    const int    ncols = 14;
+    const int    ncols = 15;
     cudaError_t  e     = cudaMalloc(&b.base, col * ncols);
     if (e != cudaSuccess) return e;
     char* p = static_cast<char*>(b.base);
@@ -148,6 +153,7 @@ alloc_queue(QueueBuf& b, uint32_t cap) {
     b.q.dx = f(4); b.q.dy = f(5); b.q.dz = f(6); b.q.dE0 = f(7);
     b.q.hist = u(8); b.q.uid_lo = u(9); b.q.uid_hi = u(10); b.q.ctr = u(11); b.q.meta = u(12);
     b.q.cell = reinterpret_cast<int32_t*>(p + col * 13);
+    b.q.spot = u(14);
     b.q.capacity = cap;
     return cudaSuccess;
 }
@@ -241,6 +247,8 @@ mqi_destroy(mqi_ctx* c) {
         cudaFree(s.batch_s1); cudaFree(s.batch_s2);
     }
     cudaFree(c->stat_scratch);
+    cudaFree(c->plan_spots);
+    cudaFree(c->plan_cum);
     cudaFree(c->vertices);
     cudaFree(c->spot_ids);
     free_queue(c->qa);
@@ -479,14 +487,18 @@ mqi_set_vertices(mqi_ctx* c, const mqi_vertex* v, const uint32_t* spot_ids, uint
     return MQI_OK;
 }
 
+}   // extern "C"
+
+namespace
+{
+
+/// The source stream of a plan history is keyed apart from its transport streams.
+constexpr uint32_t kSourceKeyXor = 0xA5A5A5A5u;
+
+/// The queue-drain loop shared by vertex and plan sources: load (or sample) a chunk of primaries,
+/// run waves until a generation is empty, repeat.
 int
-mqi_transport(mqi_ctx* c, uint64_t h0, uint64_t h1, uint64_t seed) {
-    if (!valid_ctx(c)) return fail(c, MQI_ERR_INVALID, "mqi_transport: ctx is NULL");
-    if (c->children.empty()) return fail(c, MQI_ERR_STATE, "mqi_transport: no child geometry");
-    for (auto& ch : c->children)
-        if (!ch.has_rho) return fail(c, MQI_ERR_STATE, "mqi_transport: a child has no density");
-    if (h1 < h0 || h1 > c->n_vertices) return fail(c, MQI_ERR_INVALID, "mqi_transport: history range outside the vertices");
-    if (h0 == h1) return MQI_OK;
+run_transport(mqi_ctx* c, uint64_t h0, uint64_t h1, uint64_t seed, bool plan) {
     DeviceGuard g(c->device);
     const uint32_t chunk = c->primary_chunk;
     const uint32_t need  = chunk * 3u;
@@ -552,7 +564,12 @@ mqi_transport(mqi_ctx* c, uint64_t h0, uint64_t h1, uint64_t seed) {
     QueueBuf* B = &c->qb;
     for (uint64_t h = h0; h < h1; h += chunk) {
         const uint32_t n = (uint32_t) std::min<uint64_t>(chunk, h1 - h);
-        MQI_CUDA(c, launch_load_primaries(A->q, c->vertices, h, n, c->stream), "mqi_transport: load primaries");
+        if (plan)
+            MQI_CUDA(c, launch_sample_primaries(A->q, c->plan_spots, c->plan_cum, c->n_plan_spots, h, n, P.k0,
+                                                P.k1 ^ kSourceKeyXor, c->stream), "mqi_transport: sample primaries");
+        else
+            MQI_CUDA(c, launch_load_primaries(A->q, c->vertices, c->has_spots ? c->spot_ids : nullptr, h, n, c->stream),
+                     "mqi_transport: load primaries");
         ++c->kernel_launches;
         c->host_counts[0] = n;
         MQI_CUDA(c, cudaMemcpyAsync(c->counters + 0, c->host_counts, sizeof(uint32_t), cudaMemcpyHostToDevice, c->stream),
@@ -585,6 +602,87 @@ mqi_transport(mqi_ctx* c, uint64_t h0, uint64_t h1, uint64_t seed) {
         }
     }
     if (c->host_counts[3] & 1u) return fail(c, MQI_ERR_DEVICE, "mqi_transport: a bounded device loop gave up");
+    return MQI_OK;
+}
+
+int
+check_ready(mqi_ctx* c, const char* who) {
+    if (!valid_ctx(c)) return fail(c, MQI_ERR_INVALID, std::string(who) + ": ctx is NULL");
+    if (c->children.empty()) return fail(c, MQI_ERR_STATE, std::string(who) + ": no child geometry");
+    for (auto& ch : c->children)
+        if (!ch.has_rho) return fail(c, MQI_ERR_STATE, std::string(who) + ": a child has no density");
+    return MQI_OK;
+}
+
+}   // namespace
+
+extern "C" {
+
+int
+mqi_transport(mqi_ctx* c, uint64_t h0, uint64_t h1, uint64_t seed) {
+    const int rc = check_ready(c, "mqi_transport");
+    if (rc != MQI_OK) return rc;
+    if (h1 < h0 || h1 > c->n_vertices) return fail(c, MQI_ERR_INVALID, "mqi_transport: history range outside the vertices");
+    if (h0 == h1) return MQI_OK;
+    return run_transport(c, h0, h1, seed, false);
+}
+
+int
+mqi_set_spot_plan(mqi_ctx* c, const mqi_spot* spots, uint32_t n_spots, uint64_t* total_histories) {
+    if (!valid_ctx(c) || (!spots && n_spots)) return fail(c, MQI_ERR_INVALID, "mqi_set_spot_plan: bad argument");
+    std::vector<uint64_t> cum(n_spots + 1, 0);
+    for (uint32_t i = 0; i < n_spots; ++i) cum[i + 1] = cum[i] + spots[i].histories;
+    if (cum[n_spots] > 0xFFFFFFFFull) return fail(c, MQI_ERR_INVALID, "mqi_set_spot_plan: at most 2^32-1 histories per plan");
+    DeviceGuard g(c->device);
+    cudaFree(c->plan_spots);
+    cudaFree(c->plan_cum);
+    c->plan_spots = nullptr;
+    c->plan_cum   = nullptr;
+    MQI_CUDA(c, cudaMalloc(&c->plan_spots, std::max<size_t>(n_spots, 1) * sizeof(mqi_spot)), "mqi_set_spot_plan");
+    MQI_CUDA(c, cudaMalloc(&c->plan_cum, (n_spots + 1) * sizeof(uint64_t)), "mqi_set_spot_plan");
+    if (n_spots) MQI_CUDA(c, cudaMemcpy(c->plan_spots, spots, n_spots * sizeof(mqi_spot), cudaMemcpyHostToDevice), "mqi_set_spot_plan");
+    MQI_CUDA(c, cudaMemcpy(c->plan_cum, cum.data(), (n_spots + 1) * sizeof(uint64_t), cudaMemcpyHostToDevice), "mqi_set_spot_plan");
+    c->n_plan_spots    = n_spots;
+    c->plan_histories  = cum[n_spots];
+    c->plan_cum_host   = cum;
+    if (total_histories) *total_histories = cum[n_spots];
+    return MQI_OK;
+}
+
+int
+mqi_transport_plan(mqi_ctx* c, uint64_t h0, uint64_t h1, uint64_t seed) {
+    const int rc = check_ready(c, "mqi_transport_plan");
+    if (rc != MQI_OK) return rc;
+    if (!c->plan_spots) return fail(c, MQI_ERR_STATE, "mqi_transport_plan: no spot plan");
+    if (h1 < h0 || h1 > c->plan_histories) return fail(c, MQI_ERR_INVALID, "mqi_transport_plan: history range outside the plan");
+    if (h0 == h1) return MQI_OK;
+    return run_transport(c, h0, h1, seed, true);
+}
+
+int
+mqi_sample_plan(mqi_ctx* c, uint64_t h0, uint64_t h1, uint64_t seed, mqi_vertex* out, uint32_t* spot_out) {
+    if (!valid_ctx(c)) return fail(c, MQI_ERR_INVALID, "mqi_sample_plan: ctx is NULL");
+    if (!c->plan_spots) return fail(c, MQI_ERR_STATE, "mqi_sample_plan: no spot plan");
+    if (h1 < h0 || h1 > c->plan_histories) return fail(c, MQI_ERR_INVALID, "mqi_sample_plan: history range outside the plan");
+    if (h0 == h1) return MQI_OK;
+    if (!out) return fail(c, MQI_ERR_INVALID, "mqi_sample_plan: out is NULL");
+    DeviceGuard g(c->device);
+    const uint64_t n = h1 - h0;
+    mqi_vertex* dv = nullptr;
+    uint32_t*   ds = nullptr;
+    cudaError_t e  = cudaMalloc(&dv, n * sizeof(mqi_vertex));
+    if (e == cudaSuccess && spot_out) e = cudaMalloc(&ds, n * sizeof(uint32_t));
+    for (uint64_t off = 0; e == cudaSuccess && off < n; off += 0x40000000ull) {
+        const uint32_t m = (uint32_t) std::min<uint64_t>(0x40000000ull, n - off);
+        e = launch_sample_vertices(dv + off, ds ? ds + off : nullptr, c->plan_spots, c->plan_cum, c->n_plan_spots,
+                                   h0 + off, m, (uint32_t) seed, (uint32_t) (seed >> 32) ^ kSourceKeyXor, c->stream);
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, dv, n * sizeof(mqi_vertex), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess && ds) e = cudaMemcpyAsync(spot_out, ds, n * sizeof(uint32_t), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaFree(dv);
+    cudaFree(ds);
+    if (e != cudaSuccess) return cuda_fail(c, e, "mqi_sample_plan");
     return MQI_OK;
 }
 

@@ -55,6 +55,7 @@ struct Queue {
     uint32_t* ctr;     // next Philox block of this track
     uint32_t* meta;    // below:16 | primary:1 | ke1_zero:1 | phase:1 | child:3 | npush:10 (bit layout in kernels)
     int32_t*  cell;    // packed cell for phase STEP: x | y << 11 | z << 22 (each < 2048)
+    uint32_t* spot;    // spot (Dij column) of the history, 0xFFFFFFFF when none
     uint32_t  capacity;
 };
 
@@ -87,8 +88,12 @@ struct WaveParams {
 void set_thread_error(const char* msg);
 
 // ---- launchers (mqi_kernels.cu) ----
-cudaError_t launch_load_primaries(const Queue& q, const mqi_vertex* v, uint64_t h0, uint32_t n,
+cudaError_t launch_load_primaries(const Queue& q, const mqi_vertex* v, const uint32_t* spot_ids, uint64_t h0, uint32_t n,
                                   cudaStream_t s);
+cudaError_t launch_sample_primaries(const Queue& q, const mqi_spot* spots, const uint64_t* cum, uint32_t n_spots,
+                                    uint64_t h0, uint32_t n, uint32_t k0, uint32_t k1, cudaStream_t s);
+cudaError_t launch_sample_vertices(mqi_vertex* out, uint32_t* spot_out, const mqi_spot* spots, const uint64_t* cum,
+                                   uint32_t n_spots, uint64_t h0, uint32_t n, uint32_t k0, uint32_t k1, cudaStream_t s);
 cudaError_t launch_wave(const WaveParams& p, int grid, int block, int blocks_per_sm, cudaStream_t s);
 int         wave_smem_bytes(const WaveParams& p);
 int         wave_edge_floats(const ChildDev* c, int n);

@@ -38,6 +38,7 @@ struct Trk {
     int3     cell;
     uint64_t uid;
     uint32_t hist;
+    uint32_t spot;   // spot of the history (Dij column); inherited by daughters
     uint32_t below, npush;
     int      child;
     float    spr0;   // SPR at (voxel density, ke0) when the step computed it, else < 0
@@ -287,10 +288,10 @@ score_local_daughter(Ctx& C, float3 pw, float3 dw, float ke0, float dE0) {
 /// Returns 0 queued, 1 scored locally, 2 queue overflow.
 static __device__ __noinline__ int
 emit_daughter(const WaveParams* P, const Tables* T, int child, const float* xe, const float* ye, const float* ze,
-              bool dbg, uint32_t below, uint64_t uid, uint32_t hist, float ke0, bool ke1_zero, float3 p, float3 d,
-              float dE0) {
+              bool dbg, uint32_t below, uint64_t uid, uint32_t hist, uint32_t spot, float ke0, bool ke1_zero, float3 p,
+              float3 d, float dE0) {
     Ctx C;
-    C.P = P; C.T = T; C.child = child; C.dbg = dbg; C.tcut = 0.0f; C.spot = 0xFFFFFFFFu;
+    C.P = P; C.T = T; C.child = child; C.dbg = dbg; C.tcut = 0.0f; C.spot = spot;
     C.g = make_grid(P->child[child], xe, ye, ze);
     C.n_sec = C.n_local = C.n_drop = C.n_err = 0;
     daughter_to_world(C.g, p, d);
@@ -311,6 +312,7 @@ emit_daughter(const WaveParams* P, const Tables* T, int child, const float* xe, 
     q.ctr[i] = 0;
     q.meta[i] = (below & kMetaBelowMask) | (ke1_zero ? kMetaKe1Zero : 0u);
     q.cell[i] = 0;
+    q.spot[i] = spot;
     return 0;
 }
 
@@ -326,8 +328,8 @@ push_daughter(Ctx& C, Trk& t, float ke0, bool ke1_zero, float3 p, float3 d, floa
     const uint32_t below = t.below + t.npush;
     const uint64_t uid   = daughter_uid(t.uid, t.npush);
     ++t.npush;
-    const int r = emit_daughter(C.P, C.T, C.child, C.g.xe, C.g.ye, C.g.ze, C.dbg, below, uid, t.hist, ke0, ke1_zero, p, d,
-                                dE0);
+    const int r = emit_daughter(C.P, C.T, C.child, C.g.xe, C.g.ye, C.g.ze, C.dbg, below, uid, t.hist, t.spot, ke0, ke1_zero,
+                                p, d, dE0);
     if (r == 0) ++C.n_sec;
     else if (r == 1) ++C.n_local;
     else ++C.n_err;
@@ -629,6 +631,7 @@ load_track(const Queue& q, uint32_t i, Trk& t, Rng& rng, bool& step_phase) {
     t.dE   = q.dE0[i];
     t.ldE  = 0.0f;
     t.hist = q.hist[i];
+    t.spot = q.spot[i];
     t.uid  = (uint64_t) q.uid_lo[i] | ((uint64_t) q.uid_hi[i] << 32);
     t.below   = meta & kMetaBelowMask;
     t.primary = (meta & kMetaPrimary) != 0;
@@ -667,6 +670,7 @@ requeue_track(Ctx& C, const Trk& t, const Rng& rng) {
                 (t.ke1 != t.ke0 ? kMetaKe1Zero : 0u) | kMetaPhaseStep |
                 ((uint32_t) t.child << kMetaChildShift) | ((t.npush & 1023u) << kMetaNpushShift);
     q.cell[i] = t.cell.x | (t.cell.y << 11) | (t.cell.z << 22);
+    q.spot[i] = t.spot;
 }
 
 __device__ __forceinline__ void
@@ -756,7 +760,7 @@ wave_body(const WaveParams& P) {
             }
             C.child = t.child;
             C.g     = make_grid(P.child[t.child], s_edges[t.child][0], s_edges[t.child][1], s_edges[t.child][2]);
-            C.spot  = P.spot_ids ? P.spot_ids[t.hist] : 0xFFFFFFFFu;
+            C.spot  = t.spot;
             to_child(C.g, t.p0, t.d0);
             t.p1 = t.p0;
             t.d1 = t.d0;
@@ -790,7 +794,7 @@ wave_body(const WaveParams& P) {
             continue;
         }
         // ---- one voxel step (mqi_transport.hpp:192-233) ----
-        C.spot = P.spot_ids ? P.spot_ids[t.hist] : 0xFFFFFFFFu;
+        C.spot = t.spot;
         const uint32_t cnb = grid_cnb(C.g, t.cell);
         const float    rho = C.g.rho[cnb];
         const float    d2b = grid_exit(C.g, t.p0, t.d0, t.cell);
@@ -852,7 +856,8 @@ namespace mqi_gpu
 // (track_t::set + push_primary, mqi_track.hpp:124-133, mqi_track_stack.hpp:44-48).
 // ------------------------------------------------------------------------------------------
 __global__ void
-k_load_primaries(Queue q, const mqi_vertex* __restrict__ v, uint64_t h0, uint32_t n) {
+k_load_primaries(Queue q, const mqi_vertex* __restrict__ v, const uint32_t* __restrict__ spot_ids, uint64_t h0,
+                 uint32_t n) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const mqi_vertex x = v[h0 + i];
@@ -870,12 +875,14 @@ k_load_primaries(Queue q, const mqi_vertex* __restrict__ v, uint64_t h0, uint32_
     q.ctr[i]    = 0u;
     q.meta[i]   = kMetaPrimary;
     q.cell[i]   = 0;
+    q.spot[i]   = spot_ids ? spot_ids[h0 + i] : 0xFFFFFFFFu;
 }
 
 cudaError_t
-launch_load_primaries(const Queue& q, const mqi_vertex* v, uint64_t h0, uint32_t n, cudaStream_t s) {
+launch_load_primaries(const Queue& q, const mqi_vertex* v, const uint32_t* spot_ids, uint64_t h0, uint32_t n,
+                      cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    k_load_primaries<<<(n + 255) / 256, 256, 0, s>>>(q, v, h0, n);
+    k_load_primaries<<<(n + 255) / 256, 256, 0, s>>>(q, v, spot_ids, h0, n);
     return cudaGetLastError();
 }
 
@@ -1042,6 +1049,114 @@ cudaError_t
 launch_eval_physics(const float* t, const float* e, uint64_t n, float* out, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     k_eval_physics<<<(unsigned) ((n + 255) / 256 < 1024 ? (n + 255) / 256 : 1024), 256, 0, s>>>(t, e, n, out);
+    return cudaGetLastError();
+}
+
+}   // namespace mqi_gpu
+
+namespace mqi_gpu
+{
+
+// ------------------------------------------------------------------------------------------
+// Device-side source sampling from a spot plan.  The reference samples every vertex on the host
+// with std::default_random_engine (beamlet::operator(), moqui/base/mqi_beamlet.hpp:80-90;
+// phsp_6d, moqui/base/distributions/mqi_phsp6d.hpp:61-79; norm_1d,
+// moqui/base/distributions/mqi_norm_1d.hpp) and uploads them (upload_vertices).  Here each
+// primary is drawn on the device from its own Philox stream (history index, uid all-ones) with
+// the same phase-space law, so a plan of any size needs no host vertex array and no H2D copy.
+// ------------------------------------------------------------------------------------------
+__device__ inline uint32_t
+sample_spot_vertex(const mqi_spot* __restrict__ spots, const uint64_t* __restrict__ cum, uint32_t n_spots, uint64_t h,
+                   uint32_t k0, uint32_t k1, float3& pos, float3& dir, float& ke) {
+    // spot s with cum[s] <= h < cum[s+1]
+    uint32_t lo = 0, hi = n_spots;
+    while (hi - lo > 1) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (cum[mid] <= h) lo = mid; else hi = mid;
+    }
+    const mqi_spot& S = spots[lo];
+    // six normals (Box-Muller) from two Philox blocks of the history's source stream
+    const u32x4 b0 = philox4x32_10(u32x4{ 0u, (uint32_t) h, 0xFFFFFFFFu, 0xFFFFFFFFu }, k0, k1);
+    const u32x4 b1 = philox4x32_10(u32x4{ 1u, (uint32_t) h, 0xFFFFFFFFu, 0xFFFFFFFFu }, k0, k1);
+    float z[6];
+    const uint32_t w[6] = { b0.x, b0.y, b0.z, b0.w, b1.x, b1.y };
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float r = sqrtf(-2.0f * logf(u01(w[2 * k])));
+        float       sn, cs;
+        sincospif(2.0f * u01(w[2 * k + 1]), &sn, &cs);
+        z[2 * k]     = r * cs;
+        z[2 * k + 1] = r * sn;
+    }
+    const float Ux = z[0], Vx = z[1], Uy = z[2], Vy = z[3], Uz = z[4], Ue = z[5];
+    // phsp_6d: position, then direction correlated with position (mqi_phsp6d.hpp:66-78)
+    const float x  = S.mean[0] + S.sigma[0] * Ux;
+    const float y  = S.mean[1] + S.sigma[1] * Uy;
+    const float zz = S.mean[2] + S.sigma[2] * Uz;
+    const float xp = S.mean[3] + S.sigma[3] * (S.corr[0] * Ux + Vx * sqrtf(1.0f - S.corr[0] * S.corr[0]));
+    const float yp = S.mean[4] + S.sigma[4] * (S.corr[1] * Uy + Vy * sqrtf(1.0f - S.corr[1] * S.corr[1]));
+    const float zp = -sqrtf(fmaxf(1.0f - xp * xp - yp * yp, 0.0f));
+    // beamlet: pos = R p + T, dir = R d (mqi_beamlet.hpp:80-90)
+    const float* R = S.rot;
+    pos = make_float3(R[0] * x + R[1] * y + R[2] * zz + S.trans[0], R[3] * x + R[4] * y + R[5] * zz + S.trans[1],
+                      R[6] * x + R[7] * y + R[8] * zz + S.trans[2]);
+    dir = make_float3(R[0] * xp + R[1] * yp + R[2] * zp, R[3] * xp + R[4] * yp + R[5] * zp,
+                      R[6] * xp + R[7] * yp + R[8] * zp);
+    ke  = S.energy + S.energy_sigma * Ue;
+    return lo;
+}
+
+__global__ void
+k_sample_primaries(Queue q, const mqi_spot* __restrict__ spots, const uint64_t* __restrict__ cum, uint32_t n_spots,
+                   uint64_t h0, uint32_t n, uint32_t k0, uint32_t k1) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint64_t h = h0 + i;
+    float3 p, d;
+    float  ke;
+    const uint32_t s = sample_spot_vertex(spots, cum, n_spots, h, k0, k1, p, d, ke);
+    q.px[i] = p.x; q.py[i] = p.y; q.pz[i] = p.z;
+    q.dx[i] = d.x; q.dy[i] = d.y; q.dz[i] = d.z;
+    q.ke[i]     = ke;
+    q.dE0[i]    = 0.0f;
+    q.hist[i]   = (uint32_t) h;
+    q.uid_lo[i] = 0u;
+    q.uid_hi[i] = 0u;
+    q.ctr[i]    = 0u;
+    q.meta[i]   = kMetaPrimary;
+    q.cell[i]   = 0;
+    q.spot[i]   = s;
+}
+
+__global__ void
+k_sample_vertices(mqi_vertex* __restrict__ out, uint32_t* __restrict__ spot_out, const mqi_spot* __restrict__ spots,
+                  const uint64_t* __restrict__ cum, uint32_t n_spots, uint64_t h0, uint32_t n, uint32_t k0, uint32_t k1) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float3 p, d;
+    float  ke;
+    const uint32_t s = sample_spot_vertex(spots, cum, n_spots, h0 + i, k0, k1, p, d, ke);
+    mqi_vertex v;
+    v.ke = ke;
+    v.pos[0] = p.x; v.pos[1] = p.y; v.pos[2] = p.z;
+    v.dir[0] = d.x; v.dir[1] = d.y; v.dir[2] = d.z;
+    out[i] = v;
+    if (spot_out) spot_out[i] = s;
+}
+
+cudaError_t
+launch_sample_primaries(const Queue& q, const mqi_spot* spots, const uint64_t* cum, uint32_t n_spots, uint64_t h0,
+                        uint32_t n, uint32_t k0, uint32_t k1, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_sample_primaries<<<(n + 127) / 128, 128, 0, s>>>(q, spots, cum, n_spots, h0, n, k0, k1);
+    return cudaGetLastError();
+}
+
+cudaError_t
+launch_sample_vertices(mqi_vertex* out, uint32_t* spot_out, const mqi_spot* spots, const uint64_t* cum, uint32_t n_spots,
+                       uint64_t h0, uint32_t n, uint32_t k0, uint32_t k1, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_sample_vertices<<<(n + 127) / 128, 128, 0, s>>>(out, spot_out, spots, cum, n_spots, h0, n, k0, k1);
     return cudaGetLastError();
 }
 

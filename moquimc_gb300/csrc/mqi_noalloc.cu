@@ -38,7 +38,7 @@ namespace
 constexpr uint32_t kNoallocChunk        = 1u << 16;            // primaries per queue generation
 constexpr uint32_t kNoallocQueueCap     = 3u * kNoallocChunk;  // entries per queue
 constexpr size_t   kNoallocCol          = (size_t) kNoallocQueueCap * 4;   // bytes per queue column
-constexpr int      kNoallocCols         = 14;
+constexpr int      kNoallocCols         = 15;
 constexpr size_t   kNoallocQueueBytes   = kNoallocCol * kNoallocCols;
 constexpr size_t   kNoallocCounterBytes = 256;                 // 8 x u32 counters, 8 x u64 stats
 constexpr size_t   kNoallocScratchBytes = 24u << 20;
@@ -109,6 +109,7 @@ carve_queue(unsigned char* base) {
     q.dx = f(4); q.dy = f(5); q.dz = f(6); q.dE0 = f(7);
     q.hist = u(8); q.uid_lo = u(9); q.uid_hi = u(10); q.ctr = u(11); q.meta = u(12);
     q.cell = reinterpret_cast<int32_t*>(base + kNoallocCol * 13);
+    q.spot = u(14);
     q.capacity = kNoallocQueueCap;
     return q;
 }
@@ -187,7 +188,7 @@ mqi_transport_noalloc(int nx, int ny, int nz, const float* d_xe, const float* d_
     Queue*    B = &qb;
     for (uint64_t h = 0; h < n_histories; h += kNoallocChunk) {
         const uint32_t n = (uint32_t) ((n_histories - h) < kNoallocChunk ? (n_histories - h) : kNoallocChunk);
-        e = launch_load_primaries(*A, d_vertices, h, n, stream);
+        e = launch_load_primaries(*A, d_vertices, nullptr, h, n, stream);
         if (e == cudaSuccess) e = cudaMemcpyAsync(counters, &n, sizeof(uint32_t), cudaMemcpyHostToDevice, stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(stream);   // `n` lives on this stack frame
         if (e != cudaSuccess) return noalloc_fail(MQI_ERR_CUDA, std::string("mqi_transport_noalloc: ") + cudaGetErrorString(e));

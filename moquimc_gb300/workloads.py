@@ -6,6 +6,12 @@
 * ``c2``: a 256^3 phantom of 1 mm voxels centred at (0, 0, -128): water (HU 0) with a 30 mm lung
   slab (HU -700) and a 15 mm bone slab (HU 1200) at depths drawn from numpy's default_rng(2) in
   40-180 mm, full lateral extent; one 150 MeV Gaussian spot (sigma 4 mm), 1e6 histories.
+* ``c3``: a synthetic CT of 512x512x200 voxels at 0.98x0.98x2 mm centred at the origin: an
+  ellipsoidal body (semi-axes 180/120/180 mm on x/y/z) whose HU is a Gaussian-smoothed (sigma 5 mm)
+  random field rescaled to mean 40 and s.d. 150, clipped to [-1000, 1500], in air (HU -1000); a
+  plan of 2000 Gaussian spots (sigma 4 mm, no divergence) on a 5 mm grid (50 on x by 40 on y)
+  entering at z = 195 mm along -z, energies uniform in 70-230 MeV, history counts lognormal
+  (median 1e4) clipped to 1e3-1e5.
 """
 from __future__ import annotations
 
@@ -72,4 +78,84 @@ def c2(histories: int = 1_000_000, physics_debug: bool = False) -> Workload:
                     {"lung_depth_mm": lung, "bone_depth_mm": bone})
 
 
-WORKLOADS = {"c1": c1, "c2": c2}
+def ct_hu(nxyz=(512, 512, 200), dxyz=(0.98, 0.98, 2.0), semi=(180.0, 120.0, 180.0), mean=40.0, sd=150.0,
+          smooth_mm=5.0, seed=3) -> np.ndarray:
+    """int16 HU [nz][ny][nx] of the synthetic CT body.  The random field is drawn and smoothed only
+    on the body's bounding box (the air outside does not use it)."""
+    from scipy.ndimage import gaussian_filter
+
+    nx, ny, nz = nxyz
+    centres = [(np.arange(n, dtype=np.float64) + 0.5) * d - 0.5 * n * d for n, d in zip(nxyz, dxyz)]
+    box = [np.where(np.abs(c) <= a + d)[0] for c, a, d in zip(centres, semi, dxyz)]
+    sl = tuple(slice(int(b[0]), int(b[-1]) + 1) for b in box)          # x, y, z ranges
+    rng = np.random.default_rng(seed)
+    shape = (sl[2].stop - sl[2].start, sl[1].stop - sl[1].start, sl[0].stop - sl[0].start)
+    field = rng.standard_normal(shape, dtype=np.float32)
+    field = gaussian_filter(field, sigma=(smooth_mm / dxyz[2], smooth_mm / dxyz[1], smooth_mm / dxyz[0]),
+                            mode="reflect", truncate=3.0)
+    field = (field - field.mean()) / field.std()
+    hu_box = np.clip(np.rint(mean + sd * field), -1000, 1500).astype(np.int16)
+    cz, cy, cx = np.meshgrid(centres[2][sl[2]], centres[1][sl[1]], centres[0][sl[0]], indexing="ij")
+    inside = (cx / semi[0]) ** 2 + (cy / semi[1]) ** 2 + (cz / semi[2]) ** 2 <= 1.0
+    hu = np.full((nz, ny, nx), -1000, np.int16)
+    hu[sl[2], sl[1], sl[0]] = np.where(inside, hu_box, np.int16(-1000))
+    return hu
+
+
+def spot_plan(n_x=50, n_y=40, pitch=5.0, z0=195.0, sigma=4.0, e_range=(70.0, 230.0), median=1e4,
+              h_range=(1e3, 1e5), seed=4) -> np.ndarray:
+    """Spots on a pitch grid centred on the beam axis, beam along -z (identity beam-to-world
+    transform), energies uniform in e_range, history counts lognormal clipped to h_range."""
+    from .capi import SPOT_DTYPE
+
+    rng = np.random.default_rng(seed)
+    n = n_x * n_y
+    sp = np.zeros(n, SPOT_DTYPE)
+    gx = (np.arange(n_x) - 0.5 * (n_x - 1)) * pitch
+    gy = (np.arange(n_y) - 0.5 * (n_y - 1)) * pitch
+    X, Y = np.meshgrid(gx, gy, indexing="xy")
+    sp["energy"] = rng.uniform(*e_range, n).astype(np.float32)
+    sp["mean"][:, 0] = X.ravel()
+    sp["mean"][:, 1] = Y.ravel()
+    sp["mean"][:, 2] = z0
+    sp["sigma"][:, 0] = sigma
+    sp["sigma"][:, 1] = sigma
+    sp["rot"] = np.eye(3, dtype=np.float32).ravel()
+    h = np.exp(rng.normal(np.log(median), np.log(10.0) / 2.0, n))
+    sp["histories"] = np.clip(np.rint(h), h_range[0], h_range[1]).astype(np.uint64)
+    return sp
+
+
+@dataclass
+class PlanWorkload:
+    name: str
+    lxyz: tuple
+    pxyz: tuple
+    nxyz: tuple
+    hu: np.ndarray
+    spots: np.ndarray
+    physics_debug: bool
+    meta: dict = field(default_factory=dict)
+
+    def edges(self):
+        return ph.phantom_box_edges(self.lxyz, self.pxyz, self.nxyz)
+
+    @property
+    def histories(self) -> int:
+        return int(self.spots["histories"].sum())
+
+
+_CT_CACHE: dict = {}
+
+
+def c3(physics_debug: bool = False) -> PlanWorkload:
+    nxyz = (512, 512, 200)
+    key = ("c3", nxyz)
+    if key not in _CT_CACHE:
+        _CT_CACHE[key] = ct_hu(nxyz)
+    hu = _CT_CACHE[key]
+    lxyz = (float(np.float32(512 * 0.98)), float(np.float32(512 * 0.98)), 400.0)
+    return PlanWorkload("c3_synthetic_ct_2000_spots", lxyz, (0.0, 0.0, 0.0), nxyz, hu, spot_plan(), physics_debug)
+
+
+WORKLOADS = {"c1": c1, "c2": c2, "c3": c3}

@@ -55,3 +55,33 @@ def test_create_without_device_fails_cleanly(built_lib):
     assert rc in (-1, -2)
     assert h.value is None
     assert built_lib.mqi_last_error(None)
+
+
+def test_struct_layouts_match_the_header(tmp_path):
+    """The numpy dtypes the binding passes across the ABI have the C structs' offsets and sizes."""
+    import shutil
+    import subprocess
+
+    import numpy as np
+
+    from moquimc_gb300 import capi
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    src = tmp_path / "layout.c"
+    src.write_text(
+        '#include <stdio.h>\n#include <stddef.h>\n#include "mqi_gpu.h"\n'
+        "#define O(t, f) printf(\"%zu \", offsetof(t, f))\n"
+        "int main(void) {\n"
+        " O(mqi_spot, energy); O(mqi_spot, energy_sigma); O(mqi_spot, mean); O(mqi_spot, sigma);\n"
+        " O(mqi_spot, corr); O(mqi_spot, rot); O(mqi_spot, trans); O(mqi_spot, histories);\n"
+        " printf(\"%zu %zu\\n\", sizeof(mqi_spot), sizeof(mqi_vertex));\n return 0;\n}\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = [int(x) for x in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()]
+    d = capi.SPOT_DTYPE
+    assert got[:8] == [d.fields[n][1] for n in d.names]
+    assert got[8] == d.itemsize
+    assert got[9] == capi.VERTEX_DTYPE.itemsize == 28
+    assert np.dtype(capi.SPOT_DTYPE).names[-1] == "histories"
