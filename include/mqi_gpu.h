@@ -170,6 +170,40 @@ int mqi_transport_plan(mqi_ctx* ctx, uint64_t h0, uint64_t h1, uint64_t seed);
  * beamsource produces (mqi_beamlet.hpp:80-90).  Host buffers of h1-h0 entries. */
 int mqi_sample_plan(mqi_ctx* ctx, uint64_t h0, uint64_t h1, uint64_t seed, mqi_vertex* out, uint32_t* spot_out);
 
+/* ---- Dij ------------------------------------------------------------------------------------ */
+
+/* Add a Dij scorer to a child: moqui's DOSE_Dij scorer (scorer<R>(name, 512*512*300*5, fp_dose)
+ * over a key_value table, mqi_tps_env.hpp:920-931): dose_to_water per step keyed by (voxel cnb,
+ * spot index of the history), gated by the ROI like the dense scorers, inserted into an
+ * open-addressing table (insert_hashtable, mqi_transport.hpp:68-111).  `capacity` = table slots,
+ * rounded up to a power of two, 16 bytes each (0: 2^26); a full table makes the transport call
+ * return MQI_ERR_OVERFLOW. */
+int mqi_add_dij_scorer(mqi_ctx* ctx, int child_id, int roi_method, uint32_t roi_length,
+                       const uint32_t* roi_start, const uint32_t* roi_stride, const uint32_t* roi_acc,
+                       uint64_t capacity, int* scorer_id);
+
+/* Build the Dij matrix from the table: n_spots columns (0: the spot plan's count), values = FP64
+ * tally * scale rounded once to FP32 (save_sparse_file's scale: particles per history * RBE *
+ * fractions, mqi_tps_env.hpp:1905-1930).  Builds the spot-row CSR and the voxel-row layout the
+ * products read.  `nnz` receives the entry count.  Transporting again invalidates the matrix. */
+int mqi_dij_build(mqi_ctx* ctx, int scorer_id, uint32_t n_spots, double scale, uint64_t* nnz);
+
+/* The spot-row CSR, the layout of save_to_npz (moqui/base/mqi_io.hpp:251-320): shape
+ * [n_spots, n_voxels], indptr (n_spots + 1), voxel indices ascending within a row, FP32 values. */
+int mqi_dij_get_csr(mqi_ctx* ctx, int scorer_id, uint64_t* indptr, uint32_t* indices, float* data,
+                    int on_device);
+
+/* Table slots, occupied slots, and (after a build) entries and voxel rows of the matrix. */
+int mqi_dij_info(mqi_ctx* ctx, int scorer_id, uint64_t* table_slots, uint64_t* occupied,
+                 uint64_t* nnz, uint64_t* n_voxel_rows);
+
+/* dose = D.w (n_voxels outputs from n_spots weights) and grad = D^T.g (n_spots outputs from
+ * n_voxels inputs); fp64 selects double buffers (the matrix stays FP32).  With on_device = 1 the
+ * buffers are device pointers and the work is queued on the context's stream without a sync.
+ * No reference counterpart: moqui stops at writing the matrix. */
+int mqi_dij_matvec(mqi_ctx* ctx, int scorer_id, const void* w, void* dose, int fp64, int on_device);
+int mqi_dij_rmatvec(mqi_ctx* ctx, int scorer_id, const void* g, void* grad, int fp64, int on_device);
+
 /* Copy scorer `scorer_id`'s tally (FP64, roi mask size) to `out`.  Replaces download_node
  * (mqi_download_data.hpp:35-121) followed by x_environment::reshape_data
  * (moqui/base/environments/mqi_xenvironment.hpp:150-167).  `n_out` receives the element count;

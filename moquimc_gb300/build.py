@@ -22,7 +22,7 @@ LIB = os.path.join(LIB_DIR, "libmqigpu.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
-CUDA_SOURCES = ["mqi_kernels.cu", "mqi_capi.cu", "mqi_noalloc.cu", "mqi_stat.cu"]
+CUDA_SOURCES = ["mqi_kernels.cu", "mqi_capi.cu", "mqi_capi_dij.cu", "mqi_dij.cu", "mqi_noalloc.cu", "mqi_stat.cu"]
 
 
 def nvcc() -> str:

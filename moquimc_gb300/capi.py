@@ -15,6 +15,8 @@ import numpy as np
 from . import build as _build
 
 MQI_OK = 0
+(MQI_ERR_INVALID, MQI_ERR_CUDA, MQI_ERR_NOMEM, MQI_ERR_STATE, MQI_ERR_UNSUPPORTED, MQI_ERR_OVERFLOW,
+ MQI_ERR_DEVICE) = range(-1, -8, -1)
 ERRORS = {
     -1: "MQI_ERR_INVALID", -2: "MQI_ERR_CUDA", -3: "MQI_ERR_NOMEM", -4: "MQI_ERR_STATE",
     -5: "MQI_ERR_UNSUPPORTED", -6: "MQI_ERR_OVERFLOW", -7: "MQI_ERR_DEVICE",
@@ -35,7 +37,8 @@ EXPORTS = (
     "mqi_trace_rays", "mqi_eval_physics", "mqi_set_tuning", "mqi_transport_noalloc", "mqi_version",
     "mqi_add_stat_scorers", "mqi_stat_uncertainty", "mqi_batch_accumulate", "mqi_batch_uncertainty",
     "mqi_get_batch_mean", "mqi_scale_tally", "mqi_run_until_stat", "mqi_set_spot_plan", "mqi_transport_plan",
-    "mqi_sample_plan",
+    "mqi_sample_plan", "mqi_add_dij_scorer", "mqi_dij_build", "mqi_dij_get_csr", "mqi_dij_info",
+    "mqi_dij_matvec", "mqi_dij_rmatvec",
 )
 
 VERTEX_DTYPE = np.dtype([("ke", "<f4"), ("pos", "<f4", (3,)), ("dir", "<f4", (3,))])
@@ -110,6 +113,12 @@ def load(path: Optional[str] = None) -> C.CDLL:
         "mqi_set_spot_plan": (i32, [vp, vp, u32, P(u64)]),
         "mqi_transport_plan": (i32, [vp, u64, u64, u64]),
         "mqi_sample_plan": (i32, [vp, u64, u64, u64, vp, vp]),
+        "mqi_add_dij_scorer": (i32, [vp, i32, i32, u32, vp, vp, vp, u64, P(i32)]),
+        "mqi_dij_build": (i32, [vp, i32, u32, C.c_double, P(u64)]),
+        "mqi_dij_get_csr": (i32, [vp, i32, vp, vp, vp, i32]),
+        "mqi_dij_info": (i32, [vp, i32, P(u64), P(u64), P(u64), P(u64)]),
+        "mqi_dij_matvec": (i32, [vp, i32, vp, vp, i32, i32]),
+        "mqi_dij_rmatvec": (i32, [vp, i32, vp, vp, i32, i32]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -133,6 +142,8 @@ class Context:
         self.h = h
         self.children: list[tuple[int, int, int]] = []
         self.scorers: list[int] = []
+        self._dij_child: dict[int, int] = {}
+        self.plan_cum = np.zeros(1, np.uint64)
 
     def _check(self, rc: int, h) -> None:
         if rc != MQI_OK:
@@ -334,3 +345,41 @@ class Context:
         sid = np.empty(h1 - h0, dtype=np.uint32)
         self._check(self.lib.mqi_sample_plan(self.h, h0, h1, seed & 0xFFFFFFFFFFFFFFFF, _ptr(v), _ptr(sid)), self.h)
         return v, sid
+
+    # ---- Dij ----
+    def add_dij_scorer(self, child: int, capacity: int = 0, roi_method: int = ROI_DIRECT) -> int:
+        out = C.c_int(-1)
+        self._check(self.lib.mqi_add_dij_scorer(self.h, child, roi_method, 0, None, None, None, capacity,
+                                                C.byref(out)), self.h)
+        self.scorers.append(out.value)
+        self._dij_child[out.value] = child
+        return out.value
+
+    def dij_build(self, scorer: int, n_spots: int = 0, scale: float = 1.0):
+        """Build the Dij matrix; returns a dij.DijOperator."""
+        from .dij import DijOperator
+
+        nnz = C.c_uint64(0)
+        self._check(self.lib.mqi_dij_build(self.h, scorer, n_spots, scale, C.byref(nnz)), self.h)
+        n_vox = int(np.prod(self.children[self._dij_child[scorer]]))
+        ns = n_spots or len(self.plan_cum) - 1
+        return DijOperator(self, scorer, ns, n_vox, nnz.value)
+
+    def dij_info(self, scorer: int) -> dict:
+        v = [C.c_uint64(0) for _ in range(4)]
+        self._check(self.lib.mqi_dij_info(self.h, scorer, *[C.byref(x) for x in v]), self.h)
+        return dict(zip(("table_slots", "occupied", "nnz", "voxel_rows"), (x.value for x in v)))
+
+    def dij_matvec(self, scorer: int, w: np.ndarray, n_voxels: int) -> np.ndarray:
+        fp64 = w.dtype == np.float64
+        w = np.ascontiguousarray(w, np.float64 if fp64 else np.float32)
+        out = np.empty(n_voxels, w.dtype)
+        self._check(self.lib.mqi_dij_matvec(self.h, scorer, _ptr(w), _ptr(out), int(fp64), 0), self.h)
+        return out
+
+    def dij_rmatvec(self, scorer: int, g: np.ndarray, n_spots: int) -> np.ndarray:
+        fp64 = g.dtype == np.float64
+        g = np.ascontiguousarray(g, np.float64 if fp64 else np.float32)
+        out = np.empty(n_spots, g.dtype)
+        self._check(self.lib.mqi_dij_rmatvec(self.h, scorer, _ptr(g), _ptr(out), int(fp64), 0), self.h)
+        return out

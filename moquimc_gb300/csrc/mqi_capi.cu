@@ -14,122 +14,13 @@
 
 #include "mqi_device.cuh"
 #include "mqi_gpu.h"
+#include "mqi_ctx.h"
 #include "mqi_internal.h"
 
 using namespace mqi_gpu;
 
 namespace
 {
-
-thread_local std::string g_thread_error;
-
-struct ChildHost {
-    int    nx = 0, ny = 0, nz = 0;
-    float* xe = nullptr;
-    float* ye = nullptr;
-    float* ze = nullptr;
-    float* rho = nullptr;
-    bool   has_rho = false;
-    float  rf[9], ri[9], tr[3];
-    int    identity = 1;
-};
-
-struct ScorerHost {
-    int       child = 0;
-    int       type = 0;
-    int       roi_method = 0;
-    int       stat_mode = 0;
-    uint32_t  roi_len = 0;
-    uint32_t* start = nullptr;
-    uint32_t* stride = nullptr;
-    uint32_t* acc = nullptr;
-    double*   tally = nullptr;
-    uint64_t  tally_len = 0;
-    double*   batch_s1 = nullptr;   // batch estimator: running sums of batch tallies and squares
-    double*   batch_s2 = nullptr;
-    uint64_t  n_batches = 0;
-};
-
-struct QueueBuf {
-    Queue    q{};
-    void*    base = nullptr;
-};
-
-}   // namespace
-
-struct mqi_ctx {
-    int                     device = 0;
-    cudaStream_t            stream = nullptr;
-    bool                    own_stream = false;
-    std::string             err;
-    int                     physics_debug = 0;
-    int                     score_local = 1;
-    std::vector<ChildHost>  children;
-    std::vector<ScorerHost> scorers;
-    mqi_vertex*             vertices = nullptr;
-    uint64_t                n_vertices = 0;
-    uint64_t                vertex_cap = 0;
-    uint32_t*               spot_ids = nullptr;
-    uint64_t                spot_cap = 0;
-    bool                    has_spots = false;
-    QueueBuf                qa, qb;
-    uint32_t                queue_cap = 0;
-    uint32_t*               counters = nullptr;     // [0,1] queue sizes, [2] head, [3] error flag
-    unsigned long long*     stats = nullptr;        // 8 x u64
-    uint32_t*               host_counts = nullptr;  // pinned: 4 x u32
-    float*                  tables = nullptr;       // 6*600 physics + 3996 HU correction
-    int                     num_sms = 0;
-    int                     wave_block = 128;
-    int                     wave_grid = 0;
-    uint32_t                max_slice_steps = 0;
-    uint32_t                primary_chunk = 1u << 21;
-    uint64_t                waves = 0;
-    uint64_t                kernel_launches = 0;
-    uint64_t                wave_launches = 0;
-    double                  wave_ms = 0.0;
-    cudaEvent_t             ev0 = nullptr, ev1 = nullptr;
-    unsigned long long*     stat_scratch = nullptr;   // 3 x u64 for the statistics reductions
-    mqi_spot*               plan_spots = nullptr;     // spot plan (device)
-    uint64_t*               plan_cum = nullptr;       // cumulative histories, n_plan_spots + 1 (device)
-    uint32_t                n_plan_spots = 0;
-    uint64_t                plan_histories = 0;
-    std::vector<uint64_t>   plan_cum_host;
-};
-
-namespace
-{
-
-int
-fail(mqi_ctx* c, int code, const std::string& msg) {
-    if (c) c->err = msg;
-    g_thread_error = msg;
-    return code;
-}
-
-int
-cuda_fail(mqi_ctx* c, cudaError_t e, const char* what) {
-    return fail(c, e == cudaErrorMemoryAllocation ? MQI_ERR_NOMEM : MQI_ERR_CUDA,
-                std::string(what) + ": " + cudaGetErrorString(e));
-}
-
-#define MQI_CUDA(c, expr, what)                           \
-    do {                                                  \
-        cudaError_t _e = (expr);                          \
-        if (_e != cudaSuccess) return cuda_fail(c, _e, what); \
-    } while (0)
-
-struct DeviceGuard {
-    int prev = -1;
-    explicit DeviceGuard(int dev) {
-        cudaGetDevice(&prev);
-        if (prev != dev) cudaSetDevice(dev);
-    }
-    ~DeviceGuard() {
-        int cur = -1;
-        cudaGetDevice(&cur);
-        if (prev >= 0 && cur != prev) cudaSetDevice(prev);
-    }
-};
 
 void
 free_queue(QueueBuf& b) {
@@ -163,16 +54,17 @@ identity3(float* m) {
     for (int i = 0; i < 9; ++i) m[i] = (i % 4 == 0) ? 1.0f : 0.0f;
 }
 
-bool
-valid_ctx(mqi_ctx* c) {
-    return c != nullptr;
-}
-
 }   // namespace
+
+std::string&
+mqi_gpu::thread_error_slot() {
+    thread_local std::string msg;
+    return msg;
+}
 
 void
 mqi_gpu::set_thread_error(const char* msg) {
-    g_thread_error = msg ? msg : "";
+    thread_error_slot() = msg ? msg : "";
 }
 
 extern "C" {
@@ -184,7 +76,7 @@ mqi_version(void) {
 
 const char*
 mqi_last_error(const mqi_ctx* ctx) {
-    return ctx ? ctx->err.c_str() : g_thread_error.c_str();
+    return ctx ? ctx->err.c_str() : thread_error_slot().c_str();
 }
 
 int
@@ -245,6 +137,7 @@ mqi_destroy(mqi_ctx* c) {
     for (auto& s : c->scorers) {
         cudaFree(s.start); cudaFree(s.stride); cudaFree(s.acc); cudaFree(s.tally);
         cudaFree(s.batch_s1); cudaFree(s.batch_s2);
+        dij_release(s);
     }
     cudaFree(c->stat_scratch);
     cudaFree(c->plan_spots);
@@ -531,6 +424,11 @@ run_transport(mqi_ctx* c, uint64_t h0, uint64_t h1, uint64_t seed, bool plan) {
         d.type = s.type; d.roi_method = s.roi_method; d.stat_mode = s.stat_mode;
         d.roi_len = s.roi_len; d.start = s.start; d.stride = s.stride; d.acc = s.acc;
         d.tally = s.tally; d.tally_len = s.tally_len;
+        d.dij = s.dij; d.dij_mask = s.dij_cap ? s.dij_cap - 1 : 0; d.dij_count = s.dij_count;
+        if (s.dij) {
+            c->scorers[i].csr.built = false;   // new entries invalidate a built matrix
+            P.has_dij = 1;
+        }
         ChildDev& ch = P.child[s.child];
         if (ch.n_scorers == 0) ch.scorer_begin = i;
         ++ch.n_scorers;
@@ -601,6 +499,8 @@ run_transport(mqi_ctx* c, uint64_t h0, uint64_t h1, uint64_t seed, bool plan) {
             cur = 1 - cur;
         }
     }
+    if (c->host_counts[3] & 4u)
+        return fail(c, MQI_ERR_OVERFLOW, "mqi_transport: a Dij table is full (raise its capacity)");
     if (c->host_counts[3] & 1u) return fail(c, MQI_ERR_DEVICE, "mqi_transport: a bounded device loop gave up");
     return MQI_OK;
 }
@@ -704,8 +604,10 @@ int
 mqi_reset_tallies(mqi_ctx* c) {
     if (!valid_ctx(c)) return fail(c, MQI_ERR_INVALID, "mqi_reset_tallies: ctx is NULL");
     DeviceGuard g(c->device);
-    for (auto& s : c->scorers)
-        MQI_CUDA(c, cudaMemsetAsync(s.tally, 0, s.tally_len * sizeof(double), c->stream), "mqi_reset_tallies");
+    for (auto& s : c->scorers) {
+        if (s.type == MQI_SCORER_DIJ) MQI_CUDA(c, dij_reset(s, c->num_sms, c->stream), "mqi_reset_tallies");
+        else MQI_CUDA(c, cudaMemsetAsync(s.tally, 0, s.tally_len * sizeof(double), c->stream), "mqi_reset_tallies");
+    }
     MQI_CUDA(c, cudaMemsetAsync(c->stats, 0, 8 * sizeof(unsigned long long), c->stream), "mqi_reset_tallies");
     MQI_CUDA(c, cudaMemsetAsync(c->counters + 3, 0, sizeof(uint32_t), c->stream), "mqi_reset_tallies");
     MQI_CUDA(c, cudaStreamSynchronize(c->stream), "mqi_reset_tallies");

@@ -1,0 +1,441 @@
+// Dij kernels: compaction of the (spot, voxel) hash table, a stable LSD radix sort, the two CSR
+// layouts, and the sparse products dose = D.w and grad = D^T.g.
+//
+// The reference scores Dij into an open-addressing table keyed by (voxel, spot)
+// (insert_hashtable, moqui/kernel_functions/mqi_transport.hpp:68-111) and writes it as a
+// spot-row CSR npz in table-scan order (save_to_npz, moqui/base/mqi_io.hpp:251-320).  Here the
+// table is compacted and sorted on the device, so both layouts come out in a fixed order:
+//   spot rows  (the reference's npz layout, shape [n_spots, n_voxels]): indptr / voxel / value,
+//              voxels ascending in a row -- the transposed operator, read by D^T.g;
+//   voxel rows (only voxels with an entry, "doubly compressed"): row voxel / indptr / spot /
+//              value, spots ascending in a row -- read by D.w.
+// Both products are gathers with a fixed reduction order: no atomics, reproducible results.
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "mqi_internal.h"
+
+namespace mqi_gpu
+{
+
+namespace
+{
+
+constexpr int kThreads = 256;   // radix sort block
+constexpr int kItems   = 8;     // keys per thread per pass
+constexpr int kTile    = kThreads * kItems;
+constexpr int kScanTile = 2048;
+
+__device__ inline unsigned
+lanemask_lt() {
+    return (1u << (threadIdx.x & 31)) - 1u;
+}
+
+// ---- compaction -----------------------------------------------------------------------------
+
+/// Append every occupied slot as (spot * n_voxels + voxel, slot index); warp-aggregated cursor.
+__global__ void
+k_dij_compact(const DijSlot* __restrict__ tab, uint64_t cap, uint64_t n_voxels, unsigned long long* __restrict__ keys,
+              uint32_t* __restrict__ idx, uint64_t n_max, unsigned long long* __restrict__ cursor) {
+    const uint64_t stride = (uint64_t) gridDim.x * blockDim.x;
+    const uint64_t span   = (cap + stride - 1) / stride * stride;   // every lane runs the same trip count
+    for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < span; i += stride) {
+        unsigned long long k = 0;
+        if (i < cap) k = tab[i].key;
+        const bool     valid = k != 0ull;
+        const unsigned b     = __ballot_sync(0xFFFFFFFFu, valid);
+        if (!b) continue;
+        unsigned long long base = 0;
+        const int          lead = __ffs(b) - 1;
+        if ((int) (threadIdx.x & 31) == lead) base = atomicAdd(cursor, (unsigned long long) __popc(b));
+        base = __shfl_sync(0xFFFFFFFFu, base, lead);
+        if (valid) {
+            const unsigned long long raw   = k - 1ull;
+            const uint64_t           spot  = raw >> 32;
+            const uint64_t           voxel = raw & 0xFFFFFFFFull;
+            const uint64_t           pos   = base + __popc(b & lanemask_lt());
+            if (pos < n_max) {   // the host compares the cursor with n_max afterwards
+                keys[pos] = spot * n_voxels + voxel;
+                idx[pos]  = (uint32_t) i;
+            }
+        }
+    }
+}
+
+// ---- exclusive scan of u32 ------------------------------------------------------------------
+
+__device__ inline uint32_t
+block_exclusive_scan(uint32_t v, uint32_t* warp_sums, uint32_t& total) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    uint32_t  x    = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_sums[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t s = lane < nw ? warp_sums[lane] : 0u;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, s, o);
+            if (lane >= o) s += y;
+        }
+        if (lane < nw) warp_sums[lane] = s;
+    }
+    __syncthreads();
+    const uint32_t warp_off = warp ? warp_sums[warp - 1] : 0u;
+    total                   = warp_sums[nw - 1];
+    __syncthreads();
+    return warp_off + x - v;
+}
+
+/// Per-tile exclusive scan (kScanTile elements per 256-thread block, 8 per thread in order);
+/// tile totals to `sums`.
+__global__ void
+k_scan_tiles(const uint32_t* __restrict__ in, uint32_t* __restrict__ out, uint64_t n, uint32_t* __restrict__ sums) {
+    __shared__ uint32_t ws[32];
+    const uint64_t t0 = (uint64_t) blockIdx.x * kScanTile + (uint64_t) threadIdx.x * 8;
+    uint32_t       v[8], s = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        v[k] = (t0 + k < n) ? in[t0 + k] : 0u;
+        s += v[k];
+    }
+    uint32_t total;
+    uint32_t run = block_exclusive_scan(s, ws, total);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+        if (t0 + k < n) out[t0 + k] = run;
+        run += v[k];
+    }
+    if (threadIdx.x == 0) sums[blockIdx.x] = total;
+}
+
+/// Exclusive scan of the tile totals by one block, in order.
+__global__ void
+k_scan_sums(uint32_t* __restrict__ sums, uint64_t n) {
+    __shared__ uint32_t ws[32];
+    uint32_t carry = 0;
+    for (uint64_t b = 0; b < n; b += blockDim.x) {
+        const uint64_t i = b + threadIdx.x;
+        const uint32_t v = i < n ? sums[i] : 0u;
+        uint32_t total;
+        const uint32_t e = block_exclusive_scan(v, ws, total);
+        if (i < n) sums[i] = carry + e;
+        carry += total;
+        __syncthreads();
+    }
+}
+
+__global__ void
+k_scan_add(uint32_t* __restrict__ out, uint64_t n, const uint32_t* __restrict__ sums) {
+    const uint64_t i = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] += sums[i / kScanTile];
+}
+
+// ---- radix sort -----------------------------------------------------------------------------
+
+__global__ void
+k_radix_hist(const unsigned long long* __restrict__ keys, uint64_t n, int shift, uint32_t* __restrict__ hist,
+             uint32_t n_tiles) {
+    __shared__ uint32_t cnt[256];
+    cnt[threadIdx.x] = 0;
+    __syncthreads();
+    const uint64_t t0 = (uint64_t) blockIdx.x * kTile;
+#pragma unroll
+    for (int r = 0; r < kItems; ++r) {
+        const uint64_t i = t0 + (uint64_t) r * kThreads + threadIdx.x;
+        if (i < n) atomicAdd(&cnt[(keys[i] >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    hist[(uint64_t) threadIdx.x * n_tiles + blockIdx.x] = cnt[threadIdx.x];
+}
+
+/// Stable scatter of one 8-bit digit.  The tile is visited in input order (round, warp, lane);
+/// an element's destination is its tile's digit offset + the count of equal digits before it in
+/// earlier rounds, earlier warps of its round, and lower lanes of its warp.
+__global__ void
+k_radix_scatter(const unsigned long long* __restrict__ kin, const uint32_t* __restrict__ vin,
+                unsigned long long* __restrict__ kout, uint32_t* __restrict__ vout, uint64_t n, int shift,
+                const uint32_t* __restrict__ offs, uint32_t n_tiles) {
+    constexpr int kWarps = kThreads / 32;
+    __shared__ uint32_t base[256];
+    __shared__ uint32_t wcnt[kWarps][256];
+    __shared__ uint32_t wpre[kWarps][256];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    base[threadIdx.x] = offs[(uint64_t) threadIdx.x * n_tiles + blockIdx.x];
+#pragma unroll
+    for (int w = 0; w < kWarps; ++w) wcnt[w][threadIdx.x] = 0;
+    __syncthreads();
+    const uint64_t t0 = (uint64_t) blockIdx.x * kTile;
+    for (int r = 0; r < kItems; ++r) {
+        const uint64_t i     = t0 + (uint64_t) r * kThreads + threadIdx.x;
+        const bool     valid = i < n;
+        unsigned long long k = 0;
+        uint32_t           v = 0;
+        uint32_t           d = 0x100u;   // matches no digit
+        if (valid) {
+            k = kin[i];
+            v = vin[i];
+            d = (uint32_t) ((k >> shift) & 255u);
+        }
+        const unsigned peers = __match_any_sync(0xFFFFFFFFu, d);
+        const uint32_t rank  = __popc(peers & lanemask_lt());
+        if (valid && lane == __ffs(peers) - 1) wcnt[warp][d] = __popc(peers);
+        __syncthreads();
+        {
+            const int dd  = threadIdx.x;
+            uint32_t  run = base[dd];
+#pragma unroll
+            for (int w = 0; w < kWarps; ++w) {
+                const uint32_t c = wcnt[w][dd];
+                wpre[w][dd]      = run;
+                run += c;
+                wcnt[w][dd] = 0;
+            }
+            base[dd] = run;
+        }
+        __syncthreads();
+        if (valid) {
+            const uint32_t pos = wpre[warp][d] + rank;
+            kout[pos] = k;
+            vout[pos] = v;
+        }
+        __syncthreads();
+    }
+}
+
+// ---- CSR assembly ---------------------------------------------------------------------------
+
+/// indptr[r] = lower_bound(keys, r * row_span) for r in [0, n_rows].
+__global__ void
+k_row_bounds(const unsigned long long* __restrict__ keys, uint64_t n, uint64_t row_span, uint64_t n_rows,
+             uint64_t* __restrict__ indptr) {
+    const uint64_t r = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x;
+    if (r > n_rows) return;
+    const unsigned long long target = r * row_span;
+    uint64_t lo = 0, hi = n;
+    while (lo < hi) {
+        const uint64_t mid = (lo + hi) >> 1;
+        if (keys[mid] < target) lo = mid + 1; else hi = mid;
+    }
+    indptr[r] = lo;
+}
+
+/// Spot-row CSR entries: voxel column and FP32 value (FP64 tally x scale, rounded once).
+__global__ void
+k_spot_rows(const unsigned long long* __restrict__ keys, const uint32_t* __restrict__ slot, uint64_t n,
+            uint64_t n_voxels, const DijSlot* __restrict__ tab, double scale, uint32_t* __restrict__ vox,
+            float* __restrict__ val, unsigned long long* __restrict__ vkeys, uint32_t* __restrict__ vpos) {
+    const uint64_t k = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const uint32_t v = (uint32_t) (keys[k] % n_voxels);
+    vox[k]   = v;
+    val[k]   = (float) (tab[slot[k]].value * scale);
+    vkeys[k] = v;
+    vpos[k]  = (uint32_t) k;
+}
+
+__global__ void
+k_row_flags(const unsigned long long* __restrict__ vkeys, uint64_t n, uint32_t* __restrict__ flags) {
+    const uint64_t j = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x;
+    if (j < n) flags[j] = (j == 0 || vkeys[j] != vkeys[j - 1]) ? 1u : 0u;
+}
+
+/// Voxel-row entries: spot column and value from the spot-row entry they came from; row starts.
+__global__ void
+k_voxel_rows(const unsigned long long* __restrict__ vkeys, const uint32_t* __restrict__ vpos, uint64_t n,
+             const unsigned long long* __restrict__ skeys, uint64_t n_voxels, const float* __restrict__ sval,
+             const uint32_t* __restrict__ flags, const uint32_t* __restrict__ rowid, uint32_t* __restrict__ row_voxel,
+             uint64_t* __restrict__ indptr, uint32_t* __restrict__ spot, float* __restrict__ val) {
+    const uint64_t j = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const uint32_t p = vpos[j];
+    spot[j] = (uint32_t) (skeys[p] / n_voxels);
+    val[j]  = sval[p];
+    if (flags[j]) {
+        row_voxel[rowid[j]] = (uint32_t) vkeys[j];
+        indptr[rowid[j]]    = j;
+    }
+    if (j == n - 1) indptr[rowid[j] + flags[j]] = n;
+}
+
+// ---- products -------------------------------------------------------------------------------
+
+/// dose[row_voxel[r]] = sum_k val[k] * w[spot[k]] over voxel rows; 8 lanes per row, the lanes'
+/// partial sums combined in a fixed butterfly.  Accumulates in T.
+template<typename T>
+__global__ void
+k_dij_forward(const uint32_t* __restrict__ row_voxel, const uint64_t* __restrict__ indptr,
+              const uint32_t* __restrict__ spot, const float* __restrict__ val, uint64_t n_rows,
+              const T* __restrict__ w, T* __restrict__ dose) {
+    const uint64_t g      = ((uint64_t) blockIdx.x * blockDim.x + threadIdx.x) >> 3;
+    const int      sub    = threadIdx.x & 7;
+    const uint64_t stride = ((uint64_t) gridDim.x * blockDim.x) >> 3;
+    const uint64_t span   = (n_rows + stride - 1) / stride * stride;
+    for (uint64_t r = g; r < span; r += stride) {
+        T s = T(0);
+        if (r < n_rows) {
+            const uint64_t e = indptr[r + 1];
+            for (uint64_t k = indptr[r] + sub; k < e; k += 8) s += (T) val[k] * w[spot[k]];
+        }
+#pragma unroll
+        for (int o = 4; o > 0; o >>= 1) s += __shfl_xor_sync(0xFFFFFFFFu, s, o, 8);
+        if (r < n_rows && sub == 0) dose[row_voxel[r]] = s;
+    }
+}
+
+/// grad[s] = sum_k val[k] * g[voxel[k]] over spot rows (the transposed operator); one block per
+/// row, per-thread partials in T, block tree in double.
+template<typename T>
+__global__ void
+k_dij_backward(const uint64_t* __restrict__ indptr, const uint32_t* __restrict__ vox, const float* __restrict__ val,
+               uint32_t n_rows, const T* __restrict__ g, T* __restrict__ grad) {
+    __shared__ double part[32];
+    for (uint32_t r = blockIdx.x; r < n_rows; r += gridDim.x) {
+        const uint64_t b = indptr[r], e = indptr[r + 1];
+        T              s = T(0);
+        for (uint64_t k = b + threadIdx.x; k < e; k += blockDim.x) s += (T) val[k] * g[vox[k]];
+        double d = (double) s;
+        for (int o = 16; o > 0; o >>= 1) d += __shfl_down_sync(0xFFFFFFFFu, d, o);
+        if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = d;
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            d = threadIdx.x < (blockDim.x >> 5) ? part[threadIdx.x] : 0.0;
+            for (int o = 16; o > 0; o >>= 1) d += __shfl_down_sync(0xFFFFFFFFu, d, o);
+            if (threadIdx.x == 0) grad[r] = (T) d;
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void
+k_dij_clear(DijSlot* __restrict__ tab, uint64_t cap) {
+    const uint64_t stride = (uint64_t) gridDim.x * blockDim.x;
+    for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < cap; i += stride) {
+        tab[i].key   = 0ull;
+        tab[i].value = 0.0;
+    }
+}
+
+unsigned
+blocks_for(uint64_t n, int per_block) {
+    return (unsigned) ((n + per_block - 1) / per_block);
+}
+
+}   // namespace
+
+cudaError_t
+dij_clear(DijSlot* tab, uint64_t cap, int sms, cudaStream_t s) {
+    k_dij_clear<<<sms * 8, 256, 0, s>>>(tab, cap);
+    return cudaGetLastError();
+}
+
+cudaError_t
+dij_compact(const DijSlot* tab, uint64_t cap, uint64_t n_voxels, unsigned long long* keys, uint32_t* idx,
+            uint64_t n_max, unsigned long long* cursor, int sms, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(cursor, 0, sizeof(unsigned long long), s);
+    if (e != cudaSuccess) return e;
+    k_dij_compact<<<sms * 8, 256, 0, s>>>(tab, cap, n_voxels, keys, idx, n_max, cursor);
+    return cudaGetLastError();
+}
+
+uint64_t
+scan_scratch_words(uint64_t n) {
+    return (n + kScanTile - 1) / kScanTile + 1;
+}
+
+cudaError_t
+scan_exclusive_u32(const uint32_t* in, uint32_t* out, uint64_t n, uint32_t* scratch, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    const uint64_t tiles = (n + kScanTile - 1) / kScanTile;
+    k_scan_tiles<<<(unsigned) tiles, 256, 0, s>>>(in, out, n, scratch);
+    k_scan_sums<<<1, 1024, 0, s>>>(scratch, tiles);
+    k_scan_add<<<blocks_for(n, 256), 256, 0, s>>>(out, n, scratch);
+    return cudaGetLastError();
+}
+
+uint64_t
+radix_hist_words(uint64_t n) {
+    return 256ull * ((n + kTile - 1) / kTile);
+}
+
+cudaError_t
+radix_sort_pairs(unsigned long long*& keys, uint32_t*& vals, unsigned long long*& keys_alt, uint32_t*& vals_alt,
+                 uint64_t n, int bits, uint32_t* hist, uint32_t* offs, uint32_t* scan_scratch, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    const uint32_t n_tiles = (uint32_t) ((n + kTile - 1) / kTile);
+    const uint64_t words   = 256ull * n_tiles;
+    for (int shift = 0; shift < bits; shift += 8) {
+        k_radix_hist<<<n_tiles, kThreads, 0, s>>>(keys, n, shift, hist, n_tiles);
+        cudaError_t e = scan_exclusive_u32(hist, offs, words, scan_scratch, s);
+        if (e != cudaSuccess) return e;
+        k_radix_scatter<<<n_tiles, kThreads, 0, s>>>(keys, vals, keys_alt, vals_alt, n, shift, offs, n_tiles);
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+        unsigned long long* tk = keys;
+        keys                   = keys_alt;
+        keys_alt               = tk;
+        uint32_t* tv           = vals;
+        vals                   = vals_alt;
+        vals_alt               = tv;
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t
+dij_row_bounds(const unsigned long long* keys, uint64_t n, uint64_t row_span, uint64_t n_rows, uint64_t* indptr,
+               cudaStream_t s) {
+    k_row_bounds<<<blocks_for(n_rows + 1, 256), 256, 0, s>>>(keys, n, row_span, n_rows, indptr);
+    return cudaGetLastError();
+}
+
+cudaError_t
+dij_spot_rows(const unsigned long long* keys, const uint32_t* slot, uint64_t n, uint64_t n_voxels, const DijSlot* tab,
+              double scale, uint32_t* vox, float* val, unsigned long long* vkeys, uint32_t* vpos, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_spot_rows<<<blocks_for(n, 256), 256, 0, s>>>(keys, slot, n, n_voxels, tab, scale, vox, val, vkeys, vpos);
+    return cudaGetLastError();
+}
+
+cudaError_t
+dij_row_flags(const unsigned long long* vkeys, uint64_t n, uint32_t* flags, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_row_flags<<<blocks_for(n, 256), 256, 0, s>>>(vkeys, n, flags);
+    return cudaGetLastError();
+}
+
+cudaError_t
+dij_voxel_rows(const unsigned long long* vkeys, const uint32_t* vpos, uint64_t n, const unsigned long long* skeys,
+               uint64_t n_voxels, const float* sval, const uint32_t* flags, const uint32_t* rowid, uint32_t* row_voxel,
+               uint64_t* indptr, uint32_t* spot, float* val, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_voxel_rows<<<blocks_for(n, 256), 256, 0, s>>>(vkeys, vpos, n, skeys, n_voxels, sval, flags, rowid, row_voxel,
+                                                   indptr, spot, val);
+    return cudaGetLastError();
+}
+
+cudaError_t
+dij_forward(const uint32_t* row_voxel, const uint64_t* indptr, const uint32_t* spot, const float* val, uint64_t n_rows,
+            const void* w, void* dose, int fp64, int sms, cudaStream_t s) {
+    if (n_rows == 0) return cudaSuccess;
+    const uint64_t want = (n_rows * 8 + 255) / 256;
+    const unsigned grid = (unsigned) (want < (uint64_t) sms * 16 ? want : (uint64_t) sms * 16);
+    if (fp64)
+        k_dij_forward<double><<<grid, 256, 0, s>>>(row_voxel, indptr, spot, val, n_rows, (const double*) w, (double*) dose);
+    else
+        k_dij_forward<float><<<grid, 256, 0, s>>>(row_voxel, indptr, spot, val, n_rows, (const float*) w, (float*) dose);
+    return cudaGetLastError();
+}
+
+cudaError_t
+dij_backward(const uint64_t* indptr, const uint32_t* vox, const float* val, uint32_t n_rows, const void* g, void* grad,
+             int fp64, cudaStream_t s) {
+    if (n_rows == 0) return cudaSuccess;
+    if (fp64)
+        k_dij_backward<double><<<n_rows, 256, 0, s>>>(indptr, vox, val, n_rows, (const double*) g, (double*) grad);
+    else
+        k_dij_backward<float><<<n_rows, 256, 0, s>>>(indptr, vox, val, n_rows, (const float*) g, (float*) grad);
+    return cudaGetLastError();
+}
+
+}   // namespace mqi_gpu

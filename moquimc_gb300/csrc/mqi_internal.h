@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cstdint>
+#include <string>
 #include <cuda_runtime.h>
 
 #include "mqi_gpu.h"
@@ -11,6 +12,16 @@ namespace mqi_gpu
 
 constexpr int kMaxChildren = 4;
 constexpr int kMaxScorers  = 8;
+
+/// One slot of a Dij table: key = ((spot << 32) | voxel) + 1, 0 = empty; value = FP64 dose.
+/// The reference's key_value holds two 32-bit keys claimed by two separate CAS operations
+/// (insert_hashtable, mqi_transport.hpp:68-111); one 64-bit CAS claims a slot atomically here.
+struct alignas(16) DijSlot {
+    unsigned long long key;
+    double             value;
+};
+
+constexpr uint32_t kDijMaxProbes = 4096;   // linear-probe bound before the table counts as full
 
 /// Flat device description of one scorer (scorer<R> + roi_t, mqi_scorer.hpp:39-79,
 /// mqi_roi.hpp:18-194).
@@ -25,6 +36,9 @@ struct ScorerDev {
     const uint32_t* acc;
     double*         tally;         // dense, length = tally_len
     uint64_t        tally_len;
+    DijSlot*        dij;           // MQI_SCORER_DIJ: open-addressing table of dij_mask + 1 slots
+    uint64_t        dij_mask;
+    unsigned long long* dij_count; // device: occupied slots
 };
 
 /// One child geometry: grid + the contiguous range of its scorers.
@@ -71,6 +85,7 @@ struct WaveParams {
     uint32_t  k0, k1;           // Philox key (run seed)
     uint32_t  max_slice_steps;  // 0 = run each track to completion
     int       inline_local;     // score deposit-only daughters at creation (single-child worlds)
+    int       has_dij;          // a Dij scorer is present (selects the kDij wave kernel)
     Queue     in;
     Queue     out;
     const uint32_t* n_in;       // device: number of entries in `in`
@@ -78,14 +93,41 @@ struct WaveParams {
     uint32_t*       head;       // device: fetch cursor of `in`
     unsigned long long* stats;  // device: mqi_stats fields (8 x u64)
     const uint32_t* spot_ids;   // per history (may be null)
-    uint32_t*       error_flag; // device: set when a bounded loop gives up or a queue overflows
+    uint32_t*       error_flag; // device: 1 a bounded loop gave up, 2 queue overflow, 4 Dij table full
     int             smem_edge_floats; // shared-memory floats for staged child edges
     const float*    tables;     // device: the six physics tables, 6 x 600 floats in Tables order
                                 // (followed by the 3996 HU density-correction factors)
 };
 
+std::string& thread_error_slot();
+
 /// Record the calling thread's last error message (returned by mqi_last_error(NULL)).
 void set_thread_error(const char* msg);
+
+// ---- Dij (mqi_dij.cu) ----
+cudaError_t dij_clear(DijSlot* tab, uint64_t cap, int sms, cudaStream_t s);
+cudaError_t dij_compact(const DijSlot* tab, uint64_t cap, uint64_t n_voxels, unsigned long long* keys, uint32_t* idx,
+                        uint64_t n_max, unsigned long long* cursor, int sms, cudaStream_t s);
+uint64_t    scan_scratch_words(uint64_t n);
+cudaError_t scan_exclusive_u32(const uint32_t* in, uint32_t* out, uint64_t n, uint32_t* scratch, cudaStream_t s);
+uint64_t    radix_hist_words(uint64_t n);
+cudaError_t radix_sort_pairs(unsigned long long*& keys, uint32_t*& vals, unsigned long long*& keys_alt,
+                             uint32_t*& vals_alt, uint64_t n, int bits, uint32_t* hist, uint32_t* offs,
+                             uint32_t* scan_scratch, cudaStream_t s);
+cudaError_t dij_row_bounds(const unsigned long long* keys, uint64_t n, uint64_t row_span, uint64_t n_rows,
+                           uint64_t* indptr, cudaStream_t s);
+cudaError_t dij_spot_rows(const unsigned long long* keys, const uint32_t* slot, uint64_t n, uint64_t n_voxels,
+                          const DijSlot* tab, double scale, uint32_t* vox, float* val, unsigned long long* vkeys,
+                          uint32_t* vpos, cudaStream_t s);
+cudaError_t dij_row_flags(const unsigned long long* vkeys, uint64_t n, uint32_t* flags, cudaStream_t s);
+cudaError_t dij_voxel_rows(const unsigned long long* vkeys, const uint32_t* vpos, uint64_t n,
+                           const unsigned long long* skeys, uint64_t n_voxels, const float* sval, const uint32_t* flags,
+                           const uint32_t* rowid, uint32_t* row_voxel, uint64_t* indptr, uint32_t* spot, float* val,
+                           cudaStream_t s);
+cudaError_t dij_forward(const uint32_t* row_voxel, const uint64_t* indptr, const uint32_t* spot, const float* val,
+                        uint64_t n_rows, const void* w, void* dose, int fp64, int sms, cudaStream_t s);
+cudaError_t dij_backward(const uint64_t* indptr, const uint32_t* vox, const float* val, uint32_t n_rows, const void* g,
+                         void* grad, int fp64, cudaStream_t s);
 
 // ---- launchers (mqi_kernels.cu) ----
 cudaError_t launch_load_primaries(const Queue& q, const mqi_vertex* v, const uint32_t* spot_ids, uint64_t h0, uint32_t n,

@@ -102,6 +102,59 @@ tally_add(double* tally, uint32_t key, double v, bool valid) {
     if ((int) (threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&tally[key], s);
 }
 
+/// Hash of a Dij key: the splitmix64 finalizer (Steele, Lea & Flood, "Fast splittable
+/// pseudorandom number generators", OOPSLA 2014).
+__device__ inline uint64_t
+dij_hash(uint64_t k) {
+    k ^= k >> 30;
+    k *= 0xBF58476D1CE4E5B9ull;
+    k ^= k >> 27;
+    k *= 0x94D049BB133111EBull;
+    k ^= k >> 31;
+    return k;
+}
+
+/// Add v to the Dij entry (spot, voxel).  Lanes of the warp with the same table and key are
+/// combined first (two match rounds: the key, then the table), so one insertion is issued per
+/// distinct entry.  The leader probes linearly from the hashed slot: a slot holding the key takes
+/// the add; an empty slot is claimed with one 64-bit CAS.  After kDijMaxProbes probes the table
+/// counts as full and the error flag's bit 4 is set.
+__device__ inline void
+dij_add(DijSlot* table, uint64_t table_mask, unsigned long long* count, uint32_t* error_flag, uint32_t spot,
+        uint32_t voxel, double v, bool valid) {
+    const unsigned           mask  = __activemask();
+    const unsigned long long key   = ((((unsigned long long) spot) << 32) | voxel) + 1ull;
+    const unsigned           peers = __match_any_sync(mask, valid ? key : 0ull) &
+                           __match_any_sync(mask, (unsigned long long) table);
+    if (!valid) return;
+    double   sum = v;
+    if (__popc(peers) > 1) {
+        sum = 0.0;
+        unsigned m = peers;
+        while (m) {
+            const int src = __ffs(m) - 1;
+            sum += __shfl_sync(peers, v, src);
+            m &= m - 1;
+        }
+        if ((int) (threadIdx.x & 31) != __ffs(peers) - 1) return;
+    }
+    uint64_t slot = dij_hash(key) & table_mask;
+    for (uint32_t probe = 0; probe < kDijMaxProbes; ++probe) {
+        DijSlot* e = table + slot;
+        unsigned long long k = *reinterpret_cast<volatile unsigned long long*>(&e->key);
+        if (k == 0ull) {
+            k = atomicCAS(&e->key, 0ull, key);
+            if (k == 0ull) atomicAdd(count, 1ull);
+        }
+        if (k == 0ull || k == key) {
+            atomicAdd(&e->value, sum);
+            return;
+        }
+        slot = (slot + 1) & table_mask;
+    }
+    atomicOr(error_flag, 4u);
+}
+
 /// roi_t::idx / get_mask_idx for the three mapping methods (mqi_roi.hpp:47-71, 87-160).
 __device__ inline int32_t
 roi_lower_bound(const ScorerDev& s, uint32_t v) {
@@ -182,7 +235,9 @@ compute_hit(int type, const Trk& t, float rho, float vol, float spr_ke0) {
     }
 }
 
-/// Score one step of track t in voxel cnb with every scorer of the current child.
+/// Score one step of track t in voxel cnb with every scorer of the current child.  kDij = false
+/// compiles the Dij insertion out (wave kernels of runs without a Dij scorer).
+template<bool kDij = true>
 __device__ inline void
 score_step(Ctx& C, const Trk& t, uint32_t cnb, float rho, float vol) {
     const WaveParams& P   = *C.P;
@@ -202,6 +257,14 @@ score_step(Ctx& C, const Trk& t, uint32_t cnb, float rho, float vol) {
         }
         double v = 0.0;
         if (ok) v = compute_hit(s.type, t, rho, vol, spr);
+        if (kDij && s.type == MQI_SCORER_DIJ) {
+            // insert_hashtable(data_, cnb, spot_ind, ...) (mqi_transport.hpp:204-225); a history
+            // without a spot index lands in column 0
+            const bool valid = ok && v > 0.0;
+            const uint32_t col = C.spot == 0xFFFFFFFFu ? 0u : C.spot;
+            dij_add(s.dij, s.dij_mask, s.dij_count, P.error_flag, col, cnb, s.double_score ? v + v : v, valid);
+            continue;
+        }
         const bool valid = ok && v > 0.0 && key < s.tally_len;
         if (s.double_score) tally_add(s.tally, key, v + v, valid);
         else tally_add(s.tally, key, v, valid);
@@ -673,6 +736,7 @@ requeue_track(Ctx& C, const Trk& t, const Rng& rng) {
     q.spot[i] = t.spot;
 }
 
+template<bool kDij>
 __device__ __forceinline__ void
 wave_body(const WaveParams& P) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -808,7 +872,7 @@ wave_body(const WaveParams& P) {
         if (d2b < 0.0f) {
             leave = true;
         } else {
-            score_step(C, t, cnb, rho, grid_volume(C.g, t.cell));
+            score_step<kDij>(C, t, cnb, rho, grid_volume(C.g, t.cell));
             if (!t.stopped) {
                 grid_step_index(C.g, t.p1, t.d1, t.cell);
                 t.p0  = t.p1;
@@ -887,11 +951,12 @@ launch_load_primaries(const Queue& q, const mqi_vertex* v, const uint32_t* spot_
 }
 
 /// The wave kernel in the launch shapes the tuner chooses from: (threads per block, minimum
-/// resident blocks per SM).  The register budget each shape implies is what differs.
-template<int kBlock, int kMinBlocks>
+/// resident blocks per SM).  The register budget each shape implies is what differs.  Runs with
+/// a Dij scorer use the kDij instance (one shape, 128 x 5).
+template<int kBlock, int kMinBlocks, bool kDij>
 __global__ void __launch_bounds__(kBlock, kMinBlocks)
 k_wave(const __grid_constant__ WaveParams P) {
-    wave_body(P);
+    wave_body<kDij>(P);
 }
 
 int
@@ -910,18 +975,19 @@ wave_edge_floats(const ChildDev* c, int n) {
     return (f + 3) & ~3;
 }
 
-template<int B, int M>
+template<int B, int M, bool D = false>
 static cudaError_t
 launch_variant(const WaveParams& p, int grid, cudaStream_t s) {
     const int   smem = wave_smem_bytes(p);
-    cudaError_t e    = cudaFuncSetAttribute(k_wave<B, M>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaError_t e    = cudaFuncSetAttribute(k_wave<B, M, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
-    k_wave<B, M><<<grid, B, smem, s>>>(p);
+    k_wave<B, M, D><<<grid, B, smem, s>>>(p);
     return cudaGetLastError();
 }
 
 cudaError_t
 launch_wave(const WaveParams& p, int grid, int block, int blocks_per_sm, cudaStream_t s) {
+    if (p.has_dij) return launch_variant<128, 5, true>(p, grid / (blocks_per_sm > 0 ? blocks_per_sm : 1) * 5, s);
     if (block == 128) {
         if (blocks_per_sm >= 6) return launch_variant<128, 6>(p, grid, s);
         if (blocks_per_sm == 5) return launch_variant<128, 5>(p, grid, s);
