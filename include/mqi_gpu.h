@@ -165,6 +165,28 @@ int mqi_set_spot_plan(mqi_ctx* ctx, const mqi_spot* spots, uint32_t n_spots, uin
  * mqi_tps_env.hpp:1477-1603). */
 int mqi_transport_plan(mqi_ctx* ctx, uint64_t h0, uint64_t h1, uint64_t seed);
 
+/* ---- robust scenarios ----------------------------------------------------------------------- */
+
+/* Robust scenarios: n instances of child `child_id` that differ in their voxel edges and density
+ * scale, transported together.  tps_env runs one scenario per job: XShift/YShift/ZShift move the
+ * CT origin before its edges are formed (mqi_tps_env.hpp:475-477, 507-514) and DensityScaling
+ * multiplies every voxel density (mqi_tps_env.hpp:766-769).  Here every transport call runs each
+ * history once per scenario in one queue drain (the scenarios of a history share its random
+ * numbers), and every scorer holds one tally per scenario, scenario-major (mqi_get_tally returns
+ * n * tally length; the statistics calls return the worst scenario).  xe/ye/ze hold n x (nx+1),
+ * n x (ny+1), n x (nz+1) edges; density_scale n factors (NULL: 1); the child's density must be
+ * the unscaled one.  At most 64 scenarios; spot indices stay below 2^24 - 1.  n <= 1 removes the
+ * scenarios.  Existing tallies are reallocated and zeroed.  Not with a Dij scorer. */
+int mqi_set_scenarios(mqi_ctx* ctx, int child_id, uint32_t n, const float* xe, const float* ye,
+                      const float* ze, const float* density_scale);
+
+/* Statistical stopping over whole passes of the spot plan: transport the plan with a fresh seed
+ * per pass until the reference estimate (mqi_stat_uncertainty, worst scenario) is <= criteria
+ * or max_passes ran, then scale the child's other scorers to one pass (tps_env::run with
+ * record_statistics + calculate_average_results, mqi_tps_env.hpp:1238-1300, 1428-1476). */
+int mqi_run_plan_until_stat(mqi_ctx* ctx, int dose_id, int dose2_id, float criteria, float threshold,
+                            uint64_t max_passes, uint64_t seed, uint64_t* passes_done, double* achieved);
+
 /* Write the source vertices (and spot ids, when spot_out is not NULL) that mqi_transport_plan
  * with run seed `seed` starts for histories [h0, h1) of the plan: the sampled beamlet vertices
  * beamsource produces (mqi_beamlet.hpp:80-90).  Host buffers of h1-h0 entries. */

@@ -38,7 +38,7 @@ EXPORTS = (
     "mqi_add_stat_scorers", "mqi_stat_uncertainty", "mqi_batch_accumulate", "mqi_batch_uncertainty",
     "mqi_get_batch_mean", "mqi_scale_tally", "mqi_run_until_stat", "mqi_set_spot_plan", "mqi_transport_plan",
     "mqi_sample_plan", "mqi_add_dij_scorer", "mqi_dij_build", "mqi_dij_get_csr", "mqi_dij_info",
-    "mqi_dij_matvec", "mqi_dij_rmatvec",
+    "mqi_dij_matvec", "mqi_dij_rmatvec", "mqi_set_scenarios", "mqi_run_plan_until_stat",
 )
 
 VERTEX_DTYPE = np.dtype([("ke", "<f4"), ("pos", "<f4", (3,)), ("dir", "<f4", (3,))])
@@ -119,6 +119,8 @@ def load(path: Optional[str] = None) -> C.CDLL:
         "mqi_dij_info": (i32, [vp, i32, P(u64), P(u64), P(u64), P(u64)]),
         "mqi_dij_matvec": (i32, [vp, i32, vp, vp, i32, i32]),
         "mqi_dij_rmatvec": (i32, [vp, i32, vp, vp, i32, i32]),
+        "mqi_set_scenarios": (i32, [vp, i32, u32, vp, vp, vp, vp]),
+        "mqi_run_plan_until_stat": (i32, [vp, i32, i32, f32, f32, u64, u64, P(u64), P(C.c_double)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(lib, name)
@@ -383,3 +385,26 @@ class Context:
         out = np.empty(n_spots, g.dtype)
         self._check(self.lib.mqi_dij_rmatvec(self.h, scorer, _ptr(g), _ptr(out), int(fp64), 0), self.h)
         return out
+
+    # ---- robust scenarios ----
+    def set_scenarios(self, child: int, xe_list, ye_list, ze_list, density_scale=None) -> None:
+        """One (xe, ye, ze) edge set per scenario and optional density scales; [] removes them."""
+        n = len(xe_list)
+        if n <= 1:
+            self._check(self.lib.mqi_set_scenarios(self.h, child, 0, None, None, None, None), self.h)
+            self.n_scen = 1
+            return
+        xe = np.ascontiguousarray(np.stack(xe_list), np.float32)
+        ye = np.ascontiguousarray(np.stack(ye_list), np.float32)
+        ze = np.ascontiguousarray(np.stack(ze_list), np.float32)
+        sc = None if density_scale is None else np.ascontiguousarray(density_scale, np.float32)
+        self._check(self.lib.mqi_set_scenarios(self.h, child, n, _ptr(xe), _ptr(ye), _ptr(ze), _ptr(sc)), self.h)
+        self.n_scen = n
+
+    def run_plan_until_stat(self, dose_id: int, dose2_id: int, criteria: float, threshold: float,
+                            max_passes: int, seed: int) -> tuple[int, float]:
+        p, a = C.c_uint64(0), C.c_double(0)
+        self._check(self.lib.mqi_run_plan_until_stat(self.h, dose_id, dose2_id, C.c_float(criteria),
+                                                     C.c_float(threshold), max_passes, seed & 0xFFFFFFFFFFFFFFFF,
+                                                     C.byref(p), C.byref(a)), self.h)
+        return p.value, a.value

@@ -142,6 +142,7 @@ mqi_destroy(mqi_ctx* c) {
     cudaFree(c->stat_scratch);
     cudaFree(c->plan_spots);
     cudaFree(c->plan_cum);
+    cudaFree(c->scen_edges);
     cudaFree(c->vertices);
     cudaFree(c->spot_ids);
     free_queue(c->qa);
@@ -346,8 +347,9 @@ mqi_add_scorer(mqi_ctx* c, int child_id, int type, int roi_method, uint32_t roi_
     } else {
         return fail(c, MQI_ERR_INVALID, "mqi_add_scorer: unknown roi method");
     }
-    MQI_CUDA(c, cudaMalloc(&s.tally, s.tally_len * sizeof(double)), "mqi_add_scorer");
-    MQI_CUDA(c, cudaMemset(s.tally, 0, s.tally_len * sizeof(double)), "mqi_add_scorer");
+    s.copies = c->n_scen;
+    MQI_CUDA(c, cudaMalloc(&s.tally, s.total() * sizeof(double)), "mqi_add_scorer");
+    MQI_CUDA(c, cudaMemset(s.tally, 0, s.total() * sizeof(double)), "mqi_add_scorer");
     c->scorers.push_back(s);
     if (scorer_id) *scorer_id = (int) c->scorers.size() - 1;
     return MQI_OK;
@@ -364,6 +366,9 @@ mqi_set_vertices(mqi_ctx* c, const mqi_vertex* v, const uint32_t* spot_ids, uint
         MQI_CUDA(c, cudaMalloc(&c->vertices, n * sizeof(mqi_vertex)), "mqi_set_vertices");
         c->vertex_cap = n;
     }
+    if (spot_ids && !on_device)
+        for (uint64_t i = 0; i < n; ++i)
+            if (spot_ids[i] >= kNoSpot) return fail(c, MQI_ERR_INVALID, "mqi_set_vertices: spot indices must be < 2^24 - 1");
     const cudaMemcpyKind k = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     if (n) MQI_CUDA(c, cudaMemcpyAsync(c->vertices, v, n * sizeof(mqi_vertex), k, c->stream), "mqi_set_vertices");
     c->has_spots = spot_ids != nullptr;
@@ -457,19 +462,28 @@ run_transport(mqi_ctx* c, uint64_t h0, uint64_t h1, uint64_t seed, bool plan) {
     P.spot_ids        = c->has_spots ? c->spot_ids : nullptr;
     P.tables          = c->tables;
     P.smem_edge_floats = wave_edge_floats(P.child, P.n_children);
+    if (c->n_scen > 1) {
+        P.n_scen      = (int) c->n_scen;
+        P.scen_child  = c->scen_child;
+        P.scen_stride = c->scen_stride;
+        P.scen_edges  = c->scen_edges;
+        for (uint32_t k = 0; k < c->n_scen; ++k) P.scen_scale[k] = c->scen_scale[k];
+    }
     MQI_CUDA(c, cudaMemsetAsync(c->counters + 3, 0, sizeof(uint32_t), c->stream), "mqi_transport");
     QueueBuf* A = &c->qa;
     QueueBuf* B = &c->qb;
-    for (uint64_t h = h0; h < h1; h += chunk) {
-        const uint32_t n = (uint32_t) std::min<uint64_t>(chunk, h1 - h);
+    const uint32_t S       = c->n_scen;
+    const uint32_t per_ld  = std::max<uint32_t>(chunk / S, 1u);   // histories per load; S queue entries each
+    for (uint64_t h = h0; h < h1; h += per_ld) {
+        const uint32_t n = (uint32_t) std::min<uint64_t>(per_ld, h1 - h);
         if (plan)
-            MQI_CUDA(c, launch_sample_primaries(A->q, c->plan_spots, c->plan_cum, c->n_plan_spots, h, n, P.k0,
+            MQI_CUDA(c, launch_sample_primaries(A->q, c->plan_spots, c->plan_cum, c->n_plan_spots, h, n, S, P.k0,
                                                 P.k1 ^ kSourceKeyXor, c->stream), "mqi_transport: sample primaries");
         else
-            MQI_CUDA(c, launch_load_primaries(A->q, c->vertices, c->has_spots ? c->spot_ids : nullptr, h, n, c->stream),
+            MQI_CUDA(c, launch_load_primaries(A->q, c->vertices, c->has_spots ? c->spot_ids : nullptr, h, n, S, c->stream),
                      "mqi_transport: load primaries");
         ++c->kernel_launches;
-        c->host_counts[0] = n;
+        c->host_counts[0] = n * S;
         MQI_CUDA(c, cudaMemcpyAsync(c->counters + 0, c->host_counts, sizeof(uint32_t), cudaMemcpyHostToDevice, c->stream),
                  "mqi_transport");
         int cur = 0;
@@ -530,6 +544,7 @@ mqi_transport(mqi_ctx* c, uint64_t h0, uint64_t h1, uint64_t seed) {
 int
 mqi_set_spot_plan(mqi_ctx* c, const mqi_spot* spots, uint32_t n_spots, uint64_t* total_histories) {
     if (!valid_ctx(c) || (!spots && n_spots)) return fail(c, MQI_ERR_INVALID, "mqi_set_spot_plan: bad argument");
+    if (n_spots >= kNoSpot) return fail(c, MQI_ERR_INVALID, "mqi_set_spot_plan: at most 2^24 - 2 spots");
     std::vector<uint64_t> cum(n_spots + 1, 0);
     for (uint32_t i = 0; i < n_spots; ++i) cum[i + 1] = cum[i] + spots[i].histories;
     if (cum[n_spots] > 0xFFFFFFFFull) return fail(c, MQI_ERR_INVALID, "mqi_set_spot_plan: at most 2^32-1 histories per plan");
@@ -546,6 +561,95 @@ mqi_set_spot_plan(mqi_ctx* c, const mqi_spot* spots, uint32_t n_spots, uint64_t*
     c->plan_histories  = cum[n_spots];
     c->plan_cum_host   = cum;
     if (total_histories) *total_histories = cum[n_spots];
+    return MQI_OK;
+}
+
+int
+mqi_set_scenarios(mqi_ctx* c, int child_id, uint32_t n, const float* xe, const float* ye, const float* ze,
+                  const float* density_scale) {
+    if (!valid_ctx(c)) return fail(c, MQI_ERR_INVALID, "mqi_set_scenarios: ctx is NULL");
+    if (n > (uint32_t) kMaxScenarios) return fail(c, MQI_ERR_INVALID, "mqi_set_scenarios: at most 64 scenarios");
+    if (n > 1) {
+        if (child_id < 0 || child_id >= (int) c->children.size())
+            return fail(c, MQI_ERR_INVALID, "mqi_set_scenarios: no such child");
+        if (!xe || !ye || !ze) return fail(c, MQI_ERR_INVALID, "mqi_set_scenarios: edge arrays are required");
+    }
+    for (auto& s : c->scorers)
+        if (s.type == MQI_SCORER_DIJ && n > 1)
+            return fail(c, MQI_ERR_UNSUPPORTED, "mqi_set_scenarios: a Dij scorer cannot run with robust scenarios");
+    const uint32_t copies = n > 1 ? n : 1;
+    DeviceGuard g(c->device);
+    float* edges = nullptr;
+    int    stride = 0;
+    if (n > 1) {
+        const ChildHost& ch = c->children[child_id];
+        stride = ch.nx + ch.ny + ch.nz + 3;
+        std::vector<float> host((size_t) n * stride);
+        for (uint32_t k = 0; k < n; ++k) {
+            float* e = host.data() + (size_t) k * stride;
+            std::memcpy(e, xe + (size_t) k * (ch.nx + 1), (ch.nx + 1) * sizeof(float));
+            std::memcpy(e + ch.nx + 1, ye + (size_t) k * (ch.ny + 1), (ch.ny + 1) * sizeof(float));
+            std::memcpy(e + ch.nx + ch.ny + 2, ze + (size_t) k * (ch.nz + 1), (ch.nz + 1) * sizeof(float));
+        }
+        MQI_CUDA(c, cudaMalloc(&edges, host.size() * sizeof(float)), "mqi_set_scenarios");
+        cudaError_t e = cudaMemcpy(edges, host.data(), host.size() * sizeof(float), cudaMemcpyHostToDevice);
+        if (e != cudaSuccess) {
+            cudaFree(edges);
+            return cuda_fail(c, e, "mqi_set_scenarios");
+        }
+    }
+    // one tally per scenario for every scorer; accumulated results are dropped
+    for (auto& s : c->scorers) {
+        cudaFree(s.batch_s1);
+        cudaFree(s.batch_s2);
+        s.batch_s1 = s.batch_s2 = nullptr;
+        s.n_batches = 0;
+        if (s.type == MQI_SCORER_DIJ) continue;
+        cudaFree(s.tally);
+        s.tally  = nullptr;
+        s.copies = copies;
+        MQI_CUDA(c, cudaMalloc(&s.tally, s.total() * sizeof(double)), "mqi_set_scenarios");
+        MQI_CUDA(c, cudaMemset(s.tally, 0, s.total() * sizeof(double)), "mqi_set_scenarios");
+    }
+    cudaFree(c->scen_edges);
+    c->scen_edges  = edges;
+    c->scen_stride = stride;
+    c->scen_child  = n > 1 ? child_id : -1;
+    c->n_scen      = copies;
+    c->scen_scale.assign(copies, 1.0f);
+    if (density_scale && n > 1)
+        for (uint32_t k = 0; k < n; ++k) c->scen_scale[k] = density_scale[k];
+    return MQI_OK;
+}
+
+int
+mqi_run_plan_until_stat(mqi_ctx* c, int dose_id, int dose2_id, float criteria, float threshold, uint64_t max_passes,
+                        uint64_t seed, uint64_t* passes_done, double* achieved) {
+    if (!valid_ctx(c)) return fail(c, MQI_ERR_INVALID, "mqi_run_plan_until_stat: ctx is NULL");
+    if (!c->plan_spots || c->plan_histories == 0) return fail(c, MQI_ERR_STATE, "mqi_run_plan_until_stat: no spot plan");
+    if (dose_id < 0 || dose_id >= (int) c->scorers.size() || !c->scorers[dose_id].stat_mode)
+        return fail(c, MQI_ERR_INVALID, "mqi_run_plan_until_stat: dose_id must be a stat scorer");
+    const uint64_t N = c->plan_histories;
+    uint64_t passes = 0;
+    double   stat   = 1.0;   // current_stat = 100% before the first run (mqi_tps_env.hpp:1244)
+    for (; passes < max_passes && stat > (double) criteria; ++passes) {
+        const int rc = mqi_transport_plan(c, 0, N, seed + 0x9E3779B97F4A7C15ull * passes);
+        if (rc != MQI_OK) return rc;
+        const int rs = mqi_stat_uncertainty(c, dose_id, dose2_id, N * (passes + 1), threshold, &stat, nullptr);
+        if (rs != MQI_OK) return rs;
+    }
+    // calculate_average_results (mqi_tps_env.hpp:1428-1476): the child's other scorers are scaled
+    // to one pass of the plan
+    const int child = c->scorers[dose_id].child;
+    for (int i = 0; i < (int) c->scorers.size(); ++i) {
+        const ScorerHost& s = c->scorers[i];
+        if (s.child == child && !s.stat_mode && s.type != MQI_SCORER_DIJ && passes > 0) {
+            const int rc = mqi_scale_tally(c, i, 1.0 / (double) passes);
+            if (rc != MQI_OK) return rc;
+        }
+    }
+    if (passes_done) *passes_done = passes;
+    if (achieved) *achieved = stat;
     return MQI_OK;
 }
 
@@ -591,10 +695,10 @@ mqi_get_tally(mqi_ctx* c, int id, double* out, uint64_t* n_out, int on_device) {
     if (!valid_ctx(c)) return fail(c, MQI_ERR_INVALID, "mqi_get_tally: ctx is NULL");
     if (id < 0 || id >= (int) c->scorers.size()) return fail(c, MQI_ERR_INVALID, "mqi_get_tally: no such scorer");
     const ScorerHost& s = c->scorers[id];
-    if (n_out) *n_out = s.tally_len;
+    if (n_out) *n_out = s.total();
     if (!out) return MQI_OK;
     DeviceGuard g(c->device);
-    MQI_CUDA(c, cudaMemcpyAsync(out, s.tally, s.tally_len * sizeof(double), on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+    MQI_CUDA(c, cudaMemcpyAsync(out, s.tally, s.total() * sizeof(double), on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
                                 c->stream), "mqi_get_tally");
     MQI_CUDA(c, cudaStreamSynchronize(c->stream), "mqi_get_tally");
     return MQI_OK;
@@ -606,7 +710,7 @@ mqi_reset_tallies(mqi_ctx* c) {
     DeviceGuard g(c->device);
     for (auto& s : c->scorers) {
         if (s.type == MQI_SCORER_DIJ) MQI_CUDA(c, dij_reset(s, c->num_sms, c->stream), "mqi_reset_tallies");
-        else MQI_CUDA(c, cudaMemsetAsync(s.tally, 0, s.tally_len * sizeof(double), c->stream), "mqi_reset_tallies");
+        else MQI_CUDA(c, cudaMemsetAsync(s.tally, 0, s.total() * sizeof(double), c->stream), "mqi_reset_tallies");
     }
     MQI_CUDA(c, cudaMemsetAsync(c->stats, 0, 8 * sizeof(unsigned long long), c->stream), "mqi_reset_tallies");
     MQI_CUDA(c, cudaMemsetAsync(c->counters + 3, 0, sizeof(uint32_t), c->stream), "mqi_reset_tallies");
@@ -792,8 +896,9 @@ mqi_add_stat_scorers(mqi_ctx* c, int child_id, int roi_method, uint32_t roi_leng
             MQI_CUDA(c, cudaMemcpy(s.stride, roi_stride, roi_length * sizeof(uint32_t), cudaMemcpyHostToDevice), "mqi_add_stat_scorers");
             MQI_CUDA(c, cudaMemcpy(s.acc, roi_acc, roi_length * sizeof(uint32_t), cudaMemcpyHostToDevice), "mqi_add_stat_scorers");
         }
-        MQI_CUDA(c, cudaMalloc(&s.tally, s.tally_len * sizeof(double)), "mqi_add_stat_scorers");
-        MQI_CUDA(c, cudaMemset(s.tally, 0, s.tally_len * sizeof(double)), "mqi_add_stat_scorers");
+        s.copies = c->n_scen;
+        MQI_CUDA(c, cudaMalloc(&s.tally, s.total() * sizeof(double)), "mqi_add_stat_scorers");
+        MQI_CUDA(c, cudaMemset(s.tally, 0, s.total() * sizeof(double)), "mqi_add_stat_scorers");
         c->scorers.push_back(s);
         ids[k] = (int) c->scorers.size() - 1;
     }
@@ -814,9 +919,21 @@ mqi_stat_uncertainty(mqi_ctx* c, int dose_id, int dose2_id, uint64_t n_histories
     if (n_histories < 2) return fail(c, MQI_ERR_INVALID, "mqi_stat_uncertainty: needs at least 2 histories");
     DeviceGuard g(c->device);
     if (ensure_stat_scratch(c) != MQI_OK) return MQI_ERR_NOMEM;
-    MQI_CUDA(c, launch_stat(a.tally, b.tally, a.tally_len, (double) n_histories, 0, threshold, c->num_sms, c->stat_scratch,
-                            c->stream), "mqi_stat_uncertainty");
-    return read_stat(c, mean_rel_sigma, n_voxels);
+    // robust scenarios: each scenario's estimate; the worst one is returned
+    double   worst = -1.0;
+    uint64_t worst_n = 0;
+    for (uint32_t k = 0; k < a.copies; ++k) {
+        MQI_CUDA(c, launch_stat(a.tally + k * a.tally_len, b.tally + k * b.tally_len, a.tally_len, (double) n_histories, 0,
+                                threshold, c->num_sms, c->stat_scratch, c->stream), "mqi_stat_uncertainty");
+        double   v = 0.0;
+        uint64_t nv = 0;
+        const int rc = read_stat(c, &v, &nv);
+        if (rc != MQI_OK) return rc;
+        if (v > worst) { worst = v; worst_n = nv; }
+    }
+    if (mean_rel_sigma) *mean_rel_sigma = worst;
+    if (n_voxels) *n_voxels = worst_n;
+    return MQI_OK;
 }
 
 int
@@ -826,13 +943,13 @@ mqi_batch_accumulate(mqi_ctx* c, int scorer_id) {
     ScorerHost& s = c->scorers[scorer_id];
     DeviceGuard g(c->device);
     if (!s.batch_s1) {
-        MQI_CUDA(c, cudaMalloc(&s.batch_s1, s.tally_len * sizeof(double)), "mqi_batch_accumulate");
-        MQI_CUDA(c, cudaMalloc(&s.batch_s2, s.tally_len * sizeof(double)), "mqi_batch_accumulate");
-        MQI_CUDA(c, cudaMemsetAsync(s.batch_s1, 0, s.tally_len * sizeof(double), c->stream), "mqi_batch_accumulate");
-        MQI_CUDA(c, cudaMemsetAsync(s.batch_s2, 0, s.tally_len * sizeof(double), c->stream), "mqi_batch_accumulate");
+        MQI_CUDA(c, cudaMalloc(&s.batch_s1, s.total() * sizeof(double)), "mqi_batch_accumulate");
+        MQI_CUDA(c, cudaMalloc(&s.batch_s2, s.total() * sizeof(double)), "mqi_batch_accumulate");
+        MQI_CUDA(c, cudaMemsetAsync(s.batch_s1, 0, s.total() * sizeof(double), c->stream), "mqi_batch_accumulate");
+        MQI_CUDA(c, cudaMemsetAsync(s.batch_s2, 0, s.total() * sizeof(double), c->stream), "mqi_batch_accumulate");
         s.n_batches = 0;
     }
-    MQI_CUDA(c, launch_batch_fold(s.tally, s.batch_s1, s.batch_s2, s.tally_len, c->num_sms, c->stream), "mqi_batch_accumulate");
+    MQI_CUDA(c, launch_batch_fold(s.tally, s.batch_s1, s.batch_s2, s.total(), c->num_sms, c->stream), "mqi_batch_accumulate");
     MQI_CUDA(c, cudaStreamSynchronize(c->stream), "mqi_batch_accumulate");
     ++s.n_batches;
     return MQI_OK;
@@ -848,9 +965,21 @@ mqi_batch_uncertainty(mqi_ctx* c, int scorer_id, float threshold, double* mean_r
     if (s.n_batches < 2) return fail(c, MQI_ERR_STATE, "mqi_batch_uncertainty: needs at least 2 accumulated batches");
     DeviceGuard g(c->device);
     if (ensure_stat_scratch(c) != MQI_OK) return MQI_ERR_NOMEM;
-    MQI_CUDA(c, launch_stat(s.batch_s1, s.batch_s2, s.tally_len, (double) s.n_batches, 1, threshold, c->num_sms,
-                            c->stat_scratch, c->stream), "mqi_batch_uncertainty");
-    return read_stat(c, mean_rel_sigma, n_voxels);
+    double   worst = -1.0;
+    uint64_t worst_n = 0;
+    for (uint32_t k = 0; k < s.copies; ++k) {
+        MQI_CUDA(c, launch_stat(s.batch_s1 + k * s.tally_len, s.batch_s2 + k * s.tally_len, s.tally_len,
+                                (double) s.n_batches, 1, threshold, c->num_sms, c->stat_scratch, c->stream),
+                 "mqi_batch_uncertainty");
+        double   v = 0.0;
+        uint64_t nv = 0;
+        const int rc = read_stat(c, &v, &nv);
+        if (rc != MQI_OK) return rc;
+        if (v > worst) { worst = v; worst_n = nv; }
+    }
+    if (mean_rel_sigma) *mean_rel_sigma = worst;
+    if (n_voxels) *n_voxels = worst_n;
+    return MQI_OK;
 }
 
 int
@@ -858,15 +987,15 @@ mqi_get_batch_mean(mqi_ctx* c, int scorer_id, double* out, uint64_t* n_out, int 
     if (!valid_ctx(c)) return fail(c, MQI_ERR_INVALID, "mqi_get_batch_mean: ctx is NULL");
     if (scorer_id < 0 || scorer_id >= (int) c->scorers.size()) return fail(c, MQI_ERR_INVALID, "mqi_get_batch_mean: no such scorer");
     const ScorerHost& s = c->scorers[scorer_id];
-    if (n_out) *n_out = s.tally_len;
+    if (n_out) *n_out = s.total();
     if (!out) return MQI_OK;
     if (s.n_batches == 0) return fail(c, MQI_ERR_STATE, "mqi_get_batch_mean: no accumulated batch");
     DeviceGuard g(c->device);
     double* dst = out;
-    if (!on_device) MQI_CUDA(c, cudaMalloc(&dst, s.tally_len * sizeof(double)), "mqi_get_batch_mean");
-    cudaError_t e = launch_copy_scaled(s.batch_s1, dst, s.tally_len, 1.0 / (double) s.n_batches, c->num_sms, c->stream);
+    if (!on_device) MQI_CUDA(c, cudaMalloc(&dst, s.total() * sizeof(double)), "mqi_get_batch_mean");
+    cudaError_t e = launch_copy_scaled(s.batch_s1, dst, s.total(), 1.0 / (double) s.n_batches, c->num_sms, c->stream);
     if (e == cudaSuccess && !on_device)
-        e = cudaMemcpyAsync(out, dst, s.tally_len * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+        e = cudaMemcpyAsync(out, dst, s.total() * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (!on_device) cudaFree(dst);
     if (e != cudaSuccess) return cuda_fail(c, e, "mqi_get_batch_mean");
@@ -879,7 +1008,7 @@ mqi_scale_tally(mqi_ctx* c, int scorer_id, double weight) {
     if (scorer_id < 0 || scorer_id >= (int) c->scorers.size()) return fail(c, MQI_ERR_INVALID, "mqi_scale_tally: no such scorer");
     const ScorerHost& s = c->scorers[scorer_id];
     DeviceGuard g(c->device);
-    MQI_CUDA(c, launch_scale(s.tally, s.tally_len, weight, c->num_sms, c->stream), "mqi_scale_tally");
+    MQI_CUDA(c, launch_scale(s.tally, s.total(), weight, c->num_sms, c->stream), "mqi_scale_tally");
     MQI_CUDA(c, cudaStreamSynchronize(c->stream), "mqi_scale_tally");
     return MQI_OK;
 }

@@ -94,6 +94,7 @@ int
 mqi_add_dij_scorer(mqi_ctx* c, int child_id, int roi_method, uint32_t roi_length, const uint32_t* roi_start,
                    const uint32_t* roi_stride, const uint32_t* roi_acc, uint64_t capacity, int* scorer_id) {
     if (!valid_ctx(c)) return fail(c, MQI_ERR_INVALID, "mqi_add_dij_scorer: ctx is NULL");
+    if (c->n_scen > 1) return fail(c, MQI_ERR_UNSUPPORTED, "mqi_add_dij_scorer: not with robust scenarios");
     if (capacity == 0) capacity = 1ull << 26;
     if (capacity > (1ull << 32)) return fail(c, MQI_ERR_INVALID, "mqi_add_dij_scorer: at most 2^32 slots");
     uint64_t cap = 1;

@@ -57,7 +57,8 @@ struct ScorerHost {
     uint32_t* stride = nullptr;
     uint32_t* acc = nullptr;
     double*   tally = nullptr;
-    uint64_t  tally_len = 0;
+    uint64_t  tally_len = 0;       // per scenario; the tally holds copies * tally_len doubles
+    uint32_t  copies = 1;          // robust scenarios: one tally per scenario, scenario-major
     double*   batch_s1 = nullptr;   // batch estimator: running sums of batch tallies and squares
     double*   batch_s2 = nullptr;
     uint64_t  n_batches = 0;
@@ -65,6 +66,8 @@ struct ScorerHost {
     uint64_t  dij_cap = 0;
     unsigned long long* dij_count = nullptr;
     DijCsr    csr;
+
+    uint64_t total() const { return tally_len * copies; }
 };
 
 struct QueueBuf {
@@ -132,6 +135,11 @@ struct mqi_ctx {
     uint32_t                n_plan_spots = 0;
     uint64_t                plan_histories = 0;
     std::vector<uint64_t>   plan_cum_host;
+    uint32_t                n_scen = 1;               // robust scenarios (1: none)
+    int                     scen_child = -1;
+    int                     scen_stride = 0;
+    float*                  scen_edges = nullptr;     // device: n_scen x scen_stride
+    std::vector<float>      scen_scale;
 };
 
 namespace mqi_gpu

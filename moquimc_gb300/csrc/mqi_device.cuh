@@ -302,6 +302,7 @@ struct Grid {
     const float* ri;   // rotation inverse
     const float* tr;   // translation
     int          identity;   // rf == I and tr == 0
+    float        rho_scale;  // density scale of the track's scenario (1: none)
 };
 
 __device__ inline float fadd(float a, float b) { return __fadd_rn(a, b); }

@@ -10,8 +10,15 @@
 namespace mqi_gpu
 {
 
-constexpr int kMaxChildren = 4;
-constexpr int kMaxScorers  = 8;
+constexpr int kMaxChildren  = 4;
+constexpr int kMaxScorers   = 8;
+constexpr int kMaxScenarios = 64;
+
+/// The queue's spot word: spot index (Dij column) in the low 24 bits, robust scenario in the high
+/// 8 bits.  kNoSpot marks a history without a spot index.
+constexpr uint32_t kSpotMask  = 0x00FFFFFFu;
+constexpr uint32_t kNoSpot    = 0x00FFFFFFu;
+constexpr int      kScenShift = 24;
 
 /// One slot of a Dij table: key = ((spot << 32) | voxel) + 1, 0 = empty; value = FP64 dose.
 /// The reference's key_value holds two 32-bit keys claimed by two separate CAS operations
@@ -69,7 +76,7 @@ struct Queue {
     uint32_t* ctr;     // next Philox block of this track
     uint32_t* meta;    // below:16 | primary:1 | ke1_zero:1 | phase:1 | child:3 | npush:10 (bit layout in kernels)
     int32_t*  cell;    // packed cell for phase STEP: x | y << 11 | z << 22 (each < 2048)
-    uint32_t* spot;    // spot (Dij column) of the history, 0xFFFFFFFF when none
+    uint32_t* spot;    // spot word of the history: spot | scenario << 24 (kNoSpot: no spot)
     uint32_t  capacity;
 };
 
@@ -86,6 +93,11 @@ struct WaveParams {
     uint32_t  max_slice_steps;  // 0 = run each track to completion
     int       inline_local;     // score deposit-only daughters at creation (single-child worlds)
     int       has_dij;          // a Dij scorer is present (selects the kDij wave kernel)
+    int       n_scen;           // robust scenarios (0 or 1: none)
+    int       scen_child;       // the child the scenarios vary
+    int       scen_stride;      // floats per scenario in scen_edges: nx+1 + ny+1 + nz+1
+    const float* scen_edges;    // device: per-scenario x, y, z edges of scen_child
+    float     scen_scale[kMaxScenarios];   // per-scenario density scale
     Queue     in;
     Queue     out;
     const uint32_t* n_in;       // device: number of entries in `in`
@@ -130,10 +142,12 @@ cudaError_t dij_backward(const uint64_t* indptr, const uint32_t* vox, const floa
                          void* grad, int fp64, cudaStream_t s);
 
 // ---- launchers (mqi_kernels.cu) ----
+// Loaders: n histories from h0, each once per scenario (n_scen >= 1), scenario-interleaved:
+// queue entry i holds history h0 + i / n_scen in scenario i % n_scen.
 cudaError_t launch_load_primaries(const Queue& q, const mqi_vertex* v, const uint32_t* spot_ids, uint64_t h0, uint32_t n,
-                                  cudaStream_t s);
+                                  uint32_t n_scen, cudaStream_t s);
 cudaError_t launch_sample_primaries(const Queue& q, const mqi_spot* spots, const uint64_t* cum, uint32_t n_spots,
-                                    uint64_t h0, uint32_t n, uint32_t k0, uint32_t k1, cudaStream_t s);
+                                    uint64_t h0, uint32_t n, uint32_t n_scen, uint32_t k0, uint32_t k1, cudaStream_t s);
 cudaError_t launch_sample_vertices(mqi_vertex* out, uint32_t* spot_out, const mqi_spot* spots, const uint64_t* cum,
                                    uint32_t n_spots, uint64_t h0, uint32_t n, uint32_t k0, uint32_t k1, cudaStream_t s);
 cudaError_t launch_wave(const WaveParams& p, int grid, int block, int blocks_per_sm, cudaStream_t s);

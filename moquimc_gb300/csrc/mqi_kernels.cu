@@ -69,7 +69,29 @@ make_grid(const ChildDev& c, const float* sxe, const float* sye, const float* sz
     g.ri  = c.ri;
     g.tr  = c.tr;
     g.identity = c.identity;
+    g.rho_scale = 1.0f;
     return g;
+}
+
+/// The grid of `child` as the track with spot word `sw` sees it: a robust scenario of the
+/// scenario child has its own edges (setup shift) and density scale.
+__device__ inline void
+apply_scenario(const WaveParams& P, Grid& g, int child, uint32_t sw) {
+    if (P.n_scen > 1 && child == P.scen_child) {
+        const int    s = (int) (sw >> kScenShift);
+        const float* e = P.scen_edges + (size_t) s * P.scen_stride;
+        g.xe        = e;
+        g.ye        = e + g.nx + 1;
+        g.ze        = e + g.nx + g.ny + 2;
+        g.rho_scale = P.scen_scale[s];
+    }
+}
+
+/// Density of voxel cnb in the track's scenario: hu_to_density(hu) * DensityScaling as one FP32
+/// product (mqi_tps_env.hpp:766-769); the scale is 1 outside robust runs.
+__device__ inline float
+voxel_rho(const Grid& g, uint32_t cnb) {
+    return __fmul_rn(g.rho[cnb], g.rho_scale);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -261,13 +283,14 @@ score_step(Ctx& C, const Trk& t, uint32_t cnb, float rho, float vol) {
             // insert_hashtable(data_, cnb, spot_ind, ...) (mqi_transport.hpp:204-225); a history
             // without a spot index lands in column 0
             const bool valid = ok && v > 0.0;
-            const uint32_t col = C.spot == 0xFFFFFFFFu ? 0u : C.spot;
+            const uint32_t col = (C.spot & kSpotMask) == kNoSpot ? 0u : (C.spot & kSpotMask);
             dij_add(s.dij, s.dij_mask, s.dij_count, P.error_flag, col, cnb, s.double_score ? v + v : v, valid);
             continue;
         }
         const bool valid = ok && v > 0.0 && key < s.tally_len;
-        if (s.double_score) tally_add(s.tally, key, v + v, valid);
-        else tally_add(s.tally, key, v, valid);
+        double* tally = s.tally + (uint64_t) (C.spot >> kScenShift) * s.tally_len;   // scenario's tally
+        if (s.double_score) tally_add(tally, key, v + v, valid);
+        else tally_add(tally, key, v, valid);
     }
 }
 
@@ -327,7 +350,7 @@ score_local_daughter(Ctx& C, float3 pw, float3 dw, float ke0, float dE0) {
     t.cell = grid_index(C.g, p, d);
     if (!grid_valid(C.g, t.cell)) return false;
     const uint32_t cnb = grid_cnb(C.g, t.cell);
-    const float    rho = C.g.rho[cnb];
+    const float    rho = voxel_rho(C.g, cnb);
     if (rho < 1.0e-7f) return false;
     const float d2b = grid_exit(C.g, p, d, t.cell);
     if (d2b < 0.0f) return true;   // the voxel loop breaks before scoring
@@ -356,6 +379,7 @@ emit_daughter(const WaveParams* P, const Tables* T, int child, const float* xe, 
     Ctx C;
     C.P = P; C.T = T; C.child = child; C.dbg = dbg; C.tcut = 0.0f; C.spot = spot;
     C.g = make_grid(P->child[child], xe, ye, ze);
+    apply_scenario(*P, C.g, child, spot);
     C.n_sec = C.n_local = C.n_drop = C.n_err = 0;
     daughter_to_world(C.g, p, d);
     if (P->inline_local && ke0 <= kTpCut && score_local_daughter(C, p, d, ke0, dE0)) return 1;
@@ -591,7 +615,7 @@ post_interaction(const WaveParams* P, const Tables* T, Grid g, int child, bool d
                  PostState s) {
     Ctx C;
     C.P = P; C.T = T; C.g = g; C.child = child; C.dbg = dbg; C.tcut = tcut;
-    C.spot = 0xFFFFFFFFu;
+    C.spot = s.t.spot;
     C.n_sec = C.n_local = C.n_drop = C.n_err = 0;
     if (proc == 0) post_delta(C, s.t, s.rng);
     else if (proc == 1) post_pp(C, s.t, s.rng);
@@ -756,6 +780,7 @@ wave_body(const WaveParams& P) {
         for (int c = 0; c < P.n_children; ++c) {
             const ChildDev& ch = P.child[c];
             const int need     = ch.nx + ch.ny + ch.nz + 3;
+            if (P.n_scen > 1 && c == P.scen_child) continue;   // scenario edges are read from global memory
             if (off + need > P.smem_edge_floats) break;
             float* e = sedges + off;
             for (int i = threadIdx.x; i <= ch.nx; i += blockDim.x) e[i] = ch.xe[i];
@@ -812,6 +837,7 @@ wave_body(const WaveParams& P) {
                 if (step_phase) {
                     C.child = t.child;
                     C.g     = make_grid(P.child[t.child], s_edges[t.child][0], s_edges[t.child][1], s_edges[t.child][2]);
+                    apply_scenario(P, C.g, t.child, t.spot);
                 }
             }
         }
@@ -824,6 +850,7 @@ wave_body(const WaveParams& P) {
             }
             C.child = t.child;
             C.g     = make_grid(P.child[t.child], s_edges[t.child][0], s_edges[t.child][1], s_edges[t.child][2]);
+            apply_scenario(P, C.g, t.child, t.spot);
             C.spot  = t.spot;
             to_child(C.g, t.p0, t.d0);
             t.p1 = t.p0;
@@ -860,7 +887,7 @@ wave_body(const WaveParams& P) {
         // ---- one voxel step (mqi_transport.hpp:192-233) ----
         C.spot = t.spot;
         const uint32_t cnb = grid_cnb(C.g, t.cell);
-        const float    rho = C.g.rho[cnb];
+        const float    rho = voxel_rho(C.g, cnb);
         const float    d2b = grid_exit(C.g, t.p0, t.d0, t.cell);
         stepping(C, t, rng, rho, d2b);
         ++n_steps;
@@ -921,10 +948,12 @@ namespace mqi_gpu
 // ------------------------------------------------------------------------------------------
 __global__ void
 k_load_primaries(Queue q, const mqi_vertex* __restrict__ v, const uint32_t* __restrict__ spot_ids, uint64_t h0,
-                 uint32_t n) {
+                 uint32_t n, uint32_t n_scen) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const mqi_vertex x = v[h0 + i];
+    if (i >= n * n_scen) return;
+    const uint32_t   scen = i % n_scen;
+    const uint64_t   h    = h0 + i / n_scen;
+    const mqi_vertex x    = v[h];
     q.ke[i]     = x.ke;
     q.px[i]     = x.pos[0];
     q.py[i]     = x.pos[1];
@@ -933,20 +962,21 @@ k_load_primaries(Queue q, const mqi_vertex* __restrict__ v, const uint32_t* __re
     q.dy[i]     = x.dir[1];
     q.dz[i]     = x.dir[2];
     q.dE0[i]    = 0.0f;
-    q.hist[i]   = (uint32_t) (h0 + i);
+    q.hist[i]   = (uint32_t) h;
     q.uid_lo[i] = 0u;
     q.uid_hi[i] = 0u;
     q.ctr[i]    = 0u;
     q.meta[i]   = kMetaPrimary;
     q.cell[i]   = 0;
-    q.spot[i]   = spot_ids ? spot_ids[h0 + i] : 0xFFFFFFFFu;
+    q.spot[i]   = ((spot_ids ? spot_ids[h] : kNoSpot) & kSpotMask) | (scen << kScenShift);
 }
 
 cudaError_t
 launch_load_primaries(const Queue& q, const mqi_vertex* v, const uint32_t* spot_ids, uint64_t h0, uint32_t n,
-                      cudaStream_t s) {
+                      uint32_t n_scen, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    k_load_primaries<<<(n + 255) / 256, 256, 0, s>>>(q, v, spot_ids, h0, n);
+    const uint32_t m = n * n_scen;
+    k_load_primaries<<<(m + 255) / 256, 256, 0, s>>>(q, v, spot_ids, h0, n, n_scen);
     return cudaGetLastError();
 }
 
@@ -1174,10 +1204,11 @@ sample_spot_vertex(const mqi_spot* __restrict__ spots, const uint64_t* __restric
 
 __global__ void
 k_sample_primaries(Queue q, const mqi_spot* __restrict__ spots, const uint64_t* __restrict__ cum, uint32_t n_spots,
-                   uint64_t h0, uint32_t n, uint32_t k0, uint32_t k1) {
+                   uint64_t h0, uint32_t n, uint32_t n_scen, uint32_t k0, uint32_t k1) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const uint64_t h = h0 + i;
+    if (i >= n * n_scen) return;
+    const uint32_t scen = i % n_scen;
+    const uint64_t h    = h0 + i / n_scen;
     float3 p, d;
     float  ke;
     const uint32_t s = sample_spot_vertex(spots, cum, n_spots, h, k0, k1, p, d, ke);
@@ -1191,7 +1222,7 @@ k_sample_primaries(Queue q, const mqi_spot* __restrict__ spots, const uint64_t* 
     q.ctr[i]    = 0u;
     q.meta[i]   = kMetaPrimary;
     q.cell[i]   = 0;
-    q.spot[i]   = s;
+    q.spot[i]   = (s & kSpotMask) | (scen << kScenShift);
 }
 
 __global__ void
@@ -1212,9 +1243,10 @@ k_sample_vertices(mqi_vertex* __restrict__ out, uint32_t* __restrict__ spot_out,
 
 cudaError_t
 launch_sample_primaries(const Queue& q, const mqi_spot* spots, const uint64_t* cum, uint32_t n_spots, uint64_t h0,
-                        uint32_t n, uint32_t k0, uint32_t k1, cudaStream_t s) {
+                        uint32_t n, uint32_t n_scen, uint32_t k0, uint32_t k1, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
-    k_sample_primaries<<<(n + 127) / 128, 128, 0, s>>>(q, spots, cum, n_spots, h0, n, k0, k1);
+    const uint32_t m = n * n_scen;
+    k_sample_primaries<<<(m + 127) / 128, 128, 0, s>>>(q, spots, cum, n_spots, h0, n, n_scen, k0, k1);
     return cudaGetLastError();
 }
 

@@ -188,7 +188,7 @@ mqi_transport_noalloc(int nx, int ny, int nz, const float* d_xe, const float* d_
     Queue*    B = &qb;
     for (uint64_t h = 0; h < n_histories; h += kNoallocChunk) {
         const uint32_t n = (uint32_t) ((n_histories - h) < kNoallocChunk ? (n_histories - h) : kNoallocChunk);
-        e = launch_load_primaries(*A, d_vertices, nullptr, h, n, stream);
+        e = launch_load_primaries(*A, d_vertices, nullptr, h, n, 1, stream);
         if (e == cudaSuccess) e = cudaMemcpyAsync(counters, &n, sizeof(uint32_t), cudaMemcpyHostToDevice, stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(stream);   // `n` lives on this stack frame
         if (e != cudaSuccess) return noalloc_fail(MQI_ERR_CUDA, std::string("mqi_transport_noalloc: ") + cudaGetErrorString(e));
