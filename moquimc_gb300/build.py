@@ -73,7 +73,7 @@ def build_host_tools(force: bool = False) -> str:
     out = os.path.join(LIB_DIR, "phantom_env")
     deps = [src, LIB] + [os.path.join(HOST, f) for f in os.listdir(HOST) if f.endswith((".hpp", ".h"))]
     if force or _stale(out, deps):
-        _run(["g++", "-std=c++17", "-O2", f"-I{INCLUDE}", f"-I{HOST}", src, "-o", out,
+        _run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", f"-I{INCLUDE}", f"-I{HOST}", src, "-o", out,
               f"-L{LIB_DIR}", "-lmqigpu", f"-Wl,-rpath,{LIB_DIR}"])
     return out
 

@@ -20,6 +20,8 @@
 //   sample <out.bin> <n> <seed>
 //       Draws n samples from each sampling routine at fixed inputs (along_step, the four
 //       post_step processes) for distribution tests.
+//   vertices <out.bin> <n> <seed> <gaussian> x y z sx sy energy colli gantry couch iec
+//       Samples phantom_env's beam source with the reference's own distribution classes.
 #include <moqui/base/environments/mqi_phantom_env.hpp>
 #include <moqui/kernel_functions/mqi_transport.hpp>
 
@@ -399,6 +401,47 @@ run_sample(const char* out_path, long n, unsigned seed) {
     return 0;
 }
 
+/// The beam source of phantom_env (mqi_phantom_env.hpp:204-232) built from the reference's own
+/// classes -- coordinate_transform, phsp_6d_uniform or phsp_6d, const_1d, beamlet, beamsource --
+/// and sampled with std::default_random_engine seeded like phantom_env's beam_rng.  Arguments:
+/// out n seed gaussian x y z sx sy energy colli gantry couch iec.  Output: vec<f32> of 7 floats
+/// per vertex (ke, pos, dir).
+int
+run_vertices(int argc, char** argv) {
+    if (argc < 16) return 2;
+    const char* out  = argv[2];
+    const long  n    = std::atol(argv[3]);
+    const int   seed = std::atoi(argv[4]);
+    const bool  gaus = std::atoi(argv[5]) != 0;
+    std::array<float, 3> pos  = { std::stof(argv[6]), std::stof(argv[7]), std::stof(argv[8]) };
+    std::array<float, 2> size = { std::stof(argv[9]), std::stof(argv[10]) };
+    const float energy        = std::stof(argv[11]);
+    std::array<float, 4> ang  = { std::stof(argv[12]), std::stof(argv[13]), std::stof(argv[14]), std::stof(argv[15]) };
+    mqi::coordinate_transform<float> p_coord(ang, { 0, 0, 0 });
+    mqi::vec3<float>                 dir(0, 0, -1);
+    std::array<float, 6> mean = { pos[0], pos[1], pos[2], dir.x, dir.y, dir.z };
+    std::array<float, 6> sigm = { size[0], size[1], 0, 0, 0, 0 };
+    std::array<float, 2> corr = { 0.0, 0.0 };
+    mqi::pdf_Md<float, 6>* phsp;
+    if (gaus) phsp = new mqi::phsp_6d<float>(mean, sigm, corr);
+    else phsp = new mqi::phsp_6d_uniform<float>(mean, sigm, corr);
+    auto* e = new mqi::const_1d<float>({ energy }, { 0.0f });
+    mqi::beamsource<float> src;
+    src.append_beamlet(mqi::beamlet<float>(e, phsp), static_cast<size_t>(n), p_coord);
+    std::default_random_engine rng;
+    rng.seed(seed);
+    std::vector<float> v;
+    v.reserve(7 * n);
+    for (long i = 0; i < n; ++i) {
+        auto             bl = src(i);
+        mqi::vertex_t<float> x = bl(&rng);
+        v.insert(v.end(), { x.ke, x.pos.x, x.pos.y, x.pos.z, x.dir.x, x.dir.y, x.dir.z });
+    }
+    std::ofstream fout(out, std::ios::binary);
+    write_vec(fout, v);
+    return 0;
+}
+
 }   // namespace
 
 void
@@ -424,6 +467,7 @@ main(int argc, char** argv) {
     if (mode == "phantom") return run_phantom(argc, argv);
     if (mode == "raywalk" && argc >= 4) return run_raywalk(argv[2], argv[3]);
     if (mode == "physics" && argc >= 3) return run_physics(argv[2]);
+    if (mode == "vertices") return run_vertices(argc, argv);
     if (mode == "sample" && argc >= 5)
         return run_sample(argv[2], std::atol(argv[3]), static_cast<unsigned>(std::atol(argv[4])));
     std::fprintf(stderr, "bad arguments\n");

@@ -16,6 +16,9 @@ reference headers by oracle/build_oracle.py -- is run here to produce them:
                     12500 histories (1e5 in total).
 * ``dose_c2.npz``   the slab phantom (256^3, lung + bone, 150 MeV Gaussian sigma 4 mm, release
                     physics): the same statistics over 8 batches of 12500 histories.
+* ``vertices.npz``  phantom_env's host beam source (coordinate_transform + phsp_6d_uniform or
+                    phsp_6d + const_1d, std::default_random_engine) for a few seeds, spot shapes and
+                    gantry/couch angles: the vertices the C++ host driver must reproduce bit for bit.
 
 Run from the repository root: ``python tests/golden/make_golden.py``.  It needs the reference sources
 (to stage and build the CPU oracle) and takes about a minute on 8 cores.
@@ -130,10 +133,35 @@ def make_dose(wl, fname, batches=8, each=12500, seed0=31000, coarse_bins=(10, 10
     print(fname, "R80", r80, "per-core primaries/s", each / secs.mean())
 
 
+VERTEX_CASES = [
+    # seed, gaussian, position, size, energy, angles (collimator, gantry, couch, iec2dicom)
+    (1234, 0, (0.0, 0.0, 0.5), (30.0, 30.0), 200.0, (0.0, 0.0, 0.0, 0.0)),
+    (7, 0, (1.0, 2.0, 3.0), (10.0, 5.0), 150.0, (10.0, 30.0, 5.0, 90.0)),
+    (99, 1, (0.0, 0.0, 0.5), (4.0, 4.0), 150.0, (0.0, 45.0, 0.0, 0.0)),
+]
+
+
+def make_vertices(n=2000):
+    import subprocess
+    import tempfile
+
+    out = {}
+    for k, (seed, gaus, pos, size, e, ang) in enumerate(VERTEX_CASES):
+        with tempfile.TemporaryDirectory() as td:
+            f = os.path.join(td, "v.bin")
+            cmd = [mqo.ref_binary(False), "vertices", f, str(n), str(seed), str(gaus), *map(str, pos), *map(str, size),
+                   str(e), *map(str, ang)]
+            subprocess.run(cmd, check=True, capture_output=True)
+            out[f"case{k}"] = mqo.read_vecs(f, [np.float32])[0].reshape(-1, 7)
+        out[f"args{k}"] = np.array([seed, gaus, *pos, *size, e, *ang], np.float64)
+    np.savez_compressed(os.path.join(OUT, "vertices.npz"), **out)
+    print("vertices", {k: v.shape for k, v in out.items()})
+
+
 def main():
     if not mqo.ref_available():
         raise SystemExit("the reference CPU build is not available")
-    which = sys.argv[1:] or ["raywalk", "physics", "dose_c1", "dose_c2"]
+    which = sys.argv[1:] or ["raywalk", "physics", "dose_c1", "dose_c2", "vertices"]
     if "raywalk" in which:
         make_raywalk()
     if "physics" in which:
@@ -142,6 +170,8 @@ def main():
         make_dose(workloads.c1(), "dose_c1.npz")
     if "dose_c2" in which:
         make_dose(workloads.c2(), "dose_c2.npz", seed0=41000, coarse_bins=(8, 8, 4))
+    if "vertices" in which:
+        make_vertices()
 
 
 if __name__ == "__main__":
