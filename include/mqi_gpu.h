@@ -108,8 +108,9 @@ int mqi_destroy(mqi_ctx* ctx);
 /* Last error message of this context (or of the calling thread when ctx is NULL). */
 const char* mqi_last_error(const mqi_ctx* ctx);
 
-/* Run all subsequent work of this context on `cuda_stream` (a cudaStream_t; NULL = the
- * context's own stream). */
+/* Run all subsequent work of this context on `cuda_stream` (a cudaStream_t; NULL = a new stream
+ * of the context's own, which does not synchronise with the legacy default stream: pass
+ * cudaStreamLegacy, (void*) 1, to order the work with that stream). */
 int mqi_set_stream(mqi_ctx* ctx, void* cuda_stream);
 
 /* Physics options.  physics_debug = 1 reproduces moqui built with -D__PHYSICS_DEBUG__ (the

@@ -177,7 +177,10 @@ class Context:
         self._check(self.lib.mqi_set_tuning(self.h, block, blocks_per_sm, slice_steps, primary_chunk), self.h)
 
     def set_stream(self, stream_ptr: Optional[int]) -> None:
+        """Run the context's work on a cudaStream_t handle (1 = the legacy default stream;
+        None = a stream of the context's own)."""
         self._check(self.lib.mqi_set_stream(self.h, stream_ptr), self.h)
+        self._stream_handle = stream_ptr
 
     def add_child(self, xe, ye, ze, rot_fwd=None, translation=None) -> int:
         xe = np.ascontiguousarray(xe, dtype=np.float32)

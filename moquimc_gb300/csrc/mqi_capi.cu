@@ -161,6 +161,7 @@ mqi_destroy(mqi_ctx* c) {
 int
 mqi_set_stream(mqi_ctx* c, void* s) {
     if (!valid_ctx(c)) return fail(c, MQI_ERR_INVALID, "mqi_set_stream: ctx is NULL");
+    if (s && !c->own_stream && c->stream == static_cast<cudaStream_t>(s)) return MQI_OK;
     DeviceGuard g(c->device);
     if (c->own_stream && c->stream) {
         cudaStreamSynchronize(c->stream);

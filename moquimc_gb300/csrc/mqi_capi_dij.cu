@@ -27,6 +27,7 @@ void
 free_csr(DijCsr& m) {
     cudaFree(m.s_indptr); cudaFree(m.s_voxel); cudaFree(m.s_value);
     cudaFree(m.v_row); cudaFree(m.v_indptr); cudaFree(m.v_spot); cudaFree(m.v_value);
+    cudaFree(m.seg_start); cudaFree(m.row_seg); cudaFree(m.partial);
     m = DijCsr{};
 }
 
@@ -181,10 +182,30 @@ mqi_dij_build(mqi_ctx* c, int id, uint32_t n_spots, double scale, uint64_t* nnz_
     MQI_CUDA(c, radix_sort_pairs(skeys, sslot, kb, ib, n, bit_length((uint64_t) n_spots * nvox - 1), hist, offs, scan, st),
              "mqi_dij_build: sort");
     MQI_CUDA(c, dij_row_bounds(skeys, n, nvox, n_spots, m.s_indptr, st), "mqi_dij_build");
-    uint64_t last = 0;
-    MQI_CUDA(c, cudaMemcpyAsync(&last, m.s_indptr + n_spots, sizeof(last), cudaMemcpyDeviceToHost, st), "mqi_dij_build");
+    std::vector<uint64_t> indptr(n_spots + 1);
+    MQI_CUDA(c, cudaMemcpyAsync(indptr.data(), m.s_indptr, indptr.size() * sizeof(uint64_t), cudaMemcpyDeviceToHost, st),
+             "mqi_dij_build");
     MQI_CUDA(c, cudaStreamSynchronize(st), "mqi_dij_build");
-    if (last != n) return fail(c, MQI_ERR_INVALID, "mqi_dij_build: the table holds a spot index >= n_spots");
+    if (indptr[n_spots] != n) return fail(c, MQI_ERR_INVALID, "mqi_dij_build: the table holds a spot index >= n_spots");
+    // backward segments: each row cut into runs of at most kDijSegment entries
+    {
+        std::vector<uint64_t> seg;
+        std::vector<uint32_t> row_seg(n_spots + 1);
+        for (uint32_t r = 0; r < n_spots; ++r) {
+            row_seg[r] = (uint32_t) seg.size();
+            for (uint64_t b = indptr[r]; b < indptr[r + 1]; b += kDijSegment) seg.push_back(b);
+        }
+        row_seg[n_spots] = (uint32_t) seg.size();
+        m.n_seg = seg.size();
+        seg.push_back(n);
+        MQI_CUDA(c, sc.alloc(m.seg_start, seg.size()), "mqi_dij_build: allocation");
+        MQI_CUDA(c, sc.alloc(m.row_seg, row_seg.size()), "mqi_dij_build: allocation");
+        MQI_CUDA(c, sc.alloc(m.partial, m.n_seg), "mqi_dij_build: allocation");
+        MQI_CUDA(c, cudaMemcpy(m.seg_start, seg.data(), seg.size() * sizeof(uint64_t), cudaMemcpyHostToDevice),
+                 "mqi_dij_build");
+        MQI_CUDA(c, cudaMemcpy(m.row_seg, row_seg.data(), row_seg.size() * sizeof(uint32_t), cudaMemcpyHostToDevice),
+                 "mqi_dij_build");
+    }
 
     // 3. spot-row entries, and (voxel, position) pairs for the voxel-row layout
     unsigned long long* vkeys = (skeys == ka) ? kb : ka;
@@ -213,7 +234,7 @@ mqi_dij_build(mqi_ctx* c, int id, uint32_t n_spots, double scale, uint64_t* nnz_
                                m.v_value, st), "mqi_dij_build");
     MQI_CUDA(c, cudaStreamSynchronize(st), "mqi_dij_build");
     for (void* p : { (void*) m.s_indptr, (void*) m.s_voxel, (void*) m.s_value, (void*) m.v_row, (void*) m.v_indptr,
-                     (void*) m.v_spot, (void*) m.v_value })
+                     (void*) m.v_spot, (void*) m.v_value, (void*) m.seg_start, (void*) m.row_seg, (void*) m.partial })
         sc.release(p);
     m.built = true;
     s.csr   = m;
@@ -301,7 +322,8 @@ mqi_dij_rmatvec(mqi_ctx* c, int id, const void* gin, void* grad, int fp64, int o
         dg = tg;
         dr = tr;
     }
-    MQI_CUDA(c, dij_backward(m.s_indptr, m.s_voxel, m.s_value, m.n_spots, dg, dr, fp64, c->stream), "mqi_dij_rmatvec");
+    MQI_CUDA(c, dij_backward(m.seg_start, m.n_seg, m.row_seg, m.n_spots, m.s_voxel, m.s_value, m.partial, dg, dr, fp64,
+                             c->num_sms, c->stream), "mqi_dij_rmatvec");
     if (!on_device) {
         MQI_CUDA(c, cudaMemcpyAsync(grad, dr, m.n_spots * es, cudaMemcpyDeviceToHost, c->stream), "mqi_dij_rmatvec");
         MQI_CUDA(c, cudaStreamSynchronize(c->stream), "mqi_dij_rmatvec");

@@ -45,6 +45,10 @@ struct DijCsr {
     uint64_t* v_indptr = nullptr;   // n_vrows + 1
     uint32_t* v_spot = nullptr;     // nnz
     float*    v_value = nullptr;    // nnz
+    uint64_t  n_seg = 0;            // backward segments: contiguous runs of one row's entries
+    uint64_t* seg_start = nullptr;  // n_seg + 1
+    uint32_t* row_seg = nullptr;    // n_spots + 1: first segment of each row
+    double*   partial = nullptr;    // n_seg
 };
 
 struct ScorerHost {

@@ -285,28 +285,42 @@ k_dij_forward(const uint32_t* __restrict__ row_voxel, const uint64_t* __restrict
     }
 }
 
-/// grad[s] = sum_k val[k] * g[voxel[k]] over spot rows (the transposed operator); one block per
-/// row, per-thread partials in T, block tree in double.
+/// grad[s] = sum_k val[k] * g[voxel[k]] over spot rows (the transposed operator), in two passes
+/// with a fixed order.  Pass 1: the entries are cut into segments of at most kDijSegment entries
+/// that never cross a row; one block per segment sums its products in FP64 (signed terms of a
+/// gradient cancel, so FP32 partials lose digits) and writes one partial.  Pass 2: one thread per
+/// row adds its segments' partials in order.  Rows of very different lengths (1e4 to 3e6 entries
+/// at 2000 spots) thereby spread over every SM.
 template<typename T>
 __global__ void
-k_dij_backward(const uint64_t* __restrict__ indptr, const uint32_t* __restrict__ vox, const float* __restrict__ val,
-               uint32_t n_rows, const T* __restrict__ g, T* __restrict__ grad) {
+k_dij_backward_segments(const uint64_t* __restrict__ seg_start, uint64_t n_seg, const uint32_t* __restrict__ vox,
+                        const float* __restrict__ val, const T* __restrict__ g, double* __restrict__ partial) {
     __shared__ double part[32];
-    for (uint32_t r = blockIdx.x; r < n_rows; r += gridDim.x) {
-        const uint64_t b = indptr[r], e = indptr[r + 1];
-        T              s = T(0);
-        for (uint64_t k = b + threadIdx.x; k < e; k += blockDim.x) s += (T) val[k] * g[vox[k]];
-        double d = (double) s;
+    for (uint64_t sg = blockIdx.x; sg < n_seg; sg += gridDim.x) {
+        const uint64_t b = seg_start[sg], e = seg_start[sg + 1];
+        double         d = 0.0;
+        for (uint64_t k = b + threadIdx.x; k < e; k += blockDim.x) d += (double) val[k] * (double) g[vox[k]];
         for (int o = 16; o > 0; o >>= 1) d += __shfl_down_sync(0xFFFFFFFFu, d, o);
         if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = d;
         __syncthreads();
         if (threadIdx.x < 32) {
             d = threadIdx.x < (blockDim.x >> 5) ? part[threadIdx.x] : 0.0;
             for (int o = 16; o > 0; o >>= 1) d += __shfl_down_sync(0xFFFFFFFFu, d, o);
-            if (threadIdx.x == 0) grad[r] = (T) d;
+            if (threadIdx.x == 0) partial[sg] = d;
         }
         __syncthreads();
     }
+}
+
+template<typename T>
+__global__ void
+k_dij_backward_rows(const uint32_t* __restrict__ row_seg, uint32_t n_rows, const double* __restrict__ partial,
+                    T* __restrict__ grad) {
+    const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= n_rows) return;
+    double d = 0.0;
+    for (uint32_t k = row_seg[r]; k < row_seg[r + 1]; ++k) d += partial[k];
+    grad[r] = (T) d;
 }
 
 __global__ void
@@ -428,13 +442,19 @@ dij_forward(const uint32_t* row_voxel, const uint64_t* indptr, const uint32_t* s
 }
 
 cudaError_t
-dij_backward(const uint64_t* indptr, const uint32_t* vox, const float* val, uint32_t n_rows, const void* g, void* grad,
-             int fp64, cudaStream_t s) {
+dij_backward(const uint64_t* seg_start, uint64_t n_seg, const uint32_t* row_seg, uint32_t n_rows, const uint32_t* vox,
+             const float* val, double* partial, const void* g, void* grad, int fp64, int sms, cudaStream_t s) {
     if (n_rows == 0) return cudaSuccess;
-    if (fp64)
-        k_dij_backward<double><<<n_rows, 256, 0, s>>>(indptr, vox, val, n_rows, (const double*) g, (double*) grad);
-    else
-        k_dij_backward<float><<<n_rows, 256, 0, s>>>(indptr, vox, val, n_rows, (const float*) g, (float*) grad);
+    if (n_seg) {
+        const unsigned grid = (unsigned) (n_seg < (uint64_t) sms * 64 ? n_seg : (uint64_t) sms * 64);
+        if (fp64)
+            k_dij_backward_segments<double><<<grid, 256, 0, s>>>(seg_start, n_seg, vox, val, (const double*) g, partial);
+        else
+            k_dij_backward_segments<float><<<grid, 256, 0, s>>>(seg_start, n_seg, vox, val, (const float*) g, partial);
+    }
+    const unsigned rb = (n_rows + 255) / 256;
+    if (fp64) k_dij_backward_rows<double><<<rb, 256, 0, s>>>(row_seg, n_rows, partial, (double*) grad);
+    else k_dij_backward_rows<float><<<rb, 256, 0, s>>>(row_seg, n_rows, partial, (float*) grad);
     return cudaGetLastError();
 }
 

@@ -138,8 +138,10 @@ cudaError_t dij_voxel_rows(const unsigned long long* vkeys, const uint32_t* vpos
                            cudaStream_t s);
 cudaError_t dij_forward(const uint32_t* row_voxel, const uint64_t* indptr, const uint32_t* spot, const float* val,
                         uint64_t n_rows, const void* w, void* dose, int fp64, int sms, cudaStream_t s);
-cudaError_t dij_backward(const uint64_t* indptr, const uint32_t* vox, const float* val, uint32_t n_rows, const void* g,
-                         void* grad, int fp64, cudaStream_t s);
+constexpr uint64_t kDijSegment = 16384;   // entries per backward segment
+cudaError_t dij_backward(const uint64_t* seg_start, uint64_t n_seg, const uint32_t* row_seg, uint32_t n_rows,
+                         const uint32_t* vox, const float* val, double* partial, const void* g, void* grad, int fp64,
+                         int sms, cudaStream_t s);
 
 // ---- launchers (mqi_kernels.cu) ----
 // Loaders: n histories from h0, each once per scenario (n_scen >= 1), scenario-interleaved:

@@ -27,7 +27,13 @@ class DijOperator:
         self.nnz = nnz
 
     def _bind_stream(self, torch):
-        self.ctx.set_stream(torch.cuda.current_stream().cuda_stream)
+        # torch's default stream has the handle 0, which the C ABI reads as "the context's own
+        # stream"; name the legacy default stream (cudaStreamLegacy = 1) instead so that the
+        # products are ordered with the surrounding torch work.
+        handle = torch.cuda.current_stream().cuda_stream or 1
+        if getattr(self.ctx, "_stream_handle", None) != handle:
+            self.ctx.set_stream(handle)
+            self.ctx._stream_handle = handle
 
     def matvec(self, w):
         """dose = D.w for a CUDA tensor w of n_spots entries (float32 or float64)."""

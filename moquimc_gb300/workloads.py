@@ -7,11 +7,16 @@
   slab (HU -700) and a 15 mm bone slab (HU 1200) at depths drawn from numpy's default_rng(2) in
   40-180 mm, full lateral extent; one 150 MeV Gaussian spot (sigma 4 mm), 1e6 histories.
 * ``c3``: a synthetic CT of 512x512x200 voxels at 0.98x0.98x2 mm centred at the origin: an
-  ellipsoidal body (semi-axes 180/120/180 mm on x/y/z) whose HU is a Gaussian-smoothed (sigma 5 mm)
-  random field rescaled to mean 40 and s.d. 150, clipped to [-1000, 1500], in air (HU -1000); a
-  plan of 2000 Gaussian spots (sigma 4 mm, no divergence) on a 5 mm grid (50 on x by 40 on y)
-  entering at z = 195 mm along -z, energies uniform in 70-230 MeV, history counts lognormal
-  (median 1e4) clipped to 1e3-1e5.
+  ellipsoidal body (semi-axes 180/120/180 mm on x/y/z) whose HU is white noise from
+  default_rng(4), Gaussian-smoothed (sigma 5 mm) and rescaled to mean 40 and s.d. 150, clipped to
+  [-1000, 1500], in air (HU -1000); a plan of 2000 Gaussian spots (sigma 4 mm, no divergence) on a
+  5 mm grid (50 on x by 40 on y) entering at z = 195 mm along -z, energies uniform in 70-230 MeV
+  (default_rng(5)), history counts lognormal (default_rng(6)) with the 1st-99th percentiles at
+  1e3-1e5, clipped to that range.
+* ``c4``: the c3 CT and plan x 21 robust scenarios: setup shifts 0, +-3 mm on x, y and z, each with
+  DensityScaling 1, 1.035 and 0.965.
+* ``c5``: the c3 Dij with a 60 mm spherical target at the body centre and a 20 mm spherical organ
+  placed by default_rng(7) outside it; finite differences on 64 spots drawn by default_rng(8).
 """
 from __future__ import annotations
 
@@ -79,7 +84,7 @@ def c2(histories: int = 1_000_000, physics_debug: bool = False) -> Workload:
 
 
 def ct_hu(nxyz=(512, 512, 200), dxyz=(0.98, 0.98, 2.0), semi=(180.0, 120.0, 180.0), mean=40.0, sd=150.0,
-          smooth_mm=5.0, seed=3) -> np.ndarray:
+          smooth_mm=5.0, seed=4) -> np.ndarray:
     """int16 HU [nz][ny][nx] of the synthetic CT body.  The random field is drawn and smoothed only
     on the body's bounding box (the air outside does not use it)."""
     from scipy.ndimage import gaussian_filter
@@ -102,26 +107,28 @@ def ct_hu(nxyz=(512, 512, 200), dxyz=(0.98, 0.98, 2.0), semi=(180.0, 120.0, 180.
     return hu
 
 
-def spot_plan(n_x=50, n_y=40, pitch=5.0, z0=195.0, sigma=4.0, e_range=(70.0, 230.0), median=1e4,
-              h_range=(1e3, 1e5), seed=4) -> np.ndarray:
+def spot_plan(n_x=50, n_y=40, pitch=5.0, z0=195.0, sigma=4.0, e_range=(70.0, 230.0), h_range=(1e3, 1e5),
+              seeds=(5, 6)) -> np.ndarray:
     """Spots on a pitch grid centred on the beam axis, beam along -z (identity beam-to-world
-    transform), energies uniform in e_range, history counts lognormal clipped to h_range."""
+    transform), energies uniform in e_range, history counts lognormal with the 1st and 99th
+    percentiles at h_range, clipped to it."""
     from .capi import SPOT_DTYPE
 
-    rng = np.random.default_rng(seed)
     n = n_x * n_y
     sp = np.zeros(n, SPOT_DTYPE)
     gx = (np.arange(n_x) - 0.5 * (n_x - 1)) * pitch
     gy = (np.arange(n_y) - 0.5 * (n_y - 1)) * pitch
     X, Y = np.meshgrid(gx, gy, indexing="xy")
-    sp["energy"] = rng.uniform(*e_range, n).astype(np.float32)
+    sp["energy"] = np.random.default_rng(seeds[0]).uniform(*e_range, n).astype(np.float32)
     sp["mean"][:, 0] = X.ravel()
     sp["mean"][:, 1] = Y.ravel()
     sp["mean"][:, 2] = z0
     sp["sigma"][:, 0] = sigma
     sp["sigma"][:, 1] = sigma
     sp["rot"] = np.eye(3, dtype=np.float32).ravel()
-    h = np.exp(rng.normal(np.log(median), np.log(10.0) / 2.0, n))
+    lo, hi = np.log(h_range[0]), np.log(h_range[1])
+    z99 = 2.3263478740408408                                   # standard normal 99th percentile
+    h = np.exp(np.random.default_rng(seeds[1]).normal(0.5 * (lo + hi), 0.5 * (hi - lo) / z99, n))
     sp["histories"] = np.clip(np.rint(h), h_range[0], h_range[1]).astype(np.uint64)
     return sp
 
@@ -156,6 +163,38 @@ def c3(physics_debug: bool = False) -> PlanWorkload:
     hu = _CT_CACHE[key]
     lxyz = (float(np.float32(512 * 0.98)), float(np.float32(512 * 0.98)), 400.0)
     return PlanWorkload("c3_synthetic_ct_2000_spots", lxyz, (0.0, 0.0, 0.0), nxyz, hu, spot_plan(), physics_debug)
+
+
+def c4_scenarios():
+    """The 21 robust scenarios: (shift mm, density scale)."""
+    shifts = [(0.0, 0.0, 0.0)] + [tuple(sg * 3.0 if i == ax else 0.0 for i in range(3)) for ax in range(3)
+                                  for sg in (1, -1)]
+    return [(sh, sc) for sh in shifts for sc in (1.0, 1.035, 0.965)]
+
+
+def scenario_edges(wl, shift):
+    """Edges of the shifted CT: the origin moves by the shift, then the edges are formed from it
+    (tps_env, mqi_tps_env.hpp:475-477 and 507-514)."""
+    p = tuple(np.float32(a) + np.float32(b) for a, b in zip(wl.pxyz, shift))
+    return ph.phantom_box_edges(wl.lxyz, p, wl.nxyz)
+
+
+def c5_structures(wl, target_radius=60.0, organ_radius=20.0, seed=7):
+    """Boolean voxel masks (flat, x fastest) of the spherical target at the body centre and of the
+    organ placed by default_rng(seed) outside the target and inside the body."""
+    rng = np.random.default_rng(seed)
+    semi = np.array([180.0, 120.0, 180.0])
+    while True:
+        d = rng.standard_normal(3)
+        d /= np.linalg.norm(d)
+        c = d * rng.uniform(target_radius + organ_radius + 5.0, target_radius + organ_radius + 35.0)
+        if np.sum(((np.abs(c) + organ_radius) / semi) ** 2) <= 1.0:
+            break
+    centres = [ph.uniform_edges(-0.5 * l, 0.5 * l, n) for l, n in zip(wl.lxyz, wl.nxyz)]
+    x, y, z = [0.5 * (e[1:] + e[:-1]).astype(np.float64) for e in centres]
+    r2t = (z[:, None, None] ** 2 + y[None, :, None] ** 2 + x[None, None, :] ** 2)
+    r2o = ((z[:, None, None] - c[2]) ** 2 + (y[None, :, None] - c[1]) ** 2 + (x[None, None, :] - c[0]) ** 2)
+    return (r2t <= target_radius ** 2).ravel(), (r2o <= organ_radius ** 2).ravel(), c
 
 
 WORKLOADS = {"c1": c1, "c2": c2, "c3": c3}

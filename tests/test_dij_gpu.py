@@ -147,6 +147,25 @@ def test_dij_autograd_matches_finite_differences(gpu_ctx_factory, wl):
     np.testing.assert_allclose(grad, A @ gd, rtol=1e-4, atol=1e-6 * np.abs(A @ gd).max())
 
 
+def test_dij_products_are_ordered_with_torch_work(gpu_ctx_factory, wl):
+    """Chained device products on torch's default stream equal the synchronous host path."""
+    torch = pytest.importorskip("torch")
+    sp = _spots(9, 1500, seed=7)
+    c, cid = _ctx(gpu_ctx_factory, wl)
+    sid = c.add_dij_scorer(cid, capacity=1 << 23)
+    N = c.set_spot_plan(sp)
+    c.transport_plan(0, N, 4)
+    op = c.dij_build(sid, scale=1e6)
+    dev = torch.device("cuda:0")
+    host_d = c.dij_matvec(sid, np.ones(op.n_spots, np.float32), op.n_voxels)
+    host_g = c.dij_rmatvec(sid, host_d, op.n_spots)
+    for _ in range(3):
+        d = op.matvec(torch.ones(op.n_spots, device=dev))
+        g = op.rmatvec(d * 1.0)
+        np.testing.assert_array_equal(d.cpu().numpy(), host_d)
+        np.testing.assert_allclose(g.cpu().numpy(), host_g, rtol=1e-6)
+
+
 def test_dij_save_npz_loads_as_scipy_csr(gpu_ctx_factory, wl, tmp_path):
     sps = pytest.importorskip("scipy.sparse")
     sp = _spots(2, 500, seed=4)
