@@ -9,6 +9,12 @@ tally 134 MB) exceed the 129 MB L2, so no flush is needed between steps.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl mqi|reference] [--workload c2|c1]
 
+The line also carries plan-level sections measured on rank 0 (skip with --no-plan): "plan" -- the
+synthetic CT with 2000 spots, one batched call vs one call per spot, and the time to the
+reference's 1% criterion in the >50% dose region; "robust" -- 21 setup/density scenarios in one
+queue drain; "dij" -- the Dij of the plan, its products and 100 optimisation iterations with a
+finite-difference check of the gradient.
+
 --impl reference times the reference's own CPU implementation (the staged reference build in
 oracle/_ref) on the host cores for the same workload and metric.
 
@@ -174,6 +180,144 @@ def workload_config(wl, histories, note=""):
 
 
 # ------------------------------------------------------------------------------------------
+# Plan-level measurements (synthetic CT, 2000 spots): batched vs plain, time to 1% sigma, the Dij
+# and its optimisation loop, robust scenarios.  Rank 0 only.
+# ------------------------------------------------------------------------------------------
+
+def _cuda_time(torch, fn):
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    r = fn()
+    torch.cuda.synchronize()
+    return time.perf_counter() - t, r
+
+
+def plan_section(torch, capi, workloads, args) -> dict:
+    """C3: one batched plan call vs one call per spot (identical tracks and tallies), and the time
+    to the reference's 1% criterion (mean sigma/mean over voxels above 50% of the maximum) by
+    whole plan passes."""
+    wl = workloads.c3()
+    c = capi.Context(0)
+    c.set_physics(False)
+    cid = c.add_child(*wl.edges())
+    c.set_hu(cid, wl.hu)
+    c.add_scorer(cid, capi.DOSE_W)
+    d1, d2 = c.add_stat_scorers(cid)
+    N = c.set_spot_plan(wl.spots)
+    cum = c.plan_cum
+    c.transport_plan(0, min(N, 200_000), 1)                       # warm-up
+    c.reset()
+    t_b, _ = _cuda_time(torch, lambda: c.transport_plan(0, N, 2))
+    est1, nv = c.stat_uncertainty(d1, d2, N, 0.5)
+    st = c.stats()
+    c.reset()
+    sub = list(range(0, len(wl.spots), args.plain_stride))
+    h_sub = int(sum(int(cum[s + 1] - cum[s]) for s in sub))
+
+    def plain():
+        for s in sub:
+            c.transport_plan(int(cum[s]), int(cum[s + 1]), 2)
+
+    t_p, _ = _cuda_time(torch, plain)
+    c.reset()
+    t_s, (passes, achieved) = _cuda_time(
+        torch, lambda: c.run_plan_until_stat(d1, d2, 0.01, 0.5, args.max_passes, 0x5EED))
+    batched = N / t_b
+    plain_rate = h_sub / t_p
+    out = {
+        "workload": wl.name, "voxels": list(wl.nxyz), "voxel_mm": [0.98, 0.98, 2.0], "spots": len(wl.spots),
+        "histories_per_pass": N, "physics_debug": False,
+        "batched": {"primaries_per_s": batched, "seconds_per_pass": t_b, "steps_per_primary": st["steps"] / N,
+                    "waves": st["waves"], "estimate_after_one_pass": est1, "voxels_above_50pct": nv},
+        "plain_per_spot": {"primaries_per_s": plain_rate, "spots_timed": len(sub), "histories_timed": h_sub,
+                           "sample": f"every {args.plain_stride}th spot, one mqi_transport_plan call per spot"},
+        "batched_over_plain": batched / plain_rate,
+        "time_to_1pct_sigma": {"criterion": "reference estimator <= 1% over voxels > 50% of max dose",
+                               "batched_s": t_s, "passes": passes, "achieved": achieved,
+                               "histories": passes * N, "plain_s_derived": passes * N / plain_rate},
+    }
+    c.close()
+    return out
+
+
+def dij_section(torch, capi, workloads, optimize) -> dict:
+    """C3 Dij (one batched pass) and C5: 100 projected-gradient iterations, FD check on 64 spots."""
+    wl = workloads.c3()
+    dev = torch.device("cuda:0")
+    c = capi.Context(0)
+    c.set_physics(False)
+    cid = c.add_child(*wl.edges())
+    c.set_hu(cid, wl.hu)
+    sid = c.add_dij_scorer(cid, capacity=1 << 31)
+    N = c.set_spot_plan(wl.spots)
+    t_tr, _ = _cuda_time(torch, lambda: c.transport_plan(0, N, 7))
+    t_bd, op = _cuda_time(torch, lambda: c.dij_build(sid, scale=1.0))
+    target, organ, _ = workloads.c5_structures(wl)
+    tgt = torch.from_numpy(target).to(dev)
+    org = torch.from_numpy(organ).to(dev)
+    d1 = op.matvec(torch.ones(op.n_spots, device=dev, dtype=torch.float64))
+    op = c.dij_build(sid, scale=2.0 / float(d1[tgt].mean()))    # w = 1: 2 Gy mean target dose
+    obj = optimize.make_objective(torch, tgt, org)
+    lip = optimize.lipschitz(op, tgt, org)
+    t_opt, (w, hist) = _cuda_time(
+        torch, lambda: optimize.projected_gradient(op, obj, torch.ones(op.n_spots, device=dev), 100, lip=lip))
+    spots = np.random.default_rng(8).choice(op.n_spots, 64, replace=False)
+    rel32, _, fd = optimize.fd_check(op, obj, w, spots, dtype=torch.float32)
+    rel64, _, _ = optimize.fd_check(op, obj, w, spots, dtype=torch.float64)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    times = {}
+    for name, fn, arg in (("forward", op.matvec, w), ("backward", op.rmatvec, torch.rand(op.n_voxels, device=dev))):
+        fn(arg)
+        ev0.record()
+        for _ in range(10):
+            fn(arg)
+        ev1.record()
+        torch.cuda.synchronize()
+        times[name] = ev0.elapsed_time(ev1) / 10
+    vr = c.dij_info(sid)["voxel_rows"]
+    fwd_bytes = op.nnz * 8 + vr * 12 + op.n_voxels * 8
+    bwd_bytes = op.nnz * 12 + op.n_spots * 16
+    hbm = measured_peaks()["hbm_gbs"]
+    out = {
+        "workload": "c3 Dij + c5 objective", "histories": N, "nnz": op.nnz, "voxel_rows": vr,
+        "transport_primaries_per_s": N / t_tr, "build_s": t_bd,
+        "forward_ms": times["forward"], "backward_ms": times["backward"],
+        "forward_frac_hbm": fwd_bytes / (times["forward"] / 1e3) / 1e9 / hbm,
+        "backward_frac_hbm": bwd_bytes / (times["backward"] / 1e3) / 1e9 / hbm,
+        "optimisation": {"iterations": 100, "ms_per_iteration": t_opt * 10, "objective_first": float(hist[0]),
+                         "objective_last": float(hist[-1])},
+        "fd_check": {"spots": 64, "h": 1e-3, "nonzero": int((np.abs(fd) > 0).sum()),
+                     "max_rel_err_fp32_grad": float(rel32.max()), "max_rel_err_fp64_grad": float(rel64.max())},
+    }
+    c.close()
+    return out
+
+
+def robust_section(torch, capi, workloads, args) -> dict:
+    """C4 sample: 21 scenarios x every 20th spot of the plan in one queue drain."""
+    wl = workloads.c3()
+    scen = workloads.c4_scenarios()
+    sub = wl.spots[::args.robust_stride].copy()
+    c = capi.Context(0)
+    c.set_physics(False)
+    cid = c.add_child(*wl.edges())
+    c.set_density(cid, c.hu_to_density(wl.hu.ravel()))
+    c.add_scorer(cid, capi.DOSE_W)
+    d1, d2 = c.add_stat_scorers(cid)
+    es = [workloads.scenario_edges(wl, sh) for sh, _ in scen]
+    c.set_scenarios(cid, [e[0] for e in es], [e[1] for e in es], [e[2] for e in es], [k for _, k in scen])
+    N = c.set_spot_plan(sub)
+    c.transport_plan(0, min(N, 50_000), 1)
+    c.reset()
+    t, _ = _cuda_time(torch, lambda: c.transport_plan(0, N, 2))
+    est, _ = c.stat_uncertainty(d1, d2, N, 0.5)
+    c.close()
+    return {"scenarios": len(scen), "spots": len(sub), "histories": N, "instances": N * len(scen),
+            "instance_primaries_per_s": N * len(scen) / t, "seconds": t, "worst_scenario_estimate": est,
+            "sample": f"every {args.robust_stride}th spot of the c3 plan"}
+
+
+# ------------------------------------------------------------------------------------------
 # GPU arm
 # ------------------------------------------------------------------------------------------
 
@@ -308,6 +452,16 @@ def run_gpu(args, wl):
             "transport": {"steps_per_primary": steps / (N * args.steps), "tracks": s1["tracks"] - s0["tracks"],
                           "waves": s1["waves"] - s0["waves"], "host_wall_s": t_wall1 - t_wall0},
         }
+        if not args.no_plan:
+            from moquimc_gb300 import optimize, workloads
+
+            for key, fn in (("plan", lambda: plan_section(torch, capi, workloads, args)),
+                            ("robust", lambda: robust_section(torch, capi, workloads, args)),
+                            ("dij", lambda: dij_section(torch, capi, workloads, optimize))):
+                try:
+                    line[key] = fn()
+                except Exception as exc:  # noqa: BLE001  (a failed section is reported, not hidden)
+                    line[key] = {"error": f"{type(exc).__name__}: {exc}"}
         print(json.dumps(line), flush=True)
     ctx.close()
     if ws > 1:
@@ -325,6 +479,10 @@ def main():
     ap.add_argument("--histories", type=int, default=0)
     ap.add_argument("--ref-histories", type=int, default=3000, help="histories per CPU process per sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-plan", action="store_true", help="skip the plan, robust and Dij sections")
+    ap.add_argument("--plain-stride", type=int, default=10, help="time every n-th spot for the plain per-spot rate")
+    ap.add_argument("--robust-stride", type=int, default=20, help="spots of the plan in the robust sample")
+    ap.add_argument("--max-passes", type=int, default=30, help="plan passes allowed for the 1%% criterion")
     args = ap.parse_args()
     from moquimc_gb300 import workloads
 
