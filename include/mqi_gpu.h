@@ -311,6 +311,14 @@ int mqi_run_until_stat(mqi_ctx* ctx, int dose_id, int dose2_id, uint64_t histori
  * when < 0.  Results do not depend on any of these. */
 int mqi_set_tuning(mqi_ctx* ctx, int block, int blocks_per_sm, int slice_steps, int primary_chunk);
 
+/* How the queue is driven (no counterpart in moqui, which runs one kernel over all histories).
+ * streamed = 1 (default): before every wave the queue is topped up on the device with the next
+ * histories, and graph_waves waves are captured once into a CUDA graph, so the host synchronises
+ * once per graph_waves waves; streamed = 0: queue generations -- load primary_chunk histories,
+ * run waves until a generation is empty, one host synchronisation per wave.  graph_waves must be
+ * even (default 8); values <= 0 / < 0 keep the current setting.  Results do not depend on it. */
+int mqi_set_launch_mode(mqi_ctx* ctx, int streamed, int graph_waves);
+
 /* Transport without any device allocation, for callers that cannot call cudaMalloc once running
  * (device memory owned by a pre-sized pool or another framework's allocator, plug-in hosts that
  * forbid allocation after start-up, loops that cannot afford cudaMalloc's device synchronisation).

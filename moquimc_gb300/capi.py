@@ -38,7 +38,7 @@ EXPORTS = (
     "mqi_add_stat_scorers", "mqi_stat_uncertainty", "mqi_batch_accumulate", "mqi_batch_uncertainty",
     "mqi_get_batch_mean", "mqi_scale_tally", "mqi_run_until_stat", "mqi_set_spot_plan", "mqi_transport_plan",
     "mqi_sample_plan", "mqi_add_dij_scorer", "mqi_dij_build", "mqi_dij_get_csr", "mqi_dij_info",
-    "mqi_dij_matvec", "mqi_dij_rmatvec", "mqi_set_scenarios", "mqi_run_plan_until_stat",
+    "mqi_dij_matvec", "mqi_dij_rmatvec", "mqi_set_scenarios", "mqi_run_plan_until_stat", "mqi_set_launch_mode",
 )
 
 VERTEX_DTYPE = np.dtype([("ke", "<f4"), ("pos", "<f4", (3,)), ("dir", "<f4", (3,))])
@@ -120,6 +120,7 @@ def load(path: Optional[str] = None) -> C.CDLL:
         "mqi_dij_matvec": (i32, [vp, i32, vp, vp, i32, i32]),
         "mqi_dij_rmatvec": (i32, [vp, i32, vp, vp, i32, i32]),
         "mqi_set_scenarios": (i32, [vp, i32, u32, vp, vp, vp, vp]),
+        "mqi_set_launch_mode": (i32, [vp, i32, i32]),
         "mqi_run_plan_until_stat": (i32, [vp, i32, i32, f32, f32, u64, u64, P(u64), P(C.c_double)]),
     }
     for name, (res, args) in sig.items():
@@ -175,6 +176,9 @@ class Context:
 
     def set_tuning(self, block: int = 0, blocks_per_sm: int = 0, slice_steps: int = -1, primary_chunk: int = 0) -> None:
         self._check(self.lib.mqi_set_tuning(self.h, block, blocks_per_sm, slice_steps, primary_chunk), self.h)
+
+    def set_launch_mode(self, streamed: int = -1, graph_waves: int = 0) -> None:
+        self._check(self.lib.mqi_set_launch_mode(self.h, streamed, graph_waves), self.h)
 
     def set_stream(self, stream_ptr: Optional[int]) -> None:
         """Run the context's work on a cudaStream_t handle (1 = the legacy default stream;

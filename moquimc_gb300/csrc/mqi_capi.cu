@@ -117,6 +117,9 @@ mqi_create(int device, mqi_ctx** out) {
         (e = cudaMalloc(&c->stats, 8 * sizeof(unsigned long long))) != cudaSuccess ||
         (e = cudaMemset(c->stats, 0, 8 * sizeof(unsigned long long))) != cudaSuccess ||
         (e = cudaMallocHost(&c->host_counts, 8 * sizeof(uint32_t))) != cudaSuccess ||
+        (e = cudaMallocHost(&c->host_next, sizeof(unsigned long long))) != cudaSuccess ||
+        (e = cudaMalloc(&c->topup, sizeof(TopUp))) != cudaSuccess ||
+        (e = cudaStreamCreateWithFlags(&c->cap_stream, cudaStreamNonBlocking)) != cudaSuccess ||
         (e = cudaEventCreate(&c->ev0)) != cudaSuccess || (e = cudaEventCreate(&c->ev1)) != cudaSuccess) {
         mqi_destroy(c);
         return cuda_fail(nullptr, e, "mqi_create: allocation");
@@ -151,6 +154,9 @@ mqi_destroy(mqi_ctx* c) {
     cudaFree(c->stats);
     cudaFree(c->tables);
     if (c->host_counts) cudaFreeHost(c->host_counts);
+    if (c->host_next) cudaFreeHost(c->host_next);
+    cudaFree(c->topup);
+    if (c->cap_stream) cudaStreamDestroy(c->cap_stream);
     if (c->ev0) cudaEventDestroy(c->ev0);
     if (c->ev1) cudaEventDestroy(c->ev1);
     if (c->own_stream && c->stream) cudaStreamDestroy(c->stream);
@@ -193,6 +199,18 @@ mqi_set_tuning(mqi_ctx* c, int block, int blocks_per_sm, int slice_steps, int pr
         if (primary_chunk > (1 << 24)) return fail(c, MQI_ERR_INVALID, "mqi_set_tuning: primary_chunk must be <= 2^24");
         c->primary_chunk = (uint32_t) primary_chunk;
     }
+    return MQI_OK;
+}
+
+int
+mqi_set_launch_mode(mqi_ctx* c, int streamed, int graph_waves) {
+    if (!valid_ctx(c)) return fail(c, MQI_ERR_INVALID, "mqi_set_launch_mode: ctx is NULL");
+    if (graph_waves > 0) {
+        if (graph_waves % 2 != 0 || graph_waves > 64)
+            return fail(c, MQI_ERR_INVALID, "mqi_set_launch_mode: graph_waves must be even and <= 64");
+        c->graph_waves = graph_waves;
+    }
+    if (streamed >= 0) c->streamed = streamed ? 1 : 0;
     return MQI_OK;
 }
 
@@ -394,23 +412,11 @@ namespace
 /// The source stream of a plan history is keyed apart from its transport streams.
 constexpr uint32_t kSourceKeyXor = 0xA5A5A5A5u;
 
-/// The queue-drain loop shared by vertex and plan sources: load (or sample) a chunk of primaries,
-/// run waves until a generation is empty, repeat.
-int
-run_transport(mqi_ctx* c, uint64_t h0, uint64_t h1, uint64_t seed, bool plan) {
-    DeviceGuard g(c->device);
-    const uint32_t chunk = c->primary_chunk;
-    const uint32_t need  = chunk * 3u;
-    if (c->queue_cap < need) {
-        cudaError_t e = alloc_queue(c->qa, need);
-        if (e == cudaSuccess) e = alloc_queue(c->qb, need);
-        if (e != cudaSuccess) {
-            c->queue_cap = 0;
-            return cuda_fail(c, e, "mqi_transport: queue allocation");
-        }
-        c->queue_cap = need;
-    }
-    WaveParams P{};
+/// Kernel parameters of a transport run: children, scorers (with the double-scoring quirk),
+/// physics options, seed, scenarios.
+void
+make_wave_params(mqi_ctx* c, uint64_t seed, WaveParams& P) {
+    P = WaveParams{};
     P.n_children = (int) c->children.size();
     for (int i = 0; i < P.n_children; ++i) {
         const ChildHost& h = c->children[i];
@@ -470,7 +476,13 @@ run_transport(mqi_ctx* c, uint64_t h0, uint64_t h1, uint64_t seed, bool plan) {
         P.scen_edges  = c->scen_edges;
         for (uint32_t k = 0; k < c->n_scen; ++k) P.scen_scale[k] = c->scen_scale[k];
     }
-    MQI_CUDA(c, cudaMemsetAsync(c->counters + 3, 0, sizeof(uint32_t), c->stream), "mqi_transport");
+}
+
+/// Queue generations (moqui's order of work, one host synchronisation per wave): load (or sample) a
+/// chunk of primaries, run waves until a generation is empty, repeat.
+int
+run_generations(mqi_ctx* c, WaveParams P, uint64_t h0, uint64_t h1, bool plan) {
+    const uint32_t chunk = c->primary_chunk;
     QueueBuf* A = &c->qa;
     QueueBuf* B = &c->qb;
     const uint32_t S       = c->n_scen;
@@ -514,6 +526,108 @@ run_transport(mqi_ctx* c, uint64_t h0, uint64_t h1, uint64_t seed, bool plan) {
             cur = 1 - cur;
         }
     }
+    return MQI_OK;
+}
+
+/// Streamed transport: before every wave the queue is topped up on the device with the next
+/// histories, so waves never run with the GPU half empty while the long tracks of a generation
+/// finish; `graph_waves` waves (top-up, load, wave) are captured once into a CUDA graph, and the
+/// host synchronises once per graph launch.  The work done does not depend on how it is split
+/// into waves (every random number is keyed by history and track).
+int
+run_streamed(mqi_ctx* c, WaveParams P, uint64_t h0, uint64_t h1, bool plan) {
+    const int      K = c->graph_waves;
+    const uint32_t S = c->n_scen;
+    TopUp tu{};
+    tu.next   = h0;
+    tu.end    = h1;
+    tu.target = std::max<uint32_t>(c->primary_chunk / S, 1u) * S;
+    tu.n_scen = S;
+    MQI_CUDA(c, cudaMemcpyAsync(c->topup, &tu, sizeof(tu), cudaMemcpyHostToDevice, c->stream), "mqi_transport");
+    MQI_CUDA(c, cudaMemsetAsync(c->counters, 0, 2 * sizeof(uint32_t), c->stream), "mqi_transport");
+    MQI_CUDA(c, cudaStreamSynchronize(c->stream), "mqi_transport");
+
+    cudaStream_t cs = c->cap_stream;
+    cudaGraph_t  graph = nullptr;
+    cudaError_t  e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed);
+    for (int i = 0; e == cudaSuccess && i < K; ++i) {
+        const int in  = i & 1;
+        QueueBuf& Qin = in ? c->qb : c->qa;
+        QueueBuf& Qo  = in ? c->qa : c->qb;
+        e = launch_topup(c->topup, c->counters + in, cs);
+        if (e == cudaSuccess)
+            e = plan ? launch_sample_topup(Qin.q, c->topup, c->plan_spots, c->plan_cum, c->n_plan_spots, P.k0,
+                                           P.k1 ^ kSourceKeyXor, c->num_sms, cs)
+                     : launch_load_topup(Qin.q, c->topup, c->vertices, c->has_spots ? c->spot_ids : nullptr, c->num_sms,
+                                         cs);
+        if (e == cudaSuccess) e = cudaMemsetAsync(c->counters + (1 - in), 0, sizeof(uint32_t), cs);
+        if (e == cudaSuccess) e = cudaMemsetAsync(c->counters + 2, 0, sizeof(uint32_t), cs);
+        P.in    = Qin.q;
+        P.out   = Qo.q;
+        P.n_in  = c->counters + in;
+        P.n_out = c->counters + (1 - in);
+        if (e == cudaSuccess) e = launch_wave(P, c->wave_grid, c->wave_block, c->wave_grid / c->num_sms, cs);
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c->host_counts, c->counters, 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost, cs);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c->host_next, &c->topup->next, sizeof(unsigned long long),
+                                              cudaMemcpyDeviceToHost, cs);
+    const cudaError_t e_end = cudaStreamEndCapture(cs, &graph);
+    if (e == cudaSuccess) e = e_end;
+    cudaGraphExec_t exec = nullptr;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+    if (graph) cudaGraphDestroy(graph);
+    if (e != cudaSuccess) {
+        if (exec) cudaGraphExecDestroy(exec);
+        return cuda_fail(c, e, "mqi_transport: graph capture");
+    }
+    int rc = MQI_OK;
+    for (uint64_t launch = 0;; ++launch) {
+        if (launch * (uint64_t) K > 200000) {
+            rc = fail(c, MQI_ERR_DEVICE, "mqi_transport: wave limit reached");
+            break;
+        }
+        e = cudaEventRecord(c->ev0, c->stream);
+        if (e == cudaSuccess) e = cudaGraphLaunch(exec, c->stream);
+        if (e == cudaSuccess) e = cudaEventRecord(c->ev1, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) {
+            rc = cuda_fail(c, e, "mqi_transport: graph launch");
+            break;
+        }
+        c->waves += K;
+        c->wave_launches += K;
+        c->kernel_launches += 3 * (uint64_t) K;
+        float ms = 0.0f;
+        if (cudaEventElapsedTime(&ms, c->ev0, c->ev1) == cudaSuccess) c->wave_ms += ms;
+        if (c->host_counts[3] & 2u) {
+            rc = fail(c, MQI_ERR_OVERFLOW, "mqi_transport: particle queue overflow");
+            break;
+        }
+        if (*c->host_next >= h1 && c->host_counts[0] == 0) break;
+    }
+    cudaGraphExecDestroy(exec);
+    return rc;
+}
+
+/// Transport histories [h0, h1) from the vertices or the spot plan.
+int
+run_transport(mqi_ctx* c, uint64_t h0, uint64_t h1, uint64_t seed, bool plan) {
+    DeviceGuard g(c->device);
+    const uint32_t need = c->primary_chunk * 3u;
+    if (c->queue_cap < need) {
+        cudaError_t e = alloc_queue(c->qa, need);
+        if (e == cudaSuccess) e = alloc_queue(c->qb, need);
+        if (e != cudaSuccess) {
+            c->queue_cap = 0;
+            return cuda_fail(c, e, "mqi_transport: queue allocation");
+        }
+        c->queue_cap = need;
+    }
+    WaveParams P;
+    make_wave_params(c, seed, P);
+    MQI_CUDA(c, cudaMemsetAsync(c->counters + 3, 0, sizeof(uint32_t), c->stream), "mqi_transport");
+    const int rc = c->streamed ? run_streamed(c, P, h0, h1, plan) : run_generations(c, P, h0, h1, plan);
+    if (rc != MQI_OK) return rc;
     if (c->host_counts[3] & 4u)
         return fail(c, MQI_ERR_OVERFLOW, "mqi_transport: a Dij table is full (raise its capacity)");
     if (c->host_counts[3] & 1u) return fail(c, MQI_ERR_DEVICE, "mqi_transport: a bounded device loop gave up");

@@ -139,6 +139,11 @@ struct mqi_ctx {
     uint32_t                n_plan_spots = 0;
     uint64_t                plan_histories = 0;
     std::vector<uint64_t>   plan_cum_host;
+    int                     streamed = 1;             // 1: device top-up + graph-captured waves; 0: generations
+    int                     graph_waves = 8;          // waves per captured graph (even)
+    mqi_gpu::TopUp*         topup = nullptr;          // device: streamed-transport state
+    unsigned long long*     host_next = nullptr;      // pinned: TopUp::next after a graph launch
+    cudaStream_t            cap_stream = nullptr;     // stream the graphs are captured on
     uint32_t                n_scen = 1;               // robust scenarios (1: none)
     int                     scen_child = -1;
     int                     scen_stride = 0;

@@ -113,6 +113,18 @@ struct WaveParams {
 
 std::string& thread_error_slot();
 
+/// Device state of a streamed transport: before every wave the queue is topped up to `target`
+/// entries with the next histories, so the GPU stays full until the last histories drain.
+struct TopUp {
+    unsigned long long next;   // next history to load
+    unsigned long long end;    // one past the last history
+    unsigned long long base;   // first history of the current top-up
+    uint32_t target;           // queue entries a wave should start with
+    uint32_t n_scen;           // queue entries per history (robust scenarios)
+    uint32_t count;            // entries appended by the current top-up
+    uint32_t dst;              // first appended entry
+};
+
 /// Record the calling thread's last error message (returned by mqi_last_error(NULL)).
 void set_thread_error(const char* msg);
 
@@ -152,6 +164,13 @@ cudaError_t launch_sample_primaries(const Queue& q, const mqi_spot* spots, const
                                     uint64_t h0, uint32_t n, uint32_t n_scen, uint32_t k0, uint32_t k1, cudaStream_t s);
 cudaError_t launch_sample_vertices(mqi_vertex* out, uint32_t* spot_out, const mqi_spot* spots, const uint64_t* cum,
                                    uint32_t n_spots, uint64_t h0, uint32_t n, uint32_t k0, uint32_t k1, cudaStream_t s);
+// Streamed loaders: k_topup sizes the top-up of the queue whose count is *n_in (one thread), the
+// loaders then append tu->count entries at tu->dst.
+cudaError_t launch_topup(TopUp* tu, uint32_t* n_in, cudaStream_t s);
+cudaError_t launch_load_topup(const Queue& q, const TopUp* tu, const mqi_vertex* v, const uint32_t* spot_ids, int sms,
+                              cudaStream_t s);
+cudaError_t launch_sample_topup(const Queue& q, const TopUp* tu, const mqi_spot* spots, const uint64_t* cum,
+                                uint32_t n_spots, uint32_t k0, uint32_t k1, int sms, cudaStream_t s);
 cudaError_t launch_wave(const WaveParams& p, int grid, int block, int blocks_per_sm, cudaStream_t s);
 int         wave_smem_bytes(const WaveParams& p);
 int         wave_edge_floats(const ChildDev* c, int n);

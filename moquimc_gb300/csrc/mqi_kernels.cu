@@ -946,14 +946,10 @@ namespace mqi_gpu
 // Primaries: vertex_t<float> AoS (mqi_vertex.hpp:16-29) -> queue entries
 // (track_t::set + push_primary, mqi_track.hpp:124-133, mqi_track_stack.hpp:44-48).
 // ------------------------------------------------------------------------------------------
-__global__ void
-k_load_primaries(Queue q, const mqi_vertex* __restrict__ v, const uint32_t* __restrict__ spot_ids, uint64_t h0,
-                 uint32_t n, uint32_t n_scen) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n * n_scen) return;
-    const uint32_t   scen = i % n_scen;
-    const uint64_t   h    = h0 + i / n_scen;
-    const mqi_vertex x    = v[h];
+__device__ inline void
+write_vertex_entry(const Queue& q, uint32_t i, const mqi_vertex* __restrict__ v, const uint32_t* __restrict__ spot_ids,
+                   uint64_t h, uint32_t scen) {
+    const mqi_vertex x = v[h];
     q.ke[i]     = x.ke;
     q.px[i]     = x.pos[0];
     q.py[i]     = x.pos[1];
@@ -969,6 +965,37 @@ k_load_primaries(Queue q, const mqi_vertex* __restrict__ v, const uint32_t* __re
     q.meta[i]   = kMetaPrimary;
     q.cell[i]   = 0;
     q.spot[i]   = ((spot_ids ? spot_ids[h] : kNoSpot) & kSpotMask) | (scen << kScenShift);
+}
+
+__global__ void
+k_load_primaries(Queue q, const mqi_vertex* __restrict__ v, const uint32_t* __restrict__ spot_ids, uint64_t h0,
+                 uint32_t n, uint32_t n_scen) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n * n_scen) return;
+    write_vertex_entry(q, i, v, spot_ids, h0 + i / n_scen, i % n_scen);
+}
+
+/// One thread: size the top-up of the queue holding *n_in entries (what the previous wave left).
+__global__ void
+k_topup(TopUp* tu, uint32_t* n_in) {
+    const uint32_t have = *n_in;
+    uint64_t       want = have < tu->target ? (tu->target - have) / tu->n_scen : 0ull;
+    const uint64_t left = tu->end - tu->next;
+    if (want > left) want = left;
+    tu->base  = tu->next;
+    tu->dst   = have;
+    tu->count = (uint32_t) (want * tu->n_scen);
+    tu->next += want;
+    *n_in = have + tu->count;
+}
+
+__global__ void
+k_load_topup(Queue q, const TopUp* __restrict__ tu, const mqi_vertex* __restrict__ v,
+             const uint32_t* __restrict__ spot_ids) {
+    const uint32_t n = tu->count, S = tu->n_scen, dst = tu->dst;
+    const uint64_t base = tu->base;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        write_vertex_entry(q, dst + i, v, spot_ids, base + i / S, i % S);
 }
 
 cudaError_t
@@ -1202,13 +1229,9 @@ sample_spot_vertex(const mqi_spot* __restrict__ spots, const uint64_t* __restric
     return lo;
 }
 
-__global__ void
-k_sample_primaries(Queue q, const mqi_spot* __restrict__ spots, const uint64_t* __restrict__ cum, uint32_t n_spots,
-                   uint64_t h0, uint32_t n, uint32_t n_scen, uint32_t k0, uint32_t k1) {
-    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n * n_scen) return;
-    const uint32_t scen = i % n_scen;
-    const uint64_t h    = h0 + i / n_scen;
+__device__ inline void
+write_sampled_entry(const Queue& q, uint32_t i, const mqi_spot* __restrict__ spots, const uint64_t* __restrict__ cum,
+                    uint32_t n_spots, uint64_t h, uint32_t scen, uint32_t k0, uint32_t k1) {
     float3 p, d;
     float  ke;
     const uint32_t s = sample_spot_vertex(spots, cum, n_spots, h, k0, k1, p, d, ke);
@@ -1223,6 +1246,23 @@ k_sample_primaries(Queue q, const mqi_spot* __restrict__ spots, const uint64_t* 
     q.meta[i]   = kMetaPrimary;
     q.cell[i]   = 0;
     q.spot[i]   = (s & kSpotMask) | (scen << kScenShift);
+}
+
+__global__ void
+k_sample_primaries(Queue q, const mqi_spot* __restrict__ spots, const uint64_t* __restrict__ cum, uint32_t n_spots,
+                   uint64_t h0, uint32_t n, uint32_t n_scen, uint32_t k0, uint32_t k1) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n * n_scen) return;
+    write_sampled_entry(q, i, spots, cum, n_spots, h0 + i / n_scen, i % n_scen, k0, k1);
+}
+
+__global__ void
+k_sample_topup(Queue q, const TopUp* __restrict__ tu, const mqi_spot* __restrict__ spots,
+               const uint64_t* __restrict__ cum, uint32_t n_spots, uint32_t k0, uint32_t k1) {
+    const uint32_t n = tu->count, S = tu->n_scen, dst = tu->dst;
+    const uint64_t base = tu->base;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        write_sampled_entry(q, dst + i, spots, cum, n_spots, base + i / S, i % S, k0, k1);
 }
 
 __global__ void
@@ -1255,6 +1295,26 @@ launch_sample_vertices(mqi_vertex* out, uint32_t* spot_out, const mqi_spot* spot
                        uint64_t h0, uint32_t n, uint32_t k0, uint32_t k1, cudaStream_t s) {
     if (n == 0) return cudaSuccess;
     k_sample_vertices<<<(n + 127) / 128, 128, 0, s>>>(out, spot_out, spots, cum, n_spots, h0, n, k0, k1);
+    return cudaGetLastError();
+}
+
+cudaError_t
+launch_topup(TopUp* tu, uint32_t* n_in, cudaStream_t s) {
+    k_topup<<<1, 1, 0, s>>>(tu, n_in);
+    return cudaGetLastError();
+}
+
+cudaError_t
+launch_load_topup(const Queue& q, const TopUp* tu, const mqi_vertex* v, const uint32_t* spot_ids, int sms,
+                  cudaStream_t s) {
+    k_load_topup<<<sms * 8, 256, 0, s>>>(q, tu, v, spot_ids);
+    return cudaGetLastError();
+}
+
+cudaError_t
+launch_sample_topup(const Queue& q, const TopUp* tu, const mqi_spot* spots, const uint64_t* cum, uint32_t n_spots,
+                    uint32_t k0, uint32_t k1, int sms, cudaStream_t s) {
+    k_sample_topup<<<sms * 8, 128, 0, s>>>(q, tu, spots, cum, n_spots, k0, k1);
     return cudaGetLastError();
 }
 

@@ -151,3 +151,29 @@ def test_per_spot_calls_equal_one_batched_call(gpu_ctx_factory):
     a, b = res
     assert a[1:] == b[1:]
     np.testing.assert_allclose(a[0], b[0], rtol=1e-12, atol=1e-300)
+
+
+def test_streamed_graph_equals_generations(gpu_ctx_factory):
+    """The device top-up + graph-captured waves and the generation loop run the same tracks: equal
+    step counts and tallies equal up to FP64 summation order, for vertices and plans, and with
+    chunks smaller than the run so that the top-up interleaves new histories with daughters."""
+    wl = workloads.c2(histories=30_000)
+    sp = _plan([12_000, 8_000, 10_000])
+    v = wl.vertices(20_000, 4)
+    res = {}
+    for mode in ("generations", "streamed", "streamed2"):
+        c, cid = _ctx(wl, gpu_ctx_factory)
+        d = c.add_scorer(cid, capi.DOSE_W)
+        c.set_tuning(primary_chunk=4096)
+        c.set_launch_mode(0 if mode == "generations" else 1, 2 if mode == "streamed2" else 8)
+        N = c.set_spot_plan(sp)
+        c.transport_plan(0, N, 31)
+        c.set_vertices(v)
+        c.transport(0, len(v), 32)
+        st = c.stats()
+        res[mode] = (c.tally(d), st["steps"], st["histories"], st["secondaries"])
+    a = res["generations"]
+    for m in ("streamed", "streamed2"):
+        b = res[m]
+        assert a[1:] == b[1:]
+        np.testing.assert_allclose(a[0], b[0], rtol=1e-12, atol=1e-300)
