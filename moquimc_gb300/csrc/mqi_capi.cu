@@ -554,7 +554,7 @@ run_streamed(mqi_ctx* c, WaveParams P, uint64_t h0, uint64_t h1, bool plan) {
         const int in  = i & 1;
         QueueBuf& Qin = in ? c->qb : c->qa;
         QueueBuf& Qo  = in ? c->qa : c->qb;
-        e = launch_topup(c->topup, c->counters + in, cs);
+        e = launch_topup(c->topup, c->counters + in, c->counters + 3, cs);
         if (e == cudaSuccess)
             e = plan ? launch_sample_topup(Qin.q, c->topup, c->plan_spots, c->plan_cum, c->n_plan_spots, P.k0,
                                            P.k1 ^ kSourceKeyXor, c->num_sms, cs)

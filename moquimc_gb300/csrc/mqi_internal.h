@@ -166,7 +166,7 @@ cudaError_t launch_sample_vertices(mqi_vertex* out, uint32_t* spot_out, const mq
                                    uint32_t n_spots, uint64_t h0, uint32_t n, uint32_t k0, uint32_t k1, cudaStream_t s);
 // Streamed loaders: k_topup sizes the top-up of the queue whose count is *n_in (one thread), the
 // loaders then append tu->count entries at tu->dst.
-cudaError_t launch_topup(TopUp* tu, uint32_t* n_in, cudaStream_t s);
+cudaError_t launch_topup(TopUp* tu, uint32_t* n_in, const uint32_t* error_flag, cudaStream_t s);
 cudaError_t launch_load_topup(const Queue& q, const TopUp* tu, const mqi_vertex* v, const uint32_t* spot_ids, int sms,
                               cudaStream_t s);
 cudaError_t launch_sample_topup(const Queue& q, const TopUp* tu, const mqi_spot* spots, const uint64_t* cum,

@@ -812,7 +812,11 @@ wave_body(const WaveParams& P) {
     bool in_grid = false;
     uint32_t slice = 0;
     uint32_t track_steps = 0;   // per-track guard: a track is abandoned after kMaxTrackSteps
-    const uint32_t n_in = *P.n_in;
+    // The input count can exceed the queue's capacity only after an overflowed append (the
+    // append cursor counts on; nothing was written past the end).  The wave then does nothing:
+    // the host reports the overflow, and no entry past the capacity is ever read.
+    const uint32_t n_raw = *P.n_in;
+    const uint32_t n_in  = (n_raw > P.in.capacity || (*P.error_flag & 2u)) ? 0u : n_raw;
     const int lane = threadIdx.x & 31;
 
     for (;;) {
@@ -976,8 +980,15 @@ k_load_primaries(Queue q, const mqi_vertex* __restrict__ v, const uint32_t* __re
 }
 
 /// One thread: size the top-up of the queue holding *n_in entries (what the previous wave left).
+/// After a queue overflow (error bit 2) nothing more is loaded and the remaining waves of the
+/// graph find an empty queue.
 __global__ void
-k_topup(TopUp* tu, uint32_t* n_in) {
+k_topup(TopUp* tu, uint32_t* n_in, const uint32_t* error_flag) {
+    if (*error_flag & 2u) {
+        tu->count = 0;
+        *n_in     = 0;
+        return;
+    }
     const uint32_t have = *n_in;
     uint64_t       want = have < tu->target ? (tu->target - have) / tu->n_scen : 0ull;
     const uint64_t left = tu->end - tu->next;
@@ -1299,8 +1310,8 @@ launch_sample_vertices(mqi_vertex* out, uint32_t* spot_out, const mqi_spot* spot
 }
 
 cudaError_t
-launch_topup(TopUp* tu, uint32_t* n_in, cudaStream_t s) {
-    k_topup<<<1, 1, 0, s>>>(tu, n_in);
+launch_topup(TopUp* tu, uint32_t* n_in, const uint32_t* error_flag, cudaStream_t s) {
+    k_topup<<<1, 1, 0, s>>>(tu, n_in, error_flag);
     return cudaGetLastError();
 }
 
