@@ -81,3 +81,17 @@ def r80(idd: np.ndarray, dz: float) -> float:
     j = i + int(tail[0])
     frac = (idd[j - 1] - 0.8 * m) / (idd[j - 1] - idd[j])
     return float(((j - 1) + 0.5 + frac) * dz)
+
+
+def column_crop(dose: np.ndarray, lxyz, nxyz, x: float, y: float, half: int = 24, bins=(7, 7, 4)) -> np.ndarray:
+    """The (2 half + 1)^2-voxel column around the beam axis (x, y) of a grid centred at the origin,
+    summed in bins (bx, by, bz): shape (nz / bz, (2 half + 1) / by, (2 half + 1) / bx)."""
+    nx, ny, nz = nxyz
+    d = dose.reshape(nz, ny, nx)
+    ix = int((x + 0.5 * lxyz[0]) / (lxyz[0] / nx))
+    iy = int((y + 0.5 * lxyz[1]) / (lxyz[1] / ny))
+    w = 2 * half + 1
+    c = d[:, iy - half:iy + half + 1, ix - half:ix + half + 1]
+    bx, by, bz = bins
+    return c.reshape(nz // bz, bz, w // by, by, w // bx, bx).sum(axis=(1, 3, 5))
+

@@ -200,6 +200,14 @@ def ref_phantom_parallel(debug: bool, lxyz, pxyz, nxyz, energy, position, size, 
         procs.append(subprocess.Popen(cmd, stdout=log, stderr=subprocess.STDOUT))
         log.close()
     rcs = [q.wait() for q in procs]
+    # The reference CPU build has crashed with SIGSEGV, rarely and not reproducibly with the same
+    # seed when rerun alone; a process that dies by a signal is rerun once with the same seed.
+    for i, r in enumerate(rcs):
+        if r < 0:
+            cmd = ref_phantom_cmd(debug, lxyz, pxyz, nxyz, energy, position, size, histories_each, ph, dirs[i],
+                                  seed0 + i, beam)
+            with open(os.path.join(dirs[i], "log_retry.txt"), "w") as log:
+                rcs[i] = subprocess.run(cmd, stdout=log, stderr=subprocess.STDOUT).returncode
     if any(rcs):
         bad = [i for i, r in enumerate(rcs) if r]
         with open(os.path.join(dirs[bad[0]], "log.txt"), errors="replace") as f:

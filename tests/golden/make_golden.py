@@ -16,6 +16,10 @@ reference headers by oracle/build_oracle.py -- is run here to produce them:
                     12500 histories (1e5 in total).
 * ``dose_c2.npz``   the slab phantom (256^3, lung + bone, 150 MeV Gaussian sigma 4 mm, release
                     physics): the same statistics over 8 batches of 12500 histories.
+* ``dose_c3.npz``   three Gaussian spots (sigma 4 mm) of different energies and positions on the
+                    synthetic CT (512x512x200, 0.98x0.98x2 mm, release physics): per-batch
+                    laterally integrated depth dose and a coarse dose in a 49x49-voxel column around
+                    each spot, 8 batches of 12500 histories per spot.
 * ``vertices.npz``  phantom_env's host beam source (coordinate_transform + phsp_6d_uniform or
                     phsp_6d + const_1d, std::default_random_engine) for a few seeds, spot shapes and
                     gantry/couch angles: the vertices the C++ host driver must reproduce bit for bit.
@@ -133,6 +137,31 @@ def make_dose(wl, fname, batches=8, each=12500, seed0=31000, coarse_bins=(10, 10
     print(fname, "R80", r80, "per-core primaries/s", each / secs.mean())
 
 
+C3_SPOTS = [(0.0, 0.0, 150.0), (-40.0, 30.0, 200.0), (60.0, -20.0, 110.0)]   # x, y (mm), energy (MeV)
+C3_CROP = 24          # voxels either side of the spot's column
+C3_BINS = (7, 7, 4)   # coarse bins of the 49 x 49 x 200 crop
+
+
+def c3_crop(dose, wl, x, y):
+    """The 49 x 49 voxel column around the spot (x, y), binned 7 x 7 x 4: shape (50, 7, 7)."""
+    return ph.column_crop(dose, wl.lxyz, wl.nxyz, x, y, C3_CROP, C3_BINS)
+
+
+def make_dose_c3(batches=8, each=12500, seed0=51000):
+    wl = workloads.c3()
+    out = {"spots": np.array(C3_SPOTS), "histories_per_batch": np.int64(each), "bins": np.array(C3_BINS),
+           "crop": np.int64(C3_CROP)}
+    for k, (x, y, e) in enumerate(C3_SPOTS):
+        _, recs, doses = mqo.ref_phantom_parallel(False, wl.lxyz, wl.pxyz, wl.nxyz, e, (x, y, 195.0), (4.0, 4.0), each,
+                                                  batches, wl.hu, seed0 + 100 * k, beam="gaussian")
+        out[f"idd{k}"] = np.array([ph.depth_dose(d, wl.nxyz) for d in doses]) / each
+        out[f"coarse{k}"] = np.array([c3_crop(d, wl, x, y) for d in doses]) / each
+        out[f"seconds{k}"] = np.array([r["transport_seconds"] for r in recs])
+        print("c3 spot", k, "R80", ph.r80(out[f"idd{k}"].mean(0), 2.0), "per-core primaries/s",
+              each / out[f"seconds{k}"].mean(), flush=True)
+    np.savez_compressed(os.path.join(OUT, "dose_c3.npz"), **out)
+
+
 VERTEX_CASES = [
     # seed, gaussian, position, size, energy, angles (collimator, gantry, couch, iec2dicom)
     (1234, 0, (0.0, 0.0, 0.5), (30.0, 30.0), 200.0, (0.0, 0.0, 0.0, 0.0)),
@@ -161,7 +190,7 @@ def make_vertices(n=2000):
 def main():
     if not mqo.ref_available():
         raise SystemExit("the reference CPU build is not available")
-    which = sys.argv[1:] or ["raywalk", "physics", "dose_c1", "dose_c2", "vertices"]
+    which = sys.argv[1:] or ["raywalk", "physics", "dose_c1", "dose_c2", "dose_c3", "vertices"]
     if "raywalk" in which:
         make_raywalk()
     if "physics" in which:
@@ -170,6 +199,8 @@ def main():
         make_dose(workloads.c1(), "dose_c1.npz")
     if "dose_c2" in which:
         make_dose(workloads.c2(), "dose_c2.npz", seed0=41000, coarse_bins=(8, 8, 4))
+    if "dose_c3" in which:
+        make_dose_c3()
     if "vertices" in which:
         make_vertices()
 

@@ -281,3 +281,36 @@ def test_transport_before_setup_is_a_state_error(gpu_ctx_factory):
     with pytest.raises(capi.MqiError) as e:
         c.transport(0, 0, 1)
     assert e.value.code == -4
+
+
+def test_gpu_dose_matches_reference_on_the_synthetic_ct(golden, gpu_ctx_factory):
+    """Three Gaussian spots on the synthetic CT (heterogeneous HU field, 0.98 x 0.98 x 2 mm,
+    release physics) against the reference CPU build: depth dose and a coarse dose in the column
+    around each spot within 2% or 3 sigma in bins above 10% of the maximum, R80 within 0.2 mm."""
+    gd = golden("dose_c3.npz")
+    half, bins = int(gd["crop"]), tuple(int(b) for b in gd["bins"])
+    wl = workloads.c3()
+    each = int(gd["histories_per_batch"])
+    c = gpu_ctx_factory()
+    c.set_physics(False)
+    cid = c.add_child(*wl.edges())
+    c.set_hu(cid, wl.hu)
+    sid = c.add_scorer(cid, capi.DOSE_W)
+    for k, (x, y, e) in enumerate(gd["spots"]):
+        idd, crs = [], []
+        for b in range(8):
+            c.reset()
+            rng = np.random.default_rng(7000 + 10 * k + b)
+            c.set_vertices(ph.gaussian_spot_vertices(each, rng, float(e), (float(x), float(y), 195.0), (4.0, 4.0)))
+            c.transport(0, each, 99 + 10 * k + b)
+            d = c.tally(sid)
+            idd.append(ph.depth_dose(d, wl.nxyz) / each)
+            crs.append(ph.column_crop(d, wl.lxyz, wl.nxyz, float(x), float(y), half, bins) / each)
+        for mine, ref in ((np.array(idd), gd[f"idd{k}"]), (np.array(crs), gd[f"coarse{k}"])):
+            tm, ts = mine.mean(0), mine.std(0, ddof=1) / np.sqrt(len(mine))
+            rm, rs = ref.mean(0), ref.std(0, ddof=1) / np.sqrt(len(ref))
+            sel = rm > 0.1 * rm.max()
+            ok = (np.abs(tm - rm) <= 0.02 * rm) | (np.abs(tm - rm) <= 3 * np.sqrt(rs ** 2 + ts ** 2))
+            assert ok[sel].mean() >= 0.95, (k, ok[sel].mean())
+        tm, rm = np.array(idd).mean(0), gd[f"idd{k}"].mean(0)
+        assert abs(ph.r80(tm, 2.0) - ph.r80(rm, 2.0)) <= 0.2, (k, ph.r80(tm, 2.0), ph.r80(rm, 2.0))
