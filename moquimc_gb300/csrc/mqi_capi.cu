@@ -138,7 +138,8 @@ mqi_destroy(mqi_ctx* c) {
         cudaFree(ch.xe); cudaFree(ch.ye); cudaFree(ch.ze); cudaFree(ch.rho);
     }
     for (auto& s : c->scorers) {
-        cudaFree(s.start); cudaFree(s.stride); cudaFree(s.acc); cudaFree(s.tally);
+        cudaFree(s.start); cudaFree(s.stride); cudaFree(s.acc);
+        if (s.owns) cudaFree(s.tally);
         cudaFree(s.batch_s1); cudaFree(s.batch_s2);
         dij_release(s);
     }
@@ -435,7 +436,7 @@ make_wave_params(mqi_ctx* c, uint64_t seed, WaveParams& P) {
         ScorerDev&        d = P.scorer[i];
         d.type = s.type; d.roi_method = s.roi_method; d.stat_mode = s.stat_mode;
         d.roi_len = s.roi_len; d.start = s.start; d.stride = s.stride; d.acc = s.acc;
-        d.tally = s.tally; d.tally_len = s.tally_len;
+        d.tally = s.tally; d.tally_len = s.tally_len; d.tstride = s.tstride;
         d.dij = s.dij; d.dij_mask = s.dij_cap ? s.dij_cap - 1 : 0; d.dij_count = s.dij_count;
         if (s.dij) {
             c->scorers[i].csr.built = false;   // new entries invalidate a built matrix
@@ -719,12 +720,16 @@ mqi_set_scenarios(mqi_ctx* c, int child_id, uint32_t n, const float* xe, const f
         cudaFree(s.batch_s2);
         s.batch_s1 = s.batch_s2 = nullptr;
         s.n_batches = 0;
-        if (s.type == MQI_SCORER_DIJ) continue;
+        if (s.type == MQI_SCORER_DIJ || !s.owns) continue;
         cudaFree(s.tally);
         s.tally  = nullptr;
         s.copies = copies;
-        MQI_CUDA(c, cudaMalloc(&s.tally, s.total() * sizeof(double)), "mqi_set_scenarios");
-        MQI_CUDA(c, cudaMemset(s.tally, 0, s.total() * sizeof(double)), "mqi_set_scenarios");
+        MQI_CUDA(c, cudaMalloc(&s.tally, s.tstride * s.total() * sizeof(double)), "mqi_set_scenarios");
+        MQI_CUDA(c, cudaMemset(s.tally, 0, s.tstride * s.total() * sizeof(double)), "mqi_set_scenarios");
+        if (s.partner >= 0) {   // the stat pair's dose^2 half lives in the same buffer
+            c->scorers[s.partner].tally  = s.tally + 1;
+            c->scorers[s.partner].copies = copies;
+        }
     }
     cudaFree(c->scen_edges);
     c->scen_edges  = edges;
@@ -813,8 +818,21 @@ mqi_get_tally(mqi_ctx* c, int id, double* out, uint64_t* n_out, int on_device) {
     if (n_out) *n_out = s.total();
     if (!out) return MQI_OK;
     DeviceGuard g(c->device);
-    MQI_CUDA(c, cudaMemcpyAsync(out, s.tally, s.total() * sizeof(double), on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
-                                c->stream), "mqi_get_tally");
+    const size_t bytes = s.total() * sizeof(double);
+    if (s.tstride == 1) {
+        MQI_CUDA(c, cudaMemcpyAsync(out, s.tally, bytes, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                                    c->stream), "mqi_get_tally");
+    } else if (on_device) {
+        MQI_CUDA(c, launch_copy_strided(s.tally, s.tstride, out, s.total(), c->num_sms, c->stream), "mqi_get_tally");
+    } else {
+        double* tmp = nullptr;
+        MQI_CUDA(c, cudaMalloc(&tmp, bytes), "mqi_get_tally");
+        cudaError_t e = launch_copy_strided(s.tally, s.tstride, tmp, s.total(), c->num_sms, c->stream);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(out, tmp, bytes, cudaMemcpyDeviceToHost, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        cudaFree(tmp);
+        if (e != cudaSuccess) return cuda_fail(c, e, "mqi_get_tally");
+    }
     MQI_CUDA(c, cudaStreamSynchronize(c->stream), "mqi_get_tally");
     return MQI_OK;
 }
@@ -825,7 +843,8 @@ mqi_reset_tallies(mqi_ctx* c) {
     DeviceGuard g(c->device);
     for (auto& s : c->scorers) {
         if (s.type == MQI_SCORER_DIJ) MQI_CUDA(c, dij_reset(s, c->num_sms, c->stream), "mqi_reset_tallies");
-        else MQI_CUDA(c, cudaMemsetAsync(s.tally, 0, s.total() * sizeof(double), c->stream), "mqi_reset_tallies");
+        else if (s.owns)
+            MQI_CUDA(c, cudaMemsetAsync(s.tally, 0, s.tstride * s.total() * sizeof(double), c->stream), "mqi_reset_tallies");
     }
     MQI_CUDA(c, cudaMemsetAsync(c->stats, 0, 8 * sizeof(unsigned long long), c->stream), "mqi_reset_tallies");
     MQI_CUDA(c, cudaMemsetAsync(c->counters + 3, 0, sizeof(uint32_t), c->stream), "mqi_reset_tallies");
@@ -1012,11 +1031,20 @@ mqi_add_stat_scorers(mqi_ctx* c, int child_id, int roi_method, uint32_t roi_leng
             MQI_CUDA(c, cudaMemcpy(s.acc, roi_acc, roi_length * sizeof(uint32_t), cudaMemcpyHostToDevice), "mqi_add_stat_scorers");
         }
         s.copies = c->n_scen;
-        MQI_CUDA(c, cudaMalloc(&s.tally, s.total() * sizeof(double)), "mqi_add_stat_scorers");
-        MQI_CUDA(c, cudaMemset(s.tally, 0, s.total() * sizeof(double)), "mqi_add_stat_scorers");
+        s.tstride = 2;
+        if (k == 0) {
+            // dose and dose^2 of a voxel side by side: the two per-step updates hit one 16-byte slot
+            MQI_CUDA(c, cudaMalloc(&s.tally, 2 * s.total() * sizeof(double)), "mqi_add_stat_scorers");
+            MQI_CUDA(c, cudaMemset(s.tally, 0, 2 * s.total() * sizeof(double)), "mqi_add_stat_scorers");
+        } else {
+            s.tally = c->scorers[ids[0]].tally + 1;
+            s.owns  = false;
+        }
         c->scorers.push_back(s);
         ids[k] = (int) c->scorers.size() - 1;
     }
+    c->scorers[ids[0]].partner = ids[1];
+    c->scorers[ids[1]].partner = ids[0];
     if (dose_id) *dose_id = ids[0];
     if (dose2_id) *dose2_id = ids[1];
     return MQI_OK;
@@ -1030,7 +1058,8 @@ mqi_stat_uncertainty(mqi_ctx* c, int dose_id, int dose2_id, uint64_t n_histories
         return fail(c, MQI_ERR_INVALID, "mqi_stat_uncertainty: no such scorer");
     const ScorerHost& a = c->scorers[dose_id];
     const ScorerHost& b = c->scorers[dose2_id];
-    if (a.tally_len != b.tally_len) return fail(c, MQI_ERR_INVALID, "mqi_stat_uncertainty: tallies differ in size");
+    if (a.tally_len != b.tally_len || a.tstride != b.tstride)
+        return fail(c, MQI_ERR_INVALID, "mqi_stat_uncertainty: tallies differ in layout");
     if (n_histories < 2) return fail(c, MQI_ERR_INVALID, "mqi_stat_uncertainty: needs at least 2 histories");
     DeviceGuard g(c->device);
     if (ensure_stat_scratch(c) != MQI_OK) return MQI_ERR_NOMEM;
@@ -1038,8 +1067,9 @@ mqi_stat_uncertainty(mqi_ctx* c, int dose_id, int dose2_id, uint64_t n_histories
     double   worst = -1.0;
     uint64_t worst_n = 0;
     for (uint32_t k = 0; k < a.copies; ++k) {
-        MQI_CUDA(c, launch_stat(a.tally + k * a.tally_len, b.tally + k * b.tally_len, a.tally_len, (double) n_histories, 0,
-                                threshold, c->num_sms, c->stat_scratch, c->stream), "mqi_stat_uncertainty");
+        MQI_CUDA(c, launch_stat(a.tally + k * a.tally_len * a.tstride, b.tally + k * b.tally_len * b.tstride, a.tally_len,
+                                a.tstride, (double) n_histories, 0, threshold, c->num_sms, c->stat_scratch, c->stream),
+                 "mqi_stat_uncertainty");
         double   v = 0.0;
         uint64_t nv = 0;
         const int rc = read_stat(c, &v, &nv);
@@ -1064,7 +1094,8 @@ mqi_batch_accumulate(mqi_ctx* c, int scorer_id) {
         MQI_CUDA(c, cudaMemsetAsync(s.batch_s2, 0, s.total() * sizeof(double), c->stream), "mqi_batch_accumulate");
         s.n_batches = 0;
     }
-    MQI_CUDA(c, launch_batch_fold(s.tally, s.batch_s1, s.batch_s2, s.total(), c->num_sms, c->stream), "mqi_batch_accumulate");
+    MQI_CUDA(c, launch_batch_fold(s.tally, s.tstride, s.batch_s1, s.batch_s2, s.total(), c->num_sms, c->stream),
+             "mqi_batch_accumulate");
     MQI_CUDA(c, cudaStreamSynchronize(c->stream), "mqi_batch_accumulate");
     ++s.n_batches;
     return MQI_OK;
@@ -1083,7 +1114,7 @@ mqi_batch_uncertainty(mqi_ctx* c, int scorer_id, float threshold, double* mean_r
     double   worst = -1.0;
     uint64_t worst_n = 0;
     for (uint32_t k = 0; k < s.copies; ++k) {
-        MQI_CUDA(c, launch_stat(s.batch_s1 + k * s.tally_len, s.batch_s2 + k * s.tally_len, s.tally_len,
+        MQI_CUDA(c, launch_stat(s.batch_s1 + k * s.tally_len, s.batch_s2 + k * s.tally_len, s.tally_len, 1,
                                 (double) s.n_batches, 1, threshold, c->num_sms, c->stat_scratch, c->stream),
                  "mqi_batch_uncertainty");
         double   v = 0.0;
@@ -1123,7 +1154,7 @@ mqi_scale_tally(mqi_ctx* c, int scorer_id, double weight) {
     if (scorer_id < 0 || scorer_id >= (int) c->scorers.size()) return fail(c, MQI_ERR_INVALID, "mqi_scale_tally: no such scorer");
     const ScorerHost& s = c->scorers[scorer_id];
     DeviceGuard g(c->device);
-    MQI_CUDA(c, launch_scale(s.tally, s.total(), weight, c->num_sms, c->stream), "mqi_scale_tally");
+    MQI_CUDA(c, launch_scale(s.tally, s.tstride, s.total(), weight, c->num_sms, c->stream), "mqi_scale_tally");
     MQI_CUDA(c, cudaStreamSynchronize(c->stream), "mqi_scale_tally");
     return MQI_OK;
 }

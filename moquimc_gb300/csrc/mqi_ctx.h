@@ -61,8 +61,11 @@ struct ScorerHost {
     uint32_t* stride = nullptr;
     uint32_t* acc = nullptr;
     double*   tally = nullptr;
-    uint64_t  tally_len = 0;       // per scenario; the tally holds copies * tally_len doubles
+    uint64_t  tally_len = 0;       // per scenario; the tally holds copies * tally_len values
     uint32_t  copies = 1;          // robust scenarios: one tally per scenario, scenario-major
+    uint32_t  tstride = 1;         // doubles between consecutive values (2: the interleaved stat pair)
+    int       partner = -1;        // the stat pair's other scorer (shares the buffer)
+    bool      owns = true;         // this scorer allocated `tally` (the dose half of the stat pair does)
     double*   batch_s1 = nullptr;   // batch estimator: running sums of batch tallies and squares
     double*   batch_s2 = nullptr;
     uint64_t  n_batches = 0;
@@ -71,7 +74,7 @@ struct ScorerHost {
     unsigned long long* dij_count = nullptr;
     DijCsr    csr;
 
-    uint64_t total() const { return tally_len * copies; }
+    uint64_t total() const { return tally_len * copies; }   // values (not doubles: see tstride)
 };
 
 struct QueueBuf {

@@ -41,8 +41,9 @@ struct ScorerDev {
     const uint32_t* start;
     const uint32_t* stride;
     const uint32_t* acc;
-    double*         tally;         // dense, length = tally_len
+    double*         tally;         // dense: value of key k in scenario c at tally[(c * tally_len + k) * tstride]
     uint64_t        tally_len;
+    uint32_t        tstride;       // 1, or 2 for the interleaved statistics pair (dose, dose^2)
     DijSlot*        dij;           // MQI_SCORER_DIJ: open-addressing table of dij_mask + 1 slots
     uint64_t        dij_mask;
     unsigned long long* dij_count; // device: occupied slots
@@ -178,10 +179,12 @@ cudaError_t launch_hu_to_density(const float* corr, const int16_t* hu, float* rh
                                  cudaStream_t s);
 cudaError_t launch_trace_rays(const ChildDev& c, const float* rays, uint64_t n_rays, uint32_t max_steps,
                               uint64_t* cnb, float* dist, int32_t* cells, uint32_t* counts, cudaStream_t s);
-cudaError_t launch_stat(const double* s1, const double* s2, uint64_t n, double nh, int mode, float threshold, int sms,
+cudaError_t launch_stat(const double* s1, const double* s2, uint64_t n, uint32_t stride, double nh, int mode,
+                        float threshold, int sms,
                         unsigned long long* scratch, cudaStream_t s);
-cudaError_t launch_batch_fold(double* tally, double* s1, double* s2, uint64_t n, int sms, cudaStream_t s);
-cudaError_t launch_scale(double* a, uint64_t n, double w, int sms, cudaStream_t s);
+cudaError_t launch_batch_fold(double* tally, uint32_t stride, double* s1, double* s2, uint64_t n, int sms, cudaStream_t s);
+cudaError_t launch_scale(double* a, uint32_t stride, uint64_t n, double w, int sms, cudaStream_t s);
+cudaError_t launch_copy_strided(const double* a, uint32_t stride, double* out, uint64_t n, int sms, cudaStream_t s);
 cudaError_t launch_copy_scaled(const double* a, double* out, uint64_t n, double w, int sms, cudaStream_t s);
 cudaError_t launch_eval_physics(const float* tables, const float* e, uint64_t n, float* out, cudaStream_t s);
 

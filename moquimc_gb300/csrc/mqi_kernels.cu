@@ -99,29 +99,15 @@ voxel_rho(const Grid& g, uint32_t cnb) {
 // moqui/base/scorers/mqi_scorer_energy_deposit.hpp:12-177; insert_hashtable :68-111).
 // ------------------------------------------------------------------------------------------
 
-/// Add v to tally[key]; lanes of the warp that hit the same key are combined first so that
-/// one FP64 atomic is issued per distinct voxel.
+/// Add v to tally[key] with one FP64 atomic (a fire-and-forget reduction at L2).  Combining the
+/// lanes of a warp that hit the same voxel first (__match_any_sync, shuffles, one atomic per
+/// distinct voxel) was measured slower on every workload -- 5.7% on the slab phantom, 6.6% on the
+/// synthetic-CT plan, 15% with the statistics pair -- because lanes of a warp run different
+/// histories and rarely share a voxel, while the match costs issue slots in an issue-bound kernel.
+/// The Dij insertion keeps the aggregation: there it saves hash probes.
 __device__ inline void
-tally_add(double* tally, uint32_t key, double v, bool valid) {
-    // Lanes are grouped by the target address, not by the voxel alone: under independent thread
-    // scheduling lanes of one warp can reach this instruction from different iterations of the
-    // scorer loop (different tallies) with the same voxel index.
-    const unsigned           mask  = __activemask();
-    const unsigned long long k     = valid ? (unsigned long long) (tally + key) : 0ull;
-    const unsigned           peers = __match_any_sync(mask, k);
-    if (!valid) return;
-    if (__popc(peers) == 1) {
-        atomicAdd(&tally[key], v);
-        return;
-    }
-    double   s = 0.0;
-    unsigned m = peers;
-    while (m) {
-        const int src = __ffs(m) - 1;
-        s += __shfl_sync(peers, v, src);
-        m &= m - 1;
-    }
-    if ((int) (threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&tally[key], s);
+tally_add(double* tally, uint64_t slot, double v, bool valid) {
+    if (valid) atomicAdd(&tally[slot], v);
 }
 
 /// Hash of a Dij key: the splitmix64 finalizer (Steele, Lea & Flood, "Fast splittable
@@ -219,7 +205,7 @@ roi_mask_idx(const ScorerDev& s, uint32_t v) {
 
 /// fp_compute_hit for the enum'd scorers.
 __device__ inline double
-compute_hit(int type, const Trk& t, float rho, float vol, float spr_ke0) {
+compute_hit(int type, const Trk& t, float rho, float vol, float dose_w) {
     const float edep = t.dE + t.ldE;
     switch (type) {
     case MQI_SCORER_EDEP: return (double) edep;
@@ -229,13 +215,9 @@ compute_hit(int type, const Trk& t, float rho, float vol, float spr_ke0) {
     // it in double) and accumulated in FP64.  GB300's FP64 pipe is narrow, so the per-step
     // division stays in FP32.
     case MQI_SCORER_DOSE_W:
-    case MQI_SCORER_DIJ: {
-        if (rho < 1.0e-7f) return 0.0;
-        return (double) (edep * 1.60218e-10f / (vol * rho * spr_ke0));
-    }
+    case MQI_SCORER_DIJ: return (double) dose_w;
     case MQI_SCORER_DOSE_W2: {
-        if (rho < 1.0e-7f) return 0.0;
-        const double d = (double) (edep * 1.60218e-10f / (vol * rho * spr_ke0));
+        const double d = (double) dose_w;
         return d * d;
     }
     case MQI_SCORER_DOSE_M:
@@ -265,6 +247,9 @@ score_step(Ctx& C, const Trk& t, uint32_t cnb, float rho, float vol) {
     const WaveParams& P   = *C.P;
     const ChildDev&   ch  = P.child[C.child];
     const float       spr = t.spr0 >= 0.0f ? t.spr0 : spr_default(rho, t.ke0, C.dbg);
+    // dose_to_water of the step, shared by the dose, dose^2 and Dij scorers (Dw_pointer,
+    // mqi_scorer_energy_deposit.hpp:23-40): 0 in vacuum voxels
+    const float dose_w = (rho < 1.0e-7f) ? 0.0f : (t.dE + t.ldE) * 1.60218e-10f / (vol * rho * spr);
     for (int si = 0; si < ch.n_scorers; ++si) {
         const ScorerDev& s = P.scorer[ch.scorer_begin + si];
         bool     ok;
@@ -278,7 +263,7 @@ score_step(Ctx& C, const Trk& t, uint32_t cnb, float rho, float vol) {
             key = cnb;
         }
         double v = 0.0;
-        if (ok) v = compute_hit(s.type, t, rho, vol, spr);
+        if (ok) v = compute_hit(s.type, t, rho, vol, dose_w);
         if (kDij && s.type == MQI_SCORER_DIJ) {
             // insert_hashtable(data_, cnb, spot_ind, ...) (mqi_transport.hpp:204-225); a history
             // without a spot index lands in column 0
@@ -288,9 +273,8 @@ score_step(Ctx& C, const Trk& t, uint32_t cnb, float rho, float vol) {
             continue;
         }
         const bool valid = ok && v > 0.0 && key < s.tally_len;
-        double* tally = s.tally + (uint64_t) (C.spot >> kScenShift) * s.tally_len;   // scenario's tally
-        if (s.double_score) tally_add(tally, key, v + v, valid);
-        else tally_add(tally, key, v, valid);
+        const uint64_t slot = ((uint64_t) (C.spot >> kScenShift) * s.tally_len + key) * s.tstride;   // scenario's tally
+        tally_add(s.tally, slot, s.double_score ? v + v : v, valid);
     }
 }
 

@@ -165,6 +165,7 @@ mqi_transport_noalloc(int nx, int ny, int nz, const float* d_xe, const float* d_
     sc.roi_method = MQI_ROI_DIRECT;
     sc.tally      = d_tally;
     sc.tally_len  = (uint64_t) nx * ny * nz;
+    sc.tstride    = 1;
     P.physics_debug    = physics_debug ? 1 : 0;
     P.score_local      = 1;
     P.stack_limit      = physics_debug ? 200 : 10;

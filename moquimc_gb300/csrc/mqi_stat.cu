@@ -58,15 +58,15 @@ batch_mean_rel(double s1, double s2, double B, double& mean, double& rel) {
 }
 
 __global__ void
-k_stat_max(const double* __restrict__ s1, const double* __restrict__ s2, uint64_t n, double nh, int mode,
-           unsigned long long* out_max) {
+k_stat_max(const double* __restrict__ s1, const double* __restrict__ s2, uint64_t n, uint32_t stride, double nh,
+           int mode, unsigned long long* out_max) {
     double m = 0.0;
     for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n; i += (uint64_t) gridDim.x * blockDim.x) {
-        const double a = s1[i];
+        const double a = s1[i * stride];
         if (a > 0.0) {
             if (mode == 0) {
                 float mean, sigma;
-                ref_mean_sigma(a, s2[i], nh, mean, sigma);
+                ref_mean_sigma(a, s2[i * stride], nh, mean, sigma);
                 m = fmax(m, (double) mean);
             } else {
                 m = fmax(m, a / nh);
@@ -78,24 +78,25 @@ k_stat_max(const double* __restrict__ s1, const double* __restrict__ s2, uint64_
 }
 
 __global__ void
-k_stat_sum(const double* __restrict__ s1, const double* __restrict__ s2, uint64_t n, double nh, int mode,
-           const unsigned long long* max_bits, float threshold, double* out_sum, unsigned long long* out_count) {
+k_stat_sum(const double* __restrict__ s1, const double* __restrict__ s2, uint64_t n, uint32_t stride, double nh,
+           int mode, const unsigned long long* max_bits, float threshold, double* out_sum,
+           unsigned long long* out_count) {
     const double cut = __longlong_as_double((long long) *max_bits) * (double) threshold;
     double       acc = 0.0;
     unsigned long long cnt = 0;
     for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n; i += (uint64_t) gridDim.x * blockDim.x) {
-        const double a = s1[i];
+        const double a = s1[i * stride];
         if (!(a > 0.0)) continue;
         if (mode == 0) {
             float mean, sigma;
-            ref_mean_sigma(a, s2[i], nh, mean, sigma);
+            ref_mean_sigma(a, s2[i * stride], nh, mean, sigma);
             if ((double) mean > cut) {   // dose_mean[i] > dose_max * stat_threshold (mqi_tps_env.hpp:1418)
                 acc += (double) (sigma / mean);
                 ++cnt;
             }
         } else {
             double mean, rel;
-            batch_mean_rel(a, s2[i], nh, mean, rel);
+            batch_mean_rel(a, s2[i * stride], nh, mean, rel);
             if (mean > cut) {
                 acc += rel;
                 ++cnt;
@@ -111,21 +112,27 @@ k_stat_sum(const double* __restrict__ s1, const double* __restrict__ s2, uint64_
 }
 
 __global__ void
-k_batch_fold(double* __restrict__ tally, double* __restrict__ s1, double* __restrict__ s2, uint64_t n) {
+k_batch_fold(double* __restrict__ tally, uint32_t stride, double* __restrict__ s1, double* __restrict__ s2, uint64_t n) {
     for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n; i += (uint64_t) gridDim.x * blockDim.x) {
-        const double t = tally[i];
+        const double t = tally[i * stride];
         if (t != 0.0) {
             s1[i] += t;
             s2[i] += t * t;
-            tally[i] = 0.0;
+            tally[i * stride] = 0.0;
         }
     }
 }
 
 __global__ void
-k_scale(double* __restrict__ a, uint64_t n, double w) {
+k_scale(double* __restrict__ a, uint32_t stride, uint64_t n, double w) {
     for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n; i += (uint64_t) gridDim.x * blockDim.x)
-        a[i] *= w;
+        a[i * stride] *= w;
+}
+
+__global__ void
+k_copy_strided(const double* __restrict__ a, uint32_t stride, double* __restrict__ out, uint64_t n) {
+    for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n; i += (uint64_t) gridDim.x * blockDim.x)
+        out[i] = a[i * stride];
 }
 
 __global__ void
@@ -144,27 +151,33 @@ grid_for(uint64_t n, int sms) {
 }   // namespace
 
 cudaError_t
-launch_stat(const double* s1, const double* s2, uint64_t n, double nh, int mode, float threshold, int sms,
-            unsigned long long* scratch, cudaStream_t s) {
+launch_stat(const double* s1, const double* s2, uint64_t n, uint32_t stride, double nh, int mode, float threshold,
+            int sms, unsigned long long* scratch, cudaStream_t s) {
     // scratch: [0] max bits, [1] count, [2] sum (as double bits)
     cudaError_t e = cudaMemsetAsync(scratch, 0, 3 * sizeof(unsigned long long), s);
     if (e != cudaSuccess) return e;
     const unsigned g = grid_for(n, sms);
-    k_stat_max<<<g, 256, 0, s>>>(s1, s2, n, nh, mode, scratch);
-    k_stat_sum<<<g, 256, 0, s>>>(s1, s2, n, nh, mode, scratch, threshold, reinterpret_cast<double*>(scratch + 2),
+    k_stat_max<<<g, 256, 0, s>>>(s1, s2, n, stride, nh, mode, scratch);
+    k_stat_sum<<<g, 256, 0, s>>>(s1, s2, n, stride, nh, mode, scratch, threshold, reinterpret_cast<double*>(scratch + 2),
                                  scratch + 1);
     return cudaGetLastError();
 }
 
 cudaError_t
-launch_batch_fold(double* tally, double* s1, double* s2, uint64_t n, int sms, cudaStream_t s) {
-    k_batch_fold<<<grid_for(n, sms), 256, 0, s>>>(tally, s1, s2, n);
+launch_batch_fold(double* tally, uint32_t stride, double* s1, double* s2, uint64_t n, int sms, cudaStream_t s) {
+    k_batch_fold<<<grid_for(n, sms), 256, 0, s>>>(tally, stride, s1, s2, n);
     return cudaGetLastError();
 }
 
 cudaError_t
-launch_scale(double* a, uint64_t n, double w, int sms, cudaStream_t s) {
-    k_scale<<<grid_for(n, sms), 256, 0, s>>>(a, n, w);
+launch_scale(double* a, uint32_t stride, uint64_t n, double w, int sms, cudaStream_t s) {
+    k_scale<<<grid_for(n, sms), 256, 0, s>>>(a, stride, n, w);
+    return cudaGetLastError();
+}
+
+cudaError_t
+launch_copy_strided(const double* a, uint32_t stride, double* out, uint64_t n, int sms, cudaStream_t s) {
+    k_copy_strided<<<grid_for(n, sms), 256, 0, s>>>(a, stride, out, n);
     return cudaGetLastError();
 }
 
