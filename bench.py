@@ -261,6 +261,16 @@ def dij_section(torch, capi, workloads, optimize) -> dict:
     lip = optimize.lipschitz(op, tgt, org)
     t_opt, (w, hist) = _cuda_time(
         torch, lambda: optimize.projected_gradient(op, obj, torch.ones(op.n_spots, device=dev), 100, lip=lip))
+    # where an iteration's time goes: the forward product alone, then forward + objective + backward
+    w1 = torch.ones(op.n_spots, device=dev)
+    t_f, _ = _cuda_time(torch, lambda: [op.matvec(w1) for _ in range(10)])
+
+    def fwd_bwd():
+        for _ in range(10):
+            wv = w1.detach().requires_grad_(True)
+            obj(optimize.dijmod.dose(op, wv)).backward()
+
+    t_fb, _ = _cuda_time(torch, fwd_bwd)
     spots = np.random.default_rng(8).choice(op.n_spots, 64, replace=False)
     rel32, _, fd = optimize.fd_check(op, obj, w, spots, dtype=torch.float32)
     rel64, _, _ = optimize.fd_check(op, obj, w, spots, dtype=torch.float64)
@@ -285,7 +295,8 @@ def dij_section(torch, capi, workloads, optimize) -> dict:
         "forward_frac_hbm": fwd_bytes / (times["forward"] / 1e3) / 1e9 / hbm,
         "backward_frac_hbm": bwd_bytes / (times["backward"] / 1e3) / 1e9 / hbm,
         "optimisation": {"iterations": 100, "ms_per_iteration": t_opt * 10, "objective_first": float(hist[0]),
-                         "objective_last": float(hist[-1])},
+                         "objective_last": float(hist[-1]), "forward_call_ms": t_f * 100,
+                         "forward_objective_backward_ms": t_fb * 100},
         "fd_check": {"spots": 64, "h": 1e-3, "nonzero": int((np.abs(fd) > 0).sum()),
                      "max_rel_err_fp32_grad": float(rel32.max()), "max_rel_err_fp64_grad": float(rel64.max())},
     }

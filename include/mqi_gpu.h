@@ -319,6 +319,25 @@ int mqi_set_tuning(mqi_ctx* ctx, int block, int blocks_per_sm, int slice_steps, 
  * even (default 8); values <= 0 / < 0 keep the current setting.  Results do not depend on it. */
 int mqi_set_launch_mode(mqi_ctx* ctx, int streamed, int graph_waves);
 
+/* One candidate of mqi_autotune and its measured rate. */
+typedef struct {
+    int      block;            /* threads per block of the wave kernel */
+    int      blocks_per_sm;    /* resident blocks per SM it is launched with */
+    int      streamed;         /* launch mode (mqi_set_launch_mode) */
+    int      graph_waves;
+    uint32_t primary_chunk;    /* queue entries a wave starts with / histories per generation */
+    double   histories_per_s;  /* measured on the sample */
+} mqi_tune_result;
+
+/* Tuner (no counterpart in moqui): transport the sample [h0, h1) of the current source (vertices,
+ * or the spot plan when source_plan = 1) once per candidate launch shape, queue size and launch
+ * mode, into scratch tallies (the caller's tallies and counters are kept), and keep the fastest
+ * candidate as the context's setting.  Up to max_results measurements go to `results`;
+ * n_results receives the number of candidates run.  Results of later runs do not depend on the
+ * choice.  Not with a Dij scorer present (add it after tuning). */
+int mqi_autotune(mqi_ctx* ctx, int source_plan, uint64_t h0, uint64_t h1, uint64_t seed,
+                 mqi_tune_result* results, uint32_t max_results, uint32_t* n_results);
+
 /* Transport without any device allocation, for callers that cannot call cudaMalloc once running
  * (device memory owned by a pre-sized pool or another framework's allocator, plug-in hosts that
  * forbid allocation after start-up, loops that cannot afford cudaMalloc's device synchronisation).

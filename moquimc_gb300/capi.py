@@ -39,9 +39,13 @@ EXPORTS = (
     "mqi_get_batch_mean", "mqi_scale_tally", "mqi_run_until_stat", "mqi_set_spot_plan", "mqi_transport_plan",
     "mqi_sample_plan", "mqi_add_dij_scorer", "mqi_dij_build", "mqi_dij_get_csr", "mqi_dij_info",
     "mqi_dij_matvec", "mqi_dij_rmatvec", "mqi_set_scenarios", "mqi_run_plan_until_stat", "mqi_set_launch_mode",
+    "mqi_autotune",
 )
 
 VERTEX_DTYPE = np.dtype([("ke", "<f4"), ("pos", "<f4", (3,)), ("dir", "<f4", (3,))])
+# mqi_tune_result (include/mqi_gpu.h)
+TUNE_DTYPE = np.dtype([("block", "<i4"), ("blocks_per_sm", "<i4"), ("streamed", "<i4"), ("graph_waves", "<i4"),
+                       ("primary_chunk", "<u4"), ("pad", "<u4"), ("histories_per_s", "<f8")])
 # mqi_spot (include/mqi_gpu.h): 26 floats, then the 64-bit history count at byte 104
 SPOT_DTYPE = np.dtype({"names": ["energy", "energy_sigma", "mean", "sigma", "corr", "rot", "trans", "histories"],
                        "formats": ["<f4", "<f4", ("<f4", (5,)), ("<f4", (5,)), ("<f4", (2,)), ("<f4", (9,)),
@@ -121,6 +125,7 @@ def load(path: Optional[str] = None) -> C.CDLL:
         "mqi_dij_rmatvec": (i32, [vp, i32, vp, vp, i32, i32]),
         "mqi_set_scenarios": (i32, [vp, i32, u32, vp, vp, vp, vp]),
         "mqi_set_launch_mode": (i32, [vp, i32, i32]),
+        "mqi_autotune": (i32, [vp, i32, u64, u64, u64, vp, u32, P(u32)]),
         "mqi_run_plan_until_stat": (i32, [vp, i32, i32, f32, f32, u64, u64, P(u64), P(C.c_double)]),
     }
     for name, (res, args) in sig.items():
@@ -176,6 +181,14 @@ class Context:
 
     def set_tuning(self, block: int = 0, blocks_per_sm: int = 0, slice_steps: int = -1, primary_chunk: int = 0) -> None:
         self._check(self.lib.mqi_set_tuning(self.h, block, blocks_per_sm, slice_steps, primary_chunk), self.h)
+
+    def autotune(self, h0: int, h1: int, seed: int = 1, plan: bool = False) -> np.ndarray:
+        """Time every candidate launch configuration on histories [h0, h1) and keep the fastest;
+        returns the measurements (TUNE_DTYPE)."""
+        res = np.zeros(64, TUNE_DTYPE)
+        n = C.c_uint32(0)
+        self._check(self.lib.mqi_autotune(self.h, int(plan), h0, h1, seed, _ptr(res), len(res), C.byref(n)), self.h)
+        return res[: n.value]
 
     def set_launch_mode(self, streamed: int = -1, graph_waves: int = 0) -> None:
         self._check(self.lib.mqi_set_launch_mode(self.h, streamed, graph_waves), self.h)

@@ -5,6 +5,7 @@
 // `new` (mqi_upload_data.hpp:69-142).  Here a context owns flat device buffers, and every kernel
 // receives what it reads by value.
 #include <algorithm>
+#include <chrono>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -781,6 +782,101 @@ mqi_transport_plan(mqi_ctx* c, uint64_t h0, uint64_t h1, uint64_t seed) {
     if (h1 < h0 || h1 > c->plan_histories) return fail(c, MQI_ERR_INVALID, "mqi_transport_plan: history range outside the plan");
     if (h0 == h1) return MQI_OK;
     return run_transport(c, h0, h1, seed, true);
+}
+
+int
+mqi_autotune(mqi_ctx* c, int source_plan, uint64_t h0, uint64_t h1, uint64_t seed, mqi_tune_result* results,
+             uint32_t max_results, uint32_t* n_results) {
+    const int rc0 = check_ready(c, "mqi_autotune");
+    if (rc0 != MQI_OK) return rc0;
+    if (source_plan ? (!c->plan_spots || h1 > c->plan_histories) : (h1 > c->n_vertices))
+        return fail(c, MQI_ERR_INVALID, "mqi_autotune: sample range outside the source");
+    if (h1 <= h0) return fail(c, MQI_ERR_INVALID, "mqi_autotune: empty sample");
+    for (auto& s : c->scorers)
+        if (s.type == MQI_SCORER_DIJ) return fail(c, MQI_ERR_STATE, "mqi_autotune: tune before adding a Dij scorer");
+    DeviceGuard g(c->device);
+    // The sample is transported into scratch tallies: the caller's tallies and counters are kept.
+    std::vector<double*> saved(c->scorers.size(), nullptr);
+    std::vector<double*> scratch(c->scorers.size(), nullptr);
+    unsigned long long   stats_saved[8];
+    MQI_CUDA(c, cudaMemcpy(stats_saved, c->stats, sizeof(stats_saved), cudaMemcpyDeviceToHost), "mqi_autotune");
+    const uint64_t waves0 = c->waves, kl0 = c->kernel_launches, wl0 = c->wave_launches;
+    const double   wms0   = c->wave_ms;
+    const int blk0 = c->wave_block, grid0 = c->wave_grid, str0 = c->streamed, gw0 = c->graph_waves;
+    const uint32_t chunk0 = c->primary_chunk;
+    int rc = MQI_OK;
+    for (size_t i = 0; i < c->scorers.size() && rc == MQI_OK; ++i) {
+        ScorerHost& s = c->scorers[i];
+        if (!s.owns) continue;
+        const size_t bytes = s.tstride * s.total() * sizeof(double);
+        cudaError_t e = cudaMalloc(&scratch[i], bytes);
+        if (e == cudaSuccess) e = cudaMemset(scratch[i], 0, bytes);
+        if (e != cudaSuccess) rc = cuda_fail(c, e, "mqi_autotune: scratch tallies");
+    }
+    auto swap_tallies = [&]() {
+        for (size_t i = 0; i < c->scorers.size(); ++i) {
+            ScorerHost& s = c->scorers[i];
+            if (!s.owns) continue;
+            std::swap(s.tally, scratch[i]);
+            if (s.partner >= 0) c->scorers[s.partner].tally = s.tally + 1;
+        }
+    };
+    struct Cand { int block, bps, streamed, graph_waves; uint32_t chunk; };
+    std::vector<Cand> cands;
+    for (int streamed : { 1, 0 })
+        for (uint32_t chunk : { 1u << 19, 1u << 20, 1u << 21 })
+            for (auto shape : { std::make_pair(128, 5), std::make_pair(128, 4), std::make_pair(128, 6), std::make_pair(256, 2) })
+                cands.push_back({ shape.first, shape.second, streamed, 8, chunk });
+    uint32_t n = 0;
+    int best = -1;
+    double best_rate = 0.0;
+    if (rc == MQI_OK) {
+        swap_tallies();
+        for (size_t k = 0; k < cands.size() && rc == MQI_OK; ++k) {
+            const Cand& q = cands[k];
+            c->wave_block = q.block;
+            c->wave_grid = c->num_sms * q.bps;
+            c->streamed = q.streamed;
+            c->graph_waves = q.graph_waves;
+            c->primary_chunk = q.chunk;
+            MQI_CUDA(c, cudaStreamSynchronize(c->stream), "mqi_autotune");
+            const auto t0 = std::chrono::steady_clock::now();
+            rc = run_transport(c, h0, h1, seed, source_plan != 0);
+            MQI_CUDA(c, cudaStreamSynchronize(c->stream), "mqi_autotune");
+            const double sec = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+            if (rc != MQI_OK) break;
+            const double rate = (double) (h1 - h0) / sec;
+            if (results && n < max_results) {
+                results[n].block = q.block;
+                results[n].blocks_per_sm = q.bps;
+                results[n].streamed = q.streamed;
+                results[n].graph_waves = q.graph_waves;
+                results[n].primary_chunk = q.chunk;
+                results[n].histories_per_s = rate;
+            }
+            ++n;
+            if (rate > best_rate) {
+                best_rate = rate;
+                best = (int) k;
+            }
+        }
+        swap_tallies();
+    }
+    for (double* p : scratch) cudaFree(p);
+    cudaMemcpy(c->stats, stats_saved, sizeof(stats_saved), cudaMemcpyHostToDevice);
+    c->waves = waves0; c->kernel_launches = kl0; c->wave_launches = wl0; c->wave_ms = wms0;
+    if (rc != MQI_OK || best < 0) {
+        c->wave_block = blk0; c->wave_grid = grid0; c->streamed = str0; c->graph_waves = gw0; c->primary_chunk = chunk0;
+        return rc != MQI_OK ? rc : fail(c, MQI_ERR_DEVICE, "mqi_autotune: no candidate ran");
+    }
+    const Cand& q = cands[best];
+    c->wave_block = q.block;
+    c->wave_grid = c->num_sms * q.bps;
+    c->streamed = q.streamed;
+    c->graph_waves = q.graph_waves;
+    c->primary_chunk = q.chunk;
+    if (n_results) *n_results = n;
+    return MQI_OK;
 }
 
 int

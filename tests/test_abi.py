@@ -76,7 +76,8 @@ def test_struct_layouts_match_the_header(tmp_path):
         "int main(void) {\n"
         " O(mqi_spot, energy); O(mqi_spot, energy_sigma); O(mqi_spot, mean); O(mqi_spot, sigma);\n"
         " O(mqi_spot, corr); O(mqi_spot, rot); O(mqi_spot, trans); O(mqi_spot, histories);\n"
-        " printf(\"%zu %zu\\n\", sizeof(mqi_spot), sizeof(mqi_vertex));\n return 0;\n}\n")
+        " printf(\"%zu %zu \", sizeof(mqi_spot), sizeof(mqi_vertex));\n"
+        " printf(\"%zu %zu\\n\", offsetof(mqi_tune_result, histories_per_s), sizeof(mqi_tune_result));\n return 0;\n}\n")
     exe = tmp_path / "layout"
     subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
     got = [int(x) for x in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()]
@@ -84,4 +85,5 @@ def test_struct_layouts_match_the_header(tmp_path):
     assert got[:8] == [d.fields[n][1] for n in d.names]
     assert got[8] == d.itemsize
     assert got[9] == capi.VERTEX_DTYPE.itemsize == 28
+    assert got[10] == capi.TUNE_DTYPE.fields["histories_per_s"][1] and got[11] == capi.TUNE_DTYPE.itemsize
     assert np.dtype(capi.SPOT_DTYPE).names[-1] == "histories"

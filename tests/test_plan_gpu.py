@@ -177,3 +177,23 @@ def test_streamed_graph_equals_generations(gpu_ctx_factory):
         b = res[m]
         assert a[1:] == b[1:]
         np.testing.assert_allclose(a[0], b[0], rtol=1e-12, atol=1e-300)
+
+
+def test_autotune_keeps_tallies_and_picks_a_candidate(gpu_ctx_factory):
+    wl = workloads.c2(histories=20_000)
+    c, cid = _ctx(wl, gpu_ctx_factory)
+    d = c.add_scorer(cid, capi.DOSE_W)
+    c.set_vertices(wl.vertices(20_000, 8))
+    c.transport(0, 5_000, 3)
+    before, st = c.tally(d), c.stats()
+    res = c.autotune(0, 20_000, 9)
+    assert len(res) == 24 and (res["histories_per_s"] > 0).all()
+    np.testing.assert_array_equal(c.tally(d), before)
+    assert c.stats() == st
+    # the chosen setting runs the same tracks as the default one
+    c.transport(5_000, 10_000, 3)
+    e, eid = _ctx(wl, gpu_ctx_factory)
+    f = e.add_scorer(eid, capi.DOSE_W)
+    e.set_vertices(wl.vertices(20_000, 8))
+    e.transport(0, 10_000, 3)
+    np.testing.assert_allclose(c.tally(d), e.tally(f), rtol=1e-12, atol=1e-300)
