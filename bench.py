@@ -259,6 +259,9 @@ def dij_section(torch, capi, workloads, optimize) -> dict:
     op = c.dij_build(sid, scale=2.0 / float(d1[tgt].mean()))    # w = 1: 2 Gy mean target dose
     obj = optimize.make_objective(torch, tgt, org)
     lip = optimize.lipschitz(op, tgt, org)
+    # warm-up: the first autograd pass of a process loads (and on a new architecture JIT-compiles)
+    # torch's own kernels for the objective, which took ~10 s once on the box
+    optimize.projected_gradient(op, obj, torch.ones(op.n_spots, device=dev), 3, lip=lip)
     t_opt, (w, hist) = _cuda_time(
         torch, lambda: optimize.projected_gradient(op, obj, torch.ones(op.n_spots, device=dev), 100, lip=lip))
     # where an iteration's time goes: the forward product alone, then forward + objective + backward
