@@ -43,10 +43,9 @@ BYTES_PER_STEP_DOSE = 4 + 16   # density read + one FP64 tally read-modify-write
 
 
 def dist_env():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return ws, rank, local
+    from moquimc_gb300 import replicas
+
+    return replicas.world()
 
 
 class ClockSampler:
@@ -355,7 +354,10 @@ def run_gpu(args, wl):
     cid = ctx.add_child(xe, ye, ze)
     ctx.set_hu(cid, wl.hu)
     sid = ctx.add_scorer(cid, capi.DOSE_W)
-    verts = wl.vertices(N, 3 + 1000 * rank)
+    from moquimc_gb300 import replicas
+
+    vseed, seed_base = replicas.replica_seeds(rank)
+    verts = wl.vertices(N, vseed)
     d_verts = torch.from_numpy(verts.view(np.uint8)).to(f"cuda:{local}")
     torch.cuda.synchronize()
     ctx.set_vertices_ptr(d_verts.data_ptr(), N, on_device=True)
@@ -364,7 +366,9 @@ def run_gpu(args, wl):
         if ws > 1:
             torch.distributed.barrier()
 
-    seed_base = 0x5EED0000 + 7919 * rank
+    # the tuner picks the launch shape, queue size and launch mode on a sample of the workload
+    # (into scratch tallies); results do not depend on the choice
+    tune = ctx.autotune(0, min(N, args.tune_histories), seed_base + 7) if args.tune_histories > 0 else None
     for w in range(args.warmup):
         ctx.transport(0, N, seed_base + w)
     ctx.reset()
@@ -387,10 +391,7 @@ def run_gpu(args, wl):
     clk = clocks.stop()
     ms = ev0.elapsed_time(ev1)
     s1 = ctx.stats()
-    ms_t = torch.tensor([ms], device=f"cuda:{local}")
-    if ws > 1:
-        torch.distributed.all_reduce(ms_t, op=torch.distributed.ReduceOp.MAX)
-    ms_max = float(ms_t.item())
+    ms_max = replicas.max_over_ranks(ms, device=f"cuda:{local}")
     value = N * args.steps * ws / (ms_max / 1e3)
 
     steps = s1["steps"] - s0["steps"]
@@ -429,15 +430,11 @@ def run_gpu(args, wl):
     torch.cuda.synchronize()
     barrier()
     e2e_ms = e0.elapsed_time(e1)
-    e_t = torch.tensor([e2e_ms], device=f"cuda:{local}")
-    if ws > 1:
-        torch.distributed.all_reduce(e_t, op=torch.distributed.ReduceOp.MAX)
-    e2e_value = N * args.steps * ws / (float(e_t.item()) / 1e3)
+    e2e_value = N * args.steps * ws / (replicas.max_over_ranks(e2e_ms, device=f"cuda:{local}") / 1e3)
 
     # ---- the replicas' dose volumes are summed once at the end (the path's only exchange step)
     if ws > 1:
-        dose = torch.from_numpy(ctx.tally(sid)).to(f"cuda:{local}")
-        torch.distributed.all_reduce(dose)
+        replicas.sum_tallies(ctx.tally(sid), device=f"cuda:{local}")
 
     line = None
     if rank == 0:
@@ -466,6 +463,12 @@ def run_gpu(args, wl):
             "transport": {"steps_per_primary": steps / (N * args.steps), "tracks": s1["tracks"] - s0["tracks"],
                           "waves": s1["waves"] - s0["waves"], "host_wall_s": t_wall1 - t_wall0},
         }
+        if tune is not None:
+            best = tune[np.argmax(tune["histories_per_s"])]
+            line["tuning"] = {"sample_histories": min(N, args.tune_histories), "candidates": len(tune),
+                              "chosen": {"block": int(best["block"]), "blocks_per_sm": int(best["blocks_per_sm"]),
+                                         "streamed": int(best["streamed"]), "primary_chunk": int(best["primary_chunk"])},
+                              "best_over_worst": float(tune["histories_per_s"].max() / tune["histories_per_s"].min())}
         if not args.no_plan:
             from moquimc_gb300 import optimize, workloads
 
@@ -497,6 +500,7 @@ def main():
     ap.add_argument("--plain-stride", type=int, default=10, help="time every n-th spot for the plain per-spot rate")
     ap.add_argument("--robust-stride", type=int, default=20, help="spots of the plan in the robust sample")
     ap.add_argument("--max-passes", type=int, default=30, help="plan passes allowed for the 1%% criterion")
+    ap.add_argument("--tune-histories", type=int, default=200_000, help="tuner sample (0: no tuning)")
     args = ap.parse_args()
     from moquimc_gb300 import workloads
 
