@@ -225,9 +225,10 @@ compute_hit(int type, const Trk& t, float rho, float vol, float dose_w) {
     default: break;
     }
     // LET scorers (mqi_scorer_energy_deposit.hpp:91-177)
+    // the step length as the reference forms it: float differences squared in float, summed in double
     const float  density = rho * 1000.0f;
-    const double lx = (double) (t.p1.x - t.p0.x), ly = (double) (t.p1.y - t.p0.y), lz = (double) (t.p1.z - t.p0.z);
-    const double length = sqrt(lx * lx + ly * ly + lz * lz);
+    const float  lx = t.p1.x - t.p0.x, ly = t.p1.y - t.p0.y, lz = t.p1.z - t.p0.z;
+    const double length = sqrt((double) (lx * lx) + (double) (ly * ly) + (double) (lz * lz));
     if (!(length > 0.0)) return 0.0;
     const double let = (double) t.dE / length / (double) density;
     switch (type) {

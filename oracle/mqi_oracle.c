@@ -617,14 +617,43 @@ static void stepping(env_t* E, trk_t* t, float rho, float d2b) {
     }
 }
 
-/* scorer callbacks (scorers/mqi_scorer_energy_deposit.hpp:12-77) */
+/* scorer callbacks (scorers/mqi_scorer_energy_deposit.hpp:12-177): 1 energy_deposit, 2 dose_to_water,
+ * 3 dose_to_water_square, 4 dose_to_medium, 5/6 LETd_weight1/2, 7/8 LETt_weight1/2,
+ * 9/10 energy_deposit_primary/secondary */
 static double hit(const mqo_config* cfg, const trk_t* t, float rho, float vol, int dbg) {
     float edep = t->dE + t->ldE;
-    if (cfg->scorer == 1) return (double) edep;
-    if (rho < 1.0e-7f) return 0.0;
-    {
-        double d = (double) (edep * 1.60218e-10f / (vol * rho * mqo_spr(rho, t->ke0, dbg)));
+    switch (cfg->scorer) {
+    case 1: return (double) edep;
+    case 9: return t->primary ? (double) t->dE : 0.0;
+    case 10: return t->primary ? 0.0 : (double) t->dE;
+    case 2:
+    case 3: {
+        double d;
+        if (rho < 1.0e-7f) return 0.0;
+        d = (double) (edep * 1.60218e-10f / (vol * rho * mqo_spr(rho, t->ke0, dbg)));
         return cfg->scorer == 3 ? d * d : d;
+    }
+    case 4: return t->primary ? (double) t->dE * 1.60218e-13 * 1000.0 / (double) (vol * rho) : 0.0;
+    default: break;
+    }
+    {
+        /* the LET weights: the step length from float differences squared in float, summed in double */
+        const float density = rho * 1000.0f;
+        const float dx = t->p1.x - t->p0.x, dy = t->p1.y - t->p0.y, dz = t->p1.z - t->p0.z;
+        double length = (double) (dx * dx);
+        double let;
+        length += (double) (dy * dy);
+        length += (double) (dz * dz);
+        length = sqrt(length);
+        if (length <= 0.0) return 0.0;
+        let = (double) t->dE / length / (double) density;
+        switch (cfg->scorer) {
+        case 5: return (let >= 25.0) ? 0.0 : (double) t->dE * let;
+        case 6: return (let >= 25.0) ? 0.0 : (double) t->dE;
+        case 7: return length * let;
+        case 8: return length;
+        default: return 0.0;
+        }
     }
 }
 
