@@ -441,8 +441,11 @@ make_wave_params(mqi_ctx* c, uint64_t seed, WaveParams& P) {
         d.dij = s.dij; d.dij_mask = s.dij_cap ? s.dij_cap - 1 : 0; d.dij_count = s.dij_count;
         if (s.dij) {
             c->scorers[i].csr.built = false;   // new entries invalidate a built matrix
-            P.has_dij = 1;
+            P.kernel_mode |= kModeDij;
         }
+        if (s.type == MQI_SCORER_DOSE_M || (s.type >= MQI_SCORER_LETD_NUM && s.type <= MQI_SCORER_LETT_DEN))
+            P.kernel_mode |= kModeFull;
+        if (s.roi_method != MQI_ROI_DIRECT) P.kernel_mode |= kModeRoi;
         ChildDev& ch = P.child[s.child];
         if (ch.n_scorers == 0) ch.scorer_begin = i;
         ++ch.n_scorers;

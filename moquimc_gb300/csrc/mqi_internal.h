@@ -30,6 +30,12 @@ struct alignas(16) DijSlot {
 
 constexpr uint32_t kDijMaxProbes = 4096;   // linear-probe bound before the table counts as full
 
+/// Wave-kernel instance modes: the scoring code an instance carries.
+constexpr int kModeDij  = 1;   // a Dij scorer
+constexpr int kModeFull = 2;   // dose_to_medium or LET scorers
+constexpr int kModeRoi  = 4;   // INDIRECT or CONTOUR ROI mappings
+constexpr int kModeAll  = kModeDij | kModeFull | kModeRoi;
+
 /// Flat device description of one scorer (scorer<R> + roi_t, mqi_scorer.hpp:39-79,
 /// mqi_roi.hpp:18-194).
 struct ScorerDev {
@@ -93,7 +99,7 @@ struct WaveParams {
     uint32_t  k0, k1;           // Philox key (run seed)
     uint32_t  max_slice_steps;  // 0 = run each track to completion
     int       inline_local;     // score deposit-only daughters at creation (single-child worlds)
-    int       has_dij;          // a Dij scorer is present (selects the kDij wave kernel)
+    int       kernel_mode;      // kModeDij | kModeFull | kModeRoi: the scoring code the run needs
     int       n_scen;           // robust scenarios (0 or 1: none)
     int       scen_child;       // the child the scenarios vary
     int       scen_stride;      // floats per scenario in scen_edges: nx+1 + ny+1 + nz+1

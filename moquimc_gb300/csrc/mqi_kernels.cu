@@ -203,12 +203,12 @@ roi_mask_idx(const ScorerDev& s, uint32_t v) {
     return (int32_t) v;
 }
 
-/// fp_compute_hit for the enum'd scorers.
+/// fp_compute_hit of the scorers that need nothing beyond the step's deposit and its
+/// dose_to_water (mqi_scorer_energy_deposit.hpp:12-77).
 __device__ inline double
-compute_hit(int type, const Trk& t, float rho, float vol, float dose_w) {
-    const float edep = t.dE + t.ldE;
+compute_hit_simple(int type, const Trk& t, float dose_w) {
     switch (type) {
-    case MQI_SCORER_EDEP: return (double) edep;
+    case MQI_SCORER_EDEP: return (double) (t.dE + t.ldE);
     case MQI_SCORER_EDEP_PRIMARY: return t.primary ? (double) t.dE : 0.0;
     case MQI_SCORER_EDEP_SECONDARY: return t.primary ? 0.0 : (double) t.dE;
     // dose_to_water in Gy per history: formed in FP32 (one rounding per step; the reference forms
@@ -220,10 +220,17 @@ compute_hit(int type, const Trk& t, float rho, float vol, float dose_w) {
         const double d = (double) dose_w;
         return d * d;
     }
-    case MQI_SCORER_DOSE_M:
-        return t.primary ? (double) t.dE * 1.60218e-13 * 1000.0 / (double) (vol * rho) : 0.0;
-    default: break;
+    default: return 0.0;
     }
+}
+
+/// fp_compute_hit for every enum'd scorer: the simple ones plus dose_to_medium and the LET weights
+/// (FP64 square root and divisions), compiled only into the kernel instance of runs that use them.
+__device__ inline double
+compute_hit(int type, const Trk& t, float rho, float vol, float dose_w) {
+    if (type == MQI_SCORER_DOSE_M)
+        return t.primary ? (double) t.dE * 1.60218e-13 * 1000.0 / (double) (vol * rho) : 0.0;
+    if (type < MQI_SCORER_LETD_NUM || type > MQI_SCORER_LETT_DEN) return compute_hit_simple(type, t, dose_w);
     // LET scorers (mqi_scorer_energy_deposit.hpp:91-177)
     // the step length as the reference forms it: float differences squared in float, summed in double
     const float  density = rho * 1000.0f;
@@ -240,11 +247,18 @@ compute_hit(int type, const Trk& t, float rho, float vol, float dose_w) {
     }
 }
 
-/// Score one step of track t in voxel cnb with every scorer of the current child.  kDij = false
-/// compiles the Dij insertion out (wave kernels of runs without a Dij scorer).
-template<bool kDij = true>
+/// Score one step of track t in voxel cnb with every scorer of the current child.  The kernel
+/// instance's mode (kModeDij | kModeFull | kModeRoi, WaveParams::kernel_mode) compiles in only
+/// the scoring code the run uses: the Dij insertion, the dose_to_medium and LET callbacks (FP64
+/// square root and divisions), the INDIRECT / CONTOUR ROI mappings.  Code that never runs still
+/// costs registers and instruction-cache space in the step loop: carrying all of it cost 30% of
+/// the slab-phantom throughput, the ROI mappings alone another 11%.
+template<int kMode = kModeAll>
 __device__ inline void
 score_step(Ctx& C, const Trk& t, uint32_t cnb, float rho, float vol) {
+    constexpr bool kDij  = (kMode & kModeDij) != 0;
+    constexpr bool kFull = (kMode & kModeFull) != 0;
+    constexpr bool kRoi  = (kMode & kModeRoi) != 0;
     const WaveParams& P   = *C.P;
     const ChildDev&   ch  = P.child[C.child];
     const float       spr = t.spr0 >= 0.0f ? t.spr0 : spr_default(rho, t.ke0, C.dbg);
@@ -254,17 +268,18 @@ score_step(Ctx& C, const Trk& t, uint32_t cnb, float rho, float vol) {
     for (int si = 0; si < ch.n_scorers; ++si) {
         const ScorerDev& s = P.scorer[ch.scorer_begin + si];
         bool     ok;
-        uint32_t key;
-        if (s.stat_mode) {
+        uint32_t key = cnb;
+        if (!kRoi) {
+            ok = s.stat_mode || cnb > 0;   // DIRECT: idx(cnb) = cnb > 0; get_mask_idx(cnb) = cnb
+        } else if (s.stat_mode) {
             const int32_t m = roi_mask_idx(s, cnb);
             ok              = m >= 0;
             key             = (uint32_t) m;
         } else {
-            ok  = roi_idx(s, cnb) > 0;
-            key = cnb;
+            ok = roi_idx(s, cnb) > 0;
         }
         double v = 0.0;
-        if (ok) v = compute_hit(s.type, t, rho, vol, dose_w);
+        if (ok) v = kFull ? compute_hit(s.type, t, rho, vol, dose_w) : compute_hit_simple(s.type, t, dose_w);
         if (kDij && s.type == MQI_SCORER_DIJ) {
             // insert_hashtable(data_, cnb, spot_ind, ...) (mqi_transport.hpp:204-225); a history
             // without a spot index lands in column 0
@@ -745,7 +760,7 @@ requeue_track(Ctx& C, const Trk& t, const Rng& rng) {
     q.spot[i] = t.spot;
 }
 
-template<bool kDij>
+template<int kMode>
 __device__ __forceinline__ void
 wave_body(const WaveParams& P) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -888,7 +903,7 @@ wave_body(const WaveParams& P) {
         if (d2b < 0.0f) {
             leave = true;
         } else {
-            score_step<kDij>(C, t, cnb, rho, grid_volume(C.g, t.cell));
+            score_step<kMode>(C, t, cnb, rho, grid_volume(C.g, t.cell));
             if (!t.stopped) {
                 grid_step_index(C.g, t.p1, t.d1, t.cell);
                 t.p0  = t.p1;
@@ -1004,12 +1019,12 @@ launch_load_primaries(const Queue& q, const mqi_vertex* v, const uint32_t* spot_
 }
 
 /// The wave kernel in the launch shapes the tuner chooses from: (threads per block, minimum
-/// resident blocks per SM).  The register budget each shape implies is what differs.  Runs with
-/// a Dij scorer use the kDij instance (one shape, 128 x 5).
-template<int kBlock, int kMinBlocks, bool kDij>
+/// resident blocks per SM).  The register budget each shape implies is what differs.  Mode 0
+/// (DIRECT ROIs, simple scorer callbacks) comes in every shape; the other modes in 128 x 5.
+template<int kBlock, int kMinBlocks, int kMode>
 __global__ void __launch_bounds__(kBlock, kMinBlocks)
 k_wave(const __grid_constant__ WaveParams P) {
-    wave_body<kDij>(P);
+    wave_body<kMode>(P);
 }
 
 int
@@ -1028,19 +1043,26 @@ wave_edge_floats(const ChildDev* c, int n) {
     return (f + 3) & ~3;
 }
 
-template<int B, int M, bool D = false>
+template<int B, int M, int K = 0>
 static cudaError_t
 launch_variant(const WaveParams& p, int grid, cudaStream_t s) {
     const int   smem = wave_smem_bytes(p);
-    cudaError_t e    = cudaFuncSetAttribute(k_wave<B, M, D>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    cudaError_t e    = cudaFuncSetAttribute(k_wave<B, M, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
-    k_wave<B, M, D><<<grid, B, smem, s>>>(p);
+    k_wave<B, M, K><<<grid, B, smem, s>>>(p);
     return cudaGetLastError();
 }
 
 cudaError_t
 launch_wave(const WaveParams& p, int grid, int block, int blocks_per_sm, cudaStream_t s) {
-    if (p.has_dij) return launch_variant<128, 5, true>(p, grid / (blocks_per_sm > 0 ? blocks_per_sm : 1) * 5, s);
+    const int grid5 = grid / (blocks_per_sm > 0 ? blocks_per_sm : 1) * 5;
+    switch (p.kernel_mode) {
+    case 0: break;
+    case kModeFull: return launch_variant<128, 5, kModeFull>(p, grid5, s);
+    case kModeRoi: return launch_variant<128, 5, kModeRoi>(p, grid5, s);
+    case kModeFull | kModeRoi: return launch_variant<128, 5, kModeFull | kModeRoi>(p, grid5, s);
+    default: return launch_variant<128, 5, kModeAll>(p, grid5, s);   // any mode with Dij
+    }
     if (block == 128) {
         if (blocks_per_sm >= 6) return launch_variant<128, 6>(p, grid, s);
         if (blocks_per_sm == 5) return launch_variant<128, 5>(p, grid, s);
