@@ -71,12 +71,15 @@ _GRIDS = {}
 
 
 def _oracle_grid(oracle, wl):
-    if wl.name not in _GRIDS:
+    import hashlib
+
+    key = (wl.name, tuple(wl.nxyz), tuple(wl.lxyz), tuple(wl.pxyz), hashlib.md5(wl.hu.tobytes()).hexdigest())
+    if key not in _GRIDS:
         hu = np.unique(wl.hu)
         lut = np.array([oracle.hu_to_density(int(h)) for h in hu], np.float32)
         rho = lut[np.searchsorted(hu, wl.hu)].reshape(-1)
-        _GRIDS[wl.name] = oracle.Grid(*wl.edges(), rho)
-    return _GRIDS[wl.name]
+        _GRIDS[key] = oracle.Grid(*wl.edges(), rho)
+    return _GRIDS[key]
 
 
 def _laterally_coarse(wl, k):
