@@ -204,23 +204,22 @@ roi_mask_idx(const ScorerDev& s, uint32_t v) {
 }
 
 /// fp_compute_hit of the scorers that need nothing beyond the step's deposit and its
-/// dose_to_water (mqi_scorer_energy_deposit.hpp:12-77).
-__device__ inline double
+/// dose_to_water (mqi_scorer_energy_deposit.hpp:12-77), as the FP32 quantity they are formed from:
+/// the deposit, or dose_to_water (squared in FP64 by the caller for dose_to_water_square).  It is
+/// never negative, so "value > 0" (insert_hashtable's filter) is decided in FP32.
+__device__ inline float
 compute_hit_simple(int type, const Trk& t, float dose_w) {
     switch (type) {
-    case MQI_SCORER_EDEP: return (double) (t.dE + t.ldE);
-    case MQI_SCORER_EDEP_PRIMARY: return t.primary ? (double) t.dE : 0.0;
-    case MQI_SCORER_EDEP_SECONDARY: return t.primary ? 0.0 : (double) t.dE;
+    case MQI_SCORER_EDEP: return t.dE + t.ldE;
+    case MQI_SCORER_EDEP_PRIMARY: return t.primary ? t.dE : 0.0f;
+    case MQI_SCORER_EDEP_SECONDARY: return t.primary ? 0.0f : t.dE;
     // dose_to_water in Gy per history: formed in FP32 (one rounding per step; the reference forms
     // it in double) and accumulated in FP64.  GB300's FP64 pipe is narrow, so the per-step
     // division stays in FP32.
     case MQI_SCORER_DOSE_W:
-    case MQI_SCORER_DIJ: return (double) dose_w;
-    case MQI_SCORER_DOSE_W2: {
-        const double d = (double) dose_w;
-        return d * d;
-    }
-    default: return 0.0;
+    case MQI_SCORER_DOSE_W2:
+    case MQI_SCORER_DIJ: return dose_w;
+    default: return 0.0f;
     }
 }
 
@@ -230,7 +229,10 @@ __device__ inline double
 compute_hit(int type, const Trk& t, float rho, float vol, float dose_w) {
     if (type == MQI_SCORER_DOSE_M)
         return t.primary ? (double) t.dE * 1.60218e-13 * 1000.0 / (double) (vol * rho) : 0.0;
-    if (type < MQI_SCORER_LETD_NUM || type > MQI_SCORER_LETT_DEN) return compute_hit_simple(type, t, dose_w);
+    if (type < MQI_SCORER_LETD_NUM || type > MQI_SCORER_LETT_DEN) {
+        const double v = (double) compute_hit_simple(type, t, dose_w);
+        return type == MQI_SCORER_DOSE_W2 ? v * v : v;
+    }
     // LET scorers (mqi_scorer_energy_deposit.hpp:91-177)
     // the step length as the reference forms it: float differences squared in float, summed in double
     const float  density = rho * 1000.0f;
@@ -278,19 +280,29 @@ score_step(Ctx& C, const Trk& t, uint32_t cnb, float rho, float vol) {
         } else {
             ok = roi_idx(s, cnb) > 0;
         }
-        double v = 0.0;
-        if (ok) v = kFull ? compute_hit(s.type, t, rho, vol, dose_w) : compute_hit_simple(s.type, t, dose_w);
+        double v;
+        bool   pos;
+        if (kFull) {
+            v   = ok ? compute_hit(s.type, t, rho, vol, dose_w) : 0.0;
+            pos = v > 0.0;
+        } else {
+            // the FP64 pipe is narrow: filter in FP32, convert once, square only for dose^2
+            const float vf = ok ? compute_hit_simple(s.type, t, dose_w) : 0.0f;
+            pos            = vf > 0.0f;
+            v              = (double) vf;
+            if (s.type == MQI_SCORER_DOSE_W2) v *= v;
+        }
+        if (s.double_score) v += v;
         if (kDij && s.type == MQI_SCORER_DIJ) {
             // insert_hashtable(data_, cnb, spot_ind, ...) (mqi_transport.hpp:204-225); a history
             // without a spot index lands in column 0
-            const bool valid = ok && v > 0.0;
             const uint32_t col = (C.spot & kSpotMask) == kNoSpot ? 0u : (C.spot & kSpotMask);
-            dij_add(s.dij, s.dij_mask, s.dij_count, P.error_flag, col, cnb, s.double_score ? v + v : v, valid);
+            dij_add(s.dij, s.dij_mask, s.dij_count, P.error_flag, col, cnb, v, ok && pos);
             continue;
         }
-        const bool valid = ok && v > 0.0 && key < s.tally_len;
+        const bool valid = ok && pos && key < s.tally_len;
         const uint64_t slot = ((uint64_t) (C.spot >> kScenShift) * s.tally_len + key) * s.tstride;   // scenario's tally
-        tally_add(s.tally, slot, s.double_score ? v + v : v, valid);
+        tally_add(s.tally, slot, v, valid);
     }
 }
 

@@ -329,19 +329,20 @@ def test_gpu_dose_matches_reference_on_the_synthetic_ct(golden, gpu_ctx_factory)
                                    capi.LETT_DEN, capi.EDEP_PRIMARY, capi.EDEP_SECONDARY])
 def test_scorer_plugins_match_the_oracle(oracle, gpu_ctx_factory, stype):
     """Every enum'd scorer callback (scorers/mqi_scorer_energy_deposit.hpp:12-177) against the C
-    restatement run on the same Philox streams: totals within 1e-3 and depth profiles within 2% in
-    bins above 10% of the maximum (rare ulp-level branch flips change single histories)."""
-    wl = workloads.c2(histories=2000)
-    n, seed = 2000, 0xD0CE
+    restatement run on the same Philox streams, history by history: each history's scored total
+    agrees to 1e-4 unless an ulp-level branch flip changed that history, which stays rare."""
+    wl = _laterally_coarse(workloads.c2(histories=150), 16)
+    n, seed = 150, 0xD0CE
     c, cid, sid = _ctx_for(wl, gpu_ctx_factory, stype)
     v = wl.vertices(n, 41)
     c.set_vertices(v)
-    c.transport(0, n, seed)
-    g = c.tally(sid)
-    grid = _oracle_grid(oracle, wl)
-    o, _, _ = oracle.transport(grid, v, 0, n, seed, wl.physics_debug, scorer=int(stype))
+    g = np.zeros(n)
+    for h in range(n):
+        c.reset()
+        c.transport(h, h + 1, seed)
+        g[h] = c.tally(sid).sum()
+    _, o, _ = oracle.transport(_oracle_grid(oracle, wl), v, 0, n, seed, wl.physics_debug, scorer=int(stype),
+                               per_history=True)
     assert o.sum() > 0
-    assert abs(g.sum() - o.sum()) <= 1e-3 * o.sum(), (g.sum(), o.sum())
-    gi, oi = ph.depth_dose(g, wl.nxyz), ph.depth_dose(o, wl.nxyz)
-    sel = oi > 0.1 * oi.max()
-    assert (np.abs(gi - oi)[sel] <= 0.02 * oi[sel]).mean() >= 0.95
+    same = np.abs(g - o) <= 1e-4 * np.maximum(np.abs(o), 1e-30)
+    assert same.mean() >= 0.93, (same.mean(), np.flatnonzero(~same)[:10])
