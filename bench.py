@@ -368,7 +368,8 @@ def run_gpu(args, wl):
 
     # the tuner picks the launch shape, queue size and launch mode on a sample of the workload
     # (into scratch tallies); results do not depend on the choice
-    tune = ctx.autotune(0, min(N, args.tune_histories), seed_base + 7) if args.tune_histories > 0 else None
+    n_tune = N if args.tune_histories == 0 else args.tune_histories
+    tune = ctx.autotune(0, min(N, n_tune), seed_base + 7) if args.tune_histories >= 0 else None
     for w in range(args.warmup):
         ctx.transport(0, N, seed_base + w)
     ctx.reset()
@@ -465,7 +466,7 @@ def run_gpu(args, wl):
         }
         if tune is not None:
             best = tune[np.argmax(tune["histories_per_s"])]
-            line["tuning"] = {"sample_histories": min(N, args.tune_histories), "candidates": len(tune),
+            line["tuning"] = {"sample_histories": min(N, n_tune), "candidates": len(tune),
                               "chosen": {"block": int(best["block"]), "blocks_per_sm": int(best["blocks_per_sm"]),
                                          "streamed": int(best["streamed"]), "primary_chunk": int(best["primary_chunk"])},
                               "best_over_worst": float(tune["histories_per_s"].max() / tune["histories_per_s"].min())}
@@ -500,7 +501,8 @@ def main():
     ap.add_argument("--plain-stride", type=int, default=10, help="time every n-th spot for the plain per-spot rate")
     ap.add_argument("--robust-stride", type=int, default=20, help="spots of the plan in the robust sample")
     ap.add_argument("--max-passes", type=int, default=30, help="plan passes allowed for the 1%% criterion")
-    ap.add_argument("--tune-histories", type=int, default=200_000, help="tuner sample (0: no tuning)")
+    ap.add_argument("--tune-histories", type=int, default=0,
+                    help="tuner sample (0: the step's histories; -1: no tuning)")
     args = ap.parse_args()
     from moquimc_gb300 import workloads
 

@@ -825,9 +825,16 @@ mqi_autotune(mqi_ctx* c, int source_plan, uint64_t h0, uint64_t h1, uint64_t see
         }
     };
     struct Cand { int block, bps, streamed, graph_waves; uint32_t chunk; };
+    // queue sizes above the sample behave alike (one load holds the whole sample): only the
+    // largest of them is tried
+    const uint64_t n_sample = (h1 - h0) * c->n_scen;
+    std::vector<uint32_t> chunks;
+    for (uint32_t chunk : { 1u << 19, 1u << 20, 1u << 21 })
+        if (chunk < n_sample || chunks.empty()) chunks.push_back(chunk);
+        else chunks.back() = chunk;
     std::vector<Cand> cands;
     for (int streamed : { 1, 0 })
-        for (uint32_t chunk : { 1u << 19, 1u << 20, 1u << 21 })
+        for (uint32_t chunk : chunks)
             for (auto shape : { std::make_pair(128, 5), std::make_pair(128, 4), std::make_pair(128, 6), std::make_pair(256, 2) })
                 cands.push_back({ shape.first, shape.second, streamed, 8, chunk });
     uint32_t n = 0;

@@ -187,7 +187,7 @@ def test_autotune_keeps_tallies_and_picks_a_candidate(gpu_ctx_factory):
     c.transport(0, 5_000, 3)
     before, st = c.tally(d), c.stats()
     res = c.autotune(0, 20_000, 9)
-    assert len(res) == 24 and (res["histories_per_s"] > 0).all()
+    assert len(res) == 8 and (res["histories_per_s"] > 0).all()   # one queue size: all exceed the sample
     np.testing.assert_array_equal(c.tally(d), before)
     assert c.stats() == st
     # the chosen setting runs the same tracks as the default one
