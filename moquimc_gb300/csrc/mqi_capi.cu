@@ -829,9 +829,17 @@ mqi_autotune(mqi_ctx* c, int source_plan, uint64_t h0, uint64_t h1, uint64_t see
     // largest of them is tried
     const uint64_t n_sample = (h1 - h0) * c->n_scen;
     std::vector<uint32_t> chunks;
-    for (uint32_t chunk : { 1u << 19, 1u << 20, 1u << 21 })
-        if (chunk < n_sample || chunks.empty()) chunks.push_back(chunk);
-        else chunks.back() = chunk;
+    bool                  above = false;   // a queue size >= the sample is in the list
+    for (uint32_t chunk : { 1u << 19, 1u << 20, 1u << 21 }) {
+        if (chunk < n_sample) {
+            chunks.push_back(chunk);
+        } else if (!above) {
+            chunks.push_back(chunk);
+            above = true;
+        } else {
+            chunks.back() = chunk;
+        }
+    }
     std::vector<Cand> cands;
     for (int streamed : { 1, 0 })
         for (uint32_t chunk : chunks)
