@@ -136,7 +136,7 @@ mqi_destroy(mqi_ctx* c) {
     DeviceGuard g(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     for (auto& ch : c->children) {
-        cudaFree(ch.xe); cudaFree(ch.ye); cudaFree(ch.ze); cudaFree(ch.rho); cudaFree(ch.mat);
+        cudaFree(ch.xe); cudaFree(ch.ye); cudaFree(ch.ze); cudaFree(ch.rho);
     }
     for (auto& s : c->scorers) {
         cudaFree(s.start); cudaFree(s.stride); cudaFree(s.acc);
@@ -247,7 +247,6 @@ mqi_add_child(mqi_ctx* c, int nx, int ny, int nz, const float* xe, const float* 
     MQI_CUDA(c, cudaMemcpy(ch.ye, ye, (ny + 1) * sizeof(float), cudaMemcpyHostToDevice), "mqi_add_child");
     MQI_CUDA(c, cudaMemcpy(ch.ze, ze, (nz + 1) * sizeof(float), cudaMemcpyHostToDevice), "mqi_add_child");
     MQI_CUDA(c, cudaMalloc(&ch.rho, (size_t) nx * ny * nz * sizeof(float)), "mqi_add_child");
-    MQI_CUDA(c, cudaMalloc(&ch.mat, (size_t) nx * ny * nz * sizeof(float2)), "mqi_add_child");
     identity3(ch.rf);
     ch.tr[0] = ch.tr[1] = ch.tr[2] = 0.0f;
     if (rot_fwd) std::memcpy(ch.rf, rot_fwd, sizeof(ch.rf));
@@ -273,7 +272,6 @@ mqi_set_density(mqi_ctx* c, int id, const float* rho, int on_device) {
     const size_t bytes = (size_t) ch.nx * ch.ny * ch.nz * sizeof(float);
     MQI_CUDA(c, cudaMemcpyAsync(ch.rho, rho, bytes, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->stream),
              "mqi_set_density");
-    MQI_CUDA(c, launch_material_factors(ch.rho, ch.mat, (uint64_t) ch.nx * ch.ny * ch.nz, c->stream), "mqi_set_density");
     MQI_CUDA(c, cudaStreamSynchronize(c->stream), "mqi_set_density");
     ch.has_rho = true;
     return MQI_OK;
@@ -318,7 +316,6 @@ mqi_set_hu(mqi_ctx* c, int id, const int16_t* hu, float scale, int on_device) {
         src = tmp;
     }
     cudaError_t e = launch_hu_to_density(c->tables + 6 * MQI_TABLE_N, src, ch.rho, n, scale, c->stream);
-    if (e == cudaSuccess) e = launch_material_factors(ch.rho, ch.mat, n, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (tmp) cudaFree(tmp);
     if (e != cudaSuccess) return cuda_fail(c, e, "mqi_set_hu");
@@ -427,7 +424,7 @@ make_wave_params(mqi_ctx* c, uint64_t seed, WaveParams& P) {
         const ChildHost& h = c->children[i];
         ChildDev&        d = P.child[i];
         d.nx = h.nx; d.ny = h.ny; d.nz = h.nz;
-        d.xe = h.xe; d.ye = h.ye; d.ze = h.ze; d.rho = h.rho; d.mat = h.mat;
+        d.xe = h.xe; d.ye = h.ye; d.ze = h.ze; d.rho = h.rho;
         std::memcpy(d.rf, h.rf, sizeof(d.rf));
         std::memcpy(d.ri, h.ri, sizeof(d.ri));
         std::memcpy(d.tr, h.tr, sizeof(d.tr));

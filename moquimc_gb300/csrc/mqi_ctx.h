@@ -25,7 +25,6 @@ struct ChildHost {
     float* ye = nullptr;
     float* ze = nullptr;
     float* rho = nullptr;
-    float2* mat = nullptr;      // per-voxel material_factors(rho), refreshed with the density
     bool   has_rho = false;
     float  rf[9], ri[9], tr[3];
     int    identity = 1;

@@ -287,39 +287,6 @@ radiation_length_default(float rho_mass, bool physics_debug) {
     return (kWaterDensity * kX0Water) / (d * 0.001f * f);
 }
 
-/// The density-only parts of spr_default and radiation_length_default, computed once per voxel
-/// when the density is set: x = powf(d, -0.7) - 1 (the SPR fit's density term), y = the radiation
-/// length without the debug-physics water shortcut.  spr_from / x0_from reproduce spr_default /
-/// radiation_length_default bit for bit from them (the same operations on the same values).
-__host__ __device__ inline float2
-material_factors(float rho_mass) {
-    const float d = rho_mass * 1000.0f;
-    float2      f;
-    f.x = powf(d, -0.7f) - 1.0f;
-    f.y = radiation_length_default(rho_mass, false);
-    return f;
-}
-
-__host__ __device__ inline float
-spr_from(float rho_mass, float Ek, bool physics_debug, float density_term) {
-    const float d = rho_mass * 1000.0f;
-    if (physics_debug && fabsf(d - 1.0f) < 1e-3f) return 1.0f;
-    if (d <= 0.26f) {
-        if (d < 0.0012f) return 0.0f;
-        return intpl1d(d, 0.0012f, 0.26f, 0.8815f, 0.9925f);
-    }
-    float rsp = 1.0123f - 3.386e-5f * Ek;
-    rsp += 0.291f * (1.0f + powf(Ek, -0.3421f)) * density_term;
-    if (d >= 0.9f) return rsp;
-    return intpl1d(d, 0.26f, 0.9f, 0.9925f, rsp);
-}
-
-__host__ __device__ inline float
-x0_from(float rho_mass, bool physics_debug, float x0) {
-    if (physics_debug && fabsf(rho_mass * 1000.0f - 1.0f) < 1e-3f) return kX0Water;
-    return x0;
-}
-
 // ------------------------------------------------------------------------------------------
 // Geometry (moqui/base/mqi_grid3d.hpp).  All arithmetic that decides a voxel index is written
 // with round-to-nearest intrinsics so the compiler cannot contract it into FMAs: the voxel
@@ -336,7 +303,6 @@ struct Grid {
     const float* tr;   // translation
     int          identity;   // rf == I and tr == 0
     float        rho_scale;  // density scale of the track's scenario (1: none)
-    const float2* mat;       // per-voxel material_factors of the unscaled density (null: compute)
 };
 
 __device__ inline float fadd(float a, float b) { return __fadd_rn(a, b); }

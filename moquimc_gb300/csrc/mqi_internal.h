@@ -62,7 +62,6 @@ struct ChildDev {
     const float* ye;
     const float* ze;
     const float* rho;
-    const float2* mat;         // per-voxel material_factors(rho) (null: computed per step)
     float        rf[9], ri[9], tr[3];
     int          identity;
     int          scorer_begin, n_scorers;
@@ -182,7 +181,6 @@ cudaError_t launch_sample_topup(const Queue& q, const TopUp* tu, const mqi_spot*
 cudaError_t launch_wave(const WaveParams& p, int grid, int block, int blocks_per_sm, cudaStream_t s);
 int         wave_smem_bytes(const WaveParams& p);
 int         wave_edge_floats(const ChildDev* c, int n);
-cudaError_t launch_material_factors(const float* rho, float2* mat, uint64_t n, cudaStream_t s);
 cudaError_t launch_hu_to_density(const float* corr, const int16_t* hu, float* rho, uint64_t n, float scale,
                                  cudaStream_t s);
 cudaError_t launch_trace_rays(const ChildDev& c, const float* rays, uint64_t n_rays, uint32_t max_steps,

@@ -70,7 +70,6 @@ make_grid(const ChildDev& c, const float* sxe, const float* sye, const float* sz
     g.tr  = c.tr;
     g.identity = c.identity;
     g.rho_scale = 1.0f;
-    g.mat = c.mat;
     return g;
 }
 
@@ -85,7 +84,6 @@ apply_scenario(const WaveParams& P, Grid& g, int child, uint32_t sw) {
         g.ye        = e + g.nx + 1;
         g.ze        = e + g.nx + g.ny + 2;
         g.rho_scale = P.scen_scale[s];
-        if (g.rho_scale != 1.0f) g.mat = nullptr;   // the factors belong to the unscaled density
     }
 }
 
@@ -94,12 +92,6 @@ apply_scenario(const WaveParams& P, Grid& g, int child, uint32_t sw) {
 __device__ inline float
 voxel_rho(const Grid& g, uint32_t cnb) {
     return __fmul_rn(g.rho[cnb], g.rho_scale);
-}
-
-/// The voxel's material factors: precomputed, or computed here for a scaled density.
-__device__ inline float2
-voxel_factors(const Grid& g, uint32_t cnb, float rho) {
-    return g.mat ? g.mat[cnb] : material_factors(rho);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -478,8 +470,8 @@ energy_loss(const Tables& T, const Rel& rel, float rho, float len, float spr, fl
 /// block of random words is laid out as: [0] free path, [1,2] Box-Muller pair (straggling,
 /// scattering angle), [3] azimuth.
 __device__ inline void
-along_step(Ctx& C, Trk& t, const Rel& rel, float len, float rho, float spr, float x0v, float z_strag,
-           float z_mcs, float u_phi) {
+along_step(Ctx& C, Trk& t, const Rel& rel, float len, float rho, float spr, float z_strag, float z_mcs,
+           float u_phi) {
     const float dE = energy_loss(*C.T, rel, rho, len, spr, z_strag);
     float       r  = 1.0f;
     if (dE >= t.ke0) {
@@ -487,7 +479,7 @@ along_step(Ctx& C, Trk& t, const Rel& rel, float len, float rho, float spr, floa
         t.stopped = true;
     }
     const float P     = rel.momentum();
-    const float X0    = x0_from(rho, C.dbg, x0v);   // radiation_length_default(rho)
+    const float X0    = radiation_length_default(rho, C.dbg);
     const float th_sq = ((kEs / P) * (kEs / P) / rel.beta_sq) * len / X0;
     float       th    = sqrtf(th_sq);
     th                = z_mcs * (sqrtf(2.0f) * th);
@@ -647,7 +639,7 @@ post_interaction(const WaveParams* P, const Tables* T, Grid g, int child, bool d
 
 /// fippel_physics::stepping (mqi_fippel_physics.hpp:67-216).
 __device__ inline void
-stepping(Ctx& C, Trk& t, Rng& rng, float rho, float2 mf, float d2b) {
+stepping(Ctx& C, Trk& t, Rng& rng, float rho, float d2b) {
     t.spr0 = -1.0f;
     if (rho < 1.0e-7f) {
         t.p1 = advance(t.p0, t.d0, d2b);
@@ -668,7 +660,7 @@ stepping(Ctx& C, Trk& t, Rng& rng, float rho, float2 mf, float d2b) {
     const Tables& T = *C.T;
     rng.begin_step();
     const Rel   rel(t.ke0);
-    const float spr      = spr_from(rho, t.ke0, C.dbg, mf.x);   // spr_default(rho, ke0)
+    const float spr      = spr_default(rho, t.ke0, C.dbg);
     const float dedx     = dedx_lookup(T, rel.Ek);
     const float cur_min  = kMaxStep * spr * rho / kWaterDensity;
     const float max_loss = -1.0f * cur_min * dedx;
@@ -701,7 +693,7 @@ stepping(Ctx& C, Trk& t, Rng& rng, float rho, float2 mf, float d2b) {
     const bool interaction = !to_boundary && (mfp < d2b || fabsf(mfp - d2b) < kGeoTol) &&
                              (mfp < step_limit || fabsf(mfp - step_limit) < kGeoTol);
     const float len = to_boundary ? d2b : (interaction ? mfp : step_limit);
-    along_step(C, t, rel, len, rho, spr, mf.y, z1, z2, u_phi);
+    along_step(C, t, rel, len, rho, spr, z1, z2, u_phi);
     t.spr0 = spr;
     if (interaction && t.ke1 > kTpCut) {
         const float u = cs_sum * rng.uniform();
@@ -912,9 +904,8 @@ wave_body(const WaveParams& P) {
         C.spot = t.spot;
         const uint32_t cnb = grid_cnb(C.g, t.cell);
         const float    rho = voxel_rho(C.g, cnb);
-        const float2   mf  = voxel_factors(C.g, cnb, rho);
         const float    d2b = grid_exit(C.g, t.p0, t.d0, t.cell);
-        stepping(C, t, rng, rho, mf, d2b);
+        stepping(C, t, rng, rho, d2b);
         ++n_steps;
         if (++track_steps > kMaxTrackSteps) {   // no physical track comes near this; never hang
             t.stopped = true;
@@ -1119,20 +1110,6 @@ k_hu_to_density(const float* __restrict__ corr, const int16_t* __restrict__ hu, 
         f       = (float) __ddiv_rn((double) f, 1000.0);
         rho[i]  = __fmul_rn(f, scale);
     }
-}
-
-__global__ void
-k_material_factors(const float* __restrict__ rho, float2* __restrict__ mat, uint64_t n) {
-    for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n; i += (uint64_t) gridDim.x * blockDim.x)
-        mat[i] = material_factors(rho[i]);
-}
-
-cudaError_t
-launch_material_factors(const float* rho, float2* mat, uint64_t n, cudaStream_t s) {
-    if (n == 0) return cudaSuccess;
-    const uint64_t blocks = (n + 255) / 256;
-    k_material_factors<<<(unsigned) (blocks < 152 * 64 ? blocks : 152 * 64), 256, 0, s>>>(rho, mat, n);
-    return cudaGetLastError();
 }
 
 cudaError_t
