@@ -460,6 +460,11 @@ make_wave_params(mqi_ctx* c, uint64_t seed, WaveParams& P) {
         if (ch.n_scorers >= 3 && !has_stat)
             for (int k = 0; k < ch.n_scorers - 2; ++k) P.scorer[ch.scorer_begin + k].double_score = 1;
     }
+    if (P.kernel_mode == 0 && P.n_children == 1 && c->scorers.size() == 1 && c->n_scen == 1) {
+        const ScorerHost& s0 = c->scorers[0];
+        if (!s0.stat_mode && s0.tstride == 1 && (s0.type == MQI_SCORER_EDEP || s0.type == MQI_SCORER_DOSE_W))
+            P.kernel_mode = kModeSingle;
+    }
     P.physics_debug   = c->physics_debug;
     P.score_local     = c->score_local;
     P.stack_limit     = c->physics_debug ? 200 : 10;

@@ -35,6 +35,8 @@ constexpr int kModeDij  = 1;   // a Dij scorer
 constexpr int kModeFull = 2;   // dose_to_medium or LET scorers
 constexpr int kModeRoi  = 4;   // INDIRECT or CONTOUR ROI mappings
 constexpr int kModeAll  = kModeDij | kModeFull | kModeRoi;
+constexpr int kModeSingle = 8; // exactly one energy-deposit or dose-to-water scorer, DIRECT ROI,
+                               // one child, no statistics pair, no scenarios (the phantom example)
 
 /// Flat device description of one scorer (scorer<R> + roi_t, mqi_scorer.hpp:39-79,
 /// mqi_roi.hpp:18-194).

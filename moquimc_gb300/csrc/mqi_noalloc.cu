@@ -168,6 +168,8 @@ mqi_transport_noalloc(int nx, int ny, int nz, const float* d_xe, const float* d_
     sc.tstride    = 1;
     if (scorer_type == MQI_SCORER_DOSE_M || (scorer_type >= MQI_SCORER_LETD_NUM && scorer_type <= MQI_SCORER_LETT_DEN))
         P.kernel_mode = kModeFull;
+    else if (scorer_type == MQI_SCORER_EDEP || scorer_type == MQI_SCORER_DOSE_W)
+        P.kernel_mode = kModeSingle;
     P.physics_debug    = physics_debug ? 1 : 0;
     P.score_local      = 1;
     P.stack_limit      = physics_debug ? 200 : 10;
