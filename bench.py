@@ -334,6 +334,18 @@ def robust_section(torch, capi, workloads, args) -> dict:
 # GPU arm
 # ------------------------------------------------------------------------------------------
 
+def nvtx_range(torch, name):
+    """Open (name) or close (None) the NVTX range around the timed steps, so that a profiler's
+    launch list can be restricted to them (ncu --nvtx --nvtx-include "timed_steps/")."""
+    try:
+        if name is None:
+            torch.cuda.nvtx.range_pop()
+        else:
+            torch.cuda.nvtx.range_push(name)
+    except Exception:  # noqa: BLE001  (no NVTX in this torch build: nothing to mark)
+        pass
+
+
 def run_gpu(args, wl):
     import torch
 
@@ -383,8 +395,10 @@ def run_gpu(args, wl):
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
     t_wall0 = time.perf_counter()
+    nvtx_range(torch, "timed_steps")
     for k in range(args.steps):
         ctx.transport(0, N, seed_base + 100 + k)
+    nvtx_range(torch, None)
     ev1.record(stream)
     torch.cuda.synchronize()
     t_wall1 = time.perf_counter()

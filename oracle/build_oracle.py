@@ -5,6 +5,12 @@
   ``dbg`` is built with ``-D__PHYSICS_DEBUG__`` (moqui's phantom example build), ``rel`` without.
   When the reference checkout is present the copy is re-staged first; elsewhere the copy that
   travelled with the repository is compiled as is.
+* ``oracle/_ref/bin/ref_gpu_{dbg,rel}``: the reference's own CUDA kernel for sm_103a, compiled with
+  nvcc from the same staged copy and ``oracle/ref_gpu_driver.cu`` with the phantom example's flags
+  (``--use_fast_math``, and ``-D__PHYSICS_DEBUG__`` for ``dbg``) plus ``-maxrregcount=128``: uncapped, ptxas gives the
+  kernel 170 registers, and 170 x 512 threads exceeds the 65,536 registers of an SM, so the stock
+  512-thread launch would be refused.  Built on demand (``build_reference_gpu``), not by
+  ``build_all``: it takes about 20 s and only the reference-GPU timing and parity runs use it.
 * ``oracle/_build/libmqi_oracle.so``: the C restatement ``oracle/mqi_oracle.c``.
 
 All builds use ``-ffp-contract=off`` so the x86 and Arm builds round identically.
@@ -55,7 +61,8 @@ def build_reference(force: bool = False) -> bool:
     jobs = []
     for debug in (True, False):
         out = ref_binary(debug)
-        if force or _stale(out, [drv, os.path.join(REF_SRC, "moqui", "base", "mqi_p_ionization.hpp")]):
+        if force or _stale(out, [drv, os.path.join(HERE, "ref_beams.hpp"),
+                                 os.path.join(REF_SRC, "moqui", "base", "mqi_p_ionization.hpp")]):
             cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-w", f"-I{REF_SRC}", drv, "-o", out, "-lz"]
             if debug:
                 cmd.insert(4, "-D__PHYSICS_DEBUG__")
@@ -65,6 +72,33 @@ def build_reference(force: bool = False) -> bool:
         if j.returncode != 0:
             raise RuntimeError(f"reference oracle build failed:\n{err[-4000:]}")
     return True
+
+
+def ref_gpu_binary(debug: bool = True) -> str:
+    return os.path.join(REF_BIN, "ref_gpu_dbg" if debug else "ref_gpu_rel")
+
+
+def build_reference_gpu(debug: bool = True, force: bool = False) -> str:
+    """Compile the reference GPU driver; returns its path, or "" without a staged copy or nvcc."""
+    if os.path.isdir(os.path.join(REFERENCE_ROOT, "moqui")) and not os.path.isdir(os.path.join(REF_SRC, "moqui")):
+        sys.path.insert(0, HERE)
+        import stage_ref  # noqa: E402
+
+        stage_ref.stage(REFERENCE_ROOT)
+    if not os.path.isdir(os.path.join(REF_SRC, "moqui")):
+        return ""
+    nvcc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "bin", "nvcc")
+    if not os.path.exists(nvcc):
+        return ""
+    drv = os.path.join(HERE, "ref_gpu_driver.cu")
+    out = ref_gpu_binary(debug)
+    os.makedirs(REF_BIN, exist_ok=True)
+    if force or _stale(out, [drv, os.path.join(HERE, "ref_beams.hpp"),
+                             os.path.join(REF_SRC, "moqui", "base", "mqi_p_ionization.hpp")]):
+        _run([nvcc, "-std=c++17", "-O3", "-gencode", "arch=compute_103a,code=sm_103a", "--use_fast_math"]
+             + (["-D__PHYSICS_DEBUG__"] if debug else [])
+             + ["-maxrregcount=128", "-w", f"-I{REF_SRC}", "-x", "cu", drv, "-o", out, "-lz"])
+    return out
 
 
 def oracle_lib() -> str:

@@ -220,3 +220,32 @@ def ref_phantom_parallel(debug: bool, lxyz, pxyz, nxyz, energy, position, size, 
         with open(os.path.join(od, "run.json")) as f:
             recs.append(json.load(f))
     return np.sum(doses, axis=0), recs, doses
+
+
+def ref_gpu_available(debug: bool = True) -> bool:
+    """True when the reference GPU driver builds here (staged copy and nvcc present)."""
+    return bool(_build().build_reference_gpu(debug))
+
+
+def ref_gpu_phantom(debug: bool, lxyz, pxyz, nxyz, energy, position, size, histories, hu, seed, beam="uniform",
+                    workdir: Optional[str] = None, phantom_path: Optional[str] = None):
+    """One run of the reference's own CUDA kernel (oracle/ref_gpu_driver.cu, physics-debug build or
+    not) on a phantom; returns (dose, run record with the CUDA-event kernel time)."""
+    binary = _build().build_reference_gpu(debug)
+    if not binary:
+        raise RuntimeError("reference GPU driver unavailable (no staged reference copy or no nvcc)")
+    td = workdir or tempfile.mkdtemp(prefix="mqi_refgpu_")
+    if phantom_path is None:
+        phantom_path = os.path.join(td, "phantom.raw")
+        np.ascontiguousarray(hu, np.int16).tofile(phantom_path)
+    cmd = [binary] + ref_phantom_cmd(debug, lxyz, pxyz, nxyz, energy, position, size, histories, phantom_path, td,
+                                     seed, beam)[2:]
+    with open(os.path.join(td, "log.txt"), "w") as log:
+        rc = subprocess.run(cmd, stdout=log, stderr=subprocess.STDOUT).returncode
+    if rc != 0:
+        with open(os.path.join(td, "log.txt"), errors="replace") as f:
+            raise RuntimeError(f"reference GPU run failed ({rc}):\n{f.read()[-3000:]}")
+    n = int(np.prod(nxyz))
+    dose = np.fromfile(os.path.join(td, "0_water_dE_total.raw"), dtype=np.float64, count=n)
+    with open(os.path.join(td, "run.json")) as f:
+        return dose, json.load(f)

@@ -25,6 +25,8 @@
 #include <moqui/base/environments/mqi_phantom_env.hpp>
 #include <moqui/kernel_functions/mqi_transport.hpp>
 
+#include "ref_beams.hpp"
+
 #include <chrono>
 #include <csignal>
 #include <cstdio>
@@ -76,27 +78,10 @@ public:
 
     void
     setup_beamsource() override {
-        if (!gaussian) {
+        if (gaussian)
+            gaussian_phantom_beamsource(*this);
+        else
             mqi::phantom_env<float>::setup_beamsource();
-            return;
-        }
-        // Same construction as phantom_env::setup_beamsource (mqi_phantom_env.hpp:204-232)
-        // with the Gaussian 6-D phase space.
-        mqi::coordinate_transform<float> p_coord(this->spot_angles, { 0, 0, 0 });
-        mqi::vec3<float>                 dir(0, 0, -1);
-        std::array<float, 6> beamlet_mean = { this->spot_position[0], this->spot_position[1],
-                                              this->spot_position[2], dir.x, dir.y, dir.z };
-        std::array<float, 6> beamlet_sigm = { this->spot_size[0], this->spot_size[1], 0, 0, 0, 0 };
-        std::array<float, 2> corr         = { 0.0, 0.0 };
-        auto phsp   = new mqi::phsp_6d<float>(beamlet_mean, beamlet_sigm, corr);
-        auto energy = new mqi::const_1d<float>({ this->spot_energy[0] }, { this->spot_energy[1] });
-        this->beamsource.append_beamlet(mqi::beamlet<float>(energy, phsp), this->n_histories, p_coord);
-        uint32_t h1    = this->beamsource.total_histories();
-        this->vertices = new mqi::vertex_t<float>[h1];
-        for (size_t i = 0; i < h1; ++i) {
-            auto bl           = this->beamsource(i);
-            this->vertices[i] = bl(&this->beam_rng);
-        }
     }
 
     void
