@@ -11,7 +11,8 @@
   kernel 170 registers, and 170 x 512 threads exceeds the 65,536 registers of an SM, so the stock
   512-thread launch would be refused.  Built on demand (``build_reference_gpu``), not by
   ``build_all``: it takes about 20 s and only the reference-GPU timing and parity runs use it.
-* ``oracle/_build/libmqi_oracle.so``: the C restatement ``oracle/mqi_oracle.c``.
+* ``oracle/_build/libmqi_oracle.so``: the C restatement ``oracle/mqi_oracle.c`` (FP32 stepping), and
+  ``oracle/_build/libmqi_oracle64.so``: the same source with ``-DMQO_FP64``, the all-FP64 oracle.
 
 All builds use ``-ffp-contract=off`` so the x86 and Arm builds round identically.
 """
@@ -101,24 +102,28 @@ def build_reference_gpu(debug: bool = True, force: bool = False) -> str:
     return out
 
 
-def oracle_lib() -> str:
-    return os.path.join(BUILD, "libmqi_oracle.so")
+def oracle_lib(fp64: bool = False) -> str:
+    return os.path.join(BUILD, "libmqi_oracle64.so" if fp64 else "libmqi_oracle.so")
 
 
-def build_restatement(force: bool = False) -> str:
+def build_restatement(force: bool = False, fp64: bool = False) -> str:
+    """The C restatement: FP32 stepping (moqui's float instantiation) or, with fp64, the all-FP64
+    oracle (-DMQO_FP64)."""
     src = os.path.join(HERE, "mqi_oracle.c")
     hdr = os.path.join(HERE, "mqi_oracle.h")
-    out = oracle_lib()
+    out = oracle_lib(fp64)
     if not os.path.exists(src):
         return ""
     os.makedirs(BUILD, exist_ok=True)
     if force or _stale(out, [src, hdr]):
-        _run(["gcc", "-std=c11", "-O2", "-ffp-contract=off", "-fPIC", "-shared", src, "-o", out, "-lm"])
+        _run(["gcc", "-std=c11", "-O2", "-ffp-contract=off", "-fPIC", "-shared"] + (["-DMQO_FP64"] if fp64 else [])
+             + [src, "-o", out, "-lm"])
     return out
 
 
 def build_all(force: bool = False) -> None:
     build_restatement(force)
+    build_restatement(force, fp64=True)
     build_reference(force)
 
 

@@ -1,8 +1,12 @@
 /* mqi_oracle.c - CPU restatement of moqui's proton transport (TEST INFRASTRUCTURE ONLY).
  *
- * See mqi_oracle.h.  Each function cites the reference file:line it restates.  Floating point is
- * FP32 throughout the stepping, as in moqui's float instantiation; build with -ffp-contract=off so
- * x86 and Arm builds agree.
+ * See mqi_oracle.h.  Each function cites the reference file:line it restates.  The stepping
+ * arithmetic is of type `real`: FP32 by default, as in moqui's float instantiation, or FP64 when
+ * built with -DMQO_FP64 -- the all-FP64 oracle, moqui instantiated with R = double.  Its inputs stay
+ * what they are in both builds: FP32 tables (mqi_p_ionization.hpp:11 and the other process headers
+ * declare them `const float`), FP32 grid edges, densities and vertices, and the same 24-bit uniform
+ * draws, so the two builds differ only in the precision of the arithmetic.  Build with
+ * -ffp-contract=off so x86 and Arm builds agree.
  */
 #include "mqi_oracle.h"
 
@@ -12,21 +16,55 @@
 
 #include "../moquimc_gb300/csrc/mqi_tables.h"
 
+#ifdef MQO_FP64
+typedef double real;
+#define RC(x) x
+#define RABS fabs
+#define RSQRT sqrt
+#define RMIN fmin
+#define RMAX fmax
+#define RACOS acos
+#define RSIN sin
+#define RCOS cos
+#define RPOW pow
+#define RLOG log
+#define REXP exp
+#define RLOG1P log1p
+#define REXPM1 expm1
+#define RHUGE HUGE_VAL
+#else
+typedef float real;
+#define RC(x) x##f
+#define RABS fabsf
+#define RSQRT sqrtf
+#define RMIN fminf
+#define RMAX fmaxf
+#define RACOS acosf
+#define RSIN sinf
+#define RCOS cosf
+#define RPOW powf
+#define RLOG logf
+#define REXP expf
+#define RLOG1P log1pf
+#define REXPM1 expm1f
+#define RHUGE HUGE_VALF
+#endif
+
 /* ---- constants (mqi_physics_constants.hpp:14-38, mqi_interaction.hpp:24-30) ---------------- */
-#define MP 938.272046f
-#define ME 0.510998928f
-#define MO 14903.3460795634f
-#define WATER_DENSITY 0.001f
-#define X0_WATER 360.863f
-#define TP_CUT 0.5f
-#define ES 13.9f
-#define NEAR_ZERO 1e-7f
-#define GEO_TOL 1e-3f
-#define PI_F 3.14159265358979323846f
+#define MP RC(938.272046)
+#define ME RC(0.510998928)
+#define MO RC(14903.3460795634)
+#define WATER_DENSITY RC(0.001)
+#define X0_WATER RC(360.863)
+#define TP_CUT RC(0.5)
+#define ES RC(13.9)
+#define NEAR_ZERO RC(1e-7)
+#define GEO_TOL RC(1e-3)
+#define PI_F RC(3.14159265358979323846)
 
-typedef struct { float x, y, z; } v3;
+typedef struct { real x, y, z; } v3;
 
-static v3 mk(float x, float y, float z) { v3 r = { x, y, z }; return r; }
+static v3 mk(real x, real y, real z) { v3 r = { x, y, z }; return r; }
 
 /* ---- Philox4x32-10 (Salmon et al., SC'11) and the per-track stream ------------------------- */
 typedef struct { uint32_t x, y, z, w; } u4;
@@ -72,81 +110,85 @@ static uint32_t rng_next(rng_t* r) {
     return w;
 }
 
-static float rng_u(rng_t* r) { return ((float) (rng_next(r) >> 8) + 0.5f) * (1.0f / 16777216.0f); }
+static real rng_u(rng_t* r) { return ((real) (rng_next(r) >> 8) + RC(0.5)) * (RC(1.0) / RC(16777216.0)); }
 
 /* ---- helpers (mqi_math.hpp:26-30, mqi_relativistic_quantities.hpp:24-40) ------------------ */
-static float intpl1d(float x, float x0, float x1, float y0, float y1) {
+static real intpl1d(real x, real x0, real x1, real y0, real y1) {
     return (x1 == x0) ? y0 : y0 + (x - x0) * (y1 - y0) / (x1 - x0);
 }
 
-typedef struct { float Ek, Et, Et_sq, gamma, gamma_sq, beta_sq, Te_max; } rel_t;
+typedef struct { real Ek, Et, Et_sq, gamma, gamma_sq, beta_sq, Te_max; } rel_t;
 
-static rel_t rel_of(float ek) {
+static rel_t rel_of(real ek) {
     rel_t r;
-    const float MeMp = ME / MP, MeMp_sq = MeMp * MeMp;
+    const real MeMp = ME / MP, MeMp_sq = MeMp * MeMp;
     r.Ek = ek;
     r.Et = ek + MP;
     r.Et_sq = r.Et * r.Et;
     r.gamma = r.Et / MP;
     r.gamma_sq = r.gamma * r.gamma;
-    r.beta_sq = (float) (1.0 - 1.0 / (double) r.gamma_sq);   /* double intermediate, as the reference */
-    r.Te_max = (2.0f * ME * r.beta_sq * r.gamma_sq) / (1.0f + 2.0f * r.gamma * MeMp + MeMp_sq);
+    r.beta_sq = (real) (1.0 - 1.0 / (double) r.gamma_sq);   /* double intermediate, as the reference */
+    r.Te_max = (RC(2.0) * ME * r.beta_sq * r.gamma_sq) / (RC(1.0) + RC(2.0) * r.gamma * MeMp + MeMp_sq);
     return r;
 }
 
-static float momentum(const rel_t* r) { return sqrtf(r->Et * r->Et - MP * MP); }
+static real momentum(const rel_t* r) { return RSQRT(r->Et * r->Et - MP * MP); }
 
 /* ---- cross sections and stopping power (mqi_p_ionization.hpp:254-286, mqi_pp_elastic.hpp:221-235,
  *      mqi_po_elastic.hpp:243-256, mqi_po_inelastic.hpp:141-155) ---------------------------- */
-static float cs_tab(const float* t, float Ek, float lo, float hi, float rho) {
-    float cs = 0.0f;
+static real cs_tab(const float* t, real Ek, real lo, real hi, real rho) {
+    real cs = RC(0.0);
     if (Ek >= lo && Ek <= hi) {
-        int i0 = (int) ((Ek - lo) / 0.5f);
+        int i0 = (int) ((Ek - lo) / RC(0.5));
         int i1 = i0 + 1 < MQI_TABLE_N ? i0 + 1 : MQI_TABLE_N - 1;
-        float x0 = lo + (float) i0 * 0.5f;
-        float x1 = x0 + 0.5f;
+        real x0 = lo + (real) i0 * RC(0.5);
+        real x1 = x0 + RC(0.5);
         cs = intpl1d(Ek, x0, x1, t[i0], t[i1]);
     }
     return cs * rho;
 }
 
-static float dedx(float Ek) {
-    float pw = 0.0f;
-    if (Ek >= 0.1f && Ek <= 299.6f) {
-        int i0 = (int) ((Ek - 0.1f) / 0.5f);
+static real dedx(real Ek) {
+    real pw = RC(0.0);
+    if (Ek >= RC(0.1) && Ek <= RC(299.6)) {
+        int i0 = (int) ((Ek - RC(0.1)) / RC(0.5));
         int i1 = i0 + 1 < MQI_TABLE_N ? i0 + 1 : MQI_TABLE_N - 1;
-        float x0 = 0.1f + (float) i0 * 0.5f;
-        float x1 = x0 + 0.5f;
+        real x0 = RC(0.1) + (real) i0 * RC(0.5);
+        real x1 = x0 + RC(0.5);
         pw = intpl1d(Ek, x0, x1, mqi_tab_dedx[i0], mqi_tab_dedx[i1]);
-    } else if (Ek < 0.1f && Ek > 0.0f) {
+    } else if (Ek < RC(0.1) && Ek > RC(0.0)) {
         pw = mqi_tab_dedx[0];
     }
-    return -1.0f * pw;
+    return -RC(1.0) * pw;
 }
 
 /* ---- calibration (materials/mqi_patient_materials.hpp:414-473, 514-542) -------------------- */
-float mqo_spr(float rho, float Ek, int dbg) {
-    const float d = rho * 1000.0f;
-    if (dbg && fabsf(d - 1.0f) < 1e-3f) return 1.0f;
-    if (d <= 0.26f) {
-        if (d < 0.0012f) return 0.0f;
-        return intpl1d(d, 0.0012f, 0.26f, 0.8815f, 0.9925f);
+static real spr_of(real rho, real Ek, int dbg) {
+    const real d = rho * RC(1000.0);
+    if (dbg && RABS(d - RC(1.0)) < RC(1e-3)) return RC(1.0);
+    if (d <= RC(0.26)) {
+        if (d < RC(0.0012)) return RC(0.0);
+        return intpl1d(d, RC(0.0012), RC(0.26), RC(0.8815), RC(0.9925));
     }
-    float rsp = 1.0123f - 3.386e-5f * Ek;
-    rsp += 0.291f * (1.0f + powf(Ek, -0.3421f)) * (powf(d, -0.7f) - 1.0f);
-    if (d >= 0.9f) return rsp;
-    return intpl1d(d, 0.26f, 0.9f, 0.9925f, rsp);
+    real rsp = RC(1.0123) - RC(3.386e-5) * Ek;
+    rsp += RC(0.291) * (RC(1.0) + RPOW(Ek, -RC(0.3421))) * (RPOW(d, -RC(0.7)) - RC(1.0));
+    if (d >= RC(0.9)) return rsp;
+    return intpl1d(d, RC(0.26), RC(0.9), RC(0.9925), rsp);
 }
 
-float mqo_x0(float rho, int dbg) {
-    const float d = rho * 1000.0f;
-    float f;
-    if (dbg && fabsf(d - 1.0f) < 1e-3f) return X0_WATER;
-    if (d <= 0.26f) f = 0.9857f + 0.0085f * d;
-    else if (d <= 0.9f) f = 1.0446f - 0.2180f * d;
-    else f = 1.19f + 0.44f * logf(d - 0.44f);
-    return (WATER_DENSITY * X0_WATER) / (d * 0.001f * f);
+static real x0_of(real rho, int dbg) {
+    const real d = rho * RC(1000.0);
+    real f;
+    if (dbg && RABS(d - RC(1.0)) < RC(1e-3)) return X0_WATER;
+    if (d <= RC(0.26)) f = RC(0.9857) + RC(0.0085) * d;
+    else if (d <= RC(0.9)) f = RC(1.0446) - RC(0.2180) * d;
+    else f = RC(1.19) + RC(0.44) * RLOG(d - RC(0.44));
+    return (WATER_DENSITY * X0_WATER) / (d * RC(0.001) * f);
 }
+
+float mqo_spr(float rho, float Ek, int dbg) { return (float) spr_of(rho, Ek, dbg); }
+
+float mqo_x0(float rho, int dbg) { return (float) x0_of(rho, dbg); }
 
 float mqo_hu_to_density(int hu) {
     double r;
@@ -170,10 +212,10 @@ void mqo_eval_physics(const float* e, uint64_t n, float* out) {
     for (uint64_t i = 0; i < n; ++i) {
         rel_t r = rel_of(e[i]);
         float* o = out + 8 * i;
-        o[0] = cs_tab(mqi_tab_cs_p_ion, r.Ek, 0.1f, 299.6f, 1.0f);
-        o[1] = cs_tab(mqi_tab_cs_pp_e, r.Ek, 0.5f, 300.0f, 1.0f);
-        o[2] = cs_tab(mqi_tab_cs_po_e, r.Ek, 0.5f, 300.0f, 1.0f);
-        o[3] = cs_tab(mqi_tab_cs_po_i, r.Ek, 0.5f, 300.0f, 1.0f);
+        o[0] = cs_tab(mqi_tab_cs_p_ion, r.Ek, RC(0.1), RC(299.6), RC(1.0));
+        o[1] = cs_tab(mqi_tab_cs_pp_e, r.Ek, RC(0.5), RC(300.0), RC(1.0));
+        o[2] = cs_tab(mqi_tab_cs_po_e, r.Ek, RC(0.5), RC(300.0), RC(1.0));
+        o[3] = cs_tab(mqi_tab_cs_po_i, r.Ek, RC(0.5), RC(300.0), RC(1.0));
         o[4] = dedx(r.Ek);
         o[5] = r.beta_sq;
         o[6] = r.Te_max;
@@ -185,14 +227,14 @@ void mqo_eval_physics(const float* e, uint64_t n, float* out) {
 
 /* grid3d::index(p, dir) for one axis: the reference's linear scan, restated literally
  * (mqi_grid3d.hpp:751-780). */
-static int index_scan(const float* e, int n, float p, float dir) {
+static int index_scan(const float* e, int n, real p, real dir) {
     int idx = -1;
     for (int ind = 0; ind < n; ind++) {
-        if (fabsf(e[ind] - p) < GEO_TOL) {
+        if (RABS(e[ind] - p) < GEO_TOL) {
             if (dir > 0) return ind;
             if (dir < 0) return ind - 1;
             return ind;
-        } else if (fabsf(e[ind + 1] - p) < GEO_TOL) {
+        } else if (RABS(e[ind + 1] - p) < GEO_TOL) {
             if (dir > 0) return ind + 1;
             if (dir < 0) return ind;
             return ind;
@@ -210,73 +252,73 @@ static int valid(const mqo_grid* g, int x, int y, int z) {
 }
 
 /* intersect(p, d, idx) per axis (mqi_grid3d.hpp:528-605) */
-static float exit_axis(float p, float* d, float v1, float v2, int idx, int dim) {
+static real exit_axis(real p, real* d, real v1, real v2, int idx, int dim) {
     if ((*d) * (*d) > NEAR_ZERO) {
         if (*d < 0) {
-            float t = -(p - v1) / *d;
-            if (fabsf(t) < GEO_TOL && idx > 0) return 1.0f / GEO_TOL;
+            real t = -(p - v1) / *d;
+            if (RABS(t) < GEO_TOL && idx > 0) return RC(1.0) / GEO_TOL;
             return t;
         } else {
-            float t = (v2 - p) / *d;
-            if (fabsf(t) < GEO_TOL && idx < dim) return 1.0f / GEO_TOL;
+            real t = (v2 - p) / *d;
+            if (RABS(t) < GEO_TOL && idx < dim) return RC(1.0) / GEO_TOL;
             return t;
         }
     }
-    *d = 0.0f;
-    return HUGE_VALF;
+    *d = RC(0.0);
+    return RHUGE;
 }
 
-static float intersect_voxel(const mqo_grid* g, v3 p, v3* d, int cx, int cy, int cz) {
-    float tx = exit_axis(p.x, &d->x, g->xe[cx], g->xe[cx + 1], cx, g->nx);
-    float ty = exit_axis(p.y, &d->y, g->ye[cy], g->ye[cy + 1], cy, g->ny);
-    float tz = exit_axis(p.z, &d->z, g->ze[cz], g->ze[cz + 1], cz, g->nz);
-    float u;
+static real intersect_voxel(const mqo_grid* g, v3 p, v3* d, int cx, int cy, int cz) {
+    real tx = exit_axis(p.x, &d->x, g->xe[cx], g->xe[cx + 1], cx, g->nx);
+    real ty = exit_axis(p.y, &d->y, g->ye[cy], g->ye[cy + 1], cy, g->ny);
+    real tz = exit_axis(p.z, &d->z, g->ze[cz], g->ze[cz + 1], cz, g->nz);
+    real u;
     if (tx < ty) u = (tx < tz) ? tx : tz;
     else u = (ty < tz) ? ty : tz;
-    return (u > 0) ? u : -1.0f;
+    return (u > 0) ? u : -RC(1.0);
 }
 
 /* intersect(p, d) from outside (mqi_grid3d.hpp:628-743); returns entry distance or -1 */
-static float intersect_box(const mqo_grid* g, v3 p, v3* d) {
-    float x0 = g->xe[0], x1 = g->xe[g->nx], y0 = g->ye[0], y1 = g->ye[g->ny], z0 = g->ze[0], z1 = g->ze[g->nz];
-    float tminx, tmaxx, tminy, tmaxy, tminz, tmaxz, umin, umax;
-    if (p.x >= x0 && p.x <= x1 && p.y >= y0 && p.y <= y1 && p.z >= z0 && p.z <= z1) return 0.0f;
+static real intersect_box(const mqo_grid* g, v3 p, v3* d) {
+    real x0 = g->xe[0], x1 = g->xe[g->nx], y0 = g->ye[0], y1 = g->ye[g->ny], z0 = g->ze[0], z1 = g->ze[g->nz];
+    real tminx, tmaxx, tminy, tmaxy, tminz, tmaxz, umin, umax;
+    if (p.x >= x0 && p.x <= x1 && p.y >= y0 && p.y <= y1 && p.z >= z0 && p.z <= z1) return RC(0.0);
     if (d->x * d->x > NEAR_ZERO) {
         if (d->x > 0) { tminx = (x0 - p.x) / d->x; tmaxx = (x1 - p.x) / d->x; }
         else { tmaxx = (x0 - p.x) / d->x; tminx = (x1 - p.x) / d->x; }
-    } else { d->x = 0; tminx = -HUGE_VALF; tmaxx = HUGE_VALF; }
+    } else { d->x = 0; tminx = -RHUGE; tmaxx = RHUGE; }
     if (d->y * d->y > NEAR_ZERO) {
         if (d->y > 0) { tminy = (y0 - p.y) / d->y; tmaxy = (y1 - p.y) / d->y; }
         else { tmaxy = (y0 - p.y) / d->y; tminy = (y1 - p.y) / d->y; }
-    } else { d->y = 0; tminy = -HUGE_VALF; tmaxy = HUGE_VALF; }
+    } else { d->y = 0; tminy = -RHUGE; tmaxy = RHUGE; }
     if (d->z * d->z > NEAR_ZERO) {
         if (d->z > 0) { tminz = (z0 - p.z) / d->z; tmaxz = (z1 - p.z) / d->z; }
         else { tmaxz = (z0 - p.z) / d->z; tminz = (z1 - p.z) / d->z; }
-    } else { d->z = 0; tminz = -HUGE_VALF; tmaxz = HUGE_VALF; }
+    } else { d->z = 0; tminz = -RHUGE; tmaxz = RHUGE; }
     if (tminx > tminy) umin = (tminx > tminz) ? tminx : tminz;
     else umin = (tminy > tminz) ? tminy : tminz;
     if (tmaxx < tmaxy) umax = (tmaxx < tmaxz) ? tmaxx : tmaxz;
     else umax = (tmaxy < tmaxz) ? tmaxy : tmaxz;
-    if ((umin < umax || fabsf(umin - umax) < GEO_TOL) && umin >= 0 && umax >= 0) return umin;
-    return -1.0f;
+    if ((umin < umax || RABS(umin - umax) < GEO_TOL) && umin >= 0 && umax >= 0) return umin;
+    return -RC(1.0);
 }
 
 /* index(vtx1, dir1, idx) (mqi_grid3d.hpp:846-877) */
 static void index_update(const mqo_grid* g, v3 p, v3 d, int* cx, int* cy, int* cz) {
-    if (d.x < 0 && (fabsf(p.x - g->xe[*cx]) < GEO_TOL || p.x < g->xe[*cx])) *cx -= 1;
-    else if (d.x > 0 && (fabsf(p.x - g->xe[*cx + 1]) < GEO_TOL || p.x > g->xe[*cx + 1])) *cx += 1;
-    if (d.y < 0 && (fabsf(p.y - g->ye[*cy]) < GEO_TOL || p.y < g->ye[*cy])) *cy -= 1;
-    else if (d.y > 0 && (fabsf(p.y - g->ye[*cy + 1]) < GEO_TOL || p.y > g->ye[*cy + 1])) *cy += 1;
-    if (d.z < 0 && (fabsf(p.z - g->ze[*cz]) < GEO_TOL || p.z < g->ze[*cz])) *cz -= 1;
-    else if (d.z > 0 && (fabsf(p.z - g->ze[*cz + 1]) < GEO_TOL || p.z > g->ze[*cz + 1])) *cz += 1;
+    if (d.x < 0 && (RABS(p.x - g->xe[*cx]) < GEO_TOL || p.x < g->xe[*cx])) *cx -= 1;
+    else if (d.x > 0 && (RABS(p.x - g->xe[*cx + 1]) < GEO_TOL || p.x > g->xe[*cx + 1])) *cx += 1;
+    if (d.y < 0 && (RABS(p.y - g->ye[*cy]) < GEO_TOL || p.y < g->ye[*cy])) *cy -= 1;
+    else if (d.y > 0 && (RABS(p.y - g->ye[*cy + 1]) < GEO_TOL || p.y > g->ye[*cy + 1])) *cy += 1;
+    if (d.z < 0 && (RABS(p.z - g->ze[*cz]) < GEO_TOL || p.z < g->ze[*cz])) *cz -= 1;
+    else if (d.z > 0 && (RABS(p.z - g->ze[*cz + 1]) < GEO_TOL || p.z > g->ze[*cz + 1])) *cz += 1;
 }
 
 static v3 normalize(v3 v) {
-    float n = sqrtf(v.x * v.x + v.y * v.y + v.z * v.z);
+    real n = RSQRT(v.x * v.x + v.y * v.y + v.z * v.z);
     return mk(v.x / n, v.y / n, v.z / n);
 }
 
-static v3 advance(v3 p, v3 d, float len) { return mk(p.x + d.x * len, p.y + d.y * len, p.z + d.z * len); }
+static v3 advance(v3 p, v3 d, real len) { return mk(p.x + d.x * len, p.y + d.y * len, p.z + d.z * len); }
 
 int mqo_trace_ray(const mqo_grid* g, const float ray[6], int max_steps, uint64_t* cnb, float* dist, int32_t* cells) {
     v3 p0 = mk(ray[0], ray[1], ray[2]);
@@ -287,7 +329,7 @@ int mqo_trace_ray(const mqo_grid* g, const float ray[6], int max_steps, uint64_t
     int cz = index_scan(g->ze, g->nz, p0.z, d0.z);
     int k = 0;
     if (!valid(g, cx, cy, cz)) {
-        float e = intersect_box(g, p0, &d0);
+        real e = intersect_box(g, p0, &d0);
         if (e < 0) return 0;
         p0 = advance(p0, d0, e);
         d0 = d1;
@@ -296,9 +338,9 @@ int mqo_trace_ray(const mqo_grid* g, const float ray[6], int max_steps, uint64_t
         cz = index_scan(g->ze, g->nz, p0.z, d0.z);
     }
     while (valid(g, cx, cy, cz) && k < max_steps) {
-        float d2b = intersect_voxel(g, p0, &d0, cx, cy, cz);
+        real d2b = intersect_voxel(g, p0, &d0, cx, cy, cz);
         cnb[k] = (uint64_t) cz * g->nx * g->ny + (uint64_t) cy * g->nx + cx;
-        dist[k] = d2b;
+        dist[k] = (float) d2b;
         cells[3 * k] = cx; cells[3 * k + 1] = cy; cells[3 * k + 2] = cz;
         ++k;
         if (d2b < 0) break;
@@ -312,9 +354,9 @@ int mqo_trace_ray(const mqo_grid* g, const float ray[6], int max_steps, uint64_t
 
 /* ---- tracks and the LIFO stack (mqi_track.hpp:48-205, mqi_track_stack.hpp:11-67) ----------- */
 typedef struct {
-    float    ke0, ke1;
+    real    ke0, ke1;
     v3       p0, d0, p1, d1;
-    float    dE, ldE;
+    real    dE, ldE;
     int      primary, stopped;
     uint64_t uid;
     uint32_t npush;
@@ -329,12 +371,12 @@ typedef struct {
 typedef struct {
     const mqo_grid*  g;
     int              dbg;
-    float            tcut;
+    real            tcut;
     stack_t_*        stk;
     rng_t            rng;
 } env_t;
 
-static void push(env_t* E, trk_t* parent, float ke0, float ke1, v3 p, v3 d, float dE0) {
+static void push(env_t* E, trk_t* parent, real ke0, real ke1, v3 p, v3 d, real dE0) {
     stack_t_* s = E->stk;
     if (s->idx >= s->limit) {   /* push_secondary silently drops (mqi_track_stack.hpp:36-41) */
         s->dropped++;
@@ -354,32 +396,32 @@ static void push(env_t* E, trk_t* parent, float ke0, float ke1, v3 p, v3 d, floa
 
 /* Möller-Hughes alignment + track_t::update_post_vertex_direction (mqi_track.hpp:163-172,
  * mqi_matrix.hpp:88-150) */
-static v3 rotate_dir(v3 t, float th, float ph) {
-    float s1 = sinf(th), c1 = cosf(th), s2 = sinf(ph), c2 = cosf(ph);
+static v3 rotate_dir(v3 t, real th, real ph) {
+    real s1 = RSIN(th), c1 = RCOS(th), s2 = RSIN(ph), c2 = RCOS(ph);
     v3 dl = normalize(mk(c2 * s1, s2 * s1, c1));
-    float tn = sqrtf(t.x * t.x + t.y * t.y + t.z * t.z);
-    float c = t.z / tn;
-    float m[9];
-    if (fabsf(c - 1.0f) < GEO_TOL || fabsf(c + 1.0f) < GEO_TOL) {
-        float r2 = 1.0f / sqrtf(2.0f);
-        float ux = r2, uy = 0.0f, uz = -r2;
-        float vx = 1.0f - t.x, vy = -t.y, vz = -t.z;
-        float vn = sqrtf(vx * vx + vy * vy + vz * vz);
+    real tn = RSQRT(t.x * t.x + t.y * t.y + t.z * t.z);
+    real c = t.z / tn;
+    real m[9];
+    if (RABS(c - RC(1.0)) < GEO_TOL || RABS(c + RC(1.0)) < GEO_TOL) {
+        real r2 = RC(1.0) / RSQRT(RC(2.0));
+        real ux = r2, uy = RC(0.0), uz = -r2;
+        real vx = RC(1.0) - t.x, vy = -t.y, vz = -t.z;
+        real vn = RSQRT(vx * vx + vy * vy + vz * vz);
         vx /= vn; vy /= vn; vz /= vn;
-        float du = ux * ux + uy * uy + uz * uz, dv = vx * vx + vy * vy + vz * vz, duv = vx * ux + vy * uy + vz * uz;
-        float a = 2.0f / du, b = 2.0f / dv, k = 4.0f * duv / (du * dv);
-        m[0] = 1.0f - a * ux * ux - b * vx * vx + k * vx * ux;
-        m[1] = 0.0f - a * ux * uy - b * vx * vy + k * vx * uy;
-        m[2] = 0.0f - a * ux * uz - b * vx * vz + k * vx * uz;
-        m[3] = 0.0f - a * uy * ux - b * vy * vx + k * vy * ux;
-        m[4] = 1.0f - a * uy * uy - b * vy * vy + k * vy * uy;
-        m[5] = 0.0f - a * uy * uz - b * vy * vz + k * vy * uz;
-        m[6] = 0.0f - a * uz * ux - b * vz * vx + k * vz * ux;
-        m[7] = 0.0f - a * uz * uy - b * vz * vy + k * vz * uy;
-        m[8] = 1.0f - a * uz * uz - b * vz * vz + k * vz * uz;
+        real du = ux * ux + uy * uy + uz * uz, dv = vx * vx + vy * vy + vz * vz, duv = vx * ux + vy * uy + vz * uz;
+        real a = RC(2.0) / du, b = RC(2.0) / dv, k = RC(4.0) * duv / (du * dv);
+        m[0] = RC(1.0) - a * ux * ux - b * vx * vx + k * vx * ux;
+        m[1] = RC(0.0) - a * ux * uy - b * vx * vy + k * vx * uy;
+        m[2] = RC(0.0) - a * ux * uz - b * vx * vz + k * vx * uz;
+        m[3] = RC(0.0) - a * uy * ux - b * vy * vx + k * vy * ux;
+        m[4] = RC(1.0) - a * uy * uy - b * vy * vy + k * vy * uy;
+        m[5] = RC(0.0) - a * uy * uz - b * vy * vz + k * vy * uz;
+        m[6] = RC(0.0) - a * uz * ux - b * vz * vx + k * vz * ux;
+        m[7] = RC(0.0) - a * uz * uy - b * vz * vy + k * vz * uy;
+        m[8] = RC(1.0) - a * uz * uz - b * vz * vz + k * vz * uz;
     } else {
-        float vx = -t.y, vy = t.x, vz = 0.0f;
-        float h = (1.0f - c) / (1.0f - c * c);
+        real vx = -t.y, vy = t.x, vz = RC(0.0);
+        real h = (RC(1.0) - c) / (RC(1.0) - c * c);
         m[0] = c + h * vx * vx; m[1] = h * vx * vy - vz; m[2] = h * vx * vz + vy;
         m[3] = h * vx * vy + vz; m[4] = c + h * vy * vy; m[5] = h * vy * vz - vx;
         m[6] = h * vx * vz - vy; m[7] = h * vy * vz + vx; m[8] = c + h * vz * vz;
@@ -389,63 +431,63 @@ static v3 rotate_dir(v3 t, float th, float ph) {
 }
 
 /* energy_loss + energy_straggling (mqi_p_ionization.hpp:297-345), range walk guarded at 0 */
-static float energy_loss(rel_t* rel, float rho, float len, float spr, float z) {
-    float lw = len * spr * rho / WATER_DENSITY;
-    int n = (int) ((rel->Ek - 0.1f) / 0.5f);
-    float x0, x1, r, dE_mean, Te, var, ret;
+static real energy_loss(rel_t* rel, real rho, real len, real spr, real z) {
+    real lw = len * spr * rho / WATER_DENSITY;
+    int n = (int) ((rel->Ek - RC(0.1)) / RC(0.5));
+    real x0, x1, r, dE_mean, Te, var, ret;
     if (n > MQI_TABLE_N - 2) n = MQI_TABLE_N - 2;
     if (n < 0) n = 0;
-    x0 = 0.1f + (float) n * 0.5f;
-    x1 = x0 + 0.5f;
+    x0 = RC(0.1) + (real) n * RC(0.5);
+    x1 = x0 + RC(0.5);
     if (x0 > rel->Ek && n > 0) n -= 1;
     if (x1 < rel->Ek && n < MQI_TABLE_N - 2) n += 1;
     r = intpl1d(rel->Ek, x0, x1, mqi_tab_range[n], mqi_tab_range[n + 1]);
     if (r < lw) return rel->Ek;
     r -= lw;
     while (n > 0 && r < mqi_tab_range[n]) --n;
-    x0 = 0.1f + (float) n * 0.5f;
-    x1 = x0 + 0.5f;
+    x0 = RC(0.1) + (real) n * RC(0.5);
+    x1 = x0 + RC(0.5);
     dE_mean = rel->Ek - intpl1d(r, mqi_tab_range[n], mqi_tab_range[n + 1], x0, x1);
-    Te = (rel->Te_max >= 0.08511f) ? 0.08511f : rel->Te_max;
+    Te = (rel->Te_max >= RC(0.08511)) ? RC(0.08511) : rel->Te_max;
     {
-        /* dedx_term0 (mqi_physics_constants.hpp:29-30) in float */
-        const float re = 2.8179403262e-12f, re_sq = re * re;
-        const float two_pi = (float) (2.0 * 3.14159265358979323846);
-        const float t = (float) ((double) two_pi * (double) re_sq);
-        const float t2 = t * ME;
-        const float term0 = (float) ((double) t2 * 3.3428e+23 / 1000.0);
+        /* dedx_term0 (mqi_physics_constants.hpp:29-30) in the stepping type */
+        const real re = RC(2.8179403262e-12), re_sq = re * re;
+        const real two_pi = (real) (2.0 * 3.14159265358979323846);
+        const real t = (real) ((double) two_pi * (double) re_sq);
+        const real t2 = t * ME;
+        const real term0 = (real) ((double) t2 * 3.3428e+23 / 1000.0);
         var = term0 * rho / WATER_DENSITY * lw;
     }
-    var *= Te / rel->beta_sq * (1.0f - 0.5f * rel->beta_sq);
-    ret = z * sqrtf(var) + dE_mean;
+    var *= Te / rel->beta_sq * (RC(1.0) - RC(0.5) * rel->beta_sq);
+    ret = z * RSQRT(var) + dE_mean;
     if (ret < 0) ret = -ret;
     return ret;
 }
 
 /* last_step (mqi_p_ionization.hpp:481-490) */
-static void last_step(env_t* E, trk_t* t, float rho) {
-    float lw = 0.0f, sl;
+static void last_step(env_t* E, trk_t* t, real rho) {
+    real lw = RC(0.0), sl;
     if (t->dE > 0) lw = -t->dE / dedx(t->ke0);
-    sl = lw * WATER_DENSITY / (mqo_spr(rho, t->ke0, E->dbg) * rho);
+    sl = lw * WATER_DENSITY / (spr_of(rho, t->ke0, E->dbg) * rho);
     t->p1 = advance(t->p0, t->d0, sl);
 }
 
 /* along_step (mqi_p_ionization.hpp:349-420) */
-static void along_step(env_t* E, trk_t* t, float len, float rho, float spr, float z1, float z2, float u_phi) {
+static void along_step(env_t* E, trk_t* t, real len, real rho, real spr, real z1, real z2, real u_phi) {
     rel_t rel = rel_of(t->ke0);
-    float dE = energy_loss(&rel, rho, len, spr, z1);
-    float r = 1.0f, P, X0, th_sq, th, phi;
+    real dE = energy_loss(&rel, rho, len, spr, z1);
+    real r = RC(1.0), P, X0, th_sq, th, phi;
     if (dE >= t->ke0) {
         r = t->ke0 / dE;
         t->stopped = 1;
     }
     P = momentum(&rel);
-    X0 = mqo_x0(rho, E->dbg);
+    X0 = x0_of(rho, E->dbg);
     th_sq = ((ES / P) * (ES / P) / rel.beta_sq) * len / X0;
-    th = sqrtf(th_sq);
-    th = z2 * (sqrtf(2.0f) * th);
+    th = RSQRT(th_sq);
+    th = z2 * (RSQRT(RC(2.0)) * th);
     if (th < 0) th = -th;
-    phi = 2.0f * PI_F * u_phi;
+    phi = RC(2.0) * PI_F * u_phi;
     t->d1 = rotate_dir(t->d1, th, phi);
     t->dE += dE * r;
     t->p1 = advance(t->p0, t->d0, r * len);
@@ -455,14 +497,14 @@ static void along_step(env_t* E, trk_t* t, float len, float rho, float spr, floa
 /* p_ionization post_step (mqi_p_ionization.hpp:425-477) */
 static void post_delta(env_t* E, trk_t* t) {
     rel_t rel = rel_of(t->ke1);
-    float Te = 0.0f;
+    real Te = RC(0.0);
     for (int it = 0; it < 64; ++it) {
-        float n = rng_u(&E->rng);
+        real n = rng_u(&E->rng);
         Te = E->tcut * rel.Te_max;
-        Te /= ((1.0f - n) * rel.Te_max + n * E->tcut);
-        if (rng_u(&E->rng) < 1.0f - rel.beta_sq * Te / rel.Te_max + Te * Te / (2.0f * rel.Et_sq)) break;
+        Te /= ((RC(1.0) - n) * rel.Te_max + n * E->tcut);
+        if (rng_u(&E->rng) < RC(1.0) - rel.beta_sq * Te / rel.Te_max + Te * Te / (RC(2.0) * rel.Et_sq)) break;
     }
-    if (E->dbg) push(E, t, 0.0f, 0.0f, t->p0, t->d0, Te);
+    if (E->dbg) push(E, t, RC(0.0), RC(0.0), t->p0, t->d0, Te);
     else t->dE += Te;
     t->ke1 -= Te;
 }
@@ -470,53 +512,53 @@ static void post_delta(env_t* E, trk_t* t) {
 /* pp_elastic post_step (mqi_pp_elastic.hpp:119-219) */
 static void post_pp(env_t* E, trk_t* t) {
     rel_t rel = rel_of(t->ke1);
-    const float Mp_sq = MP * MP;
-    float minv = TP_CUT / rel.Ek;
-    float u = rng_u(&E->rng) * (1.0f - 2.0f * minv) + minv;
-    float E1 = rel.Et, dE = rel.Ek * u, E3 = (rel.Ek - dE) + MP, E4 = dE + MP;
-    float P1 = momentum(&rel), P3 = sqrtf(E3 * E3 - Mp_sq), P4 = sqrtf(E4 * E4 - Mp_sq);
-    float c3 = E1 * E3 - Mp_sq - MP * (E1 - E3), c34 = E3 * E4 - E1 * MP, th3, th4, phi;
+    const real Mp_sq = MP * MP;
+    real minv = TP_CUT / rel.Ek;
+    real u = rng_u(&E->rng) * (RC(1.0) - RC(2.0) * minv) + minv;
+    real E1 = rel.Et, dE = rel.Ek * u, E3 = (rel.Ek - dE) + MP, E4 = dE + MP;
+    real P1 = momentum(&rel), P3 = RSQRT(E3 * E3 - Mp_sq), P4 = RSQRT(E4 * E4 - Mp_sq);
+    real c3 = E1 * E3 - Mp_sq - MP * (E1 - E3), c34 = E3 * E4 - E1 * MP, th3, th4, phi;
     v3 dd;
     c3 /= (P1 * P3);
     c34 /= (P3 * P4);
-    c3 = fminf(fmaxf(c3, -1.0f), 1.0f);
-    c34 = fminf(fmaxf(c34, -1.0f), 1.0f);
-    th3 = acosf(c3);
-    th4 = th3 - acosf(c34);
-    phi = 2.0f * PI_F * rng_u(&E->rng);
+    c3 = RMIN(RMAX(c3, -RC(1.0)), RC(1.0));
+    c34 = RMIN(RMAX(c34, -RC(1.0)), RC(1.0));
+    th3 = RACOS(c3);
+    th4 = th3 - RACOS(c34);
+    phi = RC(2.0) * PI_F * rng_u(&E->rng);
     t->ke1 -= dE;
     t->d1 = rotate_dir(t->d1, th3, phi);
     dd = rotate_dir(t->d1, th4, phi);
-    push(E, t, dE, dE, t->p1, dd, 0.0f);
+    push(E, t, dE, dE, t->p1, dd, RC(0.0));
 }
 
 /* po_elastic post_step (mqi_po_elastic.hpp:96-217); truncated exponential by inverse CDF */
 static void post_poe(env_t* E, trk_t* t) {
     rel_t rel = rel_of(t->ke1);
-    if (rel.Ek <= 5.5f) {
-        float dE = rel.Ek;
-        if (E->dbg) push(E, t, dE, 0.0f, t->p1, t->d1, dE);
+    if (rel.Ek <= RC(5.5)) {
+        real dE = rel.Ek;
+        if (E->dbg) push(E, t, dE, RC(0.0), t->p1, t->d1, dE);
         else t->ldE += dE;
         t->ke1 -= dE;
         t->stopped = 1;
         return;
     }
     {
-        const float MoMp = MO / MP, MoMp_sq = MoMp * MoMp;
-        float Tp_avg = 0.65f * expf(-0.0013f * rel.Ek) - 0.71f * expf(-0.0177f * rel.Ek);
-        float Tp_max = (2.0f * MO * rel.beta_sq * rel.gamma_sq) / (1.0f + 2.0f * rel.gamma * MoMp + MoMp_sq);
-        float u = rng_u(&E->rng);
-        float dE = -Tp_avg * log1pf(u * expm1f(-Tp_max / Tp_avg));
-        float E1, E3, c3, th3, phi;
-        if (!(dE >= 0.0f)) dE = 0.0f;
+        const real MoMp = MO / MP, MoMp_sq = MoMp * MoMp;
+        real Tp_avg = RC(0.65) * REXP(-RC(0.0013) * rel.Ek) - RC(0.71) * REXP(-RC(0.0177) * rel.Ek);
+        real Tp_max = (RC(2.0) * MO * rel.beta_sq * rel.gamma_sq) / (RC(1.0) + RC(2.0) * rel.gamma * MoMp + MoMp_sq);
+        real u = rng_u(&E->rng);
+        real dE = -Tp_avg * RLOG1P(u * REXPM1(-Tp_max / Tp_avg));
+        real E1, E3, c3, th3, phi;
+        if (!(dE >= RC(0.0))) dE = RC(0.0);
         if (dE > Tp_max) dE = Tp_max;
-        E1 = rel.Ek * (rel.Ek + 2.0f * MP);
-        E3 = (rel.Ek - dE) * (rel.Ek - dE + 2.0f * MP);
-        c3 = (E1 + E3 - dE * (dE + 2.0f * MO)) / 2.0f / sqrtf(E1 * E3);
-        c3 = fminf(fmaxf(c3, -1.0f), 1.0f);
-        th3 = acosf(c3);
-        phi = 2.0f * PI_F * rng_u(&E->rng);
-        if (E->dbg) push(E, t, dE, 0.0f, t->p0, t->d0, dE);
+        E1 = rel.Ek * (rel.Ek + RC(2.0) * MP);
+        E3 = (rel.Ek - dE) * (rel.Ek - dE + RC(2.0) * MP);
+        c3 = (E1 + E3 - dE * (dE + RC(2.0) * MO)) / RC(2.0) / RSQRT(E1 * E3);
+        c3 = RMIN(RMAX(c3, -RC(1.0)), RC(1.0));
+        th3 = RACOS(c3);
+        phi = RC(2.0) * PI_F * rng_u(&E->rng);
+        if (E->dbg) push(E, t, dE, RC(0.0), t->p0, t->d0, dE);
         else t->ldE += dE;
         t->ke1 -= dE;
         t->d1 = rotate_dir(t->d1, th3, phi);
@@ -525,32 +567,32 @@ static void post_poe(env_t* E, trk_t* t) {
 
 /* po_inelastic post_step (mqi_po_inelastic.hpp:158-288) */
 static void post_poi(env_t* E, trk_t* t) {
-    const float Ek = t->ke1;
-    float Eb = 5.0f, Er = Ek, P2, PL, pw;
-    if (Ek <= 215.0f && Ek > 200.0f) { P2 = 0.78f; PL = P2 + (1.0f - P2) * 0.9f; pw = 0.4f; }
-    else if (Ek > 215.0f) { P2 = 0.78f; PL = P2 + (1.0f - P2) * 1.0f; pw = 0.4f; }
-    else if (Ek > 150.0f) { P2 = 0.72f; PL = P2 + (1.0f - P2) * 0.83f; pw = 0.45f; }
-    else { P2 = 0.7f; PL = P2 + (1.0f - P2) * 0.83f; pw = 0.52f; }
-    while ((Er - Eb) > 2.0f) {
-        float dE, zeta;
+    const real Ek = t->ke1;
+    real Eb = RC(5.0), Er = Ek, P2, PL, pw;
+    if (Ek <= RC(215.0) && Ek > RC(200.0)) { P2 = RC(0.78); PL = P2 + (RC(1.0) - P2) * RC(0.9); pw = RC(0.4); }
+    else if (Ek > RC(215.0)) { P2 = RC(0.78); PL = P2 + (RC(1.0) - P2) * RC(1.0); pw = RC(0.4); }
+    else if (Ek > RC(150.0)) { P2 = RC(0.72); PL = P2 + (RC(1.0) - P2) * RC(0.83); pw = RC(0.45); }
+    else { P2 = RC(0.7); PL = P2 + (RC(1.0) - P2) * RC(0.83); pw = RC(0.52); }
+    while ((Er - Eb) > RC(2.0)) {
+        real dE, zeta;
         Er -= Eb;
-        dE = powf(rng_u(&E->rng), pw) * (Er - 2.0f) + 2.0f;
+        dE = RPOW(rng_u(&E->rng), pw) * (Er - RC(2.0)) + RC(2.0);
         if (dE >= Er) dE = Er;
         Er -= dE;
         t->ke1 -= (dE + Eb);
         zeta = rng_u(&E->rng);
         if (zeta < P2) {
-            float c = (2.0f * dE / Ek - 1.0f) + 2.0f * (1.0f - dE / Ek) * rng_u(&E->rng);
-            float th, phi;
-            c = fminf(fmaxf(c, -1.0f), 1.0f);
-            th = acosf(c);
-            phi = 2.0f * PI_F * rng_u(&E->rng);
-            push(E, t, dE, dE, t->p1, rotate_dir(t->d1, th, phi), 0.0f);
+            real c = (RC(2.0) * dE / Ek - RC(1.0)) + RC(2.0) * (RC(1.0) - dE / Ek) * rng_u(&E->rng);
+            real th, phi;
+            c = RMIN(RMAX(c, -RC(1.0)), RC(1.0));
+            th = RACOS(c);
+            phi = RC(2.0) * PI_F * rng_u(&E->rng);
+            push(E, t, dE, dE, t->p1, rotate_dir(t->d1, th, phi), RC(0.0));
         } else if (zeta < PL) {
         } else if (E->dbg) {
-            push(E, t, dE, 0.0f, t->p0, t->d0, dE);
+            push(E, t, dE, RC(0.0), t->p0, t->d0, dE);
         }
-        Eb *= 0.65f;
+        Eb *= RC(0.65);
     }
     t->dE += Er;
     t->ke1 -= Er;
@@ -558,12 +600,12 @@ static void post_poi(env_t* E, trk_t* t) {
 }
 
 /* fippel_physics::stepping (mqi_fippel_physics.hpp:67-216) */
-static void stepping(env_t* E, trk_t* t, float rho, float d2b) {
+static void stepping(env_t* E, trk_t* t, real rho, real d2b) {
     rel_t rel, rel2;
-    float spr, dd, cur_min, max_loss, cs1[4], cs2[4], sum1, sum2, cs_sum, c[4], u_mfp, mfp, step_limit;
-    float bm_u1, bm_u2, u_phi, bm_r, z1, z2;
-    if (rho < 1.0e-7f) { t->p1 = advance(t->p0, t->d0, d2b); return; }
-    if (rho > 99.9f) { t->stopped = 1; return; }
+    real spr, dd, cur_min, max_loss, cs1[4], cs2[4], sum1, sum2, cs_sum, c[4], u_mfp, mfp, step_limit;
+    real bm_u1, bm_u2, u_phi, bm_r, z1, z2;
+    if (rho < RC(1.0e-7)) { t->p1 = advance(t->p0, t->d0, d2b); return; }
+    if (rho > RC(99.9)) { t->stopped = 1; return; }
     if (t->ke0 <= TP_CUT) {
         if (t->ke0 < 0) t->ke0 = 0;
         t->dE += t->ke0;
@@ -574,36 +616,36 @@ static void stepping(env_t* E, trk_t* t, float rho, float d2b) {
     }
     rng_begin_step(&E->rng);
     rel = rel_of(t->ke0);
-    spr = mqo_spr(rho, t->ke0, E->dbg);
+    spr = spr_of(rho, t->ke0, E->dbg);
     dd = dedx(rel.Ek);
-    cur_min = 1.0f * spr * rho / WATER_DENSITY;
-    max_loss = -1.0f * cur_min * dd;
-    cs1[0] = cs_tab(mqi_tab_cs_p_ion, rel.Ek, 0.1f, 299.6f, rho);
-    cs1[1] = cs_tab(mqi_tab_cs_pp_e, rel.Ek, 0.5f, 300.0f, rho);
-    cs1[2] = cs_tab(mqi_tab_cs_po_e, rel.Ek, 0.5f, 300.0f, rho);
-    cs1[3] = cs_tab(mqi_tab_cs_po_i, rel.Ek, 0.5f, 300.0f, rho);
+    cur_min = RC(1.0) * spr * rho / WATER_DENSITY;
+    max_loss = -RC(1.0) * cur_min * dd;
+    cs1[0] = cs_tab(mqi_tab_cs_p_ion, rel.Ek, RC(0.1), RC(299.6), rho);
+    cs1[1] = cs_tab(mqi_tab_cs_pp_e, rel.Ek, RC(0.5), RC(300.0), rho);
+    cs1[2] = cs_tab(mqi_tab_cs_po_e, rel.Ek, RC(0.5), RC(300.0), rho);
+    cs1[3] = cs_tab(mqi_tab_cs_po_i, rel.Ek, RC(0.5), RC(300.0), rho);
     rel2 = rel_of(t->ke0 - max_loss);
-    cs2[0] = cs_tab(mqi_tab_cs_p_ion, rel2.Ek, 0.1f, 299.6f, rho);
-    cs2[1] = cs_tab(mqi_tab_cs_pp_e, rel2.Ek, 0.5f, 300.0f, rho);
-    cs2[2] = cs_tab(mqi_tab_cs_po_e, rel2.Ek, 0.5f, 300.0f, rho);
-    cs2[3] = cs_tab(mqi_tab_cs_po_i, rel2.Ek, 0.5f, 300.0f, rho);
+    cs2[0] = cs_tab(mqi_tab_cs_p_ion, rel2.Ek, RC(0.1), RC(299.6), rho);
+    cs2[1] = cs_tab(mqi_tab_cs_pp_e, rel2.Ek, RC(0.5), RC(300.0), rho);
+    cs2[2] = cs_tab(mqi_tab_cs_po_e, rel2.Ek, RC(0.5), RC(300.0), rho);
+    cs2[3] = cs_tab(mqi_tab_cs_po_i, rel2.Ek, RC(0.5), RC(300.0), rho);
     sum1 = cs1[0] + cs1[1] + cs1[2] + cs1[3];
     sum2 = cs2[0] + cs2[1] + cs2[2] + cs2[3];
     cs_sum = (sum1 >= sum2) ? sum1 : sum2;
     for (int k = 0; k < 4; ++k) c[k] = (sum1 >= sum2) ? cs1[k] : cs2[k];
     u_mfp = rng_u(&E->rng);
-    mfp = -1.0f * logf(u_mfp) / cs_sum;
+    mfp = -RC(1.0) * RLOG(u_mfp) / cs_sum;
     step_limit = cur_min * WATER_DENSITY / (spr * rho);
     bm_u1 = rng_u(&E->rng);
     bm_u2 = rng_u(&E->rng);
     u_phi = rng_u(&E->rng);
-    bm_r = sqrtf(-2.0f * logf(bm_u1));
-    z1 = bm_r * cosf(2.0f * PI_F * bm_u2);
-    z2 = bm_r * sinf(2.0f * PI_F * bm_u2);
+    bm_r = RSQRT(-RC(2.0) * RLOG(bm_u1));
+    z1 = bm_r * RCOS(RC(2.0) * PI_F * bm_u2);
+    z2 = bm_r * RSIN(RC(2.0) * PI_F * bm_u2);
     if (d2b < mfp && d2b < step_limit) {
         along_step(E, t, d2b, rho, spr, z1, z2, u_phi);
-    } else if ((mfp < d2b || fabsf(mfp - d2b) < GEO_TOL) && (mfp < step_limit || fabsf(mfp - step_limit) < GEO_TOL)) {
-        float u;
+    } else if ((mfp < d2b || RABS(mfp - d2b) < GEO_TOL) && (mfp < step_limit || RABS(mfp - step_limit) < GEO_TOL)) {
+        real u;
         along_step(E, t, mfp, rho, spr, z1, z2, u_phi);
         if (t->ke1 <= TP_CUT) return;
         u = cs_sum * rng_u(&E->rng);
@@ -620,8 +662,8 @@ static void stepping(env_t* E, trk_t* t, float rho, float d2b) {
 /* scorer callbacks (scorers/mqi_scorer_energy_deposit.hpp:12-177): 1 energy_deposit, 2 dose_to_water,
  * 3 dose_to_water_square, 4 dose_to_medium, 5/6 LETd_weight1/2, 7/8 LETt_weight1/2,
  * 9/10 energy_deposit_primary/secondary */
-static double hit(const mqo_config* cfg, const trk_t* t, float rho, float vol, int dbg) {
-    float edep = t->dE + t->ldE;
+static double hit(const mqo_config* cfg, const trk_t* t, real rho, real vol, int dbg) {
+    real edep = t->dE + t->ldE;
     switch (cfg->scorer) {
     case 1: return (double) edep;
     case 9: return t->primary ? (double) t->dE : 0.0;
@@ -629,17 +671,17 @@ static double hit(const mqo_config* cfg, const trk_t* t, float rho, float vol, i
     case 2:
     case 3: {
         double d;
-        if (rho < 1.0e-7f) return 0.0;
-        d = (double) (edep * 1.60218e-10f / (vol * rho * mqo_spr(rho, t->ke0, dbg)));
+        if (rho < RC(1.0e-7)) return 0.0;
+        d = (double) (edep * RC(1.60218e-10) / (vol * rho * spr_of(rho, t->ke0, dbg)));
         return cfg->scorer == 3 ? d * d : d;
     }
     case 4: return t->primary ? (double) t->dE * 1.60218e-13 * 1000.0 / (double) (vol * rho) : 0.0;
     default: break;
     }
     {
-        /* the LET weights: the step length from float differences squared in float, summed in double */
-        const float density = rho * 1000.0f;
-        const float dx = t->p1.x - t->p0.x, dy = t->p1.y - t->p0.y, dz = t->p1.z - t->p0.z;
+        /* the LET weights: the step length from differences squared in the stepping type, summed in double */
+        const real density = rho * RC(1000.0);
+        const real dx = t->p1.x - t->p0.x, dy = t->p1.y - t->p0.y, dz = t->p1.z - t->p0.z;
         double length = (double) (dx * dx);
         double let;
         length += (double) (dy * dy);
@@ -669,7 +711,7 @@ int mqo_transport(const mqo_grid* g, const mqo_config* cfg, const float* V, uint
     if (!S.t) return -3;
     E.g = g;
     E.dbg = cfg->physics_debug;
-    E.tcut = cfg->physics_debug ? 0.08511f : 0.0815f;
+    E.tcut = cfg->physics_debug ? RC(0.08511) : RC(0.0815);
     E.stk = &S;
     E.rng.k0 = (uint32_t) seed;
     E.rng.k1 = (uint32_t) (seed >> 32);
@@ -701,23 +743,24 @@ int mqo_transport(const mqo_grid* g, const mqo_config* cfg, const float* V, uint
             cy = index_scan(g->ye, g->ny, t.p0.y, t.d0.y);
             cz = index_scan(g->ze, g->nz, t.p0.z, t.d0.z);
             if (!valid(g, cx, cy, cz)) {
-                float e = intersect_box(g, t.p0, &t.d0);
+                real e = intersect_box(g, t.p0, &t.d0);
                 if (e < 0) continue;
                 t.p1 = advance(t.p0, t.d0, e);
-                t.p0 = t.p1; t.d0 = t.d1; t.ke0 = t.ke1; t.dE = t.ldE = 0.0f;
+                t.p0 = t.p1; t.d0 = t.d1; t.ke0 = t.ke1; t.dE = t.ldE = RC(0.0);
                 cx = index_scan(g->xe, g->nx, t.p0.x, t.d0.x);
                 cy = index_scan(g->ye, g->ny, t.p0.y, t.d0.y);
                 cz = index_scan(g->ze, g->nz, t.p0.z, t.d0.z);
             }
             while (valid(g, cx, cy, cz) && !t.stopped) {
                 uint64_t cnb = (uint64_t) cz * g->nx * g->ny + (uint64_t) cy * g->nx + cx;
-                float rho = g->rho[cnb];
-                float d2b = intersect_voxel(g, t.p0, &t.d0, cx, cy, cz);
+                real rho = g->rho[cnb];
+                real d2b = intersect_voxel(g, t.p0, &t.d0, cx, cy, cz);
                 stepping(&E, &t, rho, d2b);
                 if (st) st->steps++;
                 if (d2b < 0) break;
                 if (cnb > 0) {   /* DIRECT ROI: roi_->idx(cnb) > 0 */
-                    float vol = (g->xe[cx + 1] - g->xe[cx]) * (g->ye[cy + 1] - g->ye[cy]) * (g->ze[cz + 1] - g->ze[cz]);
+                    real vol = ((real) g->xe[cx + 1] - (real) g->xe[cx]) * ((real) g->ye[cy + 1] - (real) g->ye[cy]) *
+                               ((real) g->ze[cz + 1] - (real) g->ze[cz]);
                     double val = hit(cfg, &t, rho, vol, E.dbg);
                     if (val > 0) {
                         tally[cnb] += val;
@@ -726,7 +769,7 @@ int mqo_transport(const mqo_grid* g, const mqo_config* cfg, const float* V, uint
                 }
                 if (!t.stopped) {
                     index_update(g, t.p1, t.d1, &cx, &cy, &cz);
-                    t.p0 = t.p1; t.d0 = t.d1; t.ke0 = t.ke1; t.dE = t.ldE = 0.0f;
+                    t.p0 = t.p1; t.d0 = t.d1; t.ke0 = t.ke1; t.dE = t.ldE = RC(0.0);
                 }
             }
         }

@@ -40,28 +40,29 @@ class _Stats(C.Structure):
     _fields_ = [(n, C.c_uint64) for n in ("histories", "tracks", "steps", "pushed", "dropped")]
 
 
-_lib = None
+_libs = {}
 
 
-def lib():
-    global _lib
-    if _lib is None:
-        path = _build().build_restatement()
-        _lib = C.CDLL(path)
-        _lib.mqo_transport.restype = C.c_int
-        _lib.mqo_transport.argtypes = [C.POINTER(_Grid), C.POINTER(_Cfg), C.c_void_p, C.c_uint64, C.c_uint64,
-                                       C.c_uint64, C.c_void_p, C.c_void_p, C.POINTER(_Stats)]
-        _lib.mqo_eval_physics.restype = None
-        _lib.mqo_eval_physics.argtypes = [C.c_void_p, C.c_uint64, C.c_void_p]
-        _lib.mqo_spr.restype = C.c_float
-        _lib.mqo_spr.argtypes = [C.c_float, C.c_float, C.c_int]
-        _lib.mqo_x0.restype = C.c_float
-        _lib.mqo_x0.argtypes = [C.c_float, C.c_int]
-        _lib.mqo_hu_to_density.restype = C.c_float
-        _lib.mqo_hu_to_density.argtypes = [C.c_int]
-        _lib.mqo_trace_ray.restype = C.c_int
-        _lib.mqo_trace_ray.argtypes = [C.POINTER(_Grid), C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
-    return _lib
+def lib(fp64: bool = False):
+    """The C restatement: FP32 stepping, or the all-FP64 build (same source, -DMQO_FP64)."""
+    if fp64 not in _libs:
+        path = _build().build_restatement(fp64=fp64)
+        L = C.CDLL(path)
+        L.mqo_transport.restype = C.c_int
+        L.mqo_transport.argtypes = [C.POINTER(_Grid), C.POINTER(_Cfg), C.c_void_p, C.c_uint64, C.c_uint64,
+                                    C.c_uint64, C.c_void_p, C.c_void_p, C.POINTER(_Stats)]
+        L.mqo_eval_physics.restype = None
+        L.mqo_eval_physics.argtypes = [C.c_void_p, C.c_uint64, C.c_void_p]
+        L.mqo_spr.restype = C.c_float
+        L.mqo_spr.argtypes = [C.c_float, C.c_float, C.c_int]
+        L.mqo_x0.restype = C.c_float
+        L.mqo_x0.argtypes = [C.c_float, C.c_int]
+        L.mqo_hu_to_density.restype = C.c_float
+        L.mqo_hu_to_density.argtypes = [C.c_int]
+        L.mqo_trace_ray.restype = C.c_int
+        L.mqo_trace_ray.argtypes = [C.POINTER(_Grid), C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+        _libs[fp64] = L
+    return _libs[fp64]
 
 
 def _p(a):
@@ -79,24 +80,25 @@ class Grid:
 
 
 def transport(grid: Grid, vertices: np.ndarray, h0: int, h1: int, seed: int, physics_debug: bool, scorer: int = 2,
-              per_history: bool = False):
-    """Run the C restatement; returns (tally, per_history_sums or None, stats dict)."""
+              per_history: bool = False, fp64: bool = False):
+    """Run the C restatement (the all-FP64 build with fp64); returns (tally, per_history_sums or
+    None, stats dict)."""
     v = np.ascontiguousarray(vertices).view(np.float32).reshape(-1, 7)
     tally = np.zeros(grid.rho.size, np.float64)
     ph = np.zeros(h1 - h0, np.float64) if per_history else None
     st = _Stats()
     cfg = _Cfg(int(physics_debug), scorer)
-    rc = lib().mqo_transport(C.byref(grid.c), C.byref(cfg), _p(v), h0, h1, seed, _p(tally),
+    rc = lib(fp64).mqo_transport(C.byref(grid.c), C.byref(cfg), _p(v), h0, h1, seed, _p(tally),
                              None if ph is None else _p(ph), C.byref(st))
     if rc != 0:
         raise RuntimeError(f"mqo_transport failed: {rc}")
     return tally, ph, {n: int(getattr(st, n)) for n, _ in st._fields_}
 
 
-def eval_physics(energies: np.ndarray) -> np.ndarray:
+def eval_physics(energies: np.ndarray, fp64: bool = False) -> np.ndarray:
     e = np.ascontiguousarray(energies, np.float32)
     out = np.empty((len(e), 8), np.float32)
-    lib().mqo_eval_physics(_p(e), len(e), _p(out))
+    lib(fp64).mqo_eval_physics(_p(e), len(e), _p(out))
     return out
 
 

@@ -131,6 +131,48 @@ def test_oracle_dose_matches_reference_c2(golden, oracle):
     assert dr80 <= 0.2, (r_ref, r_test)
 
 
+def test_fp64_oracle_physics_is_the_same_functions(golden, oracle):
+    """The all-FP64 build evaluates the same tabulated physics: within the reference's own FP32
+    rounding (the largest differences are FP32 cancellation in beta^2, Te_max and the momentum
+    just above the 0.1 MeV table start)."""
+    p = golden("physics.npz")
+    e = p["energies"]
+    # inside the tables: at an FP32 energy equal to a table bound (e.g. 299.6f) the FP64 comparison
+    # with the double bound 299.6 falls outside, as it would in moqui instantiated with R = double
+    inside = (e > 0.6) & (e < 299.5)
+    out = oracle.eval_physics(e, fp64=True)
+    for k, name in enumerate(["cs_ion", "cs_pp", "cs_poe", "cs_poi", "dedx", "beta_sq", "te_max", "momentum"]):
+        np.testing.assert_allclose(out[inside, k], p[name][inside], rtol=1e-3, atol=1e-30, err_msg=name)
+    hi = inside & (e >= 1.0)   # away from the cancellation at the lowest energies: FP32 rounding
+    np.testing.assert_allclose(out[hi, 5], p["beta_sq"][hi], rtol=2e-4)
+    np.testing.assert_allclose(out[hi, 7], p["momentum"][hi], rtol=2e-4)
+
+
+def test_fp64_oracle_dose_matches_reference_c2(golden, oracle):
+    """Slab phantom: the all-FP64 restatement (1.6e4 histories) against the reference's FP32 CPU
+    build (1e5 histories), and against the FP32 restatement on the same random streams."""
+    gd = golden("dose_c2.npz")
+    wl = workloads.c2()
+    xe, ye, ze = wl.edges()
+    lut = {int(h): oracle.hu_to_density(int(h)) for h in np.unique(wl.hu)}
+    rho = np.vectorize(lut.get)(wl.hu).astype(np.float32).reshape(-1)
+    grid = oracle.Grid(xe, ye, ze, rho)
+    b64, tot32, tot64 = [], 0.0, 0.0
+    each = 2000
+    for b in range(8):
+        v = wl.vertices(each, 900 + b)
+        t64, _, _ = oracle.transport(grid, v, 0, each, 177 + b, False, fp64=True)
+        t32, _, _ = oracle.transport(grid, v, 0, each, 177 + b, False)
+        b64.append(ph.depth_dose(t64, wl.nxyz) / each)
+        tot32 += t32.sum()
+        tot64 += t64.sum()
+    frac, dr80, r_ref, r_test = _compare_idd(gd["idd"], np.array(b64), 1.0)
+    assert frac >= 0.95, frac
+    assert dr80 <= 0.2, (r_ref, r_test)
+    # identical draws: FP32 arithmetic moves the total dose by far less than the statistics do
+    assert abs(tot64 / tot32 - 1.0) <= 2e-3, tot64 / tot32
+
+
 def test_slab_workload_geometry():
     wl = workloads.c2(histories=10)
     lung, bone = wl.meta["lung_depth_mm"], wl.meta["bone_depth_mm"]
