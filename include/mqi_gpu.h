@@ -120,6 +120,25 @@ int mqi_set_stream(mqi_ctx* ctx, void* cuda_stream);
  * kernel argument of the same name (mqi_transport.hpp:123). */
 int mqi_set_physics(mqi_ctx* ctx, int physics_debug, int score_local_deposit);
 
+/* ---- calibration plug-in: material_t::compute_rsp_ / compute_rl_
+ *      (moqui/base/materials/mqi_material.hpp:10-25) ------------------------------------------ */
+#define MQI_CALIB_DEFAULT 0 /* spr_default / radiation_length_default (mqi_patient_materials.hpp:414-473) */
+#define MQI_CALIB_TABLE   1 /* SPR(rho, E) and X0(rho) tabulated on uniform grids */
+
+/* Select the stopping-power-ratio and radiation-length curves.  moqui's patient material installs
+ * spr_default and radiation_length_default as its compute_rsp_ / compute_rl_ function pointers
+ * (mqi_patient_materials.hpp:474-497); a user material installs its own.  Device function pointers
+ * cannot cross a C ABI, so a custom curve is given as tables on uniform grids:
+ *   spr[i_rho * n_e + i_e] at rho = rho0 + i_rho * drho (g/mm^3) and E = e0 + i_e * de (MeV);
+ *   x0[i_rho] (radiation length, mm) at the same densities.
+ * SPR is interpolated bilinearly and X0 linearly, with the fractional index (x - x0) / dx clamped
+ * to the grid (n_rho, n_e >= 2; drho, de > 0; every entry finite, X0 > 0).  Voxels below 1e-7 g/mm^3
+ * stay vacuum and above 99.9 stay stops, as with the default curves; the default curves' water
+ * shortcut of debug physics does not apply to tables.  calib = MQI_CALIB_DEFAULT restores the
+ * default curves (the other arguments are then ignored).  Applies to transports started after it. */
+int mqi_set_calibration(mqi_ctx* ctx, int calib, uint32_t n_rho, float rho0, float drho, uint32_t n_e, float e0,
+                        float de, const float* spr, const float* x0);
+
 /* Add a child geometry to the world: a rectilinear voxel grid with nx+1/ny+1/nz+1 edges (mm),
  * an optional rotation (row-major 3x3, fwd = child->world; NULL = identity) and translation
  * (NULL = 0).  Replaces the grid3d construction + upload_node/add_node_geometry

@@ -28,6 +28,8 @@ LETD_NUM, LETD_DEN, LETT_NUM, LETT_DEN = 5, 6, 7, 8
 EDEP_PRIMARY, EDEP_SECONDARY, DIJ = 9, 10, 11
 # roi methods
 ROI_DIRECT, ROI_INDIRECT, ROI_CONTOUR = 0, 1, 2
+# calibration curves
+CALIB_DEFAULT, CALIB_TABLE = 0, 1
 
 # every exported symbol declared in include/mqi_gpu.h
 EXPORTS = (
@@ -39,7 +41,7 @@ EXPORTS = (
     "mqi_get_batch_mean", "mqi_scale_tally", "mqi_run_until_stat", "mqi_set_spot_plan", "mqi_transport_plan",
     "mqi_sample_plan", "mqi_add_dij_scorer", "mqi_dij_build", "mqi_dij_get_csr", "mqi_dij_info",
     "mqi_dij_matvec", "mqi_dij_rmatvec", "mqi_set_scenarios", "mqi_run_plan_until_stat", "mqi_set_launch_mode",
-    "mqi_autotune",
+    "mqi_autotune", "mqi_set_calibration",
 )
 
 VERTEX_DTYPE = np.dtype([("ke", "<f4"), ("pos", "<f4", (3,)), ("dir", "<f4", (3,))])
@@ -51,6 +53,28 @@ SPOT_DTYPE = np.dtype({"names": ["energy", "energy_sigma", "mean", "sigma", "cor
                        "formats": ["<f4", "<f4", ("<f4", (5,)), ("<f4", (5,)), ("<f4", (2,)), ("<f4", (9,)),
                                    ("<f4", (3,)), "<u8"],
                        "offsets": [0, 4, 8, 28, 48, 56, 92, 104], "itemsize": 112})
+
+
+class CalibTable:
+    """SPR(rho, E) and X0(rho) on uniform grids: spr has shape (n_rho, n_e), x0 shape (n_rho,);
+    rho in g/mm^3, E in MeV, X0 in mm (mqi_set_calibration)."""
+
+    def __init__(self, rho0: float, drho: float, e0: float, de: float, spr, x0):
+        self.spr = np.ascontiguousarray(spr, np.float32)
+        self.x0 = np.ascontiguousarray(x0, np.float32)
+        if self.spr.ndim != 2 or self.x0.shape != (self.spr.shape[0],):
+            raise ValueError("spr must be (n_rho, n_e) and x0 (n_rho,)")
+        self.n_rho, self.n_e = self.spr.shape
+        self.rho0, self.drho, self.e0, self.de = float(rho0), float(drho), float(e0), float(de)
+
+    @classmethod
+    def sample(cls, spr_fn, x0_fn, rho0, drho, n_rho, e0, de, n_e):
+        """Tabulate curves given as functions (spr_fn(rho, E), x0_fn(rho)) on the grids."""
+        rho = (rho0 + drho * np.arange(n_rho)).astype(np.float32)
+        e = (e0 + de * np.arange(n_e)).astype(np.float32)
+        spr = np.array([[spr_fn(float(r), float(x)) for x in e] for r in rho], np.float32)
+        x0 = np.array([x0_fn(float(r)) for r in rho], np.float32)
+        return cls(rho0, drho, e0, de, spr, x0)
 
 
 class MqiStats(C.Structure):
@@ -92,6 +116,7 @@ def load(path: Optional[str] = None) -> C.CDLL:
         "mqi_last_error": (C.c_char_p, [vp]),
         "mqi_set_stream": (i32, [vp, vp]),
         "mqi_set_physics": (i32, [vp, i32, i32]),
+        "mqi_set_calibration": (i32, [vp, i32, u32, f32, f32, u32, f32, f32, vp, vp]),
         "mqi_add_child": (i32, [vp, i32, i32, i32, vp, vp, vp, vp, vp, P(i32)]),
         "mqi_set_density": (i32, [vp, i32, vp, i32]),
         "mqi_set_hu": (i32, [vp, i32, vp, f32, i32]),
@@ -178,6 +203,17 @@ class Context:
     # ---- setup ----
     def set_physics(self, physics_debug: bool, score_local_deposit: bool = True) -> None:
         self._check(self.lib.mqi_set_physics(self.h, int(physics_debug), int(score_local_deposit)), self.h)
+
+    def set_calibration(self, table=None) -> None:
+        """Tabulated SPR(rho, E) / X0(rho) curves (a CalibTable), or None for moqui's default
+        curves (spr_default / radiation_length_default)."""
+        if table is None:
+            self._check(self.lib.mqi_set_calibration(self.h, CALIB_DEFAULT, 0, 0.0, 0.0, 0, 0.0, 0.0, None, None), self.h)
+            return
+        spr = np.ascontiguousarray(table.spr, np.float32)
+        x0 = np.ascontiguousarray(table.x0, np.float32)
+        self._check(self.lib.mqi_set_calibration(self.h, CALIB_TABLE, table.n_rho, table.rho0, table.drho, table.n_e,
+                                                 table.e0, table.de, spr.ctypes.data, x0.ctypes.data), self.h)
 
     def set_tuning(self, block: int = 0, blocks_per_sm: int = 0, slice_steps: int = -1, primary_chunk: int = 0) -> None:
         self._check(self.lib.mqi_set_tuning(self.h, block, blocks_per_sm, slice_steps, primary_chunk), self.h)

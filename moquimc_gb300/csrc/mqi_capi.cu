@@ -6,6 +6,7 @@
 // receives what it reads by value.
 #include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -155,6 +156,7 @@ mqi_destroy(mqi_ctx* c) {
     cudaFree(c->counters);
     cudaFree(c->stats);
     cudaFree(c->tables);
+    cudaFree(c->calib_buf);
     if (c->host_counts) cudaFreeHost(c->host_counts);
     if (c->host_next) cudaFreeHost(c->host_next);
     cudaFree(c->topup);
@@ -221,6 +223,46 @@ mqi_set_physics(mqi_ctx* c, int physics_debug, int score_local_deposit) {
     if (!valid_ctx(c)) return fail(c, MQI_ERR_INVALID, "mqi_set_physics: ctx is NULL");
     c->physics_debug = physics_debug ? 1 : 0;
     c->score_local   = score_local_deposit ? 1 : 0;
+    return MQI_OK;
+}
+
+int
+mqi_set_calibration(mqi_ctx* c, int calib, uint32_t n_rho, float rho0, float drho, uint32_t n_e, float e0, float de,
+                    const float* spr, const float* x0) {
+    if (!valid_ctx(c)) return fail(c, MQI_ERR_INVALID, "mqi_set_calibration: ctx is NULL");
+    if (calib == MQI_CALIB_DEFAULT) {
+        c->calib = CalibDev{};
+        return MQI_OK;
+    }
+    if (calib != MQI_CALIB_TABLE) return fail(c, MQI_ERR_INVALID, "mqi_set_calibration: unknown calibration");
+    if (n_rho < 2 || n_e < 2 || !(drho > 0.0f) || !(de > 0.0f) || !std::isfinite(rho0) || !std::isfinite(e0) ||
+        !std::isfinite(drho) || !std::isfinite(de) || !spr || !x0 || n_rho > (1u << 20) || n_e > (1u << 20) ||
+        (uint64_t) n_rho * n_e > (1ull << 26))
+        return fail(c, MQI_ERR_INVALID, "mqi_set_calibration: tables need n >= 2, positive finite pitches, data");
+    const size_t n_spr = (size_t) n_rho * n_e;
+    for (size_t i = 0; i < n_spr; ++i)
+        if (!std::isfinite(spr[i])) return fail(c, MQI_ERR_INVALID, "mqi_set_calibration: SPR table is not finite");
+    for (uint32_t i = 0; i < n_rho; ++i)
+        if (!std::isfinite(x0[i]) || !(x0[i] > 0.0f))
+            return fail(c, MQI_ERR_INVALID, "mqi_set_calibration: X0 table must be finite and positive");
+    DeviceGuard g(c->device);
+    cudaStreamSynchronize(c->stream);   // a running transport may still read the previous tables
+    cudaFree(c->calib_buf);
+    c->calib_buf = nullptr;
+    c->calib     = CalibDev{};
+    MQI_CUDA(c, cudaMalloc(&c->calib_buf, (n_spr + n_rho) * sizeof(float)), "mqi_set_calibration");
+    MQI_CUDA(c, cudaMemcpy(c->calib_buf, spr, n_spr * sizeof(float), cudaMemcpyHostToDevice), "mqi_set_calibration");
+    MQI_CUDA(c, cudaMemcpy(c->calib_buf + n_spr, x0, n_rho * sizeof(float), cudaMemcpyHostToDevice),
+             "mqi_set_calibration");
+    c->calib.mode  = MQI_CALIB_TABLE;
+    c->calib.n_rho = n_rho;
+    c->calib.n_e   = n_e;
+    c->calib.rho0  = rho0;
+    c->calib.drho  = drho;
+    c->calib.e0    = e0;
+    c->calib.de    = de;
+    c->calib.spr   = c->calib_buf;
+    c->calib.x0    = c->calib_buf + n_spr;
     return MQI_OK;
 }
 
@@ -419,6 +461,7 @@ constexpr uint32_t kSourceKeyXor = 0xA5A5A5A5u;
 void
 make_wave_params(mqi_ctx* c, uint64_t seed, WaveParams& P) {
     P = WaveParams{};
+    P.calib      = c->calib;
     P.n_children = (int) c->children.size();
     for (int i = 0; i < P.n_children; ++i) {
         const ChildHost& h = c->children[i];

@@ -126,6 +126,8 @@ struct mqi_ctx {
     unsigned long long*     stats = nullptr;        // 8 x u64
     uint32_t*               host_counts = nullptr;  // pinned: 4 x u32
     float*                  tables = nullptr;       // 6*600 physics + 3996 HU correction
+    mqi_gpu::CalibDev       calib{};                // SPR / X0 curves (mode 0: the defaults)
+    float*                  calib_buf = nullptr;    // device: the tables of calib (SPR then X0)
     int                     num_sms = 0;
     int                     wave_block = 128;
     int                     wave_grid = 0;

@@ -90,6 +90,15 @@ struct Queue {
 };
 
 /// Kernel parameters for one transport wave.
+/// A tabulated calibration (mqi_set_calibration); mode 0 = the default curves.
+struct CalibDev {
+    int          mode;
+    uint32_t     n_rho, n_e;
+    float        rho0, drho, e0, de;
+    const float* spr;   // device: n_rho x n_e, E fastest
+    const float* x0;    // device: n_rho
+};
+
 struct WaveParams {
     int       n_children;
     ChildDev  child[kMaxChildren];
@@ -118,6 +127,7 @@ struct WaveParams {
     int             smem_edge_floats; // shared-memory floats for staged child edges
     const float*    tables;     // device: the six physics tables, 6 x 600 floats in Tables order
                                 // (followed by the 3996 HU density-correction factors)
+    CalibDev        calib;      // SPR / X0 curves
 };
 
 std::string& thread_error_slot();

@@ -57,6 +57,61 @@ struct Ctx {
     uint32_t          n_sec, n_local, n_drop, n_err;
 };
 
+// ------------------------------------------------------------------------------------------
+// Calibration plug-in (material_t::compute_rsp_ / compute_rl_, materials/mqi_material.hpp:10-25):
+// the default curves, or tables on uniform grids (mqi_set_calibration).
+// ------------------------------------------------------------------------------------------
+
+/// Lower node and upper weight of x on a uniform grid of n >= 2 nodes, clamped to the grid.
+__device__ inline float
+calib_index(float x, float x0, float dx, uint32_t n, int& i) {
+    const float f = (x - x0) / dx;
+    if (!(f > 0.0f)) {
+        i = 0;
+        return 0.0f;
+    }
+    if (f >= (float) (n - 1)) {
+        i = (int) n - 2;
+        return 1.0f;
+    }
+    i = (int) f;
+    return f - (float) i;
+}
+
+/// SPR(rho, E) from the table, bilinear (E first).
+__device__ __noinline__ float
+spr_table(const CalibDev& c, float rho, float Ek) {
+    int         ir, ie;
+    const float wr = calib_index(rho, c.rho0, c.drho, c.n_rho, ir);
+    const float we = calib_index(Ek, c.e0, c.de, c.n_e, ie);
+    const float* r0 = c.spr + (size_t) ir * c.n_e;
+    const float* r1 = r0 + c.n_e;
+    const float  a  = r0[ie] + we * (r0[ie + 1] - r0[ie]);
+    const float  b  = r1[ie] + we * (r1[ie + 1] - r1[ie]);
+    return a + wr * (b - a);
+}
+
+/// X0(rho) from the table, linear.
+__device__ __noinline__ float
+x0_table(const CalibDev& c, float rho) {
+    int         ir;
+    const float wr = calib_index(rho, c.rho0, c.drho, c.n_rho, ir);
+    return c.x0[ir] + wr * (c.x0[ir + 1] - c.x0[ir]);
+}
+
+/// The run's stopping-power ratio (compute_rsp_): the tables are out of line, so the default
+/// curve's step loop carries one uniform branch and a call.
+__device__ __forceinline__ float
+spr_of(const CalibDev& c, float rho, float Ek, bool dbg) {
+    return c.mode ? spr_table(c, rho, Ek) : spr_default(rho, Ek, dbg);
+}
+
+/// The run's radiation length (compute_rl_).
+__device__ __forceinline__ float
+x0_of(const CalibDev& c, float rho, bool dbg) {
+    return c.mode ? x0_table(c, rho) : radiation_length_default(rho, dbg);
+}
+
 __device__ inline Grid
 make_grid(const ChildDev& c, const float* sxe, const float* sye, const float* sze) {
     Grid g;
@@ -267,7 +322,7 @@ score_step(Ctx& C, const Trk& t, uint32_t cnb, float rho, float vol) {
         const ScorerDev& s  = C.P->scorer[0];
         float            vf = t.dE + t.ldE;
         if (s.type == MQI_SCORER_DOSE_W) {
-            const float spr = t.spr0 >= 0.0f ? t.spr0 : spr_default(rho, t.ke0, C.dbg);
+            const float spr = t.spr0 >= 0.0f ? t.spr0 : spr_of(C.P->calib, rho, t.ke0, C.dbg);
             vf              = (rho < 1.0e-7f) ? 0.0f : vf * 1.60218e-10f / (vol * rho * spr);
         }
         tally_add(s.tally, cnb, (double) vf, cnb > 0 && vf > 0.0f);
@@ -275,7 +330,7 @@ score_step(Ctx& C, const Trk& t, uint32_t cnb, float rho, float vol) {
     }
     const WaveParams& P   = *C.P;
     const ChildDev&   ch  = P.child[C.child];
-    const float       spr = t.spr0 >= 0.0f ? t.spr0 : spr_default(rho, t.ke0, C.dbg);
+    const float       spr = t.spr0 >= 0.0f ? t.spr0 : spr_of(P.calib, rho, t.ke0, C.dbg);
     // dose_to_water of the step, shared by the dose, dose^2 and Dij scorers (Dw_pointer,
     // mqi_scorer_energy_deposit.hpp:23-40): 0 in vacuum voxels
     const float dose_w = (rho < 1.0e-7f) ? 0.0f : (t.dE + t.ldE) * 1.60218e-10f / (vol * rho * spr);
@@ -355,10 +410,10 @@ to_world(const Grid& g, float3& p, float3& d) {
 /// track_t::update_post_vertex_position with the last_step length
 /// (p_ionization_tabulated::last_step, mqi_p_ionization.hpp:481-490).
 __device__ __noinline__ float3
-last_step_pos(const Tables* T, bool dbg, float3 p0, float3 d0, float ke0, float dE, float rho) {
+last_step_pos(const Tables* T, const CalibDev* cal, bool dbg, float3 p0, float3 d0, float ke0, float dE, float rho) {
     float lw = 0.0f;
     if (dE > 0.0f) lw = -dE / dedx_lookup(*T, ke0);
-    const float sl = lw * kWaterDensity / (spr_default(rho, ke0, dbg) * rho);
+    const float sl = lw * kWaterDensity / (spr_of(*cal, rho, ke0, dbg) * rho);
     return make_float3(p0.x + d0.x * sl, p0.y + d0.y * sl, p0.z + d0.z * sl);
 }
 
@@ -385,7 +440,7 @@ score_local_daughter(Ctx& C, float3 pw, float3 dw, float ke0, float dE0) {
     t.primary = false;
     if (rho <= 99.9f) {
         t.dE += t.ke0;
-        t.p1 = last_step_pos(C.T, C.dbg, p, d, t.ke0, t.dE, rho);
+        t.p1 = last_step_pos(C.T, &C.P->calib, C.dbg, p, d, t.ke0, t.dE, rho);
     }
     score_step(C, t, cnb, rho, grid_volume(C.g, t.cell));
     return true;
@@ -491,7 +546,7 @@ along_step(Ctx& C, Trk& t, const Rel& rel, float len, float rho, float spr, floa
         t.stopped = true;
     }
     const float P     = rel.momentum();
-    const float X0    = radiation_length_default(rho, C.dbg);
+    const float X0    = x0_of(C.P->calib, rho, C.dbg);
     const float th_sq = ((kEs / P) * (kEs / P) / rel.beta_sq) * len / X0;
     float       th    = sqrtf(th_sq);
     th                = z_mcs * (sqrtf(2.0f) * th);
@@ -665,14 +720,14 @@ stepping(Ctx& C, Trk& t, Rng& rng, float rho, float d2b) {
         if (t.ke0 < 0.0f) t.ke0 = 0.0f;
         t.dE += t.ke0;
         t.ke1 -= t.ke0;
-        t.p1      = last_step_pos(C.T, C.dbg, t.p0, t.d0, t.ke0, t.dE, rho);
+        t.p1      = last_step_pos(C.T, &C.P->calib, C.dbg, t.p0, t.d0, t.ke0, t.dE, rho);
         t.stopped = true;
         return;
     }
     const Tables& T = *C.T;
     rng.begin_step();
     const Rel   rel(t.ke0);
-    const float spr      = spr_default(rho, t.ke0, C.dbg);
+    const float spr      = spr_of(C.P->calib, rho, t.ke0, C.dbg);
     const float dedx     = dedx_lookup(T, rel.Ek);
     const float cur_min  = kMaxStep * spr * rho / kWaterDensity;
     const float max_loss = -1.0f * cur_min * dedx;

@@ -186,6 +186,37 @@ static real x0_of(real rho, int dbg) {
     return (WATER_DENSITY * X0_WATER) / (d * RC(0.001) * f);
 }
 
+/* The tabulated calibration (the material plug-in, materials/mqi_material.hpp:10-25, as tables):
+ * lower node and upper weight of x on a uniform grid of n >= 2 nodes, clamped to the grid. */
+static real calib_index(real x, real x0, real dx, uint32_t n, int* i) {
+    const real f = (x - x0) / dx;
+    if (!(f > RC(0.0))) { *i = 0; return RC(0.0); }
+    if (f >= (real) (n - 1)) { *i = (int) n - 2; return RC(1.0); }
+    *i = (int) f;
+    return f - (real) *i;
+}
+
+static real spr_table(const mqo_calib* c, real rho, real Ek) {
+    int ir, ie;
+    const real wr = calib_index(rho, c->rho0, c->drho, c->n_rho, &ir);
+    const real we = calib_index(Ek, c->e0, c->de, c->n_e, &ie);
+    const float* r0 = c->spr + (size_t) ir * c->n_e;
+    const float* r1 = r0 + c->n_e;
+    const real a = r0[ie] + we * ((real) r0[ie + 1] - (real) r0[ie]);
+    const real b = r1[ie] + we * ((real) r1[ie + 1] - (real) r1[ie]);
+    return a + wr * (b - a);
+}
+
+static real x0_table(const mqo_calib* c, real rho) {
+    int ir;
+    const real wr = calib_index(rho, c->rho0, c->drho, c->n_rho, &ir);
+    return c->x0[ir] + wr * ((real) c->x0[ir + 1] - (real) c->x0[ir]);
+}
+
+static real spr_cal(const mqo_calib* c, real rho, real Ek, int dbg) { return c ? spr_table(c, rho, Ek) : spr_of(rho, Ek, dbg); }
+
+static real x0_cal(const mqo_calib* c, real rho, int dbg) { return c ? x0_table(c, rho) : x0_of(rho, dbg); }
+
 float mqo_spr(float rho, float Ek, int dbg) { return (float) spr_of(rho, Ek, dbg); }
 
 float mqo_x0(float rho, int dbg) { return (float) x0_of(rho, dbg); }
@@ -371,6 +402,7 @@ typedef struct {
 typedef struct {
     const mqo_grid*  g;
     int              dbg;
+    const mqo_calib* calib;
     real            tcut;
     stack_t_*        stk;
     rng_t            rng;
@@ -468,7 +500,7 @@ static real energy_loss(rel_t* rel, real rho, real len, real spr, real z) {
 static void last_step(env_t* E, trk_t* t, real rho) {
     real lw = RC(0.0), sl;
     if (t->dE > 0) lw = -t->dE / dedx(t->ke0);
-    sl = lw * WATER_DENSITY / (spr_of(rho, t->ke0, E->dbg) * rho);
+    sl = lw * WATER_DENSITY / (spr_cal(E->calib, rho, t->ke0, E->dbg) * rho);
     t->p1 = advance(t->p0, t->d0, sl);
 }
 
@@ -482,7 +514,7 @@ static void along_step(env_t* E, trk_t* t, real len, real rho, real spr, real z1
         t->stopped = 1;
     }
     P = momentum(&rel);
-    X0 = x0_of(rho, E->dbg);
+    X0 = x0_cal(E->calib, rho, E->dbg);
     th_sq = ((ES / P) * (ES / P) / rel.beta_sq) * len / X0;
     th = RSQRT(th_sq);
     th = z2 * (RSQRT(RC(2.0)) * th);
@@ -616,7 +648,7 @@ static void stepping(env_t* E, trk_t* t, real rho, real d2b) {
     }
     rng_begin_step(&E->rng);
     rel = rel_of(t->ke0);
-    spr = spr_of(rho, t->ke0, E->dbg);
+    spr = spr_cal(E->calib, rho, t->ke0, E->dbg);
     dd = dedx(rel.Ek);
     cur_min = RC(1.0) * spr * rho / WATER_DENSITY;
     max_loss = -RC(1.0) * cur_min * dd;
@@ -672,7 +704,7 @@ static double hit(const mqo_config* cfg, const trk_t* t, real rho, real vol, int
     case 3: {
         double d;
         if (rho < RC(1.0e-7)) return 0.0;
-        d = (double) (edep * RC(1.60218e-10) / (vol * rho * spr_of(rho, t->ke0, dbg)));
+        d = (double) (edep * RC(1.60218e-10) / (vol * rho * spr_cal(cfg->calib, rho, t->ke0, dbg)));
         return cfg->scorer == 3 ? d * d : d;
     }
     case 4: return t->primary ? (double) t->dE * 1.60218e-13 * 1000.0 / (double) (vol * rho) : 0.0;
@@ -711,6 +743,7 @@ int mqo_transport(const mqo_grid* g, const mqo_config* cfg, const float* V, uint
     if (!S.t) return -3;
     E.g = g;
     E.dbg = cfg->physics_debug;
+    E.calib = cfg->calib;
     E.tcut = cfg->physics_debug ? RC(0.08511) : RC(0.0815);
     E.stk = &S;
     E.rng.k0 = (uint32_t) seed;

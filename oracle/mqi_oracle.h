@@ -30,9 +30,19 @@ typedef struct {
     const float* rho; /* g/mm^3, x fastest */
 } mqo_grid;
 
+/* A tabulated SPR(rho, E) / X0(rho) calibration on uniform grids (mqi_set_calibration's
+ * MQI_CALIB_TABLE): spr[i_rho * n_e + i_e], x0[i_rho]; bilinear / linear, clamped to the grid. */
 typedef struct {
-    int physics_debug; /* 1: moqui built with __PHYSICS_DEBUG__ */
-    int scorer;        /* 1 EDEP, 2 DOSE_W, 3 DOSE_W2 (mqi_gpu.h numbering) */
+    uint32_t     n_rho, n_e;
+    float        rho0, drho, e0, de;
+    const float* spr;
+    const float* x0;
+} mqo_calib;
+
+typedef struct {
+    int              physics_debug; /* 1: moqui built with __PHYSICS_DEBUG__ */
+    int              scorer;        /* 1 EDEP, 2 DOSE_W, 3 DOSE_W2 (mqi_gpu.h numbering) */
+    const mqo_calib* calib;         /* NULL: spr_default / radiation_length_default */
 } mqo_config;
 
 typedef struct {

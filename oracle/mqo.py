@@ -32,8 +32,13 @@ class _Grid(C.Structure):
                 ("ze", C.c_void_p), ("rho", C.c_void_p)]
 
 
+class _Calib(C.Structure):
+    _fields_ = [("n_rho", C.c_uint32), ("n_e", C.c_uint32), ("rho0", C.c_float), ("drho", C.c_float),
+                ("e0", C.c_float), ("de", C.c_float), ("spr", C.c_void_p), ("x0", C.c_void_p)]
+
+
 class _Cfg(C.Structure):
-    _fields_ = [("physics_debug", C.c_int), ("scorer", C.c_int)]
+    _fields_ = [("physics_debug", C.c_int), ("scorer", C.c_int), ("calib", C.POINTER(_Calib))]
 
 
 class _Stats(C.Structure):
@@ -80,14 +85,20 @@ class Grid:
 
 
 def transport(grid: Grid, vertices: np.ndarray, h0: int, h1: int, seed: int, physics_debug: bool, scorer: int = 2,
-              per_history: bool = False, fp64: bool = False):
-    """Run the C restatement (the all-FP64 build with fp64); returns (tally, per_history_sums or
-    None, stats dict)."""
+              per_history: bool = False, fp64: bool = False, calib=None):
+    """Run the C restatement (the all-FP64 build with fp64; `calib` an object with n_rho, n_e, rho0,
+    drho, e0, de, spr, x0 for tabulated SPR / X0 curves); returns (tally, per_history_sums or None,
+    stats dict)."""
     v = np.ascontiguousarray(vertices).view(np.float32).reshape(-1, 7)
     tally = np.zeros(grid.rho.size, np.float64)
     ph = np.zeros(h1 - h0, np.float64) if per_history else None
     st = _Stats()
-    cfg = _Cfg(int(physics_debug), scorer)
+    cfg = _Cfg(int(physics_debug), scorer, None)
+    if calib is not None:
+        spr = np.ascontiguousarray(calib.spr, np.float32)
+        x0 = np.ascontiguousarray(calib.x0, np.float32)
+        cal = _Calib(calib.n_rho, calib.n_e, calib.rho0, calib.drho, calib.e0, calib.de, _p(spr).value, _p(x0).value)
+        cfg.calib = C.pointer(cal)
     rc = lib(fp64).mqo_transport(C.byref(grid.c), C.byref(cfg), _p(v), h0, h1, seed, _p(tally),
                              None if ph is None else _p(ph), C.byref(st))
     if rc != 0:
@@ -177,16 +188,45 @@ def ref_trace_rays(grid_bounds, nxyz, rays, max_steps):
 
 
 def ref_phantom_cmd(debug: bool, lxyz, pxyz, nxyz, energy, position, size, histories, phantom_path, out_dir, seed,
-                    beam="uniform"):
-    return [ref_binary(debug), "phantom", "--lxyz", *map(str, lxyz), "--pxyz", *map(str, pxyz), "--nxyz",
-            *map(str, nxyz), "--spot_energy", str(energy), "0", "--spot_position", *map(str, position),
-            "--spot_size", *map(str, size), "--histories", str(histories), "--phantom_path", phantom_path,
-            "--output_prefix", out_dir, "--random_seed", str(seed), "--beam", beam, "--json",
-            os.path.join(out_dir, "run.json")]
+                    beam="uniform", beamline: Optional[str] = None):
+    cmd = [ref_binary(debug), "phantom", "--lxyz", *map(str, lxyz), "--pxyz", *map(str, pxyz), "--nxyz",
+           *map(str, nxyz), "--spot_energy", str(energy), "0", "--spot_position", *map(str, position),
+           "--spot_size", *map(str, size), "--histories", str(histories), "--phantom_path", phantom_path,
+           "--output_prefix", out_dir, "--random_seed", str(seed), "--beam", beam, "--json",
+           os.path.join(out_dir, "run.json")]
+    if beamline:
+        cmd += ["--beamline", beamline]
+    return cmd
+
+
+def write_beamline_file(path: str, devices) -> None:
+    """Write devices (moquimc_gb300.beamline.children_from_devices tuples) in the format of
+    ref_driver's --beamline option."""
+    with open(path, "w") as f:
+        for d in devices:
+            if d[0] == "rangeshifter":
+                _, lo, hi, dens, ang, tr = d
+                box = [lo[0], hi[0], lo[1], hi[1], lo[2], hi[2]]
+                f.write("rangeshifter " + " ".join(repr(float(np.float32(v))) for v in (*box, dens, *ang, *tr)) + "\n")
+            else:
+                _, center, volume, openings, ang, tr = d
+                vals = [*center, *volume, *ang, *tr]
+                f.write("aperture " + " ".join(repr(float(np.float32(v))) for v in vals) + f" {len(openings)}")
+                for poly in openings:
+                    p = np.asarray(poly, np.float32)
+                    f.write(f" {len(p)} " + " ".join(repr(float(v)) for v in p.reshape(-1)))
+                f.write("\n")
+
+
+def _beamline_children(beamline: Optional[str]) -> int:
+    if not beamline:
+        return 0
+    with open(beamline) as f:
+        return sum(1 for line in f if line.split())
 
 
 def ref_phantom_parallel(debug: bool, lxyz, pxyz, nxyz, energy, position, size, histories_each, n_proc, hu,
-                         seed0, beam="uniform", workdir: Optional[str] = None):
+                         seed0, beam="uniform", workdir: Optional[str] = None, beamline: Optional[str] = None):
     """Run n_proc reference CPU processes (distinct seeds) in parallel; returns (summed dose, list of
     per-process run records, per-process doses)."""
     td = workdir or tempfile.mkdtemp(prefix="mqi_ref_")
@@ -197,7 +237,8 @@ def ref_phantom_parallel(debug: bool, lxyz, pxyz, nxyz, energy, position, size, 
         od = os.path.join(td, f"p{p}")
         os.makedirs(od, exist_ok=True)
         dirs.append(od)
-        cmd = ref_phantom_cmd(debug, lxyz, pxyz, nxyz, energy, position, size, histories_each, ph, od, seed0 + p, beam)
+        cmd = ref_phantom_cmd(debug, lxyz, pxyz, nxyz, energy, position, size, histories_each, ph, od, seed0 + p, beam,
+                              beamline)
         log = open(os.path.join(od, "log.txt"), "w")
         procs.append(subprocess.Popen(cmd, stdout=log, stderr=subprocess.STDOUT))
         log.close()
@@ -207,7 +248,7 @@ def ref_phantom_parallel(debug: bool, lxyz, pxyz, nxyz, energy, position, size, 
     for i, r in enumerate(rcs):
         if r < 0:
             cmd = ref_phantom_cmd(debug, lxyz, pxyz, nxyz, energy, position, size, histories_each, ph, dirs[i],
-                                  seed0 + i, beam)
+                                  seed0 + i, beam, beamline)
             with open(os.path.join(dirs[i], "log_retry.txt"), "w") as log:
                 rcs[i] = subprocess.run(cmd, stdout=log, stderr=subprocess.STDOUT).returncode
     if any(rcs):
@@ -218,7 +259,8 @@ def ref_phantom_parallel(debug: bool, lxyz, pxyz, nxyz, energy, position, size, 
     n = int(np.prod(nxyz))
     doses, recs = [], []
     for od in dirs:
-        doses.append(np.fromfile(os.path.join(od, "0_water_dE_total.raw"), dtype=np.float64, count=n))
+        doses.append(np.fromfile(os.path.join(od, f"{_beamline_children(beamline)}_water_dE_total.raw"),
+                                 dtype=np.float64, count=n))
         with open(os.path.join(od, "run.json")) as f:
             recs.append(json.load(f))
     return np.sum(doses, axis=0), recs, doses

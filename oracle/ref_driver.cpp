@@ -5,13 +5,20 @@
 // the C restatement (oracle/mqi_oracle.c) and the CUDA path; nothing in the product links it.
 //
 // Modes (argv[1]):
-//   phantom <phantom_env CLI> [--beam uniform|gaussian] [--json <file>]
+//   phantom <phantom_env CLI> [--beam uniform|gaussian] [--json <file>] [--beamline <file>]
 //       Runs mqi::phantom_env<float> (moqui/base/environments/mqi_phantom_env.hpp:37-428) on the CPU:
 //       initialize -> run -> save_reshaped_files.  run() is overridden only to (a) seed the CPU
 //       transport RNG from --random_seed (the stock CPU branch default-constructs it, so every
 //       process would share one stream, mqi_transport.hpp:147-149 / mqi_phantom_env.hpp:420-422)
 //       and (b) time the transport call alone.  --beam gaussian swaps phsp_6d_uniform for the
 //       Gaussian phsp_6d (moqui/base/distributions/mqi_phsp6d.hpp) with sigma = --spot_size.
+//       --beamline puts beamline children before the phantom, built as tps_env builds them
+//       (mqi_tps_env.hpp:735-758, 1605-1737); one device per line:
+//         rangeshifter xmin xmax ymin ymax zmin zmax density_g_cm3 ax ay az tx ty tz
+//         aperture cx cy cz vx vy vz ax ay az tx ty tz n_openings {n_vertices x y ...}...
+//       (angles in radians for mat3x3(ax, ay, az), translation in mm).  The children's rotation
+//       matrices go to the --json record and each aperture's densities to aperture<k>.bin in the
+//       output directory.
 //   raywalk <rays.bin> <out.bin>
 //       Walks rays through a grid3d exactly as the transport kernel's voxel loop does
 //       (mqi_transport.hpp:161-239) with the physics replaced by a pure boundary step.
@@ -34,6 +41,8 @@
 #include <unistd.h>
 #include <cstring>
 #include <fstream>
+#include <iomanip>
+#include <sstream>
 #include <string>
 #include <vector>
 
@@ -67,14 +76,156 @@ read_vec(std::ifstream& f) {
 
 /// phantom_env with a seeded CPU transport RNG, a timed transport phase and an optional
 /// Gaussian spot.  Everything else is the stock reference class.
+/// One beamline device read from a --beamline file.
+struct beamline_device {
+    std::string                      kind;
+    float                            a[6] = { 0, 0, 0, 0, 0, 0 };   // rangeshifter: box; aperture: centre, volume
+    float                            density = 0.0f;
+    float                            ang[3] = { 0, 0, 0 };
+    float                            tr[3]  = { 0, 0, 0 };
+    std::vector<std::vector<float>>  openings;                       // x, y pairs
+};
+
+std::vector<beamline_device>
+read_beamline(const std::string& path) {
+    std::vector<beamline_device> out;
+    std::ifstream                f(path);
+    std::string                  line;
+    while (std::getline(f, line)) {
+        std::istringstream in(line);
+        beamline_device    d;
+        if (!(in >> d.kind)) continue;
+        for (float& v : d.a) in >> v;
+        if (d.kind == "rangeshifter") in >> d.density;
+        for (float& v : d.ang) in >> v;
+        for (float& v : d.tr) in >> v;
+        if (d.kind == "aperture") {
+            int n_open = 0;
+            in >> n_open;
+            for (int k = 0; k < n_open; ++k) {
+                int nv = 0;
+                in >> nv;
+                std::vector<float> poly(2 * nv);
+                for (float& v : poly) in >> v;
+                d.openings.push_back(poly);
+            }
+        }
+        out.push_back(d);
+    }
+    return out;
+}
+
+/// tps_env::sol1_1 (mqi_tps_env.hpp:1753-1770): crossing-number point-in-polygon test.
+bool
+inside_polygon(const mqi::vec3<float>& pos, const std::vector<mqi::vec2<float>>& seg) {
+    int c = 0;
+    const int n = (int) seg.size();
+    for (int i = 0, j = n - 1; i < n; j = i++) {
+        const mqi::vec2<float> p0 = seg[i], p1 = seg[j];
+        if ((((p0.y <= pos.y) && (pos.y < p1.y)) || ((p1.y <= pos.y) && (pos.y < p0.y))) &&
+            (pos.x < (p1.x - p0.x) * (pos.y - p0.y) / (p1.y - p0.y) + p0.x))
+            c = !c;
+    }
+    return c;
+}
+
+/// The child of a range shifter, as tps_env::create_rangeshifter (mqi_tps_env.hpp:1605-1650).
+mqi::node_t<float>*
+make_rangeshifter(const beamline_device& d) {
+    auto* n       = new mqi::node_t<float>;
+    n->n_scorers  = 0;
+    n->n_children = 0;
+    n->scorers    = nullptr;
+    n->children   = nullptr;
+    n->geo = new mqi::grid3d<mqi::density_t, float>(d.a[0], d.a[1], 2, d.a[2], d.a[3], 2, d.a[4], d.a[5], 2,
+                                                    mqi::mat3x3<float>(d.ang[0], d.ang[1], d.ang[2]));
+    n->geo->fill_data(d.density * 1e-3);
+    n->geo->translation_vector = mqi::vec3<float>(d.tr[0], d.tr[1], d.tr[2]);
+    return n;
+}
+
+/// The child of a voxelised aperture, as tps_env::create_voxelized_aperture
+/// (mqi_tps_env.hpp:1652-1737) with 1 mm voxels; the last opening decides (is_inside, :1739-1750).
+mqi::node_t<float>*
+make_aperture(const beamline_device& d, std::vector<float>& rho_out) {
+    const mqi::vec3<float> pos(d.a[0], d.a[1], d.a[2]), vol(d.a[3], d.a[4], d.a[5]), vox(1, 1, 1);
+    std::vector<std::vector<mqi::vec2<float>>> segs;
+    for (const auto& poly : d.openings) {
+        std::vector<mqi::vec2<float>> s;
+        for (size_t j = 0; j + 1 < poly.size(); j += 2) {
+            mqi::vec2<float> v;
+            v.x = poly[j] + pos.x;
+            v.y = poly[j + 1] + pos.y;
+            s.push_back(v);
+        }
+        segs.push_back(s);
+    }
+    const size_t nx = (size_t) mqi::mqi_ceil(vol.x / vox.x), ny = (size_t) mqi::mqi_ceil(vol.y / vox.y),
+                 nz = (size_t) mqi::mqi_ceil(vol.z / vox.z);
+    float* xe = new float[nx + 1];
+    float* ye = new float[ny + 1];
+    float* ze = new float[nz + 1];
+    for (size_t i = 0; i < nx + 1; i++) xe[i] = (pos.x - vol.x / 2) + i * vox.x;
+    for (size_t i = 0; i < ny + 1; i++) ye[i] = (pos.y - vol.y / 2) + i * vox.y;
+    for (size_t i = 0; i < nz + 1; i++) ze[i] = (pos.z - vol.z / 2) + i * vox.z;
+    auto* n       = new mqi::node_t<float>;
+    n->n_scorers  = 0;
+    n->n_children = 0;
+    n->scorers    = nullptr;
+    n->children   = nullptr;
+    n->geo = new mqi::grid3d<mqi::density_t, float>(xe, nx + 1, ye, ny + 1, ze, nz + 1,
+                                                    mqi::mat3x3<float>(d.ang[0], d.ang[1], d.ang[2]));
+    auto* data = new mqi::density_t[nx * ny * nz];
+    mqi::vec3<float> p(0, 0, 0);
+    for (size_t i = 0; i < nx; i++) {
+        p.x = xe[i] + vox.x * 0.5;
+        for (size_t j = 0; j < ny; j++) {
+            p.y = ye[j] + vox.y * 0.5;
+            bool inside = false;
+            for (const auto& s : segs) inside = inside_polygon(p, s);
+            for (size_t k = 0; k < nz; k++) data[k * nx * ny + j * nx + i] = inside ? 1e-8 : 100.0;
+        }
+    }
+    n->geo->set_data(data);
+    n->geo->translation_vector = mqi::vec3<float>(d.tr[0], d.tr[1], d.tr[2]);
+    rho_out.assign(data, data + nx * ny * nz);
+    return n;
+}
+
 class oracle_phantom_env : public mqi::phantom_env<float>
 {
 public:
     bool        gaussian = false;
     double      transport_seconds = 0.0;
     uint32_t    tracked = 0;
+    std::vector<beamline_device>      beamline;
+    std::vector<std::vector<float>>   aperture_rho;
+    std::vector<std::array<float, 9>> beamline_rot;
 
     oracle_phantom_env(mqi::cli& c, bool g) : mqi::phantom_env<float>(c), gaussian(g) {}
+
+    void
+    setup_world() override {
+        mqi::phantom_env<float>::setup_world();
+        if (beamline.empty()) return;
+        // beamline children first, the phantom last (mqi_tps_env.hpp:735-758)
+        mqi::node_t<float>*  phantom = this->world->children[0];
+        const int            n       = (int) beamline.size() + 1;
+        mqi::node_t<float>** kids    = new mqi::node_t<float>*[n];
+        for (size_t i = 0; i < beamline.size(); ++i) {
+            if (beamline[i].kind == "rangeshifter") {
+                kids[i] = make_rangeshifter(beamline[i]);
+            } else {
+                aperture_rho.emplace_back();
+                kids[i] = make_aperture(beamline[i], aperture_rho.back());
+            }
+            const auto& r = kids[i]->geo->rotation_matrix_fwd;
+            beamline_rot.push_back({ r.xx, r.xy, r.xz, r.yx, r.yy, r.yz, r.zx, r.zy, r.zz });
+        }
+        kids[n - 1]              = phantom;
+        this->world->children    = kids;
+        this->world->n_children  = n;
+    }
 
     void
     setup_beamsource() override {
@@ -113,7 +264,7 @@ public:
 int
 run_phantom(int argc, char** argv) {
     bool        gaussian = false;
-    std::string json;
+    std::string json, beamline;
     std::vector<char*> rest;
     rest.push_back(argv[0]);
     for (int i = 2; i < argc; ++i) {
@@ -121,6 +272,8 @@ run_phantom(int argc, char** argv) {
             gaussian = !std::strcmp(argv[++i], "gaussian");
         } else if (!std::strcmp(argv[i], "--json") && i + 1 < argc) {
             json = argv[++i];
+        } else if (!std::strcmp(argv[i], "--beamline") && i + 1 < argc) {
+            beamline = argv[++i];
         } else {
             rest.push_back(argv[i]);
         }
@@ -128,6 +281,7 @@ run_phantom(int argc, char** argv) {
     mqi::cli cl;
     cl.read(static_cast<int>(rest.size()), rest.data());
     oracle_phantom_env env(cl, gaussian);
+    if (!beamline.empty()) env.beamline = read_beamline(beamline);
     env.initialize();
     env.run();
     env.finalize();
@@ -141,7 +295,17 @@ run_phantom(int argc, char** argv) {
 #else
           << ", \"physics_debug\": 0"
 #endif
-          << "}\n";
+          << ", \"beamline_rot\": [";
+        for (size_t i = 0; i < env.beamline_rot.size(); ++i) {
+            f << (i ? ", [" : "[");
+            for (int k = 0; k < 9; ++k) f << (k ? ", " : "") << std::setprecision(9) << env.beamline_rot[i][k];
+            f << "]";
+        }
+        f << "]}\n";
+        for (size_t k = 0; k < env.aperture_rho.size(); ++k) {
+            std::ofstream a(env.output_path + "/aperture" + std::to_string(k) + ".bin", std::ios::binary);
+            a.write(reinterpret_cast<const char*>(env.aperture_rho[k].data()), env.aperture_rho[k].size() * sizeof(float));
+        }
     }
     return 0;
 }

@@ -173,6 +173,37 @@ def test_fp64_oracle_dose_matches_reference_c2(golden, oracle):
     assert abs(tot64 / tot32 - 1.0) <= 2e-3, tot64 / tot32
 
 
+def _default_curve_table(oracle, spr_scale=1.0):
+    """The default SPR / X0 curves of release physics tabulated on uniform grids (the calibration
+    plug-in as tables): 0.1-2.5 g/cm^3 by 0.01, 0.5-250 MeV by 0.5."""
+    from moquimc_gb300 import capi
+
+    return capi.CalibTable.sample(lambda r, e: spr_scale * oracle.spr(r, e, False), lambda r: oracle.x0(r, False),
+                                  1.0e-4, 1.0e-5, 241, 0.5, 0.5, 500)
+
+
+def test_oracle_tabulated_calibration(oracle):
+    """Tabulated curves in the restatement: the default curves as tables reproduce the default
+    dose (same streams; linear interpolation of the curves moves it by far less than the
+    statistics), and SPR x 1.1 pulls the distal 80% dose in by the factor 1/1.1 (the range scales
+    with 1/SPR)."""
+    wl = workloads.c2()
+    xe, ye, ze = wl.edges()
+    rho = np.full(int(np.prod(wl.nxyz)), oracle.hu_to_density(0), np.float32)   # water
+    grid = oracle.Grid(xe, ye, ze, rho)
+    each = 1500
+    v = wl.vertices(each, 4100)
+    d_def, _, _ = oracle.transport(grid, v, 0, each, 41, False)
+    d_tab, _, _ = oracle.transport(grid, v, 0, each, 41, False, calib=_default_curve_table(oracle))
+    d_big, _, _ = oracle.transport(grid, v, 0, each, 41, False, calib=_default_curve_table(oracle, 1.1))
+    assert abs(d_tab.sum() / d_def.sum() - 1.0) <= 2e-3
+    r_def = ph.r80(ph.depth_dose(d_def, wl.nxyz), 1.0)
+    r_tab = ph.r80(ph.depth_dose(d_tab, wl.nxyz), 1.0)
+    r_big = ph.r80(ph.depth_dose(d_big, wl.nxyz), 1.0)
+    assert abs(r_tab - r_def) <= 0.2, (r_tab, r_def)
+    assert abs(r_big * 1.1 / r_def - 1.0) <= 0.01, (r_big, r_def)
+
+
 def test_slab_workload_geometry():
     wl = workloads.c2(histories=10)
     lung, bone = wl.meta["lung_depth_mm"], wl.meta["bone_depth_mm"]

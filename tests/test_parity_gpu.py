@@ -118,6 +118,59 @@ def test_gpu_matches_oracle_history_by_history(oracle, gpu_ctx_factory, wname):
     assert abs(steps - ost["steps"]) <= 0.02 * ost["steps"]
 
 
+def test_tabulated_calibration_matches_oracle_history_by_history(oracle, gpu_ctx_factory):
+    """A custom calibration (mqi_set_calibration: SPR(rho, E) and X0(rho) tables; here moqui's
+    default curves scaled by 1.05 and 0.9) on the slab phantom: the GPU and the restatement on the
+    same Philox streams, history by history as above; then the default curves back."""
+    wl = _laterally_coarse(workloads.c2(histories=200), 16)
+    n, seed = 200, 0xCA11B
+    table = capi.CalibTable.sample(lambda r, e: 1.05 * oracle.spr(r, e, False), lambda r: 0.9 * oracle.x0(r, False),
+                                   1.0e-4, 1.0e-5, 241, 0.5, 0.5, 500)
+    v = wl.vertices(n, 13)
+    c, cid, sid = _ctx_for(wl, gpu_ctx_factory, capi.EDEP)
+    c.set_calibration(table)
+    c.set_vertices(v)
+    e_gpu = np.zeros(n)
+    for h in range(n):
+        c.reset()
+        c.transport(h, h + 1, seed)
+        e_gpu[h] = c.tally(sid).sum()
+    grid = _oracle_grid(oracle, wl)
+    _, e_ora, _ = oracle.transport(grid, v, 0, n, seed, wl.physics_debug, scorer=1, per_history=True, calib=table)
+    _, e_def, _ = oracle.transport(grid, v, 0, n, seed, wl.physics_debug, scorer=1, per_history=True)
+    same = np.abs(e_gpu - e_ora) <= 1e-4 * np.maximum(e_ora, 1e-9)
+    assert same.mean() >= 0.95, (same.mean(), np.flatnonzero(~same)[:10])
+    assert not np.allclose(e_ora, e_def, rtol=1e-3)   # the tables did change the transport
+    c.set_calibration(None)
+    c.reset()
+    c.transport(0, n, seed)
+    assert abs(c.tally(sid).sum() / e_def.sum() - 1.0) <= 0.02
+
+
+def test_calibration_arguments_are_checked(gpu_ctx_factory):
+    c = gpu_ctx_factory()
+    lib = c.lib
+    spr = np.ones(4, np.float32)
+    x0 = np.ones(2, np.float32)
+    bad = [
+        (capi.CALIB_TABLE, 1, 0.0, 1.0, 2, 0.0, 1.0, spr, x0),              # one density node
+        (capi.CALIB_TABLE, 2, 0.0, 0.0, 2, 0.0, 1.0, spr, x0),              # zero pitch
+        (capi.CALIB_TABLE, 2, 0.0, 1.0, 2, 0.0, 1.0, None, x0),             # no SPR table
+        (capi.CALIB_TABLE, 2, 0.0, 1.0, 2, 0.0, 1.0, spr, -x0),             # X0 <= 0
+        (7, 2, 0.0, 1.0, 2, 0.0, 1.0, spr, x0),                              # unknown calibration
+    ]
+    for mode, nr, r0, dr, ne, e0, de, s_, x_ in bad:
+        rc = lib.mqi_set_calibration(c.h, mode, nr, r0, dr, ne, e0, de,
+                                     None if s_ is None else s_.ctypes.data, x_.ctypes.data)
+        assert rc == capi.MQI_ERR_INVALID
+    nan = spr.copy()
+    nan[1] = np.nan
+    assert lib.mqi_set_calibration(c.h, capi.CALIB_TABLE, 2, 0.0, 1.0, 2, 0.0, 1.0, nan.ctypes.data,
+                                   x0.ctypes.data) == capi.MQI_ERR_INVALID
+    assert lib.mqi_set_calibration(c.h, capi.CALIB_TABLE, 2, 0.0, 1.0, 2, 0.0, 1.0, spr.ctypes.data,
+                                   x0.ctypes.data) == capi.MQI_OK
+
+
 def test_gpu_matches_oracle_in_aggregate(oracle, gpu_ctx_factory):
     """Full-resolution phantom example, 4 x 1000 histories on each side: the depth-dose curves of
     the GPU and of the C restatement agree within 2% or 3 sigma.  (Voxel-for-voxel equality on the
