@@ -239,15 +239,21 @@ def plan_section(torch, capi, workloads, args) -> dict:
     return out
 
 
-def dij_section(torch, capi, workloads, optimize) -> dict:
-    """C3 Dij (one batched pass) and C5: 100 projected-gradient iterations, FD check on 64 spots."""
+def dij_section(torch, capi, workloads, optimize, stride: int = 1) -> dict:
+    """C3 Dij (one batched pass) and C5: 100 projected-gradient iterations, FD check on 64 spots.
+    stride > 1 keeps every stride-th spot (a smaller matrix, e.g. for a profiler capture)."""
     wl = workloads.c3()
+    if stride > 1:
+        wl.spots = wl.spots[::stride].copy()
     dev = torch.device("cuda:0")
     c = capi.Context(0)
     c.set_physics(False)
     cid = c.add_child(*wl.edges())
     c.set_hu(cid, wl.hu)
-    sid = c.add_dij_scorer(cid, capacity=1 << 31)
+    cap = 1 << 31
+    while stride > 1 and cap > (1 << 26) and cap // 2 >= 4 * int(wl.spots["histories"].sum()) * 16:
+        cap //= 2   # ~16 entries per history at most, the table at most half full
+    sid = c.add_dij_scorer(cid, capacity=cap)
     N = c.set_spot_plan(wl.spots)
     t_tr, _ = _cuda_time(torch, lambda: c.transport_plan(0, N, 7))
     t_bd, op = _cuda_time(torch, lambda: c.dij_build(sid, scale=1.0))
@@ -273,7 +279,7 @@ def dij_section(torch, capi, workloads, optimize) -> dict:
             obj(optimize.dijmod.dose(op, wv)).backward()
 
     t_fb, _ = _cuda_time(torch, fwd_bwd)
-    spots = np.random.default_rng(8).choice(op.n_spots, 64, replace=False)
+    spots = np.random.default_rng(8).choice(op.n_spots, min(64, op.n_spots), replace=False)
     rel32, _, fd = optimize.fd_check(op, obj, w, spots, dtype=torch.float32)
     rel64, _, _ = optimize.fd_check(op, obj, w, spots, dtype=torch.float64)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -291,7 +297,8 @@ def dij_section(torch, capi, workloads, optimize) -> dict:
     bwd_bytes = op.nnz * 12 + op.n_spots * 16
     hbm = measured_peaks()["hbm_gbs"]
     out = {
-        "workload": "c3 Dij + c5 objective", "histories": N, "nnz": op.nnz, "voxel_rows": vr,
+        "workload": "c3 Dij + c5 objective" + (f" (every {stride}th spot)" if stride > 1 else ""),
+        "histories": N, "nnz": op.nnz, "voxel_rows": vr,
         "transport_primaries_per_s": N / t_tr, "build_s": t_bd,
         "forward_ms": times["forward"], "backward_ms": times["backward"],
         "forward_frac_hbm": fwd_bytes / (times["forward"] / 1e3) / 1e9 / hbm,
@@ -299,7 +306,7 @@ def dij_section(torch, capi, workloads, optimize) -> dict:
         "optimisation": {"iterations": 100, "ms_per_iteration": t_opt * 10, "objective_first": float(hist[0]),
                          "objective_last": float(hist[-1]), "forward_call_ms": t_f * 100,
                          "forward_objective_backward_ms": t_fb * 100},
-        "fd_check": {"spots": 64, "h": 1e-3, "nonzero": int((np.abs(fd) > 0).sum()),
+        "fd_check": {"spots": len(spots), "h": 1e-3, "nonzero": int((np.abs(fd) > 0).sum()),
                      "max_rel_err_fp32_grad": float(rel32.max()), "max_rel_err_fp64_grad": float(rel64.max())},
     }
     c.close()
@@ -489,7 +496,9 @@ def run_gpu(args, wl):
 
             for key, fn in (("plan", lambda: plan_section(torch, capi, workloads, args)),
                             ("robust", lambda: robust_section(torch, capi, workloads, args)),
-                            ("dij", lambda: dij_section(torch, capi, workloads, optimize))):
+                            ("dij", lambda: dij_section(torch, capi, workloads, optimize, args.dij_stride))):
+                if key not in args.sections.split(","):
+                    continue
                 try:
                     line[key] = fn()
                 except Exception as exc:  # noqa: BLE001  (a failed section is reported, not hidden)
@@ -512,6 +521,8 @@ def main():
     ap.add_argument("--ref-histories", type=int, default=3000, help="histories per CPU process per sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plan", action="store_true", help="skip the plan, robust and Dij sections")
+    ap.add_argument("--sections", default="plan,robust,dij", help="plan-level sections to run (comma-separated)")
+    ap.add_argument("--dij-stride", type=int, default=1, help="Dij section on every n-th spot of the plan")
     ap.add_argument("--plain-stride", type=int, default=10, help="time every n-th spot for the plain per-spot rate")
     ap.add_argument("--robust-stride", type=int, default=20, help="spots of the plan in the robust sample")
     ap.add_argument("--max-passes", type=int, default=30, help="plan passes allowed for the 1%% criterion")

@@ -27,7 +27,7 @@ void
 free_csr(DijCsr& m) {
     cudaFree(m.s_indptr); cudaFree(m.s_voxel); cudaFree(m.s_value);
     cudaFree(m.v_row); cudaFree(m.v_indptr); cudaFree(m.v_spot); cudaFree(m.v_value);
-    cudaFree(m.seg_start); cudaFree(m.row_seg); cudaFree(m.partial);
+    cudaFree(m.seg_start); cudaFree(m.row_seg); cudaFree(m.partial); cudaFree(m.fwd_row_first);
     m = DijCsr{};
 }
 
@@ -164,10 +164,11 @@ mqi_dij_build(mqi_ctx* c, int id, uint32_t n_spots, double scale, uint64_t* nnz_
     m.n_voxels = nvox;
     m.nnz      = n;
     MQI_CUDA(c, sc.alloc(m.s_indptr, (uint64_t) n_spots + 1), "mqi_dij_build: allocation");
-    MQI_CUDA(c, sc.alloc(m.s_voxel, n), "mqi_dij_build: allocation");
-    MQI_CUDA(c, sc.alloc(m.s_value, n), "mqi_dij_build: allocation");
-    MQI_CUDA(c, sc.alloc(m.v_spot, n), "mqi_dij_build: allocation");
-    MQI_CUDA(c, sc.alloc(m.v_value, n), "mqi_dij_build: allocation");
+    // entry arrays padded to whole groups of four: the products read them with 16-byte loads
+    MQI_CUDA(c, sc.alloc(m.s_voxel, n + 4), "mqi_dij_build: allocation");
+    MQI_CUDA(c, sc.alloc(m.s_value, n + 4), "mqi_dij_build: allocation");
+    MQI_CUDA(c, sc.alloc(m.v_spot, n + 4), "mqi_dij_build: allocation");
+    MQI_CUDA(c, sc.alloc(m.v_value, n + 4), "mqi_dij_build: allocation");
 
     // 1. compact the table to (spot * n_voxels + voxel, slot) pairs
     MQI_CUDA(c, dij_compact(s.dij, s.dij_cap, nvox, ka, ia, n, cursor, c->num_sms, st), "mqi_dij_build: compact");
@@ -232,9 +233,13 @@ mqi_dij_build(mqi_ctx* c, int id, uint32_t n_spots, double scale, uint64_t* nnz_
     if (n == 0) MQI_CUDA(c, cudaMemsetAsync(m.v_indptr, 0, sizeof(uint64_t), st), "mqi_dij_build");
     MQI_CUDA(c, dij_voxel_rows(vkeys, vpos, n, skeys, nvox, m.s_value, flags, rowid, m.v_row, m.v_indptr, m.v_spot,
                                m.v_value, st), "mqi_dij_build");
+    // 5. the forward blocks' first rows
+    MQI_CUDA(c, sc.alloc(m.fwd_row_first, (n + kFwdEntries - 1) / kFwdEntries + 1), "mqi_dij_build: allocation");
+    MQI_CUDA(c, dij_forward_blocks(m.v_indptr, m.n_vrows, n, m.fwd_row_first, &m.n_fwd_blocks, st), "mqi_dij_build");
     MQI_CUDA(c, cudaStreamSynchronize(st), "mqi_dij_build");
     for (void* p : { (void*) m.s_indptr, (void*) m.s_voxel, (void*) m.s_value, (void*) m.v_row, (void*) m.v_indptr,
-                     (void*) m.v_spot, (void*) m.v_value, (void*) m.seg_start, (void*) m.row_seg, (void*) m.partial })
+                     (void*) m.v_spot, (void*) m.v_value, (void*) m.seg_start, (void*) m.row_seg, (void*) m.partial,
+                     (void*) m.fwd_row_first })
         sc.release(p);
     m.built = true;
     s.csr   = m;
@@ -293,8 +298,8 @@ mqi_dij_matvec(mqi_ctx* c, int id, const void* w, void* dose, int fp64, int on_d
         dd = td;
     }
     MQI_CUDA(c, cudaMemsetAsync(dd, 0, m.n_voxels * es, c->stream), "mqi_dij_matvec");
-    MQI_CUDA(c, dij_forward(m.v_row, m.v_indptr, m.v_spot, m.v_value, m.n_vrows, dw, dd, fp64, c->num_sms, c->stream),
-             "mqi_dij_matvec");
+    MQI_CUDA(c, dij_forward(m.v_row, m.v_indptr, m.fwd_row_first, m.n_fwd_blocks, m.v_spot, m.v_value, dw, dd, fp64,
+                            c->stream), "mqi_dij_matvec");
     if (!on_device) {
         MQI_CUDA(c, cudaMemcpyAsync(dose, dd, m.n_voxels * es, cudaMemcpyDeviceToHost, c->stream), "mqi_dij_matvec");
         MQI_CUDA(c, cudaStreamSynchronize(c->stream), "mqi_dij_matvec");

@@ -49,6 +49,8 @@ struct DijCsr {
     uint64_t* seg_start = nullptr;  // n_seg + 1
     uint32_t* row_seg = nullptr;    // n_spots + 1: first segment of each row
     double*   partial = nullptr;    // n_seg
+    uint64_t  n_fwd_blocks = 0;     // forward blocks: kFwdEntries entries' worth of voxel rows each
+    uint32_t* fwd_row_first = nullptr;   // n_fwd_blocks + 1: first voxel row of each forward block
 };
 
 struct ScorerHost {

@@ -262,35 +262,123 @@ k_voxel_rows(const unsigned long long* __restrict__ vkeys, const uint32_t* __res
 
 // ---- products -------------------------------------------------------------------------------
 
-/// dose[row_voxel[r]] = sum_k val[k] * w[spot[k]] over voxel rows; 8 lanes per row, the lanes'
-/// partial sums combined in a fixed butterfly.  Accumulates in T.
-template<typename T>
+/// Block b of the staged forward owns the voxel rows that start in entries [b * kFwdEntries,
+/// (b + 1) * kFwdEntries): row_first[b] = the first row r with indptr[r] >= b * kFwdEntries.  One
+/// thread per block boundary, a binary search over indptr (once per Dij build).
 __global__ void
+k_fwd_blocks(const uint64_t* __restrict__ indptr, uint64_t n_rows, uint64_t n_blocks, uint32_t* __restrict__ row_first) {
+    const uint64_t b = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x;
+    if (b > n_blocks) return;
+    const uint64_t target = b * kFwdEntries;
+    uint64_t lo = 0, hi = n_rows;   // first r in [0, n_rows] with indptr[r] >= target
+    while (lo < hi) {
+        const uint64_t mid = (lo + hi) >> 1;
+        if (indptr[mid] < target) lo = mid + 1; else hi = mid;
+    }
+    row_first[b] = (uint32_t) (b == n_blocks ? n_rows : lo);
+}
+
+/// dose[row_voxel[r]] = sum_k val[k] * w[spot[k]] over voxel rows (D.w).  A block stages the
+/// products of its rows' entries -- a contiguous run of at most kFwdEntries + the longest row,
+/// read with coalesced loads -- in shared memory, then each thread sums whole rows from there in
+/// entry order (a fixed order: the result does not depend on the launch).  A run longer than the
+/// staging buffer (a row of more than kFwdStage - kFwdEntries entries) is summed from global
+/// memory instead, in the same order.  Accumulates in T.
+template<typename T>
+__global__ void __launch_bounds__(256)
 k_dij_forward(const uint32_t* __restrict__ row_voxel, const uint64_t* __restrict__ indptr,
-              const uint32_t* __restrict__ spot, const float* __restrict__ val, uint64_t n_rows,
+              const uint32_t* __restrict__ row_first, const uint32_t* __restrict__ spot, const float* __restrict__ val,
               const T* __restrict__ w, T* __restrict__ dose) {
-    const uint64_t g      = ((uint64_t) blockIdx.x * blockDim.x + threadIdx.x) >> 3;
-    const int      sub    = threadIdx.x & 7;
-    const uint64_t stride = ((uint64_t) gridDim.x * blockDim.x) >> 3;
-    const uint64_t span   = (n_rows + stride - 1) / stride * stride;
-    for (uint64_t r = g; r < span; r += stride) {
-        T s = T(0);
-        if (r < n_rows) {
-            const uint64_t e = indptr[r + 1];
-            for (uint64_t k = indptr[r] + sub; k < e; k += 8) s += (T) val[k] * w[spot[k]];
+    extern __shared__ __align__(16) unsigned char fwd_smem[];
+    T* prod = reinterpret_cast<T*>(fwd_smem);
+    const uint32_t r0 = row_first[blockIdx.x], r1 = row_first[blockIdx.x + 1];
+    if (r0 >= r1) return;
+    const uint64_t k0 = indptr[r0], k1 = indptr[r1];
+    const bool     staged = k1 - k0 <= kFwdStage;
+    if (staged) {
+        // 16-byte loads of whole groups of four entries (the arrays are padded to whole groups);
+        // entries of the group outside [k0, k1) are skipped
+        const uint4*   s4 = reinterpret_cast<const uint4*>(spot);
+        const float4*  v4 = reinterpret_cast<const float4*>(val);
+        const uint64_t q1 = (k1 + 3) >> 2;
+#pragma unroll 2
+        for (uint64_t q = (k0 >> 2) + threadIdx.x; q < q1; q += blockDim.x) {
+            const uint4    ss = s4[q];
+            const float4   vv = v4[q];
+            const uint64_t k  = q << 2;
+            if (k >= k0 && k < k1) prod[k - k0] = (T) vv.x * w[ss.x];
+            if (k + 1 >= k0 && k + 1 < k1) prod[k + 1 - k0] = (T) vv.y * w[ss.y];
+            if (k + 2 >= k0 && k + 2 < k1) prod[k + 2 - k0] = (T) vv.z * w[ss.z];
+            if (k + 3 >= k0 && k + 3 < k1) prod[k + 3 - k0] = (T) vv.w * w[ss.w];
         }
-#pragma unroll
-        for (int o = 4; o > 0; o >>= 1) s += __shfl_xor_sync(0xFFFFFFFFu, s, o, 8);
-        if (r < n_rows && sub == 0) dose[row_voxel[r]] = s;
+        __syncthreads();
+    }
+    for (uint32_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
+        const uint64_t b = indptr[r], e = indptr[r + 1];
+        T              acc = T(0);
+        if (staged)
+            for (uint64_t k = b; k < e; ++k) acc += prod[k - k0];
+        else
+            for (uint64_t k = b; k < e; ++k) acc += (T) val[k] * w[spot[k]];
+        dose[row_voxel[r]] = acc;
     }
 }
 
 /// grad[s] = sum_k val[k] * g[voxel[k]] over spot rows (the transposed operator), in two passes
 /// with a fixed order.  Pass 1: the entries are cut into segments of at most kDijSegment entries
-/// that never cross a row; one block per segment sums its products in FP64 (signed terms of a
-/// gradient cancel, so FP32 partials lose digits) and writes one partial.  Pass 2: one thread per
+/// that never cross a row; one block per segment sums its products (signed terms of a gradient
+/// cancel, so plain FP32 partials lose digits: a double-float accumulator per thread for FP32 g,
+/// FP64 for FP64 g; FP64 across the block) and writes one partial.  Pass 2: one thread per
 /// row adds its segments' partials in order.  Rows of very different lengths (1e4 to 3e6 entries
 /// at 2000 spots) thereby spread over every SM.
+/// s + c += a * b with no rounding error in the product (TwoProd: one FMA gives the product's
+/// rounding error) and Knuth's TwoSum for the addition: a double-float accumulator of about 48
+/// significant bits on the FP32 pipes.  GB300's FP64 pipe is far narrower than its FP32 pipes,
+/// and an FP64 multiply-add per entry (with two conversions) made the backward FP64-bound.
+__device__ __forceinline__ void
+df_fma(float& s, float& c, float a, float b) {
+    const float p   = __fmul_rn(a, b);
+    const float pe  = __fmaf_rn(a, b, -p);
+    const float t   = __fadd_rn(s, p);
+    const float z   = __fsub_rn(t, s);
+    const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(p, z));
+    c               = __fadd_rn(c, __fadd_rn(err, pe));
+    s               = t;
+}
+
+template<typename T>
+__device__ __forceinline__ double
+segment_sum(uint64_t b, uint64_t e, const uint32_t* __restrict__ vox, const float* __restrict__ val,
+            const T* __restrict__ g) {
+    if constexpr (sizeof(T) == sizeof(float)) {
+        // groups of four entries with 16-byte loads (the arrays are padded to whole groups) and four
+        // independent gathers of g in flight per group; entries outside [b, e) are skipped
+        const uint4*   v4 = reinterpret_cast<const uint4*>(vox);
+        const float4*  a4 = reinterpret_cast<const float4*>(val);
+        const uint64_t q1 = (e + 3) >> 2;
+        float          s = 0.0f, c = 0.0f;
+#pragma unroll 2
+        for (uint64_t q = (b >> 2) + threadIdx.x; q < q1; q += blockDim.x) {
+            const uint4    vv = v4[q];
+            const float4   aa = a4[q];
+            const uint64_t k  = q << 2;
+            const bool     m0 = k >= b && k < e, m1 = k + 1 >= b && k + 1 < e;
+            const bool     m2 = k + 2 >= b && k + 2 < e, m3 = k + 3 >= b && k + 3 < e;
+            const float    g0 = m0 ? g[vv.x] : 0.0f, g1 = m1 ? g[vv.y] : 0.0f;
+            const float    g2 = m2 ? g[vv.z] : 0.0f, g3 = m3 ? g[vv.w] : 0.0f;
+            if (m0) df_fma(s, c, aa.x, g0);
+            if (m1) df_fma(s, c, aa.y, g1);
+            if (m2) df_fma(s, c, aa.z, g2);
+            if (m3) df_fma(s, c, aa.w, g3);
+        }
+        return (double) s + (double) c;
+    } else {
+        double d = 0.0;
+        for (uint64_t k = b + threadIdx.x; k < e; k += blockDim.x) d += (double) val[k] * g[vox[k]];
+        return d;
+    }
+}
+
 template<typename T>
 __global__ void
 k_dij_backward_segments(const uint64_t* __restrict__ seg_start, uint64_t n_seg, const uint32_t* __restrict__ vox,
@@ -298,8 +386,7 @@ k_dij_backward_segments(const uint64_t* __restrict__ seg_start, uint64_t n_seg, 
     __shared__ double part[32];
     for (uint64_t sg = blockIdx.x; sg < n_seg; sg += gridDim.x) {
         const uint64_t b = seg_start[sg], e = seg_start[sg + 1];
-        double         d = 0.0;
-        for (uint64_t k = b + threadIdx.x; k < e; k += blockDim.x) d += (double) val[k] * (double) g[vox[k]];
+        double         d = segment_sum<T>(b, e, vox, val, g);
         for (int o = 16; o > 0; o >>= 1) d += __shfl_down_sync(0xFFFFFFFFu, d, o);
         if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = d;
         __syncthreads();
@@ -429,15 +516,32 @@ dij_voxel_rows(const unsigned long long* vkeys, const uint32_t* vpos, uint64_t n
 }
 
 cudaError_t
-dij_forward(const uint32_t* row_voxel, const uint64_t* indptr, const uint32_t* spot, const float* val, uint64_t n_rows,
-            const void* w, void* dose, int fp64, int sms, cudaStream_t s) {
-    if (n_rows == 0) return cudaSuccess;
-    const uint64_t want = (n_rows * 8 + 255) / 256;
-    const unsigned grid = (unsigned) (want < (uint64_t) sms * 16 ? want : (uint64_t) sms * 16);
-    if (fp64)
-        k_dij_forward<double><<<grid, 256, 0, s>>>(row_voxel, indptr, spot, val, n_rows, (const double*) w, (double*) dose);
-    else
-        k_dij_forward<float><<<grid, 256, 0, s>>>(row_voxel, indptr, spot, val, n_rows, (const float*) w, (float*) dose);
+dij_forward_blocks(const uint64_t* indptr, uint64_t n_rows, uint64_t nnz, uint32_t* row_first, uint64_t* n_blocks,
+                   cudaStream_t s) {
+    const uint64_t nb = (nnz + kFwdEntries - 1) / kFwdEntries;
+    *n_blocks         = nb;
+    k_fwd_blocks<<<blocks_for(nb + 1, 256), 256, 0, s>>>(indptr, n_rows, nb, row_first);
+    return cudaGetLastError();
+}
+
+cudaError_t
+dij_forward(const uint32_t* row_voxel, const uint64_t* indptr, const uint32_t* row_first, uint64_t n_blocks,
+            const uint32_t* spot, const float* val, const void* w, void* dose, int fp64, cudaStream_t s) {
+    if (n_blocks == 0) return cudaSuccess;
+    static_assert(kFwdStage * sizeof(double) <= 227 * 1024, "staging buffer exceeds shared memory");
+    if (fp64) {
+        const size_t sm = kFwdStage * sizeof(double);
+        cudaError_t  e  = cudaFuncSetAttribute(k_dij_forward<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) sm);
+        if (e != cudaSuccess) return e;
+        k_dij_forward<double><<<(unsigned) n_blocks, 256, sm, s>>>(row_voxel, indptr, row_first, spot, val,
+                                                                  (const double*) w, (double*) dose);
+    } else {
+        const size_t sm = kFwdStage * sizeof(float);
+        cudaError_t  e  = cudaFuncSetAttribute(k_dij_forward<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) sm);
+        if (e != cudaSuccess) return e;
+        k_dij_forward<float><<<(unsigned) n_blocks, 256, sm, s>>>(row_voxel, indptr, row_first, spot, val,
+                                                                 (const float*) w, (float*) dose);
+    }
     return cudaGetLastError();
 }
 

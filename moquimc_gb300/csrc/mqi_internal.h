@@ -167,8 +167,12 @@ cudaError_t dij_voxel_rows(const unsigned long long* vkeys, const uint32_t* vpos
                            const unsigned long long* skeys, uint64_t n_voxels, const float* sval, const uint32_t* flags,
                            const uint32_t* rowid, uint32_t* row_voxel, uint64_t* indptr, uint32_t* spot, float* val,
                            cudaStream_t s);
-cudaError_t dij_forward(const uint32_t* row_voxel, const uint64_t* indptr, const uint32_t* spot, const float* val,
-                        uint64_t n_rows, const void* w, void* dose, int fp64, int sms, cudaStream_t s);
+constexpr uint64_t kFwdEntries = 4096;    // entries whose rows one forward block owns
+constexpr uint64_t kFwdStage   = 8192;    // staged products per forward block (rows up to 4096 entries)
+cudaError_t dij_forward_blocks(const uint64_t* indptr, uint64_t n_rows, uint64_t nnz, uint32_t* row_first,
+                               uint64_t* n_blocks, cudaStream_t s);
+cudaError_t dij_forward(const uint32_t* row_voxel, const uint64_t* indptr, const uint32_t* row_first, uint64_t n_blocks,
+                        const uint32_t* spot, const float* val, const void* w, void* dose, int fp64, cudaStream_t s);
 constexpr uint64_t kDijSegment = 16384;   // entries per backward segment
 cudaError_t dij_backward(const uint64_t* seg_start, uint64_t n_seg, const uint32_t* row_seg, uint32_t n_rows,
                          const uint32_t* vox, const float* val, double* partial, const void* g, void* grad, int fp64,
