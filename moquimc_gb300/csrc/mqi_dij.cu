@@ -295,13 +295,22 @@ k_dij_forward(const uint32_t* __restrict__ row_voxel, const uint64_t* __restrict
     if (r0 >= r1) return;
     const uint64_t k0 = indptr[r0], k1 = indptr[r1];
     const bool     staged = k1 - k0 <= kFwdStage;
+    // the thread's first row is read before the staging, so that its latency overlaps it
+    uint32_t r  = r0 + threadIdx.x;
+    uint64_t rb = 0, re = 0;
+    uint32_t rv = 0;
+    if (r < r1) {
+        rb = indptr[r];
+        re = indptr[r + 1];
+        rv = row_voxel[r];
+    }
     if (staged) {
         // 16-byte loads of whole groups of four entries (the arrays are padded to whole groups);
         // entries of the group outside [k0, k1) are skipped
         const uint4*   s4 = reinterpret_cast<const uint4*>(spot);
         const float4*  v4 = reinterpret_cast<const float4*>(val);
         const uint64_t q1 = (k1 + 3) >> 2;
-#pragma unroll 2
+#pragma unroll 4
         for (uint64_t q = (k0 >> 2) + threadIdx.x; q < q1; q += blockDim.x) {
             const uint4    ss = s4[q];
             const float4   vv = v4[q];
@@ -313,14 +322,19 @@ k_dij_forward(const uint32_t* __restrict__ row_voxel, const uint64_t* __restrict
         }
         __syncthreads();
     }
-    for (uint32_t r = r0 + threadIdx.x; r < r1; r += blockDim.x) {
-        const uint64_t b = indptr[r], e = indptr[r + 1];
-        T              acc = T(0);
+    while (r < r1) {
+        T acc = T(0);
         if (staged)
-            for (uint64_t k = b; k < e; ++k) acc += prod[k - k0];
+            for (uint64_t k = rb; k < re; ++k) acc += prod[k - k0];
         else
-            for (uint64_t k = b; k < e; ++k) acc += (T) val[k] * w[spot[k]];
-        dose[row_voxel[r]] = acc;
+            for (uint64_t k = rb; k < re; ++k) acc += (T) val[k] * w[spot[k]];
+        dose[rv] = acc;
+        r += blockDim.x;
+        if (r < r1) {
+            rb = indptr[r];
+            re = indptr[r + 1];
+            rv = row_voxel[r];
+        }
     }
 }
 
@@ -357,7 +371,7 @@ segment_sum(uint64_t b, uint64_t e, const uint32_t* __restrict__ vox, const floa
         const float4*  a4 = reinterpret_cast<const float4*>(val);
         const uint64_t q1 = (e + 3) >> 2;
         float          s = 0.0f, c = 0.0f;
-#pragma unroll 2
+#pragma unroll 4
         for (uint64_t q = (b >> 2) + threadIdx.x; q < q1; q += blockDim.x) {
             const uint4    vv = v4[q];
             const float4   aa = a4[q];
