@@ -310,7 +310,7 @@ k_dij_forward(const uint32_t* __restrict__ row_voxel, const uint64_t* __restrict
         const uint4*   s4 = reinterpret_cast<const uint4*>(spot);
         const float4*  v4 = reinterpret_cast<const float4*>(val);
         const uint64_t q1 = (k1 + 3) >> 2;
-#pragma unroll 4
+#pragma unroll 2
         for (uint64_t q = (k0 >> 2) + threadIdx.x; q < q1; q += blockDim.x) {
             const uint4    ss = s4[q];
             const float4   vv = v4[q];
