@@ -200,7 +200,7 @@ def plan_section(torch, capi, workloads, args) -> dict:
     c.set_physics(False)
     cid = c.add_child(*wl.edges())
     c.set_hu(cid, wl.hu)
-    c.add_scorer(cid, capi.DOSE_W)
+    sid = c.add_scorer(cid, capi.DOSE_W)
     d1, d2 = c.add_stat_scorers(cid)
     N = c.set_spot_plan(wl.spots)
     cum = c.plan_cum
@@ -221,6 +221,12 @@ def plan_section(torch, capi, workloads, args) -> dict:
     c.reset()
     t_s, (passes, achieved) = _cuda_time(
         torch, lambda: c.run_plan_until_stat(d1, d2, 0.01, 0.5, args.max_passes, 0x5EED))
+    # the per-history batch estimator over the same number of passes, one batch per pass
+    c.reset()
+    for p in range(int(passes)):
+        c.transport_plan(0, N, 0x5EED + 1000 + p)
+        c.batch_accumulate(sid)
+    batch_est, batch_vox, n_batches = c.batch_uncertainty(sid, 0.5) if passes >= 2 else (float("nan"), 0, passes)
     batched = N / t_b
     plain_rate = h_sub / t_p
     out = {
@@ -233,7 +239,9 @@ def plan_section(torch, capi, workloads, args) -> dict:
         "batched_over_plain": batched / plain_rate,
         "time_to_1pct_sigma": {"criterion": "reference estimator <= 1% over voxels > 50% of max dose",
                                "batched_s": t_s, "passes": passes, "achieved": achieved,
-                               "histories": passes * N, "plain_s_derived": passes * N / plain_rate},
+                               "histories": passes * N, "plain_s_derived": passes * N / plain_rate,
+                               "batch_estimator_same_passes": {"mean_rel_sigma": batch_est, "voxels": batch_vox,
+                                                               "batches": n_batches}},
     }
     c.close()
     return out

@@ -299,10 +299,14 @@ mqi_dij_matvec(mqi_ctx* c, int id, const void* w, void* dose, int fp64, int on_d
     }
     MQI_CUDA(c, cudaMemsetAsync(dd, 0, m.n_voxels * es, c->stream), "mqi_dij_matvec");
     MQI_CUDA(c, dij_forward(m.v_row, m.v_indptr, m.fwd_row_first, m.n_fwd_blocks, m.v_spot, m.v_value, dw, dd, fp64,
-                            c->stream), "mqi_dij_matvec");
+                            c->counters + 3, c->stream), "mqi_dij_matvec");
     if (!on_device) {
+        uint32_t flag = 0;
         MQI_CUDA(c, cudaMemcpyAsync(dose, dd, m.n_voxels * es, cudaMemcpyDeviceToHost, c->stream), "mqi_dij_matvec");
+        MQI_CUDA(c, cudaMemcpyAsync(&flag, c->counters + 3, sizeof(flag), cudaMemcpyDeviceToHost, c->stream),
+                 "mqi_dij_matvec");
         MQI_CUDA(c, cudaStreamSynchronize(c->stream), "mqi_dij_matvec");
+        if (flag & 8u) return fail(c, MQI_ERR_DEVICE, "mqi_dij_matvec: a bulk copy did not complete");
     }
     return MQI_OK;
 }

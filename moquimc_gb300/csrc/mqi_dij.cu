@@ -338,6 +338,109 @@ k_dij_forward(const uint32_t* __restrict__ row_voxel, const uint64_t* __restrict
     }
 }
 
+// ---- bulk copies: the copy engine (untiled cp.async.bulk) completing on a shared-memory mbarrier
+
+__device__ __forceinline__ uint32_t
+smem_u32(const void* p) {
+    return (uint32_t) __cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void
+mbar_init(uint64_t* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void
+mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+/// Global -> shared copy of `bytes` (a multiple of 16, both addresses 16-byte aligned) that
+/// completes its bytes on `bar`.
+__device__ __forceinline__ void
+bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                 ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ bool
+mbar_try_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok)
+                 : "r"(smem_u32(bar)), "r"(parity)
+                 : "memory");
+    return ok != 0;
+}
+
+/// D.w in FP32 with the staging done by the copy engine: one thread issues two bulk copies (the
+/// run's spots and values, rounded out to whole 16-byte groups; the arrays are padded) completing
+/// on a shared-memory mbarrier, the block forms the products in place and sums each row from
+/// there, one thread per row, in entry order (the order of k_dij_forward).  The wait on the
+/// barrier is bounded: a block whose copies have not landed after ~1 s of polling sets bit 8 of
+/// `err` and returns without writing.  A run longer than kFwdBulk entries is summed from global
+/// memory.
+__global__ void __launch_bounds__(256)
+k_dij_forward_bulk(const uint32_t* __restrict__ row_voxel, const uint64_t* __restrict__ indptr,
+                   const uint32_t* __restrict__ row_first, const uint32_t* __restrict__ spot,
+                   const float* __restrict__ val, const float* __restrict__ w, float* __restrict__ dose,
+                   uint32_t* __restrict__ err) {
+    extern __shared__ __align__(16) unsigned char fwd_smem[];
+    uint64_t* bar    = reinterpret_cast<uint64_t*>(fwd_smem);
+    uint32_t* s_spot = reinterpret_cast<uint32_t*>(fwd_smem + 16);
+    float*    s_val  = reinterpret_cast<float*>(fwd_smem + 16 + kFwdBulk * sizeof(uint32_t));
+    const uint32_t r0 = row_first[blockIdx.x], r1 = row_first[blockIdx.x + 1];
+    if (r0 >= r1) return;
+    const uint64_t k0 = indptr[r0], k1 = indptr[r1];
+    const uint64_t a0 = k0 & ~3ull, a1 = (k1 + 3) & ~3ull;
+    const bool     staged = a1 - a0 <= kFwdBulk;
+    uint32_t r  = r0 + threadIdx.x;
+    uint64_t rb = 0, re = 0;
+    uint32_t rv = 0;
+    if (r < r1) {
+        rb = indptr[r];
+        re = indptr[r + 1];
+        rv = row_voxel[r];
+    }
+    if (staged) {
+        const uint32_t bytes = (uint32_t) ((a1 - a0) * sizeof(uint32_t));
+        if (threadIdx.x == 0) mbar_init(bar, 1);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            mbar_expect_tx(bar, 2 * bytes);
+            bulk_load(s_spot, spot + a0, bytes, bar);
+            bulk_load(s_val, val + a0, bytes, bar);
+        }
+        bool     done  = false;
+        uint32_t spins = 0;
+        while (!(done = mbar_try_wait(bar, 0)) && ++spins < kBulkSpinLimit) {
+        }
+        if (__syncthreads_or(!done)) {
+            if (threadIdx.x == 0) atomicOr(err, 8u);
+            return;
+        }
+        for (uint64_t k = k0 + threadIdx.x; k < k1; k += blockDim.x) s_val[k - a0] *= w[s_spot[k - a0]];
+        __syncthreads();
+    }
+    while (r < r1) {
+        float acc = 0.0f;
+        if (staged)
+            for (uint64_t k = rb; k < re; ++k) acc += s_val[k - a0];
+        else
+            for (uint64_t k = rb; k < re; ++k) acc += val[k] * w[spot[k]];
+        dose[rv] = acc;
+        r += blockDim.x;
+        if (r < r1) {
+            rb = indptr[r];
+            re = indptr[r + 1];
+            rv = row_voxel[r];
+        }
+    }
+}
+
 /// grad[s] = sum_k val[k] * g[voxel[k]] over spot rows (the transposed operator), in two passes
 /// with a fixed order.  Pass 1: the entries are cut into segments of at most kDijSegment entries
 /// that never cross a row; one block per segment sums its products (signed terms of a gradient
@@ -540,7 +643,7 @@ dij_forward_blocks(const uint64_t* indptr, uint64_t n_rows, uint64_t nnz, uint32
 
 cudaError_t
 dij_forward(const uint32_t* row_voxel, const uint64_t* indptr, const uint32_t* row_first, uint64_t n_blocks,
-            const uint32_t* spot, const float* val, const void* w, void* dose, int fp64, cudaStream_t s) {
+            const uint32_t* spot, const float* val, const void* w, void* dose, int fp64, uint32_t* err, cudaStream_t s) {
     if (n_blocks == 0) return cudaSuccess;
     static_assert(kFwdStage * sizeof(double) <= 227 * 1024, "staging buffer exceeds shared memory");
     if (fp64) {
@@ -550,11 +653,11 @@ dij_forward(const uint32_t* row_voxel, const uint64_t* indptr, const uint32_t* r
         k_dij_forward<double><<<(unsigned) n_blocks, 256, sm, s>>>(row_voxel, indptr, row_first, spot, val,
                                                                   (const double*) w, (double*) dose);
     } else {
-        const size_t sm = kFwdStage * sizeof(float);
-        cudaError_t  e  = cudaFuncSetAttribute(k_dij_forward<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) sm);
+        const size_t sm = 16 + kFwdBulk * (sizeof(uint32_t) + sizeof(float));
+        cudaError_t  e  = cudaFuncSetAttribute(k_dij_forward_bulk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) sm);
         if (e != cudaSuccess) return e;
-        k_dij_forward<float><<<(unsigned) n_blocks, 256, sm, s>>>(row_voxel, indptr, row_first, spot, val,
-                                                                 (const float*) w, (float*) dose);
+        k_dij_forward_bulk<<<(unsigned) n_blocks, 256, sm, s>>>(row_voxel, indptr, row_first, spot, val,
+                                                               (const float*) w, (float*) dose, err);
     }
     return cudaGetLastError();
 }

@@ -171,8 +171,11 @@ constexpr uint64_t kFwdEntries = 4096;    // entries whose rows one forward bloc
 constexpr uint64_t kFwdStage   = 8192;    // staged products per forward block (rows up to 4096 entries)
 cudaError_t dij_forward_blocks(const uint64_t* indptr, uint64_t n_rows, uint64_t nnz, uint32_t* row_first,
                                uint64_t* n_blocks, cudaStream_t s);
+constexpr uint64_t kFwdBulk    = 6144;    // entries a bulk-copy forward block stages (spots and values)
+constexpr uint32_t kBulkSpinLimit = 1u << 20;   // bounded polls of a bulk-copy mbarrier
 cudaError_t dij_forward(const uint32_t* row_voxel, const uint64_t* indptr, const uint32_t* row_first, uint64_t n_blocks,
-                        const uint32_t* spot, const float* val, const void* w, void* dose, int fp64, cudaStream_t s);
+                        const uint32_t* spot, const float* val, const void* w, void* dose, int fp64, uint32_t* err,
+                        cudaStream_t s);
 constexpr uint64_t kDijSegment = 16384;   // entries per backward segment
 cudaError_t dij_backward(const uint64_t* seg_start, uint64_t n_seg, const uint32_t* row_seg, uint32_t n_rows,
                          const uint32_t* vox, const float* val, double* partial, const void* g, void* grad, int fp64,
