@@ -113,6 +113,26 @@ def measured_peaks() -> dict:
     return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
+def fp64_atomic_peak(torch, device) -> float:
+    """Measured rate of FP64 atomic adds to distinct addresses of an L2-resident array (random
+    indices into 2^21 doubles = 16 MB), through torch's index_add_ (one atomicAdd per element):
+    the denominator of the tally-update roofline.  Median of three timed runs of 2^26 adds."""
+    n, m = 1 << 21, 1 << 26
+    t = torch.zeros(n, dtype=torch.float64, device=device)
+    idx = torch.randint(0, n, (m,), device=device, generator=torch.Generator(device=device).manual_seed(5))
+    src = torch.ones(m, dtype=torch.float64, device=device)
+    t.index_add_(0, idx, src)
+    rates = []
+    for _ in range(3):
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record()
+        t.index_add_(0, idx, src)
+        ev1.record()
+        torch.cuda.synchronize()
+        rates.append(m / (ev0.elapsed_time(ev1) / 1e3))
+    return float(sorted(rates)[1])
+
+
 def wave_traffic_per_step() -> float | None:
     """DRAM bytes per transport step of the wave kernel from the committed ncu summary."""
     path = os.path.join(ROOT, "profiles", "k_wave_traffic.json")
@@ -440,6 +460,15 @@ def run_gpu(args, wl):
         "avg_launch_ms": wave_ms / max(launches, 1), "transport_steps_per_s": steps / (wave_ms / 1e3) if wave_ms else 0,
         "wave_share_of_step": wave_ms / ms if ms > 0 else None,
     }
+    # the tally updates: one FP64 atomic add per transport step (the dose scorer)
+    steps_per_s = steps / (wave_ms / 1e3) if wave_ms else 0.0
+    try:
+        apeak = fp64_atomic_peak(torch, f"cuda:{local}")
+        roofline["atomics"] = {"per_step": 1, "achieved_per_s": steps_per_s, "peak_per_s": apeak,
+                               "frac": steps_per_s / apeak if apeak else None,
+                               "peak_source": "measured here: torch index_add_ of FP64 into a 16 MB array, random indices"}
+    except Exception as exc:  # noqa: BLE001  (the atomic peak is supplementary)
+        roofline["atomics"] = {"error": f"{type(exc).__name__}: {exc}"}
 
     # ---- end to end through the C ABI with host buffers (pinned), H2D + D2H inside the region
     nvox = int(np.prod(wl.nxyz))
