@@ -812,6 +812,7 @@ load_track(const Queue& q, uint32_t i, Trk& t, Rng& rng, bool& step_phase) {
     rng.uid_hi = (uint32_t) (t.uid >> 32);
     rng.ctr    = q.ctr[i];
     rng.pos    = 4;
+    rng.has2   = false;
 }
 
 /// Write a track that used up its step budget back to the next queue, mid-grid.
