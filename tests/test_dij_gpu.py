@@ -102,6 +102,33 @@ def test_dij_products_match_dense_references(gpu_ctx_factory, wl):
                                atol=1e-9 * dense.max())
 
 
+def test_dij_products_with_long_voxel_rows(gpu_ctx_factory, wl):
+    """2600 one-history spots on the same axis: the voxels on the axis get rows of up to 2600
+    entries, longer than what one forward block stages (the rows' run then exceeds the staging
+    buffer and is summed from global memory), beside short rows that are staged."""
+    sp = _spots(2600, 1, seed=4, energy=(140.0, 141.0))
+    sp["mean"][:, :2] = 0.0
+    sp["sigma"][:, :2] = 0.05
+    c, cid = _ctx(gpu_ctx_factory, wl)
+    dij = c.add_dij_scorer(cid, capacity=1 << 23)
+    N = c.set_spot_plan(sp)
+    c.transport_plan(0, N, 9)
+    op = c.dij_build(dij, scale=1e6)
+    A = _csr(op).astype(np.float64)
+    row_len = np.diff(A.T.tocsr().indptr)
+    assert row_len.max() > 2048 and (row_len > 0).sum() > 100
+    rng = np.random.default_rng(6)
+    w = rng.uniform(0.5, 1.5, op.n_spots)
+    ref_d = A.T @ w
+    d32 = c.dij_matvec(dij, w.astype(np.float32), op.n_voxels)
+    np.testing.assert_allclose(d32, ref_d, rtol=1e-5, atol=1e-6 * np.abs(ref_d).max())
+    d64 = c.dij_matvec(dij, w.astype(np.float64), op.n_voxels)
+    np.testing.assert_allclose(d64, ref_d, rtol=1e-12, atol=1e-12 * np.abs(ref_d).max())
+    g = rng.standard_normal(op.n_voxels)
+    g32 = c.dij_rmatvec(dij, g.astype(np.float32), op.n_spots)
+    np.testing.assert_allclose(g32, A @ g, rtol=1e-4, atol=1e-5 * np.abs(A @ g).max())
+
+
 def test_dij_autograd_matches_finite_differences(gpu_ctx_factory, wl):
     """Quadratic objective on D.w: the hand-written D^T.g backward against central differences
     (h = 1e-3) evaluated with the FP64 forward product, and against the dense gradient."""
