@@ -103,12 +103,13 @@ def test_dij_products_match_dense_references(gpu_ctx_factory, wl):
 
 
 def test_dij_products_with_long_voxel_rows(gpu_ctx_factory, wl):
-    """2600 one-history spots on the same axis: the voxels on the axis get rows of up to 2600
-    entries, longer than what one forward block stages (the rows' run then exceeds the staging
-    buffer and is summed from global memory), beside short rows that are staged."""
-    sp = _spots(2600, 1, seed=4, energy=(140.0, 141.0))
-    sp["mean"][:, :2] = 0.0
-    sp["sigma"][:, :2] = 0.05
+    """3000 one-history spots on one axis through voxel centres: the voxels near the entrance get
+    rows of nearly 3000 entries, longer than what one forward block stages (the rows' run then
+    exceeds the staging buffer and is summed from global memory), beside short rows that are
+    staged."""
+    sp = _spots(3000, 1, seed=4, energy=(140.0, 141.0))
+    sp["mean"][:, :2] = 0.5
+    sp["sigma"][:, :2] = 0.02
     c, cid = _ctx(gpu_ctx_factory, wl)
     dij = c.add_dij_scorer(cid, capacity=1 << 23)
     N = c.set_spot_plan(sp)

@@ -1,0 +1,76 @@
+"""The treatment-planning environment's host side on the CPU: moqui's input-file rules
+(mqi::file_parser), the tps_env keys and checks, and the output writers."""
+import os
+
+import numpy as np
+import pytest
+
+from moquimc_gb300 import tps
+
+TEXT = """
+## a tps input in moqui's format
+GPUID 0
+RandomSeed 1234   # fixed seed
+randomseed 99     # a second line with the same key: the first one wins
+Scorer Dose, LETd
+SimulationType perBeam
+ParticlesPerHistory 1000
+RBE 1.1
+NumberOfFraction 30
+OutputDir {out}
+OutputFormat mhd
+OverwriteResults TRUE
+StoppingStatistics 1
+StoppingCriteria 1.5
+StatThreshold 0.5
+XShift 3.0
+DensityScaling 1.035
+BeamNumbers 2, 1
+"""
+
+
+def test_input_file_rules(tmp_path):
+    p = tps.InputFile(TEXT.format(out=tmp_path))
+    assert p.get_int("RandomSeed", -1) == 1234
+    assert p.get_string("outputformat", "raw") == "mhd"        # keys are case-insensitive
+    assert p.get_string("Missing", "dflt") == "dflt"
+    assert p.get_bool("OverwriteResults", False) and p.get_bool("StoppingStatistics", False)
+    assert not p.get_bool("Missing", False) and p.get_bool("Missing", True)
+    assert p.get_string_vector("Scorer", ",") == ["Dose", "LETd"]
+    assert p.get_float("XShift", 0.0) == 3.0 and p.get_float("YShift", 0.0) == 0.0
+    assert p.get_int("NumberOfFraction", -1) == 30
+
+
+def test_config_from_input(tmp_path):
+    cfg = tps.TpsConfig.from_input(tps.InputFile(TEXT.format(out=tmp_path)))
+    assert cfg.scorers == ["Dose", "LETd"] and cfg.simulation_type == "perBeam"
+    assert cfg.random_seed == 1234 and cfg.n_fractions == 30 and cfg.output_format == "mhd"
+    assert cfg.stopping_statistics and cfg.stopping_criteria == 1.5 and cfg.stat_threshold == 0.5
+    assert cfg.shift == (3.0, 0.0, 0.0) and abs(cfg.density_scale - 1.035) < 1e-12
+    assert cfg.beam_numbers == [2, 1]
+    dij = tps.TpsConfig.from_input(tps.InputFile(f"Scorer Dij\nOutputDir {tmp_path}\n"))
+    assert dij.simulation_type == "perSpot"                      # Dij forces per-spot runs
+    for bad in (f"Scorer Dij, Dose\nOutputDir {tmp_path}\n", f"Scorer Heat\nOutputDir {tmp_path}\n",
+                "Scorer Dose\n", f"OutputDir {tmp_path}\nStoppingStatistics true\n",
+                f"OutputDir {tmp_path}\nStoppingStatistics true\nStoppingCriteria 1\n",
+                f"OutputDir {tmp_path}\nCalibration custom\n"):
+        with pytest.raises(ValueError):
+            tps.TpsConfig.from_input(tps.InputFile(bad))
+
+
+def test_output_writers(tmp_path):
+    edges = (np.arange(5, dtype=np.float32) * 2.0 - 4.0, np.arange(4, dtype=np.float32) - 1.5,
+             np.arange(3, dtype=np.float32) * 3.0)
+    d = np.arange(4 * 3 * 2, dtype=np.float64)
+    raw = tps.write_volume(str(tmp_path), "b_0_Dose", d, 2.5, "raw", edges)
+    np.testing.assert_array_equal(np.fromfile(raw, np.float64), d * 2.5)
+    mhd = tps.write_volume(str(tmp_path), "b_0_Dose", d, 2.5, "mhd", edges)
+    head = open(mhd).read().splitlines()
+    assert "TransformMatrix 1 0 0 0 1 0 0 0 1" in head and "Offset -3 -1 1.5" in head
+    assert "DimSize = 4 3 2" in head and "ElementSpacing = 2 1 3" in head and "ElementDataFile = b_0_Dose.raw" in head
+    np.testing.assert_array_equal(np.fromfile(os.path.join(tmp_path, "b_0_Dose.raw"), np.float64), d * 2.5)
+    mha = tps.write_volume(str(tmp_path), "b_0_Dose", d, 2.5, "mha", edges)
+    blob = open(mha, "rb").read()
+    header_end = blob.index(b"ElementDataFile = LOCAL\n") + len(b"ElementDataFile = LOCAL\n")
+    assert b"Origin = -3 -1 1.5\n" in blob[:header_end] and b"HeaderSize = -1\n" in blob[:header_end]
+    np.testing.assert_array_equal(np.frombuffer(blob[header_end:], np.float64), d * 2.5)

@@ -1,0 +1,103 @@
+"""The treatment-planning environment on the GPU: a small CT, a synthetic beam model and two
+beams run from an input file with moqui's keys; the written volumes against direct C-ABI runs of
+the same plan and seed, statistical stopping, the Dij output and a beam-frame range shifter."""
+import os
+
+import numpy as np
+import pytest
+
+from moquimc_gb300 import capi, machine, phantom, tps
+
+pytestmark = pytest.mark.gpu
+
+MODEL = """
+[geometry]
+SAD(mm) 2000 1800
+[spot]
+90.0   90.2  0.7  5.0  5.2  0.003  0.003  1.0e5
+130.0  130.3 0.7  4.2  4.4  0.0025 0.0025 1.0e5
+170.0  170.1 0.6  3.6  3.7  0.002  0.002  1.0e5
+"""
+
+
+def _ct():
+    nx, ny, nz = 60, 80, 40
+    hu = np.zeros((nz, ny, nx), np.int16)
+    hu[:, 30:36, :] = 900                      # a bone slab across the beam (along +y)
+    edges = phantom.phantom_box_edges((120.0, 160.0, 80.0), (0.0, 0.0, 0.0), (nx, ny, nz))
+    return hu, edges
+
+
+def _beams(devices=()):
+    spots = np.array([[e, x, z, 4.0] for e in (110.0, 140.0) for x in (-6.0, 0.0, 6.0) for z in (-6.0, 6.0)],
+                     np.float32)
+    return [tps.Beam("beam1", spots, devices=list(devices)), tps.Beam("Setup", spots[:1]),
+            tps.Beam("beam2", spots[::2], gantry=10.0)]
+
+
+def _env(tmp_path, extra, devices=()):
+    text = f"RandomSeed 77\nScorer Dose, LETd\nParticlesPerHistory 1000\nNumberOfFraction 2\nOutputDir {tmp_path}\n"
+    cfg = tps.TpsConfig.from_input(tps.InputFile(text + extra))
+    hu, edges = _ct()
+    return tps.TpsEnv(cfg, hu, edges, _beams(devices), machine.PBSMachine.parse(MODEL)), hu, edges
+
+
+def test_tps_run_writes_scaled_volumes(tmp_path):
+    env, hu, edges = _env(tmp_path, "OverwriteResults true\n")
+    out = env.run()
+    assert set(out) == {"beam1", "beam2"}                       # "Setup" is skipped
+    n = int(np.prod(hu.shape))
+    scale = 1000.0 * 1.1 * 2
+    dose = np.fromfile(out["beam1"]["Dose"], np.float64)
+    assert dose.size == n and dose.max() > 0
+    for name in ("LETd_numer", "LETd_denom"):
+        assert np.fromfile(out["beam1"][name], np.float64).size == n
+    # the same plan and seed through the C ABI directly
+    m = machine.PBSMachine.parse(MODEL)
+    plan = m.plan(env.beams[0].spots, -1.0, 390.0, (0.0, 0.0, 0.0, 90.0), (0.0, 0.0, 0.0), histories_from_ratio=1000.0)
+    c = capi.Context(0)
+    try:
+        c.set_physics(False)
+        cid = c.add_child(*edges)
+        c.set_hu(cid, hu)
+        sid = c.add_scorer(cid, capi.DOSE_W)
+        N = c.set_spot_plan(plan)
+        c.transport_plan(0, N, 77)
+        ref = c.tally(sid) * scale
+    finally:
+        c.close()
+    np.testing.assert_allclose(dose, ref, rtol=1e-9, atol=1e-12 * ref.max())
+    # the beam travels along +y (iec2dicom) and stops in the CT: dose beyond the bone slab
+    depth = dose.reshape(hu.shape).sum(axis=(0, 2))
+    assert depth[:20].sum() > 0 and depth[40:].sum() > 0
+
+
+def test_tps_statistical_stopping(tmp_path):
+    env, _, _ = _env(tmp_path, "StoppingStatistics true\nStoppingCriteria 2.0\nStatThreshold 0.5\nBeamNumbers 1\n")
+    out = env.run()
+    assert list(out) == ["beam1"]
+    assert int(out["beam1"]["passes"]) >= 1 and float(out["beam1"]["uncertainty"]) <= 0.02
+
+
+def test_tps_dij_output(tmp_path):
+    sps = pytest.importorskip("scipy.sparse")
+    cfg = tps.TpsConfig.from_input(tps.InputFile(f"RandomSeed 5\nScorer Dij\nParticlesPerHistory 1000\n"
+                                                 f"NumberOfFraction 1\nOutputDir {tmp_path}\nBeamNumbers 1\n"))
+    hu, edges = _ct()
+    out = tps.TpsEnv(cfg, hu, edges, _beams(), machine.PBSMachine.parse(MODEL)).run()
+    z = np.load(out["beam1"]["Dij"])
+    m = sps.csr_matrix((z["data"], z["indices"], z["indptr"]), shape=tuple(z["shape"]))
+    assert m.shape[0] == 12 and m.nnz > 0
+
+
+def test_tps_range_shifter_in_the_beam_frame(tmp_path):
+    rs = [("rangeshifter", (-100.0, -100.0, 150.0), (100.0, 100.0, 180.0), 0.0, None, (0.0, 0.0, 0.0))]
+    with_rs, hu, _ = _env(os.path.join(tmp_path, "a"), "RangeshifterDensity 1.19\nBeamNumbers 1\n", rs)
+    without, _, _ = _env(os.path.join(tmp_path, "b"), "BeamNumbers 1\n")
+    d1 = np.fromfile(with_rs.run()["beam1"]["Dose"], np.float64).reshape(hu.shape)
+    d0 = np.fromfile(without.run()["beam1"]["Dose"], np.float64).reshape(hu.shape)
+    assert os.path.exists(os.path.join(tmp_path, "a", "beam1_1_Dose.raw"))   # the CT is child 1
+    # depth profiles from the entrance (the beam travels along +y)
+    r1 = phantom.r80(d1.sum(axis=(0, 2)), 2.0)
+    r0 = phantom.r80(d0.sum(axis=(0, 2)), 2.0)
+    assert r0 - r1 > 20.0                                      # 30 mm of 1.19 g/cm^3 before the CT
