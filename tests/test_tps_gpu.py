@@ -52,21 +52,27 @@ def test_tps_run_writes_scaled_volumes(tmp_path):
     assert dose.size == n and dose.max() > 0
     for name in ("LETd_numer", "LETd_denom"):
         assert np.fromfile(out["beam1"][name], np.float64).size == n
-    # the same plan and seed through the C ABI directly
+    # the same plan, seed and scorers through the C ABI directly.  With three scorers on the CT
+    # the reference's non-statistics kernel scores the first one (Dose) twice per step
+    # (mqi_transport.hpp:204-225), and tps_env with "Scorer Dose, LETd" inherits that: so does
+    # this environment, and a single dose scorer gives half the volume.
     m = machine.PBSMachine.parse(MODEL)
     plan = m.plan(env.beams[0].spots, -1.0, 390.0, (0.0, 0.0, 0.0, 90.0), (0.0, 0.0, 0.0), histories_from_ratio=1000.0)
-    c = capi.Context(0)
-    try:
-        c.set_physics(False)
-        cid = c.add_child(*edges)
-        c.set_hu(cid, hu)
-        sid = c.add_scorer(cid, capi.DOSE_W)
-        N = c.set_spot_plan(plan)
-        c.transport_plan(0, N, 77)
-        ref = c.tally(sid) * scale
-    finally:
-        c.close()
-    np.testing.assert_allclose(dose, ref, rtol=1e-9, atol=1e-12 * ref.max())
+    refs = {}
+    for scorers in ((capi.DOSE_W, capi.LETD_NUM, capi.LETD_DEN), (capi.DOSE_W,)):
+        c = capi.Context(0)
+        try:
+            c.set_physics(False)
+            cid = c.add_child(*edges)
+            c.set_hu(cid, hu)
+            sid = [c.add_scorer(cid, t) for t in scorers][0]
+            N = c.set_spot_plan(plan)
+            c.transport_plan(0, N, 77)
+            refs[len(scorers)] = c.tally(sid) * scale
+        finally:
+            c.close()
+    np.testing.assert_allclose(dose, refs[3], rtol=1e-9, atol=1e-12 * refs[3].max())
+    np.testing.assert_allclose(dose, 2.0 * refs[1], rtol=1e-9, atol=1e-12 * refs[1].max())
     # the beam travels along +y (iec2dicom) and stops in the CT: dose beyond the bone slab
     depth = dose.reshape(hu.shape).sum(axis=(0, 2))
     assert depth[:20].sum() > 0 and depth[40:].sum() > 0
