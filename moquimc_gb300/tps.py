@@ -87,6 +87,60 @@ class InputFile:
 SCORERS = ("EnergyDeposition", "Dose", "LETd", "LETt", "Dij", "TrackLength")
 
 
+def read_mask_mha(path: str) -> np.ndarray:
+    """mask_reader::read_mha_file (moqui/base/mqi_file_handler.hpp:38-90): header lines "Key = value"
+    up to `ElementDataFile = LOCAL`, then DimSize x*y*z bytes of uint8 mask."""
+    with open(path, "rb") as f:
+        blob = f.read()
+    dims, pos = None, 0
+    while pos < len(blob):
+        end = blob.find(b"\n", pos)
+        end = len(blob) if end < 0 else end
+        line = blob[pos:end].decode("latin-1").strip()
+        pos = end + 1
+        key, _, value = line.partition("=")
+        key, value = key.strip().lower(), value.strip()
+        if key == "dimsize":
+            dims = [int(InputFile._atoi(v)) for v in value.split()[:3]]
+        elif key == "elementdatafile":
+            if value.lower() != "local":
+                raise ValueError("Mask files does not contain data.")
+            break
+    if dims is None:
+        raise ValueError(f"{path}: no DimSize")
+    n = dims[0] * dims[1] * dims[2]
+    return np.frombuffer(blob[pos:pos + n], np.uint8).copy()
+
+
+def mask_to_contour(mask_total: np.ndarray):
+    """mask_reader::mask_to_roi (mqi_file_handler.hpp:176-218): runs of voxels, in voxel order,
+    that start at a voxel whose summed mask is exactly 1 and end at the next voxel whose summed
+    mask is 0 -- a CONTOUR ROI as (start, stride, accumulated stride).  A run still open at the
+    end of the volume is closed there (the reference leaves its stride unset)."""
+    m = np.asarray(mask_total).reshape(-1)
+    start, stride = [], []
+    open_run = False
+    for v, x in enumerate(m):
+        if x == 1 and not open_run:
+            open_run = True
+            start.append(v)
+        if x == 0 and open_run:
+            open_run = False
+            stride.append(v - start[-1])
+    if open_run:
+        stride.append(len(m) - start[-1])
+    start = np.asarray(start, np.uint32)
+    stride = np.asarray(stride, np.uint32)
+    return start, stride, np.cumsum(stride, dtype=np.uint64).astype(np.uint32)
+
+
+def contour_voxels(start: np.ndarray, stride: np.ndarray) -> np.ndarray:
+    """The voxels of a CONTOUR ROI in mask order (the order of its compact tally)."""
+    if len(start) == 0:
+        return np.zeros(0, np.int64)
+    return np.concatenate([np.arange(int(a), int(a) + int(b), dtype=np.int64) for a, b in zip(start, stride)])
+
+
 @dataclass
 class TpsConfig:
     """The input keys tps_env reads (mqi_tps_env.hpp:155-330), with its defaults."""
@@ -111,6 +165,9 @@ class TpsConfig:
     stopping_criteria: float = -1.0      # percent
     stat_threshold: float = 0.0
     beam_numbers: List[int] = field(default_factory=list)
+    scoring_mask: bool = False
+    mask_files: List[str] = field(default_factory=list)
+    stat_roi_mask_files: List[str] = field(default_factory=list)
 
     @classmethod
     def from_input(cls, p: InputFile) -> "TpsConfig":
@@ -146,12 +203,18 @@ class TpsConfig:
             stopping_statistics=p.get_bool("StoppingStatistics", False),
             stat_threshold=p.get_float("StatThreshold", 0.0),
             beam_numbers=[int(InputFile._atoi(v)) for v in p.get_string_vector("BeamNumbers", ",")],
+            scoring_mask=p.get_bool("ScoringMask", False),
+            stat_roi_mask_files=p.get_string_vector("StatROIMaskFilename", ","),
         )
+        if cfg.scoring_mask:
+            cfg.mask_files = p.get_string_vector("Mask", ",")
+            if not cfg.mask_files:
+                raise ValueError("Mask filename is missing")
         if cfg.stopping_statistics:
             cfg.stopping_criteria = p.get_float("StoppingCriteria", -1.0)
             if cfg.stopping_criteria < 0:
                 raise ValueError("Statistical criteria must be positive float")
-            if cfg.stat_threshold <= 0:
+            if cfg.stat_threshold <= 0 and not cfg.stat_roi_mask_files:
                 raise ValueError("If no contour or mask is selected, the statistical threshold cannot be zero")
         if cfg.calibration.lower() != "default":
             raise ValueError("Unknown calibration method")
@@ -274,20 +337,32 @@ class TpsEnv:
             c.set_hu(cid, self.hu, cfg.density_scale)
             names: List[tuple] = []
             dij = None
+            roi = {}
+            if cfg.scoring_mask:   # the scorers' ROI: the summed masks (mqi_tps_env.hpp:775-785)
+                total = sum(read_mask_mha(f).astype(np.uint16) for f in cfg.mask_files)
+                st, sr, ac = mask_to_contour(total)
+                roi = {"roi_method": capi.ROI_CONTOUR, "start": st, "stride": sr, "acc": ac}
             for s in cfg.scorers:
                 if s == "Dose":
-                    names.append((s, c.add_scorer(cid, capi.DOSE_W)))
+                    names.append((s, c.add_scorer(cid, capi.DOSE_W, **roi)))
                 # EnergyDeposition and TrackLength are accepted names without a scorer in tps_env
                 # (its scorer set-up, :789-933, creates none for them), so they write nothing here
                 elif s == "LETd":
-                    names.append(("LETd_numer", c.add_scorer(cid, capi.LETD_NUM)))
-                    names.append(("LETd_denom", c.add_scorer(cid, capi.LETD_DEN)))
+                    names.append(("LETd_numer", c.add_scorer(cid, capi.LETD_NUM, **roi)))
+                    names.append(("LETd_denom", c.add_scorer(cid, capi.LETD_DEN, **roi)))
                 elif s == "LETt":
-                    names.append(("LETt_numer", c.add_scorer(cid, capi.LETT_NUM)))
-                    names.append(("LETt_denom", c.add_scorer(cid, capi.LETT_DEN)))
+                    names.append(("LETt_numer", c.add_scorer(cid, capi.LETT_NUM, **roi)))
+                    names.append(("LETt_denom", c.add_scorer(cid, capi.LETT_DEN, **roi)))
                 elif s == "Dij":
                     dij = c.add_dij_scorer(cid, capacity=1 << 28)
-            stat = c.add_stat_scorers(cid) if cfg.stopping_statistics else None
+            stat = None
+            if cfg.stopping_statistics:
+                if cfg.stat_roi_mask_files:   # StatROIMaskFilename, else the whole CT
+                    total = sum(read_mask_mha(f).astype(np.uint16) for f in cfg.stat_roi_mask_files)
+                    st, sr, ac = mask_to_contour(total)
+                    stat = c.add_stat_scorers(cid, capi.ROI_CONTOUR, st, sr, ac)
+                else:
+                    stat = c.add_stat_scorers(cid)
             plan = self._plan(beam)
             n = c.set_spot_plan(plan)
             seed = (cfg.random_seed + 10000 * k) & 0xFFFFFFFF
@@ -310,7 +385,12 @@ class TpsEnv:
             child_index = len(beam.devices)
             for name, sid in names:
                 fname = f"{beam.name}_{child_index}_{name}"
-                out[name] = write_volume(cfg.output_dir, fname, c.tally(sid), scale, cfg.output_format, shifted)
+                vol = c.tally(sid)
+                if roi:   # the reference's tables are keyed by voxel: write the whole CT volume
+                    full = np.zeros(self.hu.size, np.float64)
+                    full[contour_voxels(roi["start"], roi["stride"])] = vol
+                    vol = full
+                out[name] = write_volume(cfg.output_dir, fname, vol, scale, cfg.output_format, shifted)
             if dij is not None:
                 op = c.dij_build(dij, scale=scale)
                 path = os.path.join(cfg.output_dir, f"{beam.name}_{child_index}_Dij.npz")

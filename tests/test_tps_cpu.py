@@ -74,3 +74,33 @@ def test_output_writers(tmp_path):
     header_end = blob.index(b"ElementDataFile = LOCAL\n") + len(b"ElementDataFile = LOCAL\n")
     assert b"Origin = -3 -1 1.5\n" in blob[:header_end] and b"HeaderSize = -1\n" in blob[:header_end]
     np.testing.assert_array_equal(np.frombuffer(blob[header_end:], np.float64), d * 2.5)
+
+
+def _write_mask(path, mask, dims):
+    with open(path, "wb") as f:
+        f.write(("ObjectType = Image\nNDims = 3\nDimSize = %d %d %d\nElementType = MET_UCHAR\n"
+                 "ElementDataFile = LOCAL\n" % dims).encode())
+        f.write(np.ascontiguousarray(mask, np.uint8).tobytes())
+
+
+def test_mask_files_to_contour_roi(tmp_path):
+    dims = (6, 4, 3)
+    a = np.zeros(dims[::-1], np.uint8)
+    b = np.zeros(dims[::-1], np.uint8)
+    a[0, 1, 1:4] = 1          # one run of 3
+    a[2, 3, 4:] = 1           # a run open at the end of the volume
+    b[0, 1, 3:5] = 1          # overlaps a at one voxel (sum 2)
+    pa, pb = os.path.join(tmp_path, "a.mha"), os.path.join(tmp_path, "b.mha")
+    _write_mask(pa, a, dims)
+    _write_mask(pb, b, dims)
+    np.testing.assert_array_equal(tps.read_mask_mha(pa), a.reshape(-1))
+    total = tps.read_mask_mha(pa).astype(np.uint16) + tps.read_mask_mha(pb)
+    start, stride, acc = tps.mask_to_contour(total)
+    # the summed mask along row (z=0, y=1) is 0 1 1 2 1 0: a run starts at x=1 and ends at x=5
+    # (a voxel of sum 2 neither starts nor ends a run); the run at the end is closed there
+    assert list(start) == [7, 70] and list(stride) == [4, 2] and list(acc) == [4, 6]
+    np.testing.assert_array_equal(tps.contour_voxels(start, stride), [7, 8, 9, 10, 70, 71])
+    with open(os.path.join(tmp_path, "bad.mha"), "w") as f:
+        f.write("DimSize = 1 1 1\nElementDataFile = mask.raw\n")
+    with pytest.raises(ValueError):
+        tps.read_mask_mha(os.path.join(tmp_path, "bad.mha"))

@@ -107,3 +107,26 @@ def test_tps_range_shifter_in_the_beam_frame(tmp_path):
     r1 = phantom.r80(d1.sum(axis=(0, 2)), 2.0)
     r0 = phantom.r80(d0.sum(axis=(0, 2)), 2.0)
     assert r0 - r1 > 20.0                                      # 30 mm of 1.19 g/cm^3 before the CT
+
+
+def test_tps_scoring_mask(tmp_path):
+    """ScoringMask with a mask file: the dose inside the mask equals the unmasked run's (same
+    plan and seed), zero outside; the volume is written at the CT size."""
+    hu, edges = _ct()
+    mask = np.zeros(hu.shape, np.uint8)
+    mask[10:30, 20:60, 20:40] = 1
+    path = os.path.join(tmp_path, "target.mha")
+    with open(path, "wb") as f:
+        f.write(("ObjectType = Image\nNDims = 3\nDimSize = %d %d %d\nElementType = MET_UCHAR\n"
+                 "ElementDataFile = LOCAL\n" % hu.shape[::-1]).encode())
+        f.write(mask.tobytes())
+    runs = {}
+    for tag, extra in (("masked", f"ScoringMask true\nMask {path}\n"), ("full", "")):
+        text = (f"RandomSeed 31\nScorer Dose\nParticlesPerHistory 1000\nNumberOfFraction 1\n"
+                f"OutputDir {os.path.join(tmp_path, tag)}\nBeamNumbers 1\n" + extra)
+        cfg = tps.TpsConfig.from_input(tps.InputFile(text))
+        out = tps.TpsEnv(cfg, hu, edges, _beams(), machine.PBSMachine.parse(MODEL)).run()
+        runs[tag] = np.fromfile(out["beam1"]["Dose"], np.float64).reshape(hu.shape)
+    assert runs["masked"][mask == 0].max() == 0 and runs["masked"].max() > 0
+    np.testing.assert_allclose(runs["masked"][mask == 1], runs["full"][mask == 1], rtol=1e-9,
+                               atol=1e-12 * runs["full"].max())
