@@ -89,7 +89,6 @@ struct Queue {
     uint32_t  capacity;
 };
 
-/// Kernel parameters for one transport wave.
 /// A tabulated calibration (mqi_set_calibration); mode 0 = the default curves.
 struct CalibDev {
     int          mode;
@@ -99,6 +98,7 @@ struct CalibDev {
     const float* x0;    // device: n_rho
 };
 
+/// Kernel parameters for one transport wave.
 struct WaveParams {
     int       n_children;
     ChildDev  child[kMaxChildren];
