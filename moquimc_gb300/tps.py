@@ -386,7 +386,7 @@ class TpsEnv:
             for name, sid in names:
                 fname = f"{beam.name}_{child_index}_{name}"
                 vol = c.tally(sid)
-                if roi:   # the reference's tables are keyed by voxel: write the whole CT volume
+                if roi and vol.size != self.hu.size:   # a mask-indexed tally: the CT volume is written
                     full = np.zeros(self.hu.size, np.float64)
                     full[contour_voxels(roi["start"], roi["stride"])] = vol
                     vol = full
