@@ -157,7 +157,8 @@ int mqi_set_hu(mqi_ctx* ctx, int child_id, const int16_t* hu, float density_scal
 
 /* Add a scorer to a child: scorer<R>(name, capacity, fp_compute_hit) + roi_t
  * (moqui/base/mqi_scorer.hpp:39-79, moqui/base/mqi_roi.hpp:18-194).  For MQI_ROI_DIRECT the
- * three arrays may be NULL.  The tally is a dense FP64 array of roi mask size. */
+ * three arrays may be NULL.  The tally is a dense FP64 array over the child's voxels, keyed by
+ * voxel as the reference's tables are (entries outside the ROI stay zero). */
 int mqi_add_scorer(mqi_ctx* ctx, int child_id, int type, int roi_method, uint32_t roi_length,
                    const uint32_t* roi_start, const uint32_t* roi_stride, const uint32_t* roi_acc,
                    int* scorer_id);
