@@ -68,14 +68,18 @@ def build_library(force: bool = False, verbose: bool = False) -> str:
 
 
 def build_host_tools(force: bool = False) -> str:
-    """Build the phantom_env executable (C++ host over the C ABI)."""
-    src = os.path.join(HOST, "phantom_env_main.cpp")
-    out = os.path.join(LIB_DIR, "phantom_env")
-    deps = [src, LIB] + [os.path.join(HOST, f) for f in os.listdir(HOST) if f.endswith((".hpp", ".h"))]
-    if force or _stale(out, deps):
-        _run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", f"-I{INCLUDE}", f"-I{HOST}", src, "-o", out,
-              f"-L{LIB_DIR}", "-lmqigpu", f"-Wl,-rpath,{LIB_DIR}"])
-    return out
+    """Build the phantom_env and tps_env executables (C++ hosts over the C ABI)."""
+    hdrs = [os.path.join(HOST, f) for f in os.listdir(HOST) if f.endswith((".hpp", ".h"))]
+    jobs = []
+    for name in ("phantom_env", "tps_env"):
+        src = os.path.join(HOST, f"{name}_main.cpp")
+        out = os.path.join(LIB_DIR, name)
+        if os.path.exists(src) and (force or _stale(out, [src, LIB] + hdrs)):
+            jobs.append(["g++", "-std=c++17", "-O2", "-ffp-contract=off", f"-I{INCLUDE}", f"-I{HOST}", src, "-o", out,
+                         f"-L{LIB_DIR}", "-lmqigpu", f"-Wl,-rpath,{LIB_DIR}"])
+    with cf.ThreadPoolExecutor(max_workers=max(len(jobs), 1)) as ex:
+        list(ex.map(_run, jobs))
+    return os.path.join(LIB_DIR, "phantom_env")
 
 
 def build_all(force: bool = False) -> None:

@@ -41,149 +41,12 @@
 #include <vector>
 
 #include "mqi_gpu.h"
+#include "mqi_host.hpp"
 
 namespace
 {
 
-/// moqui's cli: "--name v1 v2 ..." (moqui/base/mqi_cli.hpp).
-class Cli
-{
-public:
-    Cli(int argc, char** argv) {
-        std::string key;
-        for (int i = 1; i < argc; ++i) {
-            const std::string a = argv[i];
-            if (a.size() > 2 && a[0] == '-' && a[1] == '-' && !is_number(a)) {
-                key = a;
-                opts_[key];
-            } else if (!key.empty()) {
-                opts_[key].push_back(a);
-            } else {
-                throw std::runtime_error("unexpected argument " + a);
-            }
-        }
-    }
-    const std::vector<std::string>&
-    operator[](const std::string& k) const {
-        static const std::vector<std::string> none;
-        auto it = opts_.find(k);
-        return it == opts_.end() ? none : it->second;
-    }
-
-private:
-    static bool
-    is_number(const std::string& s) {
-        char* end = nullptr;
-        std::strtod(s.c_str(), &end);
-        return end && *end == '\0';
-    }
-    std::map<std::string, std::vector<std::string>> opts_;
-};
-
-struct Mat3 {
-    float m[9] = { 1, 0, 0, 0, 1, 0, 0, 0, 1 };
-};
-
-/// mat3x3<float>(a, b, c): identity, then rotations about x, y and z in that order, each applied
-/// as the reference's rotate_x/_y/_z updates (moqui/base/mqi_matrix.hpp:69-76, 213-272).
-Mat3
-euler(float a, float b, float c) {
-    Mat3 r;
-    float& xx = r.m[0]; float& xy = r.m[1]; float& xz = r.m[2];
-    float& yx = r.m[3]; float& yy = r.m[4]; float& yz = r.m[5];
-    float& zx = r.m[6]; float& zy = r.m[7]; float& zz = r.m[8];
-    if (a != 0) {
-        const float c1 = std::cos(a), s1 = std::sin(a);
-        const float x1 = yx, y1 = yy, z1 = yz;
-        yx = c1 * x1 - s1 * zx; yy = c1 * y1 - s1 * zy; yz = c1 * z1 - s1 * zz;
-        zx = s1 * x1 + c1 * zx; zy = s1 * y1 + c1 * zy; zz = s1 * z1 + c1 * zz;
-    }
-    if (b != 0) {
-        const float c1 = std::cos(b), s1 = std::sin(b);
-        const float x1 = zx, y1 = zy, z1 = zz;
-        zx = c1 * x1 - s1 * xx; zy = c1 * y1 - s1 * xy; zz = c1 * z1 - s1 * xz;
-        xx = s1 * x1 + c1 * xx; xy = s1 * y1 + c1 * xy; xz = s1 * z1 + c1 * xz;
-    }
-    if (c != 0) {
-        const float c1 = std::cos(c), s1 = std::sin(c);
-        const float x1 = xx, y1 = xy, z1 = xz;
-        xx = c1 * x1 - s1 * yx; xy = c1 * y1 - s1 * yy; xz = c1 * z1 - s1 * yz;
-        yx = s1 * x1 + c1 * yx; yy = s1 * y1 + c1 * yy; yz = s1 * z1 + c1 * yz;
-    }
-    return r;
-}
-
-Mat3
-mul(const Mat3& a, const Mat3& b) {
-    Mat3 r;
-    for (int i = 0; i < 3; ++i)
-        for (int j = 0; j < 3; ++j)
-            r.m[3 * i + j] = a.m[3 * i] * b.m[j] + a.m[3 * i + 1] * b.m[3 + j] + a.m[3 * i + 2] * b.m[6 + j];
-    return r;
-}
-
-/// coordinate_transform: rotation = iec2dicom * couch * gantry * collimator
-/// (moqui/base/mqi_coordinate_transform.hpp:52-58).
-Mat3
-beam_rotation(const std::array<float, 4>& ang) {
-    const float d2r = (float) (3.14159265358979323846 / 180.0);   // coordinate_transform::deg2rad
-    const Mat3 col = euler(0, 0, ang[0] * d2r);
-    const Mat3 gan = euler(0, ang[1] * d2r, 0);
-    const Mat3 cou = euler(0, 0, ang[2] * d2r);
-    const Mat3 iec = euler(ang[3] * d2r, 0, 0);
-    return mul(mul(mul(iec, cou), gan), col);
-}
-
-/// grid3d's uniform edges from phantom_env::setup_world's corners (mqi_phantom_env.hpp:256-264):
-/// corners pos -/+ 0.5 l in double stored as float, then edge_i = min + i * ((max - min) / n).
-std::vector<float>
-edges(float pos, float len, int n) {
-    const float lo = (float) (pos - 0.5 * len);
-    const float hi = (float) (pos + 0.5 * len);
-    const float d  = (hi - lo) / (float) n;
-    std::vector<float> e(n + 1);
-    for (int i = 0; i <= n; ++i) e[i] = lo + (float) i * d;
-    return e;
-}
-
-float
-to_f(const std::vector<std::string>& v, size_t i, float dflt) {
-    return v.size() > i ? std::stof(v[i]) : dflt;
-}
-
-void
-write_outputs(const std::string& dir, const std::string& name, const std::string& fmt, const std::vector<double>& d,
-              const std::vector<float>& xe, const std::vector<float>& ye, const std::vector<float>& ze) {
-    const int   nx = (int) xe.size() - 1, ny = (int) ye.size() - 1, nz = (int) ze.size() - 1;
-    const float dx = xe[1] - xe[0], dy = ye[1] - ye[0], dz = ze[1] - ze[0];
-    const float x0 = xe[0] + dx * 0.5f, y0 = ye[0] + dy * 0.5f, z0 = ze[0] + dz * 0.5f;
-    if (fmt == "mha") {
-        std::ofstream f(dir + "/" + name + ".mha", std::ios::binary);
-        f << "ObjectType = Image\nNDims = 3\nBinaryData = True\nBinaryDataByteOrderMSB = False\n"
-          << "CompressedData = False\nTransformMatrix = 1 0 0 0 1 0 0 0 1\n"
-          << "Origin = " << std::setprecision(9) << x0 << " " << y0 << " " << z0 << "\n"
-          << "CenterOfRotation = 0 0 0\nAnatomicOrientation = RAI\n"
-          << "DimSize = " << nx << " " << ny << " " << nz << "\nElementType = MET_DOUBLE\nHeaderSize = -1\n"
-          << "ElementSpacing = " << std::setprecision(9) << dx << " " << dy << " " << dz << "\n"
-          << "ElementDataFile = LOCAL\n";
-        f.write(reinterpret_cast<const char*>(d.data()), d.size() * sizeof(double));
-        if (!f) throw std::runtime_error("cannot write " + dir + "/" + name + ".mha");
-        return;
-    }
-    if (fmt == "mhd") {
-        std::ofstream h(dir + "/" + name + ".mhd");
-        h << "ObjectType = Image\nNDims = 3\nBinaryData = True\nBinaryDataByteOrderMSB = False\n"
-          << "CompressedData = False\nTransformMatrix 1 0 0 0 1 0 0 0 1\n"
-          << "Offset " << x0 << " " << y0 << " " << z0 << "\nCenterOfRotation 0 0 0\n"
-          << "AnatomicOrientation = RAI\nDimSize = " << nx << " " << ny << " " << nz << "\n"
-          << "ElementType = MET_DOUBLE\nElementSpacing = " << dx << " " << dy << " " << dz << "\n"
-          << "ElementDataFile = " << name << ".raw\n";
-        if (!h) throw std::runtime_error("cannot write " + dir + "/" + name + ".mhd");
-    }
-    std::ofstream r(dir + "/" + name + ".raw", std::ios::binary);
-    r.write(reinterpret_cast<const char*>(d.data()), d.size() * sizeof(double));
-    if (!r) throw std::runtime_error("cannot write " + dir + "/" + name + ".raw");
-}
+using namespace mqi_host;
 
 /// The beam source of setup_beamsource (mqi_phantom_env.hpp:204-232): std::default_random_engine
 /// seeded with the random seed; per history the phase-space draws Ux Vx Uy Vy Uz in the
@@ -215,10 +78,6 @@ sample_vertices(uint64_t n, int seed, bool gaussian, const std::array<float, 3>&
     return v;
 }
 
-void
-check(int rc, mqi_ctx* ctx, const char* what) {
-    if (rc != MQI_OK) throw std::runtime_error(std::string(what) + ": " + mqi_last_error(ctx));
-}
 
 int
 run(const Cli& cli) {
@@ -290,7 +149,7 @@ run(const Cli& cli) {
     std::vector<double> dose(nvox);
     uint64_t n_out = 0;
     check(mqi_get_tally(ctx, scorer, dose.data(), &n_out, 0), ctx, "mqi_get_tally");
-    write_outputs(out_dir, "0_water_dE_total", fmt, dose, xe, ye, ze);
+    write_outputs(out_dir, "0_water_dE_total", fmt, dose, 1.0, xe, ye, ze);
     if (!cli["--json"].empty()) {
         std::ofstream j(cli["--json"][0]);
         j << "{\"transport_seconds\": " << secs << ", \"histories\": " << n_hist << ", \"tracked\": " << st.histories

@@ -4,7 +4,7 @@ moqui's generic PBS machine (moqui/base/mqi_treatment_machine_pbs.hpp) reads a b
 (load_beamdata, :400-520) and turns every spot of a plan into a beamlet: the energy and the spot's
 phase-space widths interpolated at the nominal energy (characterize_beamlet, :199-236), the beam
 started at source_to_isocenter_mm on the ray from the virtual source (beam_starting_position,
-:324-333), and a history count (characterize_history, :134-143, or create_beamsource's
+moqui/base/mqi_treatment_machine_ion.hpp:324-333), and a history count (characterize_history, :134-143, or create_beamsource's
 ceil(meterset x particles per history), mqi_treatment_machine_ion.hpp:147-189).  The beamlet is
 norm_1d energy x Gaussian phsp_6d (mqi_phsp6d.hpp) x the beam's coordinate_transform
 (mqi_coordinate_transform.hpp): exactly what a capi.SPOT_DTYPE entry holds, so the plan is sampled
@@ -129,7 +129,8 @@ class PBSMachine:
         return out
 
     def beam_start(self, x: float, y: float, source_to_isocenter_mm: float) -> Tuple[np.ndarray, np.ndarray]:
-        """beam_starting_position (:324-333) and the unit direction to the isocentre point (x, y, 0).
+        """beam_starting_position (mqi_treatment_machine_ion.hpp:324-333) and the unit direction to the
+        isocentre point (x, y, 0).
         An infinite SAD is a parallel beam (the reference's inf/inf would give NaN)."""
         z = f32(source_to_isocenter_mm)
         iso = np.array([x, y, 0.0], np.float32)

@@ -130,3 +130,55 @@ def test_tps_scoring_mask(tmp_path):
     assert runs["masked"][mask == 0].max() == 0 and runs["masked"].max() > 0
     np.testing.assert_allclose(runs["masked"][mask == 1], runs["full"][mask == 1], rtol=1e-9,
                                atol=1e-12 * runs["full"].max())
+
+
+def test_cpp_tps_driver_matches_the_python_environment(tmp_path):
+    """The C++ host driver (moquimc_gb300/host/tps_env_main.cpp) and the Python environment on the
+    same input file, CT, beams and beam model write the same volumes."""
+    import subprocess
+
+    from moquimc_gb300 import build
+
+    exe = os.path.join(build.LIB_DIR, "tps_env")
+    if not os.path.exists(exe):
+        build.build_host_tools()
+    hu, edges = _ct()
+    ct = os.path.join(tmp_path, "ct.raw")
+    hu.tofile(ct)
+    model = os.path.join(tmp_path, "model.txt")
+    with open(model, "w") as f:
+        f.write(MODEL)
+    rs = ("rangeshifter", (-100.0, -100.0, 150.0), (100.0, 100.0, 180.0), 0.0, None, (0.0, 0.0, 0.0))
+    beams = _beams([rs])
+    with open(os.path.join(tmp_path, "beams.txt"), "w") as f:
+        for b in beams:
+            f.write(f"beam {b.name} {b.gantry} {b.couch} {b.collimator} 0 0 0 390\n")
+            for s in b.spots:
+                f.write("spot " + " ".join(repr(float(v)) for v in s) + "\n")
+            for d in b.devices:
+                f.write("rangeshifter " + " ".join(repr(float(v)) for v in (*d[1], *d[2])) + "\n")
+    outs = {}
+    for tag in ("cpp", "py"):
+        text = (f"RandomSeed 42\nScorer Dose, LETt\nParticlesPerHistory 1000\nNumberOfFraction 3\nRBE 1.1\n"
+                f"RangeshifterDensity 1.19\nDensityScaling 1.02\nXShift 1.5\nMachine PBS:{model}\n"
+                f"OutputDir {os.path.join(tmp_path, tag)}\nOutputFormat mhd\n")
+        inp = os.path.join(tmp_path, f"{tag}.in")
+        with open(inp, "w") as f:
+            f.write(text)
+        if tag == "cpp":
+            res = subprocess.run([exe, inp, "--ct", ct, "--ct_nxyz", "60", "80", "40", "--ct_lxyz", "120", "160", "80",
+                                  "--ct_pxyz", "0", "0", "0", "--beams", os.path.join(tmp_path, "beams.txt")],
+                                 capture_output=True, text=True)
+            assert res.returncode == 0, res.stderr[-2000:]
+        else:
+            cfg = tps.TpsConfig.from_input(tps.InputFile.load(inp))
+            tps.TpsEnv(cfg, hu, edges, beams, machine.PBSMachine.load(model)).run()
+        outs[tag] = sorted(os.listdir(os.path.join(tmp_path, tag)))
+    assert outs["cpp"] == outs["py"] and "beam1_1_Dose.raw" in outs["cpp"] and "beam2_0_LETt_numer.mhd" in outs["cpp"]
+    for name in outs["cpp"]:
+        a, b = (os.path.join(tmp_path, t, name) for t in ("cpp", "py"))
+        if name.endswith(".raw"):
+            x, y = np.fromfile(a, np.float64), np.fromfile(b, np.float64)
+            np.testing.assert_allclose(x, y, rtol=1e-9, atol=1e-12 * max(np.abs(y).max(), 1e-30), err_msg=name)
+        else:
+            assert open(a).read() == open(b).read(), name
