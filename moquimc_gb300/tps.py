@@ -14,11 +14,10 @@ the input file with moqui's keys and defaults.
 """
 from __future__ import annotations
 
-import math
 import os
 import time
 from dataclasses import dataclass, field
-from typing import Dict, List, Optional, Sequence
+from typing import Dict, List, Sequence
 
 import numpy as np
 
