@@ -78,11 +78,26 @@ class DijOperator:
         return indptr.astype(np.int64), indices, data
 
     def save_npz(self, path: str) -> None:
-        """Write the spot-row CSR with the keys scipy.sparse.load_npz reads (indices, indptr,
-        shape, data, format), as the reference's save_to_npz does."""
+        """Write the spot-row CSR as the reference's save_to_npz does (write_dij_npz)."""
         indptr, indices, data = self.csr()
-        np.savez(path, indices=indices, indptr=indptr, shape=np.array([self.n_spots, self.n_voxels], np.int64),
-                 data=data, format=np.array("csr"))
+        write_dij_npz(path, indptr, indices, data, self.n_spots, self.n_voxels)
+
+
+def write_dij_npz(path: str, indptr, indices, data, n_spots: int, n_voxels: int) -> None:
+    """A spot-row CSR in the reference's npz layout (save_to_npz, moqui/base/mqi_io.hpp:251-320,
+    with mqi::io::save_npz's dtypes, moqui/base/mqi_sparse_io.hpp:283-330): members indices,
+    indptr, shape, data and format, stored uncompressed, with indices, indptr and shape as <u4
+    (shape = [n_spots, n_voxels]), data as <f8 and format as |S3 "csr" -- the keys and types
+    scipy.sparse.load_npz reads.  The reference's uint32 row pointers cap nnz below 2**32; a
+    larger matrix raises rather than wrapping."""
+    indptr = np.asarray(indptr)
+    if indptr.size != n_spots + 1 or (indptr.size and int(indptr[-1]) != len(indices)):
+        raise ValueError("indptr must hold n_spots + 1 row offsets ending at nnz")
+    if len(indices) >= 2 ** 32 or n_voxels >= 2 ** 32 or n_spots >= 2 ** 32:
+        raise ValueError("the reference's npz layout holds uint32 indices and row offsets")
+    np.savez(path, indices=np.asarray(indices, np.uint32), indptr=indptr.astype(np.uint32),
+             shape=np.array([n_spots, n_voxels], np.uint32), data=np.asarray(data, np.float64),
+             format=np.array(b"csr"))
 
 
 def _function():

@@ -104,3 +104,30 @@ def test_mask_files_to_contour_roi(tmp_path):
         f.write("DimSize = 1 1 1\nElementDataFile = mask.raw\n")
     with pytest.raises(ValueError):
         tps.read_mask_mha(os.path.join(tmp_path, "bad.mha"))
+
+
+def test_dij_npz_layout(tmp_path):
+    """The Dij file in the reference's npz layout (save_to_npz / mqi::io::save_npz): members in
+    its order with its dtypes, readable by scipy.sparse.load_npz as [n_spots, n_voxels]."""
+    import zipfile
+
+    from moquimc_gb300 import dij
+
+    path = os.path.join(tmp_path, "b_1_Dij.npz")
+    data = np.array([0.5, 1.5, 2.5, 4.0], np.float32)
+    dij.write_dij_npz(path, np.array([0, 2, 2, 4], np.int64), np.array([1, 5, 0, 7]), data, 3, 8)
+    with zipfile.ZipFile(path) as zf:
+        assert [i.filename for i in zf.infolist()] == ["indices.npy", "indptr.npy", "shape.npy", "data.npy", "format.npy"]
+        assert all(i.compress_type == zipfile.ZIP_STORED for i in zf.infolist())
+    z = np.load(path)
+    assert {k: z[k].dtype.str for k in z.files} == {"indices": "<u4", "indptr": "<u4", "shape": "<u4",
+                                                   "data": "<f8", "format": "|S3"}
+    assert z["format"].item() == b"csr" and list(z["shape"]) == [3, 8]
+    sps = pytest.importorskip("scipy.sparse")
+    m = sps.load_npz(path).toarray()
+    want = np.zeros((3, 8))
+    want[0, [1, 5]] = [0.5, 1.5]
+    want[2, [0, 7]] = [2.5, 4.0]
+    np.testing.assert_array_equal(m, want)
+    with pytest.raises(ValueError):
+        dij.write_dij_npz(path, np.array([0, 2]), np.array([1, 5, 0]), data[:3], 1, 8)
