@@ -161,6 +161,85 @@ write_outputs(const std::string& dir, const std::string& name, const std::string
     if (!r) throw std::runtime_error("cannot write " + dir + "/" + name + ".raw");
 }
 
+/// CRC-32 of the zip format (IEEE 802.3 polynomial, reflected: 0xEDB88320), continued from `crc`.
+inline uint32_t
+crc32_update(uint32_t crc, const void* data, size_t n) {
+    static const std::array<uint32_t, 256> table = [] {
+        std::array<uint32_t, 256> t{};
+        for (uint32_t i = 0; i < 256; ++i) {
+            uint32_t c = i;
+            for (int k = 0; k < 8; ++k) c = (c & 1u) ? 0xEDB88320u ^ (c >> 1) : c >> 1;
+            t[i] = c;
+        }
+        return t;
+    }();
+    const unsigned char* p = static_cast<const unsigned char*>(data);
+    crc = ~crc;
+    for (size_t i = 0; i < n; ++i) crc = table[(crc ^ p[i]) & 0xFFu] ^ (crc >> 8);
+    return ~crc;
+}
+
+/// One member of an npz file: an .npy array (format 1.0) with its dtype descriptor ("<u4",
+/// "<f8", "|S3") and shape tuple ("(12,)", "()").
+struct NpzArray {
+    std::string name;
+    std::string descr;
+    std::string shape;
+    const void* data;
+    size_t      bytes;
+};
+
+/// mqi::io::save_npz (moqui/base/mqi_sparse_io.hpp:167-399): the arrays as stored (uncompressed)
+/// members of a zip archive, in the given order.  Like the reference's writer it uses 32-bit zip
+/// sizes and offsets; a file past 4 GiB raises instead of wrapping.
+inline void
+write_npz(const std::string& path, const std::vector<NpzArray>& arrays) {
+    auto u16 = [](std::string& s, uint32_t v) { s.push_back((char) (v & 0xFF)); s.push_back((char) ((v >> 8) & 0xFF)); };
+    auto u32 = [&](std::string& s, uint32_t v) { u16(s, v & 0xFFFF); u16(s, v >> 16); };
+    std::ofstream f(path, std::ios::binary);
+    std::string   central;
+    uint64_t      offset = 0;
+    for (const auto& a : arrays) {
+        std::string dict = "{'descr': '" + a.descr + "', 'fortran_order': False, 'shape': " + a.shape + ", }";
+        dict.append(63 - (10 + dict.size()) % 64, ' ');   // header padded to a multiple of 64 bytes
+        dict.push_back('\n');
+        std::string head("\x93NUMPY\x01", 7);
+        head.push_back('\0');
+        u16(head, (uint32_t) dict.size());
+        head += dict;
+        const uint64_t size = head.size() + (uint64_t) a.bytes;
+        const std::string fname = a.name + ".npy";
+        if (size > 0xFFFFFFFFull || offset + size + 30 + fname.size() > 0xFFFFFFFFull)
+            throw std::runtime_error(path + ": npz members past 4 GiB need zip64, which is not written");
+        const uint32_t crc = crc32_update(crc32_update(0, head.data(), head.size()), a.data, a.bytes);
+        std::string rec;   // the fields the local and central headers share
+        u16(rec, 20); u16(rec, 0); u16(rec, 0);            // version needed, flags, stored
+        u16(rec, 0); u16(rec, 0x21);                        // time 00:00, date 1980-01-01
+        u32(rec, crc); u32(rec, (uint32_t) size); u32(rec, (uint32_t) size);
+        u16(rec, (uint32_t) fname.size()); u16(rec, 0);     // name length, no extra field
+        std::string local("PK\x03\x04", 4);
+        local += rec + fname;
+        f.write(local.data(), (std::streamsize) local.size());
+        f.write(head.data(), (std::streamsize) head.size());
+        f.write(static_cast<const char*>(a.data), (std::streamsize) a.bytes);
+        std::string cent("PK\x01\x02", 4);
+        u16(cent, 20);
+        cent += rec;
+        u16(cent, 0); u16(cent, 0); u16(cent, 0); u32(cent, 0);   // comment, disk, attributes
+        u32(cent, (uint32_t) offset);
+        central += cent + fname;
+        offset += local.size() + size;
+    }
+    if (offset + central.size() > 0xFFFFFFFFull)
+        throw std::runtime_error(path + ": npz past 4 GiB needs zip64, which is not written");
+    std::string end("PK\x05\x06", 4);
+    u16(end, 0); u16(end, 0); u16(end, (uint32_t) arrays.size()); u16(end, (uint32_t) arrays.size());
+    u32(end, (uint32_t) central.size()); u32(end, (uint32_t) offset); u16(end, 0);
+    f.write(central.data(), (std::streamsize) central.size());
+    f.write(end.data(), (std::streamsize) end.size());
+    if (!f) throw std::runtime_error("cannot write " + path);
+}
+
 inline void
 check(int rc, mqi_ctx* ctx, const char* what) {
     if (rc != MQI_OK) throw std::runtime_error(std::string(what) + ": " + mqi_last_error(ctx));

@@ -13,8 +13,9 @@
 // DensityScaling, XShift/YShift/ZShift, OutputDir, OutputFormat (raw, mhd, mha), OverwriteResults,
 // StoppingStatistics, StoppingCriteria (percent), StatThreshold, BeamNumbers, MaxHistoriesPerBatch.
 // Outputs: <OutputDir>/<beam>_<child>_<scorer>.{raw,mhd,mha} scaled by ParticlesPerHistory x RBE x
-// NumberOfFraction (save_reshaped_files, :1851-1900).  A Dij is scored with the C ABI but written by
-// the Python environment (moquimc_gb300/tps.py), which has an npz writer; here it is rejected.
+// NumberOfFraction (save_reshaped_files, :1851-1900); a Dij (scored alone, as tps_env requires) as
+// <beam>_<child>_Dij.npz, the spot-row CSR of save_to_npz (moqui/base/mqi_io.hpp:251-320) with the
+// same scale.
 //
 // Beams file, one item per line ('#' comments):
 //   beam <name> <gantry> <couch> <collimator> <iso x> <iso y> <iso z> <source-to-isocentre mm>
@@ -290,10 +291,11 @@ run(const std::string& input, const Cli& cli) {
     int             seed   = p.get_int("RandomSeed", -1);
     if (seed == -1) seed = (int) std::time(nullptr);
     std::vector<std::string> scorers = p.get_vector("Scorer", ',');
+    const bool score_dij = std::any_of(scorers.begin(), scorers.end(),
+                                       [](const std::string& s) { return strcasecmp(s.c_str(), "Dij") == 0; });
+    if (score_dij && scorers.size() > 1) throw std::runtime_error("Dij cannot be scored with the other quantities");
     for (const auto& s : scorers) {
-        if (strcasecmp(s.c_str(), "Dij") == 0)
-            throw std::runtime_error("Scorer Dij: use the Python environment (moquimc_gb300.tps), which writes the npz");
-        static const char* known[] = { "Dose", "LETd", "LETt", "EnergyDeposition", "TrackLength" };
+        static const char* known[] = { "Dose", "LETd", "LETt", "EnergyDeposition", "TrackLength", "Dij" };
         if (std::none_of(std::begin(known), std::end(known), [&](const char* k) { return strcasecmp(k, s.c_str()) == 0; }))
             throw std::runtime_error("Unrecognized scorer name");
     }
@@ -384,6 +386,10 @@ run(const std::string& input, const Cli& cli) {
             if (strcasecmp(s.c_str(), "LETd") == 0) { add("LETd_numer", MQI_SCORER_LETD_NUM); add("LETd_denom", MQI_SCORER_LETD_DEN); }
             if (strcasecmp(s.c_str(), "LETt") == 0) { add("LETt_numer", MQI_SCORER_LETT_NUM); add("LETt_denom", MQI_SCORER_LETT_DEN); }
         }
+        int dij = -1;
+        if (score_dij)   // the (voxel, spot) table; DOSE_Dij values
+            check(mqi_add_dij_scorer(ctx, cid, MQI_ROI_DIRECT, 0, nullptr, nullptr, nullptr, 1ull << 28, &dij), ctx,
+                  "mqi_add_dij_scorer");
         int d1 = -1, d2 = -1;
         if (use_stat)
             check(mqi_add_stat_scorers(ctx, cid, MQI_ROI_DIRECT, 0, nullptr, nullptr, nullptr, &d1, &d2), ctx,
@@ -407,7 +413,7 @@ run(const std::string& input, const Cli& cli) {
                   "mqi_run_plan_until_stat");
         } else {
             std::vector<std::pair<uint64_t, uint64_t>> ranges;
-            if (per_spot) {
+            if (per_spot && !score_dij) {   // a Dij run is batched: its table keys carry the spot
                 uint64_t h = 0;
                 for (const auto& sp : plan) { ranges.emplace_back(h, h + sp.histories); h += sp.histories; }
             } else {
@@ -425,6 +431,26 @@ run(const std::string& input, const Cli& cli) {
             check(mqi_get_tally(ctx, o.second, vol.data(), &n, 0), ctx, "mqi_get_tally");
             write_outputs(out_dir, b.name + "_" + std::to_string(b.devices.size()) + "_" + o.first, fmt, vol, scale, xe,
                           ye, ze);
+        }
+        if (dij >= 0) {
+            uint64_t nnz = 0;
+            check(mqi_dij_build(ctx, dij, 0, scale, &nnz), ctx, "mqi_dij_build");
+            std::vector<uint64_t> indptr(plan.size() + 1);
+            std::vector<uint32_t> indices(nnz);
+            std::vector<float>    value(nnz);
+            check(mqi_dij_get_csr(ctx, dij, indptr.data(), indices.data(), value.data(), 0), ctx, "mqi_dij_get_csr");
+            if (nnz >= (1ull << 32) || nvox >= (1ull << 32))
+                throw std::runtime_error("Dij: the npz layout holds uint32 indices and row offsets");
+            const std::vector<uint32_t> ptr32(indptr.begin(), indptr.end());
+            const std::vector<double>   data(value.begin(), value.end());
+            const uint32_t              shape[2] = { (uint32_t) plan.size(), (uint32_t) nvox };
+            const std::string           n1 = "(" + std::to_string(ptr32.size()) + ",)", n2 = "(" + std::to_string(nnz) + ",)";
+            write_npz(out_dir + "/" + b.name + "_" + std::to_string(b.devices.size()) + "_Dij.npz",
+                      { { "indices", "<u4", n2, indices.data(), indices.size() * sizeof(uint32_t) },
+                        { "indptr", "<u4", n1, ptr32.data(), ptr32.size() * sizeof(uint32_t) },
+                        { "shape", "<u4", "(2,)", shape, sizeof(shape) },
+                        { "data", "<f8", n2, data.data(), data.size() * sizeof(double) },
+                        { "format", "|S3", "()", "csr", 3 } });
         }
         std::printf("beam %s: %llu histories, %.3f s\n", b.name.c_str(), (unsigned long long) (total * passes), secs);
         if (json)

@@ -47,3 +47,39 @@ def test_required_options(host_exe, tmp_path):
     assert r.returncode != 0 and "output_path is required" in r.stderr
     r = subprocess.run([host_exe, "--output_prefix", str(tmp_path)], capture_output=True, text=True)
     assert r.returncode != 0 and "phantom_path is required" in r.stderr
+
+
+def test_npz_writer_of_the_host_drivers(tmp_path):
+    """mqi_host::write_npz (the tps_env driver's Dij file): a stored zip of .npy members that numpy,
+    zipfile's CRC check and scipy.sparse.load_npz read back, in the reference's member order and
+    dtypes."""
+    import zipfile
+
+    src = tmp_path / "npz.cpp"
+    src.write_text(r'''
+#include "mqi_host.hpp"
+int main(int, char** argv) {
+    const uint32_t indices[4] = {1, 5, 0, 7}, indptr[4] = {0, 2, 2, 4}, shape[2] = {3, 8};
+    const double   data[4] = {0.5, 1.5, 2.5, 4.0};
+    mqi_host::write_npz(argv[1], {{"indices", "<u4", "(4,)", indices, sizeof(indices)},
+                                  {"indptr", "<u4", "(4,)", indptr, sizeof(indptr)},
+                                  {"shape", "<u4", "(2,)", shape, sizeof(shape)},
+                                  {"data", "<f8", "(4,)", data, sizeof(data)},
+                                  {"format", "|S3", "()", "csr", 3}});
+    return 0;
+}
+''')
+    exe = tmp_path / "npz"
+    subprocess.run(["g++", "-std=c++17", "-O2", f"-I{ROOT}/include", f"-I{ROOT}/moquimc_gb300/host", str(src), "-o", str(exe)],
+                   check=True, capture_output=True)
+    path = tmp_path / "d.npz"
+    subprocess.run([str(exe), str(path)], check=True)
+    with zipfile.ZipFile(path) as zf:
+        assert zf.testzip() is None
+        assert [i.filename for i in zf.infolist()] == ["indices.npy", "indptr.npy", "shape.npy", "data.npy", "format.npy"]
+    z = np.load(path)
+    assert {k: z[k].dtype.str for k in z.files} == {"indices": "<u4", "indptr": "<u4", "shape": "<u4",
+                                                   "data": "<f8", "format": "|S3"}
+    sps = pytest.importorskip("scipy.sparse")
+    m = sps.load_npz(str(path)).toarray()
+    assert m.shape == (3, 8) and m[0, 1] == 0.5 and m[0, 5] == 1.5 and m[2, 0] == 2.5 and m[2, 7] == 4.0 and m.sum() == 8.5

@@ -132,16 +132,32 @@ def test_tps_scoring_mask(tmp_path):
                                atol=1e-12 * runs["full"].max())
 
 
-def test_cpp_tps_driver_matches_the_python_environment(tmp_path):
-    """The C++ host driver (moquimc_gb300/host/tps_env_main.cpp) and the Python environment on the
-    same input file, CT, beams and beam model write the same volumes."""
-    import subprocess
+def _write_beams(path, beams):
+    """The C++ driver's beams file: beam lines, their spots and range shifters."""
+    with open(path, "w") as f:
+        for b in beams:
+            f.write(f"beam {b.name} {b.gantry} {b.couch} {b.collimator} 0 0 0 390\n")
+            for s in b.spots:
+                f.write("spot " + " ".join(repr(float(v)) for v in s) + "\n")
+            for d in b.devices:
+                f.write("rangeshifter " + " ".join(repr(float(v)) for v in (*d[1], *d[2])) + "\n")
 
+
+def _tps_exe():
     from moquimc_gb300 import build
 
     exe = os.path.join(build.LIB_DIR, "tps_env")
     if not os.path.exists(exe):
         build.build_host_tools()
+    return exe
+
+
+def test_cpp_tps_driver_matches_the_python_environment(tmp_path):
+    """The C++ host driver (moquimc_gb300/host/tps_env_main.cpp) and the Python environment on the
+    same input file, CT, beams and beam model write the same volumes."""
+    import subprocess
+
+    exe = _tps_exe()
     hu, edges = _ct()
     ct = os.path.join(tmp_path, "ct.raw")
     hu.tofile(ct)
@@ -150,13 +166,7 @@ def test_cpp_tps_driver_matches_the_python_environment(tmp_path):
         f.write(MODEL)
     rs = ("rangeshifter", (-100.0, -100.0, 150.0), (100.0, 100.0, 180.0), 0.0, None, (0.0, 0.0, 0.0))
     beams = _beams([rs])
-    with open(os.path.join(tmp_path, "beams.txt"), "w") as f:
-        for b in beams:
-            f.write(f"beam {b.name} {b.gantry} {b.couch} {b.collimator} 0 0 0 390\n")
-            for s in b.spots:
-                f.write("spot " + " ".join(repr(float(v)) for v in s) + "\n")
-            for d in b.devices:
-                f.write("rangeshifter " + " ".join(repr(float(v)) for v in (*d[1], *d[2])) + "\n")
+    _write_beams(os.path.join(tmp_path, "beams.txt"), beams)
     outs = {}
     for tag in ("cpp", "py"):
         text = (f"RandomSeed 42\nScorer Dose, LETt\nParticlesPerHistory 1000\nNumberOfFraction 3\nRBE 1.1\n"
@@ -182,3 +192,43 @@ def test_cpp_tps_driver_matches_the_python_environment(tmp_path):
             np.testing.assert_allclose(x, y, rtol=1e-9, atol=1e-12 * max(np.abs(y).max(), 1e-30), err_msg=name)
         else:
             assert open(a).read() == open(b).read(), name
+
+
+def test_cpp_tps_driver_dij_matches_the_python_environment(tmp_path):
+    """Scorer Dij through the C++ driver and the Python environment on the same plan and seed: the
+    same spot-row CSR in the reference's npz layout (the FP32 values to 1e-6: the FP64 table sums
+    are accumulated in a different order)."""
+    import subprocess
+
+    exe = _tps_exe()
+    hu, edges = _ct()
+    ct = os.path.join(tmp_path, "ct.raw")
+    hu.tofile(ct)
+    model = os.path.join(tmp_path, "model.txt")
+    with open(model, "w") as f:
+        f.write(MODEL)
+    beams = _beams()
+    _write_beams(os.path.join(tmp_path, "beams.txt"), beams)
+    got = {}
+    for tag in ("cpp", "py"):
+        text = (f"RandomSeed 9\nScorer Dij\nParticlesPerHistory 1000\nNumberOfFraction 1\nMachine PBS:{model}\n"
+                f"OutputDir {os.path.join(tmp_path, tag)}\nBeamNumbers 1\n")
+        inp = os.path.join(tmp_path, f"{tag}.in")
+        with open(inp, "w") as f:
+            f.write(text)
+        if tag == "cpp":
+            res = subprocess.run([exe, inp, "--ct", ct, "--ct_nxyz", "60", "80", "40", "--ct_lxyz", "120", "160", "80",
+                                  "--ct_pxyz", "0", "0", "0", "--beams", os.path.join(tmp_path, "beams.txt")],
+                                 capture_output=True, text=True)
+            assert res.returncode == 0, res.stderr[-2000:]
+        else:
+            cfg = tps.TpsConfig.from_input(tps.InputFile.load(inp))
+            tps.TpsEnv(cfg, hu, edges, beams, machine.PBSMachine.load(model)).run()
+        got[tag] = np.load(os.path.join(tmp_path, tag, "beam1_0_Dij.npz"))
+    a, b = got["cpp"], got["py"]
+    assert sorted(a.files) == sorted(b.files)
+    for k in ("indices", "indptr", "shape", "format"):
+        assert a[k].dtype == b[k].dtype and np.array_equal(a[k], b[k]), k
+    assert a["data"].dtype == np.float64 and a["data"].size > 0
+    np.testing.assert_allclose(a["data"], b["data"], rtol=1e-6)
+    assert list(a["shape"]) == [12, int(np.prod(hu.shape))]
