@@ -65,7 +65,7 @@ class ClockSampler:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except (FileNotFoundError, OSError):
             self.proc = None
             return
@@ -74,9 +74,11 @@ class ClockSampler:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.lines.append(line.strip())
+            self.lines.append((time.perf_counter(), line.strip()))
 
-    def stop(self) -> dict:
+    def stop(self, t0: float = None, t1: float = None) -> dict:
+        """Summary of the samples read between t0 and t1 (perf_counter seconds, the timed region;
+        a sample is read up to one interval after it is taken); all samples when none fell there."""
         if self.proc is None:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         self.proc.terminate()
@@ -88,7 +90,8 @@ class ClockSampler:
             self.thread.join(timeout=5)
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        inside = [ln for t, ln in self.lines if t0 is not None and t0 <= t <= t1 + 0.1]
+        for ln in inside or [ln for _, ln in self.lines]:
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) < 9:
                 continue
@@ -101,7 +104,8 @@ class ClockSampler:
                 if val.lower() == "active":
                     reasons.add(name)
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
-                "reasons": sorted(reasons), "samples": len(sm)}
+                "reasons": sorted(reasons), "samples": len(sm),
+                "window": "timed region" if inside else "whole sampling run (no sample inside the timed region)"}
 
 
 def measured_peaks() -> dict:
@@ -438,7 +442,7 @@ def run_gpu(args, wl):
     torch.cuda.synchronize()
     t_wall1 = time.perf_counter()
     barrier()
-    clk = clocks.stop()
+    clk = clocks.stop(t_wall0, t_wall1)
     ms = ev0.elapsed_time(ev1)
     s1 = ctx.stats()
     ms_max = replicas.max_over_ranks(ms, device=f"cuda:{local}")
