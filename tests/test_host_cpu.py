@@ -83,3 +83,19 @@ int main(int, char** argv) {
     sps = pytest.importorskip("scipy.sparse")
     m = sps.load_npz(str(path)).toarray()
     assert m.shape == (3, 8) and m[0, 1] == 0.5 and m[0, 5] == 1.5 and m[2, 0] == 2.5 and m[2, 7] == 4.0 and m.sum() == 8.5
+
+
+def test_tps_driver_checks_its_input_before_touching_the_gpu(host_exe, tmp_path):
+    """The C++ tps_env driver rejects the inputs tps_env rejects (Dij with other scorers, an unknown
+    scorer, no OutputDir, StoppingStatistics without StoppingCriteria) with a message and status 1,
+    before it creates a context."""
+    exe = os.path.join(os.path.dirname(host_exe), "tps_env")
+    cases = {"Scorer Dij, Dose\nOutputDir {o}\n": "Dij cannot be scored with the other quantities",
+             "Scorer Heat\nOutputDir {o}\n": "Unrecognized scorer name",
+             "Scorer Dose\n": "Output directory is not provided",
+             "Scorer Dose\nOutputDir {o}\nStoppingStatistics true\n": "Statistical criteria must be positive"}
+    for k, (text, msg) in enumerate(cases.items()):
+        inp = tmp_path / f"in{k}.txt"
+        inp.write_text(text.format(o=tmp_path / f"out{k}"))
+        res = subprocess.run([exe, str(inp)], capture_output=True, text=True)
+        assert res.returncode == 1 and msg in res.stderr, (text, res.stderr)
