@@ -139,7 +139,7 @@ def fp64_atomic_peak(torch, device) -> float:
 
 def wave_traffic_per_step() -> float | None:
     """DRAM bytes per transport step of the wave kernel from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "k_wave_traffic.json")
+    path = os.path.join(ROOT, "profiles", "k_wave_traffic.txt")
     if os.path.exists(path):
         with open(path) as f:
             return float(json.load(f)["dram_bytes_per_step"])
