@@ -373,13 +373,23 @@ int mqi_autotune(mqi_ctx* ctx, int source_plan, uint64_t h0, uint64_t h1, uint64
  * library, held by every GPU that loads it until the process exits.  At most 16777216 histories
  * per call (larger requests return MQI_ERR_INVALID); a queue generation that outgrows the
  * scratch returns MQI_ERR_OVERFLOW.  All calls share the array: calls whose GPU work overlaps
- * race and must be serialised.  The first call on a device resolves the array's address and
- * uploads the physics tables (synchronous copies); make it before any stream capture begins.
+ * race and must be serialised.  Every call resolves the array's address on the current device
+ * (cudaGetSymbolAddress); the physics tables are initialised in the library's device image, so
+ * nothing is uploaded.  The first call on a device may load the library's device code there:
+ * make it before any stream capture begins.  After a non-zero return the tally holds the partial sum of the histories
+ * transported before the error: clear it before a retry.
  * Messages: mqi_last_error(NULL). */
 int mqi_transport_noalloc(int nx, int ny, int nz, const float* d_xe, const float* d_ye,
                           const float* d_ze, const float* d_rho, const mqi_vertex* d_vertices,
                           uint64_t n_histories, int scorer_type, int physics_debug, uint64_t seed,
                           double* d_tally, void* cuda_stream);
+
+/* One block of the engine's random-number generator, computed on the host: Philox4x32-10
+ * (Salmon et al., SC'11) of counter[4] under key[2], written to out[4].  Every random number of a
+ * transport is such a block, keyed by the run seed and countered by (block index, history, track
+ * uid), so a caller can reproduce any track's stream.  No counterpart in moqui, which draws from
+ * cuRAND's XORWOW state per history (mqi_transport.hpp:148). */
+int mqi_philox4x32_10(const uint32_t* counter, const uint32_t* key, uint32_t* out);
 
 /* Library version string. */
 const char* mqi_version(void);

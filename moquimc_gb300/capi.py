@@ -41,7 +41,7 @@ EXPORTS = (
     "mqi_get_batch_mean", "mqi_scale_tally", "mqi_run_until_stat", "mqi_set_spot_plan", "mqi_transport_plan",
     "mqi_sample_plan", "mqi_add_dij_scorer", "mqi_dij_build", "mqi_dij_get_csr", "mqi_dij_info",
     "mqi_dij_matvec", "mqi_dij_rmatvec", "mqi_set_scenarios", "mqi_run_plan_until_stat", "mqi_set_launch_mode",
-    "mqi_autotune", "mqi_set_calibration",
+    "mqi_autotune", "mqi_set_calibration", "mqi_philox4x32_10",
 )
 
 VERTEX_DTYPE = np.dtype([("ke", "<f4"), ("pos", "<f4", (3,)), ("dir", "<f4", (3,))])
@@ -132,6 +132,7 @@ def load(path: Optional[str] = None) -> C.CDLL:
         "mqi_set_tuning": (i32, [vp, i32, i32, i32, i32]),
         "mqi_transport_noalloc": (i32, [i32, i32, i32, vp, vp, vp, vp, vp, u64, i32, i32, u64, vp, vp]),
         "mqi_version": (C.c_char_p, []),
+        "mqi_philox4x32_10": (i32, [vp, vp, vp]),
         "mqi_add_stat_scorers": (i32, [vp, i32, i32, u32, vp, vp, vp, P(i32), P(i32)]),
         "mqi_stat_uncertainty": (i32, [vp, i32, i32, u64, f32, P(C.c_double), P(u64)]),
         "mqi_batch_accumulate": (i32, [vp, i32]),
@@ -159,6 +160,19 @@ def load(path: Optional[str] = None) -> C.CDLL:
         fn.argtypes = args
     _lib = lib
     return lib
+
+
+def philox4x32_10(counter, key) -> np.ndarray:
+    """One block of the engine's generator computed by the library on the host (no GPU needed):
+    four uint32 words of Philox4x32-10 for counter (4 words) under key (2 words)."""
+    lib = load()
+    c = np.ascontiguousarray(counter, np.uint32)
+    k = np.ascontiguousarray(key, np.uint32)
+    out = np.zeros(4, np.uint32)
+    rc = lib.mqi_philox4x32_10(c.ctypes.data, k.ctypes.data, out.ctypes.data)
+    if rc != MQI_OK:
+        raise MqiError(rc, lib.mqi_last_error(None).decode())
+    return out
 
 
 def _ptr(a: Optional[np.ndarray]):

@@ -19,7 +19,7 @@ The numbers are physics data (Geant4 TestEm0 tabulations and a Schneider-style c
 are parsed from the reference headers, rounded to float exactly as a C compiler rounds the decimal
 literals, and written as C99 hex-float literals so that every consumer reads bit-identical values.
 
-Usage: ``python gen_tables.py [--src <reference root>] [--out mqi_tables.h]``.  The generated file
+Usage: ``python gen_tables.py --src <reference root> [--out mqi_tables.h]``.  The generated file
 is committed; rerunning on an unchanged reference reproduces it byte for byte.
 """
 import argparse
@@ -70,9 +70,16 @@ def render(tables) -> str:
         "#define MQI_TABLE_N 600",
         "#define MQI_DENSITY_CORRECTION_N 3996",
         "",
+        "// constexpr in C++, so a static device array can be initialised from the tables at compile time",
+        "#ifdef __cplusplus",
+        "#define MQI_TABLE_STORAGE static constexpr float",
+        "#else",
+        "#define MQI_TABLE_STORAGE static const float",
+        "#endif",
+        "",
     ]
     for name, vals in tables:
-        out.append(f"static const float mqi_tab_{name}[{len(vals)}] = {{")
+        out.append(f"MQI_TABLE_STORAGE mqi_tab_{name}[{len(vals)}] = {{")
         for i in range(0, len(vals), 6):
             out.append("    " + ", ".join(hexf(v) for v in vals[i:i + 6]) + ",")
         out.append("};")
@@ -82,7 +89,7 @@ def render(tables) -> str:
 
 def main() -> int:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--src", default="/root/reference")
+    ap.add_argument("--src", required=True, help="root of the reference checkout (the directory holding moqui/)")
     ap.add_argument("--out", default=os.path.join(os.path.dirname(os.path.abspath(__file__)), "mqi_tables.h"))
     args = ap.parse_args()
     tables = [(name, parse_table(os.path.join(args.src, rel), cname, n)) for name, rel, cname, n in TABLES]

@@ -45,7 +45,7 @@ alloc_queue(QueueBuf& b, uint32_t cap) {
     b.q.ke = f(0); b.q.px = f(1); b.q.py = f(2); b.q.pz = f(3);
     b.q.dx = f(4); b.q.dy = f(5); b.q.dz = f(6); b.q.dE0 = f(7);
     b.q.hist = u(8); b.q.uid_lo = u(9); b.q.uid_hi = u(10); b.q.ctr = u(11); b.q.meta = u(12);
-    b.q.cell = reinterpret_cast<int32_t*>(p + col * 13);
+    b.q.cell = reinterpret_cast<uint32_t*>(p + col * 13);
     b.q.spot = u(14);
     b.q.capacity = cap;
     return cudaSuccess;
@@ -74,6 +74,20 @@ extern "C" {
 const char*
 mqi_version(void) {
     return "mqi-gb300 0.1 (sm_103a)";
+}
+
+int
+mqi_philox4x32_10(const uint32_t* counter, const uint32_t* key, uint32_t* out) {
+    if (!counter || !key || !out) {
+        set_thread_error("mqi_philox4x32_10: a pointer is NULL");
+        return MQI_ERR_INVALID;
+    }
+    const u32x4 r = philox4x32_10(u32x4{ counter[0], counter[1], counter[2], counter[3] }, key[0], key[1]);
+    out[0] = r.x;
+    out[1] = r.y;
+    out[2] = r.z;
+    out[3] = r.w;
+    return MQI_OK;
 }
 
 const char*

@@ -2,7 +2,7 @@
 //
 // Every function here restates one piece of moqui's condensed-history proton transport for a
 // single FP32 track held in registers; the reference file:line each follows is cited beside it.
-// The kernels in mqi_transport.cu drive these functions from an event queue instead of the
+// The kernels in mqi_kernels.cu drive these functions from an event queue instead of the
 // reference's per-thread LIFO stack.
 #pragma once
 

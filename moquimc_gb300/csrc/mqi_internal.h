@@ -84,7 +84,8 @@ struct Queue {
     uint32_t* uid_hi;
     uint32_t* ctr;     // next Philox block of this track
     uint32_t* meta;    // below:16 | primary:1 | ke1_zero:1 | phase:1 | child:3 | npush:10 (bit layout in kernels)
-    int32_t*  cell;    // packed cell for phase STEP: x | y << 11 | z << 22 (each < 2048)
+    uint32_t* cell;    // voxel index (cnb) of a track re-queued mid-grid (phase STEP); the
+                       // library keeps nx * ny * nz below 2^32, so any grid size round-trips
     uint32_t* spot;    // spot word of the history: spot | scenario << 24 (kNoSpot: no spot)
     uint32_t  capacity;
 };

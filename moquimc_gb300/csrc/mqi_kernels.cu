@@ -785,8 +785,10 @@ stepping(Ctx& C, Trk& t, Rng& rng, float rho, float d2b) {
 // The wave kernel
 // ------------------------------------------------------------------------------------------
 
+/// Load queue entry i.  A track re-queued mid-grid (step_phase) comes back with the voxel index
+/// it stopped in, in `cnb`; the caller turns it into a cell once the child's grid is known.
 __device__ inline void
-load_track(const Queue& q, uint32_t i, Trk& t, Rng& rng, bool& step_phase) {
+load_track(const Queue& q, uint32_t i, Trk& t, Rng& rng, bool& step_phase, uint32_t& cnb) {
     t.ke0  = q.ke[i];
     const uint32_t meta = q.meta[i];
     t.ke1  = (meta & kMetaKe1Zero) ? 0.0f : t.ke0;
@@ -805,8 +807,7 @@ load_track(const Queue& q, uint32_t i, Trk& t, Rng& rng, bool& step_phase) {
     t.npush   = (meta >> kMetaNpushShift) & 1023u;
     t.stopped = false;
     step_phase = (meta & kMetaPhaseStep) != 0;
-    const int32_t c = q.cell[i];
-    t.cell = make_int3(c & 2047, (c >> 11) & 2047, (c >> 22) & 2047);
+    cnb = q.cell[i];
     rng.hist   = t.hist;
     rng.uid_lo = (uint32_t) t.uid;
     rng.uid_hi = (uint32_t) (t.uid >> 32);
@@ -836,7 +837,7 @@ requeue_track(Ctx& C, const Trk& t, const Rng& rng) {
     q.meta[i] = (t.below & kMetaBelowMask) | (t.primary ? kMetaPrimary : 0u) |
                 (t.ke1 != t.ke0 ? kMetaKe1Zero : 0u) | kMetaPhaseStep |
                 ((uint32_t) t.child << kMetaChildShift) | ((t.npush & 1023u) << kMetaNpushShift);
-    q.cell[i] = t.cell.x | (t.cell.y << 11) | (t.cell.z << 22);
+    q.cell[i] = grid_cnb(C.g, t.cell);
     q.spot[i] = t.spot;
 }
 
@@ -911,8 +912,9 @@ wave_body(const WaveParams& P) {
             if (!have) {
                 const uint32_t idx = base + (uint32_t) __popc(needm & ((1u << lane) - 1u));
                 if (idx >= n_in) break;
-                bool step_phase;
-                load_track(P.in, idx, t, rng, step_phase);
+                bool     step_phase;
+                uint32_t cnb0;
+                load_track(P.in, idx, t, rng, step_phase, cnb0);
                 have    = true;
                 in_grid = step_phase;
                 slice   = 0;
@@ -922,6 +924,9 @@ wave_body(const WaveParams& P) {
                     C.child = t.child;
                     C.g     = make_grid(P.child[t.child], s_edges[t.child][0], s_edges[t.child][1], s_edges[t.child][2]);
                     apply_scenario(P, C.g, t.child, t.spot);
+                    const uint32_t nxy = (uint32_t) C.g.nx * (uint32_t) C.g.ny;
+                    const uint32_t rem = cnb0 % nxy;
+                    t.cell = make_int3((int) (rem % (uint32_t) C.g.nx), (int) (rem / (uint32_t) C.g.nx), (int) (cnb0 / nxy));
                 }
             }
         }

@@ -16,12 +16,15 @@
 //     at zero are cleared by the call itself, on the caller's stream;
 //   * two calls whose GPU work overlaps (different streams or host threads) race on the array:
 //     serialise them;
-//   * the first call on a device resolves the array's device address (cudaGetSymbolAddress) and
-//     copies the physics tables into a second static array with that device current; make that
-//     first call before any stream capture begins.
+//   * every call resolves the array's device address (cudaGetSymbolAddress) with the caller's
+//     device current; the physics tables sit in a second static array initialised in the module
+//     image, so nothing is copied, and a context that is torn down and created again
+//     (cudaDeviceReset) finds them again.  The first call on a device may load the library's
+//     device code there: make that first call before any stream capture begins;
+//   * each call returns after its work on the stream has completed; on an error return the
+//     tally holds a partial sum of the histories transported so far and must be cleared by the
+//     caller before a retry.
 // Errors are reported as status codes; mqi_last_error(NULL) returns the message.
-#include <cstring>
-#include <mutex>
 #include <string>
 
 #include <cuda_runtime.h>
@@ -50,17 +53,28 @@ static_assert(kNoallocCol % 256 == 0, "queue columns must stay 256-byte aligned"
 
 // The scratch: two SoA particle queues followed by the wave counters and run statistics.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratchBytes];
-// The physics tables the wave kernel stages into shared memory (copied in at first use).
-static __device__ __align__(256) float g_noalloc_tables[kNoallocTableFloats];
-
-struct DeviceSetup {
-    bool   ready = false;
-    void*  scratch = nullptr;
-    float* tables = nullptr;
+// The physics tables the wave kernel stages into shared memory, in its order (the six 600-node
+// tables, then the HU density-correction factors), initialised at compile time.
+struct NoallocTables {
+    float v[kNoallocTableFloats];
 };
 
-std::mutex  g_setup_mutex;
-DeviceSetup g_setup[64];
+constexpr NoallocTables
+noalloc_tables_init() {
+    NoallocTables t{};
+    for (int i = 0; i < MQI_TABLE_N; ++i) {
+        t.v[0 * MQI_TABLE_N + i] = mqi_tab_cs_p_ion[i];
+        t.v[1 * MQI_TABLE_N + i] = mqi_tab_dedx[i];
+        t.v[2 * MQI_TABLE_N + i] = mqi_tab_range[i];
+        t.v[3 * MQI_TABLE_N + i] = mqi_tab_cs_pp_e[i];
+        t.v[4 * MQI_TABLE_N + i] = mqi_tab_cs_po_e[i];
+        t.v[5 * MQI_TABLE_N + i] = mqi_tab_cs_po_i[i];
+    }
+    for (int i = 0; i < MQI_DENSITY_CORRECTION_N; ++i) t.v[6 * MQI_TABLE_N + i] = mqi_tab_density_correction[i];
+    return t;
+}
+
+static __device__ __align__(256) NoallocTables g_noalloc_tables = noalloc_tables_init();
 
 int
 noalloc_fail(int code, const std::string& msg) {
@@ -68,35 +82,18 @@ noalloc_fail(int code, const std::string& msg) {
     return code;
 }
 
-/// Once per device, with that device current: resolve the static arrays' device addresses and
-/// fill the table array.  The symbol name is a host-side stand-in; only the address returned here
-/// may be handed to a kernel.
+/// The static arrays' device addresses on the current device.  The symbol names are host-side
+/// stand-ins; only the addresses returned here may be handed to a kernel.
 int
-setup_device(int dev, DeviceSetup& out) {
-    std::lock_guard<std::mutex> lock(g_setup_mutex);
-    DeviceSetup& s = g_setup[dev];
-    if (!s.ready) {
-        void*       scratch = nullptr;
-        void*       tables  = nullptr;
-        cudaError_t e       = cudaGetSymbolAddress(&scratch, g_noalloc_scratch);
-        if (e != cudaSuccess) return noalloc_fail(MQI_ERR_CUDA, std::string("mqi_transport_noalloc: cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
-        e = cudaGetSymbolAddress(&tables, g_noalloc_tables);
-        if (e != cudaSuccess) return noalloc_fail(MQI_ERR_CUDA, std::string("mqi_transport_noalloc: cudaGetSymbolAddress(tables): ") + cudaGetErrorString(e));
-        float host[kNoallocTableFloats];
-        std::memcpy(&host[0 * MQI_TABLE_N], mqi_tab_cs_p_ion, sizeof(mqi_tab_cs_p_ion));
-        std::memcpy(&host[1 * MQI_TABLE_N], mqi_tab_dedx, sizeof(mqi_tab_dedx));
-        std::memcpy(&host[2 * MQI_TABLE_N], mqi_tab_range, sizeof(mqi_tab_range));
-        std::memcpy(&host[3 * MQI_TABLE_N], mqi_tab_cs_pp_e, sizeof(mqi_tab_cs_pp_e));
-        std::memcpy(&host[4 * MQI_TABLE_N], mqi_tab_cs_po_e, sizeof(mqi_tab_cs_po_e));
-        std::memcpy(&host[5 * MQI_TABLE_N], mqi_tab_cs_po_i, sizeof(mqi_tab_cs_po_i));
-        std::memcpy(&host[6 * MQI_TABLE_N], mqi_tab_density_correction, sizeof(mqi_tab_density_correction));
-        e = cudaMemcpyToSymbol(g_noalloc_tables, host, sizeof(host));
-        if (e != cudaSuccess) return noalloc_fail(MQI_ERR_CUDA, std::string("mqi_transport_noalloc: table upload: ") + cudaGetErrorString(e));
-        s.scratch = scratch;
-        s.tables  = static_cast<float*>(tables);
-        s.ready   = true;
-    }
-    out = s;
+resolve_scratch(void** scratch, float** tables) {
+    void*       t = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(scratch, g_noalloc_scratch);
+    if (e != cudaSuccess)
+        return noalloc_fail(MQI_ERR_CUDA, std::string("mqi_transport_noalloc: cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
+    e = cudaGetSymbolAddress(&t, g_noalloc_tables);
+    if (e != cudaSuccess)
+        return noalloc_fail(MQI_ERR_CUDA, std::string("mqi_transport_noalloc: cudaGetSymbolAddress(tables): ") + cudaGetErrorString(e));
+    *tables = static_cast<float*>(t);
     return MQI_OK;
 }
 
@@ -108,7 +105,7 @@ carve_queue(unsigned char* base) {
     q.ke = f(0); q.px = f(1); q.py = f(2); q.pz = f(3);
     q.dx = f(4); q.dy = f(5); q.dz = f(6); q.dE0 = f(7);
     q.hist = u(8); q.uid_lo = u(9); q.uid_hi = u(10); q.ctr = u(11); q.meta = u(12);
-    q.cell = reinterpret_cast<int32_t*>(base + kNoallocCol * 13);
+    q.cell = reinterpret_cast<uint32_t*>(base + kNoallocCol * 13);
     q.spot = u(14);
     q.capacity = kNoallocQueueCap;
     return q;
@@ -136,15 +133,15 @@ mqi_transport_noalloc(int nx, int ny, int nz, const float* d_xe, const float* d_
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return noalloc_fail(MQI_ERR_CUDA, std::string("mqi_transport_noalloc: cudaGetDevice: ") + cudaGetErrorString(e));
-    if (dev < 0 || dev >= 64) return noalloc_fail(MQI_ERR_INVALID, "mqi_transport_noalloc: device index above 63");
-    DeviceSetup S;
-    const int rc = setup_device(dev, S);
+    void*  scratch = nullptr;
+    float* tables  = nullptr;
+    const int rc = resolve_scratch(&scratch, &tables);
     if (rc != MQI_OK) return rc;
     int sms = 0;
     e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return noalloc_fail(MQI_ERR_CUDA, std::string("mqi_transport_noalloc: device query: ") + cudaGetErrorString(e));
     cudaStream_t   stream   = static_cast<cudaStream_t>(cuda_stream);
-    unsigned char* base     = static_cast<unsigned char*>(S.scratch);
+    unsigned char* base     = static_cast<unsigned char*>(scratch);
     uint32_t*      counters = reinterpret_cast<uint32_t*>(base + 2 * kNoallocQueueBytes);
     auto*          stats    = reinterpret_cast<unsigned long long*>(base + 2 * kNoallocQueueBytes + 64);
     Queue          qa       = carve_queue(base);
@@ -182,7 +179,7 @@ mqi_transport_noalloc(int nx, int ny, int nz, const float* d_xe, const float* d_
     P.error_flag       = counters + 3;
     P.stats            = stats;
     P.spot_ids         = nullptr;
-    P.tables           = S.tables;
+    P.tables           = tables;
     P.smem_edge_floats = wave_edge_floats(P.child, 1);
 
     // counters and statistics start at zero for every call (the array keeps the last call's)
@@ -194,8 +191,9 @@ mqi_transport_noalloc(int nx, int ny, int nz, const float* d_xe, const float* d_
     for (uint64_t h = 0; h < n_histories; h += kNoallocChunk) {
         const uint32_t n = (uint32_t) ((n_histories - h) < kNoallocChunk ? (n_histories - h) : kNoallocChunk);
         e = launch_load_primaries(*A, d_vertices, nullptr, h, n, 1, stream);
+        // a copy from pageable host memory returns once its source has been staged, so `n` may
+        // change before the copy reaches the device
         if (e == cudaSuccess) e = cudaMemcpyAsync(counters, &n, sizeof(uint32_t), cudaMemcpyHostToDevice, stream);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(stream);   // `n` lives on this stack frame
         if (e != cudaSuccess) return noalloc_fail(MQI_ERR_CUDA, std::string("mqi_transport_noalloc: ") + cudaGetErrorString(e));
         int cur = 0;
         for (int wave = 0;; ++wave) {

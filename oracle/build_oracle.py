@@ -26,7 +26,11 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REF_SRC = os.path.join(HERE, "_ref", "src")
 REF_BIN = os.path.join(HERE, "_ref", "bin")
 BUILD = os.path.join(HERE, "_build")
-REFERENCE_ROOT = "/root/reference"
+# The reference checkout to stage from: MOQUI_REFERENCE_ROOT (the directory holding moqui/), set
+# by the build entry point of the machine that has the checkout.  Without it the staged copy that
+# travelled with the repository is compiled as is.
+def reference_root() -> str:
+    return os.environ.get("MOQUI_REFERENCE_ROOT", "")
 
 
 def _run(cmd):
@@ -49,12 +53,13 @@ def ref_binary(debug: bool) -> str:
 def build_reference(force: bool = False) -> bool:
     """Stage (when possible) and compile the reference CPU oracle.  Returns False when no staged
     copy exists (the reference was never available to this checkout)."""
-    if os.path.isdir(os.path.join(REFERENCE_ROOT, "moqui")):
+    root = reference_root()
+    if root and os.path.isdir(os.path.join(root, "moqui")):
         sys.path.insert(0, HERE)
         import stage_ref  # noqa: E402
 
         if force or not os.path.isdir(os.path.join(REF_SRC, "moqui")):
-            stage_ref.stage(REFERENCE_ROOT)
+            stage_ref.stage(root)
     if not os.path.isdir(os.path.join(REF_SRC, "moqui")):
         return False
     os.makedirs(REF_BIN, exist_ok=True)
@@ -81,11 +86,12 @@ def ref_gpu_binary(debug: bool = True) -> str:
 
 def build_reference_gpu(debug: bool = True, force: bool = False) -> str:
     """Compile the reference GPU driver; returns its path, or "" without a staged copy or nvcc."""
-    if os.path.isdir(os.path.join(REFERENCE_ROOT, "moqui")) and not os.path.isdir(os.path.join(REF_SRC, "moqui")):
+    root = reference_root()
+    if root and os.path.isdir(os.path.join(root, "moqui")) and not os.path.isdir(os.path.join(REF_SRC, "moqui")):
         sys.path.insert(0, HERE)
         import stage_ref  # noqa: E402
 
-        stage_ref.stage(REFERENCE_ROOT)
+        stage_ref.stage(root)
     if not os.path.isdir(os.path.join(REF_SRC, "moqui")):
         return ""
     nvcc = os.path.join(os.environ.get("CUDA_HOME", "/usr/local/cuda"), "bin", "nvcc")

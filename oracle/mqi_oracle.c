@@ -81,6 +81,12 @@ static u4 philox(u4 c, uint32_t k0, uint32_t k1) {
     return c;
 }
 
+void mqo_philox(const uint32_t* counter, const uint32_t* key, uint32_t* out) {
+    u4 c = { counter[0], counter[1], counter[2], counter[3] };
+    u4 r = philox(c, key[0], key[1]);
+    out[0] = r.x; out[1] = r.y; out[2] = r.z; out[3] = r.w;
+}
+
 static uint64_t mix64(uint64_t z) {
     z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
     z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;

@@ -62,6 +62,9 @@ float mqo_spr(float rho, float ke, int physics_debug);
 float mqo_x0(float rho, int physics_debug);
 float mqo_hu_to_density(int hu);
 
+/* One Philox4x32-10 block of counter[4] under key[2] (the generator every stream is drawn from). */
+void mqo_philox(const uint32_t* counter, const uint32_t* key, uint32_t* out);
+
 /* Voxel walk of one ray (the transport's entry + voxel loop with boundary-only steps).
  * Returns the number of entries written (<= max_steps). */
 int mqo_trace_ray(const mqo_grid* g, const float ray[6], int max_steps, uint64_t* cnb, float* dist, int32_t* cells);

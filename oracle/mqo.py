@@ -64,6 +64,8 @@ def lib(fp64: bool = False):
         L.mqo_x0.argtypes = [C.c_float, C.c_int]
         L.mqo_hu_to_density.restype = C.c_float
         L.mqo_hu_to_density.argtypes = [C.c_int]
+        L.mqo_philox.restype = None
+        L.mqo_philox.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         L.mqo_trace_ray.restype = C.c_int
         L.mqo_trace_ray.argtypes = [C.POINTER(_Grid), C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
         _libs[fp64] = L
@@ -123,6 +125,15 @@ def x0(rho: float, dbg: bool) -> float:
 
 def hu_to_density(hu: int) -> float:
     return lib().mqo_hu_to_density(int(hu))
+
+
+def philox(counter, key) -> np.ndarray:
+    """One Philox4x32-10 block of the restatement's generator."""
+    c = np.ascontiguousarray(counter, np.uint32)
+    k = np.ascontiguousarray(key, np.uint32)
+    out = np.zeros(4, np.uint32)
+    lib().mqo_philox(_p(c), _p(k), _p(out))
+    return out
 
 
 def trace_rays(grid: Grid, rays: np.ndarray, max_steps: int):

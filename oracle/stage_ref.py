@@ -18,9 +18,9 @@ Two problems keep it from running unmodified, and both are handled here or in th
    the loop by the guarded form "step n down while n > 0 and r < r_steps[n]", which produces the same
    index in every case where the original does not wrap.
 
-Usage: ``python oracle/stage_ref.py [--src <reference root>]``.  The default source is the
-read-only reference checkout; the copy is only (re)written when the source is present, so on a
-machine without the reference the previously staged copy is used as is.
+Usage: ``python oracle/stage_ref.py --src <reference root>`` (the directory holding ``moqui/``; the
+checkout is only read).  The copy is only (re)written when the source is present, so on a machine
+without the reference the previously staged copy is used as is.
 """
 import argparse
 import os
@@ -29,7 +29,6 @@ import shutil
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-DEFAULT_SRC = "/root/reference"
 DEST = os.path.join(HERE, "_ref", "src")
 
 # The underflowing loop, matched loosely on whitespace (reference mqi_p_ionization.hpp:318-320).
@@ -62,7 +61,7 @@ def stage(src_root: str) -> str:
 
 def main() -> int:
     ap = argparse.ArgumentParser()
-    ap.add_argument("--src", default=DEFAULT_SRC)
+    ap.add_argument("--src", required=True)
     args = ap.parse_args()
     print(stage(args.src))
     return 0

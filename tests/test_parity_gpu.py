@@ -306,6 +306,30 @@ def test_slicing_and_launch_shape_do_not_change_results(gpu_ctx_factory):
         assert st["steps"] == st0["steps"] and st["histories"] == n
 
 
+def test_slicing_on_a_deep_grid(gpu_ctx_factory):
+    """Tracks re-queued mid-grid resume in the voxel they stopped in, at every slice index: a
+    700-slice water column (0.4 mm slices; the beam enters at slice 699 and 200 MeV protons stop
+    near slice 50, so every track crosses slices 512-699), sliced every 5 steps, gives the
+    unsliced tallies."""
+    wl = workloads.Workload("deep_water_column", (40.0, 40.0, 280.0), (0.0, 0.0, -140.0), (20, 20, 700),
+                            np.zeros((700, 20, 20), np.int16), 200.0, "gaussian", (3.0, 3.0), (0.0, 0.0, 0.5),
+                            2000, False)
+    n = 2000
+    v = wl.vertices(n, 11)
+    res = []
+    for tune in ({}, {"slice_steps": 5}):
+        c, cid, sid = _ctx_for(wl, gpu_ctx_factory)
+        if tune:
+            c.set_tuning(**tune)
+        c.set_vertices(v)
+        c.transport(0, n, 321)
+        res.append((c.tally(sid), c.stats()))
+    (d0, st0), (d1, st1) = res
+    assert d0.reshape(700, 20, 20)[600:].sum() > 0.0 and d0.reshape(700, 20, 20)[:100].sum() > 0.0
+    np.testing.assert_allclose(d1, d0, rtol=1e-9, atol=1e-300)
+    assert st1["steps"] == st0["steps"] and st1["histories"] == n
+
+
 def test_chunked_primaries_match_single_chunk(gpu_ctx_factory):
     wl = workloads.c2(histories=5000)
     n = 5000

@@ -66,6 +66,54 @@ def test_noalloc_transport_matches_context_transport_on_two_calls(built_lib):
         np.testing.assert_allclose(got, expect, rtol=1e-9, atol=1e-300)
 
 
+_SCORERS = {"edep": capi.EDEP, "dose_w": capi.DOSE_W, "dose_w2": capi.DOSE_W2, "dose_m": capi.DOSE_M}
+
+
+@pytest.mark.parametrize("physics_debug", [0, 1])
+@pytest.mark.parametrize("scorer", sorted(_SCORERS))
+def test_noalloc_every_scorer_and_physics_build(built_lib, scorer, physics_debug):
+    """Every scorer the entry point accepts (each selects its own kernel instance: EDEP and DOSE_W
+    the single-scorer one, DOSE_W2 the generic one, DOSE_M the one with the FP64 callbacks), with
+    release and debug physics, on a history count that is not a multiple of the 65536-primary
+    generation; two calls in a row, each against the context transport."""
+    import torch
+
+    wl = workloads.c2()
+    n = 65_536 + 4_465
+    stype = _SCORERS[scorer]
+    verts = wl.vertices(n, 91)
+    xe, ye, ze = wl.edges()
+    nx, ny, nz = wl.nxyz
+    seeds = (0xA11C0C, 0xA11C0D)
+    ref = []
+    with capi.Context(0) as c:
+        c.set_physics(physics_debug)
+        cid = c.add_child(xe, ye, ze)
+        c.set_hu(cid, wl.hu)
+        sid = c.add_scorer(cid, stype)
+        rho = c.hu_to_density(wl.hu.reshape(-1))
+        c.set_vertices(verts)
+        for s in seeds:
+            c.reset()
+            c.transport(0, n, s)
+            ref.append(c.tally(sid))
+    dev = torch.device("cuda", 0)
+    d_xe, d_ye, d_ze, d_rho = (torch.from_numpy(a).to(dev) for a in (xe, ye, ze, rho))
+    d_v = torch.from_numpy(verts.view(np.uint8).copy()).to(dev)
+    stream = torch.cuda.current_stream(dev)
+    d_tally = torch.zeros(nx * ny * nz, dtype=torch.float64, device=dev)
+    for s, expect in zip(seeds, ref):
+        d_tally.zero_()
+        torch.cuda.synchronize()
+        rc = built_lib.mqi_transport_noalloc(nx, ny, nz, _ptr(d_xe), _ptr(d_ye), _ptr(d_ze), _ptr(d_rho), _ptr(d_v), n,
+                                             stype, physics_debug, s, _ptr(d_tally),
+                                             ctypes.c_void_p(stream.cuda_stream))
+        assert rc == 0, built_lib.mqi_last_error(None)
+        got = d_tally.cpu().numpy()
+        assert got.sum() > 0
+        np.testing.assert_allclose(got, expect, rtol=1e-9, atol=1e-300)
+
+
 def test_noalloc_rejects_sizes_beyond_its_limit(built_lib):
     rc = built_lib.mqi_transport_noalloc(8, 8, 8, ctypes.c_void_p(1), ctypes.c_void_p(1), ctypes.c_void_p(1),
                                          ctypes.c_void_p(1), ctypes.c_void_p(1), (1 << 24) + 1, capi.DOSE_W, 0, 1,
