@@ -240,6 +240,19 @@ int mqi_dij_get_csr(mqi_ctx* ctx, int scorer_id, uint64_t* indptr, uint32_t* ind
 int mqi_dij_info(mqi_ctx* ctx, int scorer_id, uint64_t* table_slots, uint64_t* occupied,
                  uint64_t* nnz, uint64_t* n_voxel_rows);
 
+/* Record every insertion into Dij scorer `scorer_id`'s table by later transports: the voxel (cnb),
+ * the spot column and the FP64 value that moqui's insert_hashtable(table, cnb, spot, value, ...)
+ * receives for the same step (mqi_transport.hpp:68-111, called at :204-225), in the order the
+ * GPU issued them.  A log of `capacity` entries (16 bytes each) is allocated; 0 stops recording
+ * and frees it.  For checking a table against a replay through the reference's insertion. */
+int mqi_dij_record_hits(mqi_ctx* ctx, int scorer_id, uint64_t capacity);
+
+/* Copy the recorded insertions (host buffers of *n_out entries; all three may be NULL to query
+ * the count).  Returns MQI_ERR_OVERFLOW, with *n_out = capacity, when more were made than the log
+ * holds. */
+int mqi_dij_get_hits(mqi_ctx* ctx, int scorer_id, uint32_t* voxel, uint32_t* spot, double* value,
+                     uint64_t* n_out);
+
 /* dose = D.w (n_voxels outputs from n_spots weights) and grad = D^T.g (n_spots outputs from
  * n_voxels inputs); fp64 selects double buffers (the matrix stays FP32).  With on_device = 1 the
  * buffers are device pointers and the work is queued on the context's stream without a sync.

@@ -41,7 +41,7 @@ EXPORTS = (
     "mqi_get_batch_mean", "mqi_scale_tally", "mqi_run_until_stat", "mqi_set_spot_plan", "mqi_transport_plan",
     "mqi_sample_plan", "mqi_add_dij_scorer", "mqi_dij_build", "mqi_dij_get_csr", "mqi_dij_info",
     "mqi_dij_matvec", "mqi_dij_rmatvec", "mqi_set_scenarios", "mqi_run_plan_until_stat", "mqi_set_launch_mode",
-    "mqi_autotune", "mqi_set_calibration", "mqi_philox4x32_10",
+    "mqi_autotune", "mqi_set_calibration", "mqi_philox4x32_10", "mqi_dij_record_hits", "mqi_dij_get_hits",
 )
 
 VERTEX_DTYPE = np.dtype([("ke", "<f4"), ("pos", "<f4", (3,)), ("dir", "<f4", (3,))])
@@ -133,6 +133,8 @@ def load(path: Optional[str] = None) -> C.CDLL:
         "mqi_transport_noalloc": (i32, [i32, i32, i32, vp, vp, vp, vp, vp, u64, i32, i32, u64, vp, vp]),
         "mqi_version": (C.c_char_p, []),
         "mqi_philox4x32_10": (i32, [vp, vp, vp]),
+        "mqi_dij_record_hits": (i32, [vp, i32, u64]),
+        "mqi_dij_get_hits": (i32, [vp, i32, vp, vp, vp, P(u64)]),
         "mqi_add_stat_scorers": (i32, [vp, i32, i32, u32, vp, vp, vp, P(i32), P(i32)]),
         "mqi_stat_uncertainty": (i32, [vp, i32, i32, u64, f32, P(C.c_double), P(u64)]),
         "mqi_batch_accumulate": (i32, [vp, i32]),
@@ -426,6 +428,20 @@ class Context:
         self.scorers.append(out.value)
         self._dij_child[out.value] = child
         return out.value
+
+    def dij_record_hits(self, scorer: int, capacity: int) -> None:
+        """Record every insertion into the Dij table from now on (capacity 0: stop)."""
+        self._check(self.lib.mqi_dij_record_hits(self.h, scorer, capacity), self.h)
+
+    def dij_hits(self, scorer: int):
+        """The recorded insertions: (voxel uint32, spot uint32, value float64) in issue order."""
+        n = C.c_uint64(0)
+        self._check(self.lib.mqi_dij_get_hits(self.h, scorer, None, None, None, C.byref(n)), self.h)
+        vox = np.empty(n.value, np.uint32)
+        spot = np.empty(n.value, np.uint32)
+        val = np.empty(n.value, np.float64)
+        self._check(self.lib.mqi_dij_get_hits(self.h, scorer, _ptr(vox), _ptr(spot), _ptr(val), C.byref(n)), self.h)
+        return vox, spot, val
 
     def dij_build(self, scorer: int, n_spots: int = 0, scale: float = 1.0):
         """Build the Dij matrix; returns a dij.DijOperator."""

@@ -72,6 +72,11 @@ namespace mqi_gpu
 /// Called by mqi_destroy / mqi_reset_tallies.
 void
 dij_release(ScorerHost& s) {
+    cudaFree(s.hit_log);
+    cudaFree(s.hit_count);
+    s.hit_log   = nullptr;
+    s.hit_count = nullptr;
+    s.hit_cap   = 0;
     free_csr(s.csr);
     cudaFree(s.dij);
     cudaFree(s.dij_count);
@@ -122,6 +127,66 @@ mqi_add_dij_scorer(mqi_ctx* c, int child_id, int roi_method, uint32_t roi_length
         return cuda_fail(c, e, "mqi_add_dij_scorer");
     }
     if (scorer_id) *scorer_id = id;
+    return MQI_OK;
+}
+
+int
+mqi_dij_record_hits(mqi_ctx* c, int id, uint64_t capacity) {
+    ScorerHost* sp = dij_scorer(c, id, "mqi_dij_record_hits");
+    if (!sp) return MQI_ERR_INVALID;
+    ScorerHost& s = *sp;
+    DeviceGuard g(c->device);
+    MQI_CUDA(c, cudaStreamSynchronize(c->stream), "mqi_dij_record_hits");
+    cudaFree(s.hit_log);
+    cudaFree(s.hit_count);
+    s.hit_log   = nullptr;
+    s.hit_count = nullptr;
+    s.hit_cap   = 0;
+    if (capacity == 0) return MQI_OK;
+    cudaError_t e = cudaMalloc(&s.hit_log, capacity * sizeof(DijHit));
+    if (e == cudaSuccess) e = cudaMalloc(&s.hit_count, sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemsetAsync(s.hit_count, 0, sizeof(unsigned long long), c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) {
+        cudaFree(s.hit_log);
+        cudaFree(s.hit_count);
+        s.hit_log   = nullptr;
+        s.hit_count = nullptr;
+        return cuda_fail(c, e, "mqi_dij_record_hits");
+    }
+    s.hit_cap = capacity;
+    return MQI_OK;
+}
+
+int
+mqi_dij_get_hits(mqi_ctx* c, int id, uint32_t* voxel, uint32_t* spot, double* value, uint64_t* n_out) {
+    ScorerHost* sp = dij_scorer(c, id, "mqi_dij_get_hits");
+    if (!sp) return MQI_ERR_INVALID;
+    ScorerHost& s = *sp;
+    if (!n_out) return fail(c, MQI_ERR_INVALID, "mqi_dij_get_hits: n_out is NULL");
+    if (!s.hit_log) return fail(c, MQI_ERR_STATE, "mqi_dij_get_hits: recording is off (mqi_dij_record_hits)");
+    DeviceGuard g(c->device);
+    unsigned long long count = 0;
+    MQI_CUDA(c, cudaMemcpyAsync(&count, s.hit_count, sizeof(count), cudaMemcpyDeviceToHost, c->stream),
+             "mqi_dij_get_hits");
+    MQI_CUDA(c, cudaStreamSynchronize(c->stream), "mqi_dij_get_hits");
+    const uint64_t n = std::min<uint64_t>(count, s.hit_cap);
+    *n_out = n;
+    if (count > s.hit_cap)
+        return fail(c, MQI_ERR_OVERFLOW, "mqi_dij_get_hits: more insertions than the log holds (" +
+                                             std::to_string(count) + " > " + std::to_string(s.hit_cap) + ")");
+    if (!voxel && !spot && !value) return MQI_OK;
+    std::vector<DijHit> h(n);
+    if (n) {
+        MQI_CUDA(c, cudaMemcpyAsync(h.data(), s.hit_log, n * sizeof(DijHit), cudaMemcpyDeviceToHost, c->stream),
+                 "mqi_dij_get_hits");
+        MQI_CUDA(c, cudaStreamSynchronize(c->stream), "mqi_dij_get_hits");
+    }
+    for (uint64_t i = 0; i < n; ++i) {
+        if (voxel) voxel[i] = h[i].voxel;
+        if (spot) spot[i] = h[i].spot;
+        if (value) value[i] = h[i].value;
+    }
     return MQI_OK;
 }
 

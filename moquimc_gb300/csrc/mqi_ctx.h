@@ -74,6 +74,9 @@ struct ScorerHost {
     DijSlot*  dij = nullptr;        // MQI_SCORER_DIJ: hash table of dij_cap slots (power of two)
     uint64_t  dij_cap = 0;
     unsigned long long* dij_count = nullptr;
+    DijHit*   hit_log = nullptr;    // mqi_dij_record_hits: recorded insertions
+    unsigned long long* hit_count = nullptr;
+    uint64_t  hit_cap = 0;
     DijCsr    csr;
 
     uint64_t total() const { return tally_len * copies; }   // values (not doubles: see tstride)

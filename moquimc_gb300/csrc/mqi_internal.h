@@ -30,6 +30,13 @@ struct alignas(16) DijSlot {
 
 constexpr uint32_t kDijMaxProbes = 4096;   // linear-probe bound before the table counts as full
 
+/// One recorded Dij insertion (mqi_dij_record_hits): the arguments insert_hashtable receives.
+struct DijHit {
+    uint32_t voxel;
+    uint32_t spot;
+    double   value;
+};
+
 /// Wave-kernel instance modes: the scoring code an instance carries.
 constexpr int kModeDij  = 1;   // a Dij scorer
 constexpr int kModeFull = 2;   // dose_to_medium or LET scorers
@@ -55,6 +62,9 @@ struct ScorerDev {
     DijSlot*        dij;           // MQI_SCORER_DIJ: open-addressing table of dij_mask + 1 slots
     uint64_t        dij_mask;
     unsigned long long* dij_count; // device: occupied slots
+    DijHit*         hit_log;       // optional: every insertion, appended (null: not recorded)
+    unsigned long long* hit_count; // device: insertions recorded (counts on past hit_cap)
+    uint64_t        hit_cap;
 };
 
 /// One child geometry: grid + the contiguous range of its scorers.

@@ -183,8 +183,13 @@ dij_hash(uint64_t k) {
 /// the add; an empty slot is claimed with one 64-bit CAS.  After kDijMaxProbes probes the table
 /// counts as full and the error flag's bit 4 is set.
 __device__ inline void
-dij_add(DijSlot* table, uint64_t table_mask, unsigned long long* count, uint32_t* error_flag, uint32_t spot,
-        uint32_t voxel, double v, bool valid) {
+dij_add(const ScorerDev& s, uint32_t* error_flag, uint32_t spot, uint32_t voxel, double v, bool valid) {
+    DijSlot* const           table      = s.dij;
+    const uint64_t           table_mask = s.dij_mask;
+    if (s.hit_log && valid) {   // recorded insertions, for checking the table against a replay
+        const unsigned long long i = atomicAdd(s.hit_count, 1ull);
+        if (i < s.hit_cap) s.hit_log[i] = DijHit{ voxel, spot, v };
+    }
     const unsigned           mask  = __activemask();
     const unsigned long long key   = ((((unsigned long long) spot) << 32) | voxel) + 1ull;
     const unsigned           peers = __match_any_sync(mask, valid ? key : 0ull) &
@@ -207,7 +212,7 @@ dij_add(DijSlot* table, uint64_t table_mask, unsigned long long* count, uint32_t
         unsigned long long k = *reinterpret_cast<volatile unsigned long long*>(&e->key);
         if (k == 0ull) {
             k = atomicCAS(&e->key, 0ull, key);
-            if (k == 0ull) atomicAdd(count, 1ull);
+            if (k == 0ull) atomicAdd(s.dij_count, 1ull);
         }
         if (k == 0ull || k == key) {
             atomicAdd(&e->value, sum);
@@ -364,7 +369,7 @@ score_step(Ctx& C, const Trk& t, uint32_t cnb, float rho, float vol) {
             // insert_hashtable(data_, cnb, spot_ind, ...) (mqi_transport.hpp:204-225); a history
             // without a spot index lands in column 0
             const uint32_t col = (C.spot & kSpotMask) == kNoSpot ? 0u : (C.spot & kSpotMask);
-            dij_add(s.dij, s.dij_mask, s.dij_count, P.error_flag, col, cnb, v, ok && pos);
+            dij_add(s, P.error_flag, col, cnb, v, ok && pos);
             continue;
         }
         const bool valid = ok && pos && key < s.tally_len;

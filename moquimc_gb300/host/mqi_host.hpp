@@ -190,8 +190,13 @@ struct NpzArray {
 };
 
 /// mqi::io::save_npz (moqui/base/mqi_sparse_io.hpp:167-399): the arrays as stored (uncompressed)
-/// members of a zip archive, in the given order.  Like the reference's writer it uses 32-bit zip
-/// sizes and offsets; a file past 4 GiB raises instead of wrapping.
+/// members of a zip archive, in the given order, byte for byte as the reference writes numeric
+/// members: the .npy header dictionary padded with spaces until 10 + its length is a multiple of
+/// 16 (a full 16 when it already is), then a newline; zero modification time and date; version 20.
+/// Like the reference's writer it uses 32-bit zip sizes and offsets; a file past 4 GiB raises
+/// instead of wrapping.  One member differs on purpose: a string ("format", "csr") is written as
+/// its bytes, where the reference writes sizeof(std::string) bytes per character from the string's
+/// buffer (mqi_sparse_io.hpp:241-276), i.e. whatever memory follows the three characters.
 inline void
 write_npz(const std::string& path, const std::vector<NpzArray>& arrays) {
     auto u16 = [](std::string& s, uint32_t v) { s.push_back((char) (v & 0xFF)); s.push_back((char) ((v >> 8) & 0xFF)); };
@@ -201,7 +206,7 @@ write_npz(const std::string& path, const std::vector<NpzArray>& arrays) {
     uint64_t      offset = 0;
     for (const auto& a : arrays) {
         std::string dict = "{'descr': '" + a.descr + "', 'fortran_order': False, 'shape': " + a.shape + ", }";
-        dict.append(63 - (10 + dict.size()) % 64, ' ');   // header padded to a multiple of 64 bytes
+        dict.append(16 - (10 + dict.size()) % 16, ' ');
         dict.push_back('\n');
         std::string head("\x93NUMPY\x01", 7);
         head.push_back('\0');
@@ -214,7 +219,7 @@ write_npz(const std::string& path, const std::vector<NpzArray>& arrays) {
         const uint32_t crc = crc32_update(crc32_update(0, head.data(), head.size()), a.data, a.bytes);
         std::string rec;   // the fields the local and central headers share
         u16(rec, 20); u16(rec, 0); u16(rec, 0);            // version needed, flags, stored
-        u16(rec, 0); u16(rec, 0x21);                        // time 00:00, date 1980-01-01
+        u16(rec, 0); u16(rec, 0);                           // modification time and date: 0
         u32(rec, crc); u32(rec, (uint32_t) size); u32(rec, (uint32_t) size);
         u16(rec, (uint32_t) fname.size()); u16(rec, 0);     // name length, no extra field
         std::string local("PK\x03\x04", 4);

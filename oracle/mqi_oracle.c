@@ -819,3 +819,81 @@ int mqo_transport(const mqo_grid* g, const mqo_config* cfg, const float* V, uint
     free(S.t);
     return 0;
 }
+
+/* Sampling probes, mirroring the reference driver's `sample` mode: n independent draws of each
+ * process at kinetic energy ke in a medium of density rho (g/mm^3) with default calibration, track
+ * along -z from the origin.  Draw i uses the Philox stream (seed, history i, uid 0) from block 0,
+ * the words laid out as in stepping(): the along-step probe takes its Box-Muller pair and azimuth
+ * from words 1..3 of the first block, the post-step probes draw from the stream's start.
+ * process: 0 along_step over 1 mm -> out[2n] = {dE, cos theta}; 1 delta ray -> out[n] = {Te};
+ * 2 p-p elastic -> out[3n] = {dE, cos theta_3, cos theta_4 (2 without a daughter)};
+ * 3 p-O elastic -> out[2n] = {dE, cos theta_3}; 4 p-O inelastic -> out[3n] = {proton daughters,
+ * their summed kinetic energy, energy deposited by the primary}.  Each quantity is a block of n. */
+int mqo_sample(int process, float ke, float rho, uint64_t n, uint64_t seed, int physics_debug, float* out) {
+    env_t    E;
+    stack_t_ S;
+    memset(&E, 0, sizeof(E));
+    memset(&S, 0, sizeof(S));
+    S.limit = 200;
+    S.t = (trk_t*) calloc((size_t) S.limit, sizeof(trk_t));
+    if (!S.t) return -3;
+    E.dbg = physics_debug;
+    E.tcut = physics_debug ? RC(0.08511) : RC(0.0815);
+    E.stk = &S;
+    E.rng.k0 = (uint32_t) seed;
+    E.rng.k1 = (uint32_t) (seed >> 32);
+    for (uint64_t i = 0; i < n; ++i) {
+        trk_t t;
+        memset(&t, 0, sizeof(t));
+        t.ke0 = t.ke1 = ke;
+        t.p0 = t.p1 = mk(RC(0.0), RC(0.0), RC(0.0));
+        t.d0 = t.d1 = mk(RC(0.0), RC(0.0), -RC(1.0));
+        t.primary = 1;
+        S.idx = 0;
+        E.rng.hist = (uint32_t) i;
+        E.rng.lo = E.rng.hi = 0;
+        E.rng.ctr = 0;
+        E.rng.pos = 4;
+        if (process == 0) {
+            real bm_u1, bm_u2, u_phi, r;
+            (void) rng_u(&E.rng);   /* word 0: the free path in stepping() */
+            bm_u1 = rng_u(&E.rng);
+            bm_u2 = rng_u(&E.rng);
+            u_phi = rng_u(&E.rng);
+            r = RSQRT(-RC(2.0) * RLOG(bm_u1));
+            along_step(&E, &t, RC(1.0), rho, spr_of(rho, ke, physics_debug), r * RCOS(RC(2.0) * PI_F * bm_u2),
+                       r * RSIN(RC(2.0) * PI_F * bm_u2), u_phi);
+            out[i] = (float) (t.ke0 - t.ke1);
+            out[n + i] = (float) -t.d1.z;
+        } else if (process == 1) {
+            post_delta(&E, &t);
+            out[i] = (float) (t.ke0 - t.ke1);
+        } else if (process == 2) {
+            post_pp(&E, &t);
+            out[i] = (float) (t.ke0 - t.ke1);
+            out[n + i] = (float) -t.d1.z;
+            out[2 * n + i] = S.idx > 0 ? (float) -S.t[S.idx - 1].d1.z : 2.0f;
+        } else if (process == 3) {
+            post_poe(&E, &t);
+            out[i] = (float) (t.ke0 - t.ke1);
+            out[n + i] = (float) -t.d1.z;
+        } else if (process == 4) {
+            int   np = 0;
+            real  e2 = RC(0.0);
+            post_poi(&E, &t);
+            for (int k = 0; k < S.idx; ++k)
+                if (S.t[k].ke1 > RC(0.0)) {
+                    ++np;
+                    e2 += S.t[k].ke1;
+                }
+            out[i] = (float) np;
+            out[n + i] = (float) e2;
+            out[2 * n + i] = (float) t.dE;
+        } else {
+            free(S.t);
+            return -1;
+        }
+    }
+    free(S.t);
+    return 0;
+}

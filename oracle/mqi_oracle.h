@@ -65,6 +65,11 @@ float mqo_hu_to_density(int hu);
 /* One Philox4x32-10 block of counter[4] under key[2] (the generator every stream is drawn from). */
 void mqo_philox(const uint32_t* counter, const uint32_t* key, uint32_t* out);
 
+/* Sampling probes of the transport's processes at fixed energy and density (the restatement's
+ * twin of the reference driver's `sample` mode): process 0 along_step over 1 mm, 1 delta ray,
+ * 2 p-p elastic, 3 p-O elastic, 4 p-O inelastic; out holds 2, 1, 3, 2, 3 blocks of n floats. */
+int mqo_sample(int process, float ke, float rho, uint64_t n, uint64_t seed, int physics_debug, float* out);
+
 /* Voxel walk of one ray (the transport's entry + voxel loop with boundary-only steps).
  * Returns the number of entries written (<= max_steps). */
 int mqo_trace_ray(const mqo_grid* g, const float ray[6], int max_steps, uint64_t* cnb, float* dist, int32_t* cells);

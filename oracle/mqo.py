@@ -64,6 +64,8 @@ def lib(fp64: bool = False):
         L.mqo_x0.argtypes = [C.c_float, C.c_int]
         L.mqo_hu_to_density.restype = C.c_float
         L.mqo_hu_to_density.argtypes = [C.c_int]
+        L.mqo_sample.restype = C.c_int
+        L.mqo_sample.argtypes = [C.c_int, C.c_float, C.c_float, C.c_uint64, C.c_uint64, C.c_int, C.c_void_p]
         L.mqo_philox.restype = None
         L.mqo_philox.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         L.mqo_trace_ray.restype = C.c_int
@@ -136,6 +138,32 @@ def philox(counter, key) -> np.ndarray:
     return out
 
 
+SAMPLE_QUANTITIES = {0: ("along_dE", "along_cos"), 1: ("delta_Te",), 2: ("pp_dE", "pp_cos3", "pp_cos4"),
+                     3: ("poe_dE", "poe_cos3"), 4: ("poi_n", "poi_e2", "poi_dep")}
+
+
+def sample(process: int, ke: float, n: int, seed: int, rho: float = 0.001, physics_debug: bool = False) -> dict:
+    """The restatement's draws of one process (mqo_sample): {quantity name: float32 array of n}."""
+    names = SAMPLE_QUANTITIES[process]
+    out = np.zeros(len(names) * n, np.float32)
+    rc = lib().mqo_sample(process, ke, rho, n, seed, int(physics_debug), _p(out))
+    if rc != 0:
+        raise RuntimeError(f"mqo_sample failed: {rc}")
+    return {k: out[i * n:(i + 1) * n] for i, k in enumerate(names)}
+
+
+def ref_sample(n: int, seed: int, debug: bool = False) -> dict:
+    """The reference's own draws (driver mode `sample`): {(energy, quantity name): float32 array}
+    at 10, 50 and 150 MeV in water."""
+    names = ["along_dE", "along_cos", "delta_Te", "pp_dE", "pp_cos3", "pp_cos4", "poe_dE", "poe_cos3", "poi_n",
+             "poi_e2", "poi_dep"]
+    with tempfile.TemporaryDirectory() as td:
+        o = os.path.join(td, "sample.bin")
+        subprocess.run([ref_binary(debug), "sample", o, str(n), str(seed)], check=True, capture_output=True)
+        vecs = read_vecs(o, [np.float32] * (3 * len(names)))
+    return {(e, k): vecs[i * len(names) + j] for i, e in enumerate((10.0, 50.0, 150.0)) for j, k in enumerate(names)}
+
+
 def trace_rays(grid: Grid, rays: np.ndarray, max_steps: int):
     rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 6)
     offs = [0]
@@ -168,6 +196,26 @@ def ref_binary(debug: bool) -> str:
     if not os.path.exists(path):
         b.build_reference()
     return path
+
+
+def write_vecs(path, arrays):
+    """Arrays in the drivers' vector format: a u64 element count, then the elements."""
+    with open(path, "wb") as f:
+        for a in arrays:
+            a = np.ascontiguousarray(a)
+            f.write(struct.pack("<Q", a.size))
+            f.write(a.tobytes())
+
+
+def ref_dij(voxel, spot, value, capacity: int, n_spots: int, nxyz, out_dir: str, scale: float = 1.0,
+            name: str = "ref_dij") -> str:
+    """Replay Dij insertions (voxel, spot, value) through the reference's insert_hashtable into a
+    table of `capacity` slots and write it with the reference's save_to_npz; returns the npz path."""
+    hits = os.path.join(out_dir, name + "_hits.bin")
+    write_vecs(hits, [np.asarray(voxel, np.uint32), np.asarray(spot, np.uint32), np.asarray(value, np.float64)])
+    subprocess.run([ref_binary(False), "dij", hits, str(int(capacity)), str(int(n_spots)), *map(str, nxyz), repr(scale),
+                    out_dir, name], check=True, capture_output=True)
+    return os.path.join(out_dir, name + ".npz")
 
 
 def write_rays(path, grid_bounds, nxyz, max_steps, rays):

@@ -29,6 +29,8 @@
 //       post_step processes) for distribution tests.
 //   vertices <out.bin> <n> <seed> <gaussian> x y z sx sy energy colli gantry couch iec
 //       Samples phantom_env's beam source with the reference's own distribution classes.
+//   dij <hits.bin> <capacity> <n_spots> <nx> <ny> <nz> <scale> <out_dir> <name>
+//       Replays recorded Dij insertions through insert_hashtable and writes save_to_npz's file.
 #include <moqui/base/environments/mqi_phantom_env.hpp>
 #include <moqui/kernel_functions/mqi_transport.hpp>
 
@@ -591,6 +593,31 @@ run_vertices(int argc, char** argv) {
     return 0;
 }
 
+/// Dij table replay: the recorded insertions of a GPU run, in the order they were made, go
+/// through the reference's own insert_hashtable (CPU branch, mqi_transport.hpp:68-111) into a
+/// scorer's key_value table (init_table, mqi_hash_table.hpp), which the reference's
+/// save_to_npz (mqi_io.hpp:249-320) then writes.  Arguments: hits.bin (vec<u32> voxel,
+/// vec<u32> spot, vec<f64> value) capacity n_spots nx ny nz scale out_dir name.
+int
+run_dij(int argc, char** argv) {
+    if (argc < 11) return 2;
+    std::ifstream fin(argv[2], std::ios::binary);
+    const std::vector<uint32_t> vox  = read_vec<uint32_t>(fin);
+    const std::vector<uint32_t> spot = read_vec<uint32_t>(fin);
+    const std::vector<double>   val  = read_vec<double>(fin);
+    if (!fin || vox.size() != spot.size() || vox.size() != val.size()) return 3;
+    const uint32_t cap     = static_cast<uint32_t>(std::stoul(argv[3]));
+    const uint32_t n_spots = static_cast<uint32_t>(std::stoul(argv[4]));
+    const mqi::vec3<mqi::ijk_t> dim(std::atoi(argv[5]), std::atoi(argv[6]), std::atoi(argv[7]));
+    const float scale = std::stof(argv[8]);
+    mqi::scorer<float> sc("Dij", cap, nullptr);
+    sc.data_ = new mqi::key_value[cap];
+    mqi::init_table(sc.data_, cap);
+    for (size_t i = 0; i < vox.size(); ++i) mc::insert_hashtable<float>(sc.data_, vox[i], spot[i], val[i], 0, cap);
+    mqi::io::save_to_npz<float>(&sc, scale, argv[9], argv[10], dim, n_spots);
+    return 0;
+}
+
 }   // namespace
 
 void
@@ -617,6 +644,7 @@ main(int argc, char** argv) {
     if (mode == "raywalk" && argc >= 4) return run_raywalk(argv[2], argv[3]);
     if (mode == "physics" && argc >= 3) return run_physics(argv[2]);
     if (mode == "vertices") return run_vertices(argc, argv);
+    if (mode == "dij") return run_dij(argc, argv);
     if (mode == "sample" && argc >= 5)
         return run_sample(argv[2], std::atol(argv[3]), static_cast<unsigned>(std::atol(argv[4])));
     std::fprintf(stderr, "bad arguments\n");

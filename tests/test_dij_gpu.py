@@ -1,5 +1,6 @@
-"""GPU tests of the Dij scorer: the (voxel, spot) table against per-spot dense runs (bit-exact
-sparsity pattern for identical tracks), the CSR layouts, the products D.w and D^T.g against dense
+"""GPU tests of the Dij scorer: the (voxel, spot) table against the reference's own insertion and
+writer replaying the GPU's recorded insertions (bit-exact sparsity pattern for identical tracks),
+and against per-spot dense runs, the CSR layouts, the products D.w and D^T.g against dense
 references, the torch.autograd.Function against central finite differences, and the table-full
 error."""
 import numpy as np
@@ -67,6 +68,48 @@ def test_dij_rows_equal_per_spot_dense_runs(gpu_ctx_factory, wl):
         assert (np.diff(vox) > 0).all()                           # voxels ascending within a row
         np.testing.assert_array_equal(vox, np.flatnonzero(ref))   # bit-exact sparsity pattern
         np.testing.assert_allclose(data[row], ref[vox], rtol=2.0 ** -23, atol=0)
+
+
+def test_dij_sparsity_matches_the_reference_table(gpu_ctx_factory, oracle, tmp_path):
+    """Bit-exact Dij sparsity against the reference's own code for identical tracks: every
+    insertion the GPU makes during a plan transport on a heterogeneous CT crop (air, tissue noise)
+    is recorded, replayed in the same order through the reference's insert_hashtable (CPU branch,
+    mqi_transport.hpp:68-111) and written by its save_to_npz (mqi_io.hpp:249-320).  The reference
+    file's (spot, voxel) key set equals the GPU matrix's, its values agree to the matrix's FP32
+    rounding, and the GPU table holds one slot per key."""
+    if not oracle.ref_available():
+        pytest.skip("the reference's staged sources are not present")
+    nxyz, dxyz = (96, 96, 100), (0.98, 0.98, 2.0)
+    hu = workloads.ct_hu(nxyz, dxyz, semi=(40.0, 35.0, 90.0), seed=12)
+    from moquimc_gb300 import phantom as ph
+
+    lxyz = tuple(float(np.float32(n * d)) for n, d in zip(nxyz, dxyz))
+    edges = ph.phantom_box_edges(lxyz, (0.0, 0.0, 0.0), nxyz)
+    sp = _spots(6, [800, 500, 1200, 300, 900, 600], seed=9, energy=(90.0, 160.0), pitch=12.0)
+    sp["mean"][:, 2] = 99.5                                     # just outside the grid's top face
+    c = gpu_ctx_factory()
+    c.set_physics(False)
+    cid = c.add_child(*edges)
+    c.set_hu(cid, hu)
+    dij = c.add_dij_scorer(cid, capacity=1 << 22)
+    c.dij_record_hits(dij, 1 << 24)
+    N = c.set_spot_plan(sp)
+    c.transport_plan(0, N, 17)
+    vox, spot, val = c.dij_hits(dij)
+    assert len(vox) > 100_000 and (val > 0).all()
+    op = c.dij_build(dij)
+    indptr, indices, data = op.csr()
+    path = oracle.ref_dij(vox, spot, val, 1 << 22, len(sp), nxyz, str(tmp_path))
+    z = np.load(path)
+    assert list(z["shape"]) == [len(sp), int(np.prod(nxyz))]
+    for s in range(len(sp)):
+        rv = z["indices"][z["indptr"][s]:z["indptr"][s + 1]].astype(np.int64)
+        rd = z["data"][z["indptr"][s]:z["indptr"][s + 1]]
+        order = np.argsort(rv)
+        gv = indices[indptr[s]:indptr[s + 1]].astype(np.int64)
+        np.testing.assert_array_equal(gv, rv[order])           # the key set, bit-exact
+        np.testing.assert_allclose(data[indptr[s]:indptr[s + 1]], rd[order], rtol=2.0 ** -23, atol=0)
+    assert c.dij_info(dij)["occupied"] == len(z["indices"]) == op.nnz
 
 
 def test_dij_products_match_dense_references(gpu_ctx_factory, wl):
