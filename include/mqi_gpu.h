@@ -289,6 +289,22 @@ int mqi_trace_rays(mqi_ctx* ctx, int child_id, const float* rays, uint64_t n_ray
  * dEdx (negative, MeV/mm in water), beta^2, Te_max, momentum}. */
 int mqi_eval_physics(mqi_ctx* ctx, const float* energies, uint64_t n, float* out);
 
+/* Evaluate a scorer's callback on the device for given step states, for parity tests: the values
+ * the transport's scoring forms for fp_compute_hit (moqui/base/scorers/mqi_scorer_energy_deposit.hpp:
+ * 12-177) in voxel cnb[i] of child `child_id` (its densities and edges, the context's calibration
+ * and physics setting).  steps: 9 floats per step -- vtx0.ke, dE, local_dE, vtx0.pos[3],
+ * vtx1.pos[3]; primary: nonzero for a primary.  out: n doubles.  Before the ROI gate and the
+ * "value > 0" filter of insert_hashtable. */
+int mqi_eval_hits(mqi_ctx* ctx, int child_id, int scorer_type, const float* steps, const uint32_t* cnb,
+                  const int32_t* primary, uint64_t n, double* out);
+
+/* Evaluate scorer `scorer_id`'s ROI mapping on the device, for parity tests: roi_t::idx (the
+ * scoring gate) and roi_t::get_mask_idx (the statistics key) of each voxel (moqui/base/mqi_roi.hpp:
+ * 47-71, 87-160).  Where moqui's CONTOUR idx reads before its start array (a voxel below the first
+ * run), the transport returns -1 (not scored). */
+int mqi_eval_roi(mqi_ctx* ctx, int scorer_id, const uint32_t* voxels, uint64_t n, int32_t* idx,
+                 int32_t* mask_idx);
+
 /* ---- statistics --------------------------------------------------------------------------- */
 
 /* Add tps_env's statistics pair to a child (Dose_stat and DoseSquare_stat,
@@ -382,7 +398,7 @@ int mqi_autotune(mqi_ctx* ctx, int source_plan, uint64_t h0, uint64_t h1, uint64
  * EDEP, DOSE_W, DOSE_W2, DOSE_M.  Work is issued on `cuda_stream` (NULL = the legacy default
  * stream) and the call returns when it is done.
  *
- * The transport's own scratch (its particle queues) is a 24 MiB static device array in the
+ * The transport's own scratch (its particle queues) is a 40 MiB static device array in the
  * library, held by every GPU that loads it until the process exits.  At most 16777216 histories
  * per call (larger requests return MQI_ERR_INVALID); a queue generation that outgrows the
  * scratch returns MQI_ERR_OVERFLOW.  All calls share the array: calls whose GPU work overlaps

@@ -42,6 +42,7 @@ EXPORTS = (
     "mqi_sample_plan", "mqi_add_dij_scorer", "mqi_dij_build", "mqi_dij_get_csr", "mqi_dij_info",
     "mqi_dij_matvec", "mqi_dij_rmatvec", "mqi_set_scenarios", "mqi_run_plan_until_stat", "mqi_set_launch_mode",
     "mqi_autotune", "mqi_set_calibration", "mqi_philox4x32_10", "mqi_dij_record_hits", "mqi_dij_get_hits",
+    "mqi_eval_hits", "mqi_eval_roi",
 )
 
 VERTEX_DTYPE = np.dtype([("ke", "<f4"), ("pos", "<f4", (3,)), ("dir", "<f4", (3,))])
@@ -134,6 +135,8 @@ def load(path: Optional[str] = None) -> C.CDLL:
         "mqi_version": (C.c_char_p, []),
         "mqi_philox4x32_10": (i32, [vp, vp, vp]),
         "mqi_dij_record_hits": (i32, [vp, i32, u64]),
+        "mqi_eval_hits": (i32, [vp, i32, i32, vp, vp, vp, u64, vp]),
+        "mqi_eval_roi": (i32, [vp, i32, vp, u64, vp, vp]),
         "mqi_dij_get_hits": (i32, [vp, i32, vp, vp, vp, P(u64)]),
         "mqi_add_stat_scorers": (i32, [vp, i32, i32, u32, vp, vp, vp, P(i32), P(i32)]),
         "mqi_stat_uncertainty": (i32, [vp, i32, i32, u64, f32, P(C.c_double), P(u64)]),
@@ -349,6 +352,24 @@ class Context:
         return out
 
     # ---- raw-pointer variants (pinned host or device buffers owned by the caller) ----
+    def eval_hits(self, child: int, stype: int, steps: np.ndarray, cnb: np.ndarray, primary: np.ndarray) -> np.ndarray:
+        """The device's scorer callback on step states (9 floats each), voxels and primary flags."""
+        st = np.ascontiguousarray(steps, np.float32).reshape(-1, 9)
+        cb = np.ascontiguousarray(cnb, np.uint32)
+        pr = np.ascontiguousarray(primary, np.int32)
+        out = np.empty(len(cb), np.float64)
+        self._check(self.lib.mqi_eval_hits(self.h, child, stype, _ptr(st), _ptr(cb), _ptr(pr), len(cb), _ptr(out)),
+                    self.h)
+        return out
+
+    def eval_roi(self, scorer: int, voxels: np.ndarray):
+        """The device's roi_t::idx and get_mask_idx of a scorer's ROI for the given voxels."""
+        v = np.ascontiguousarray(voxels, np.uint32)
+        idx = np.empty(len(v), np.int32)
+        mask = np.empty(len(v), np.int32)
+        self._check(self.lib.mqi_eval_roi(self.h, scorer, _ptr(v), len(v), _ptr(idx), _ptr(mask)), self.h)
+        return idx, mask
+
     def set_vertices_ptr(self, ptr: int, n: int, on_device: bool) -> None:
         self._check(self.lib.mqi_set_vertices(self.h, C.c_void_p(ptr), None, n, int(on_device)), self.h)
         self.n_vertices = n

@@ -167,6 +167,7 @@ mqi_destroy(mqi_ctx* c) {
     cudaFree(c->spot_ids);
     free_queue(c->qa);
     free_queue(c->qb);
+    cudaFree(c->def);
     cudaFree(c->counters);
     cudaFree(c->stats);
     cudaFree(c->tables);
@@ -533,6 +534,8 @@ make_wave_params(mqi_ctx* c, uint64_t seed, WaveParams& P) {
     P.inline_local    = (P.n_children == 1) ? 1 : 0;
     P.head            = c->counters + 2;
     P.error_flag      = c->counters + 3;
+    P.def             = c->def;
+    P.n_def           = c->counters + 4;
     P.stats           = c->stats;
     P.spot_ids        = c->has_spots ? c->spot_ids : nullptr;
     P.tables          = c->tables;
@@ -583,7 +586,7 @@ run_generations(mqi_ctx* c, WaveParams P, uint64_t h0, uint64_t h1, bool plan) {
                      "mqi_transport");
             MQI_CUDA(c, cudaStreamSynchronize(c->stream), "mqi_transport: wave");
             ++c->waves;
-            ++c->kernel_launches;
+            c->kernel_launches += 2;   // the wave and its post-step kernel
             ++c->wave_launches;
             float ms = 0.0f;
             if (cudaEventElapsedTime(&ms, c->ev0, c->ev1) == cudaSuccess) c->wave_ms += ms;
@@ -664,7 +667,7 @@ run_streamed(mqi_ctx* c, WaveParams P, uint64_t h0, uint64_t h1, bool plan) {
         }
         c->waves += K;
         c->wave_launches += K;
-        c->kernel_launches += 3 * (uint64_t) K;
+        c->kernel_launches += 4 * (uint64_t) K;   // per wave: top-up, load, wave, post-step
         float ms = 0.0f;
         if (cudaEventElapsedTime(&ms, c->ev0, c->ev1) == cudaSuccess) c->wave_ms += ms;
         if (c->host_counts[3] & 2u) {
@@ -683,8 +686,11 @@ run_transport(mqi_ctx* c, uint64_t h0, uint64_t h1, uint64_t seed, bool plan) {
     DeviceGuard g(c->device);
     const uint32_t need = c->primary_chunk * 3u;
     if (c->queue_cap < need) {
+        cudaFree(c->def);
+        c->def        = nullptr;
         cudaError_t e = alloc_queue(c->qa, need);
         if (e == cudaSuccess) e = alloc_queue(c->qb, need);
+        if (e == cudaSuccess) e = cudaMalloc(&c->def, (size_t) need * sizeof(Deferred));
         if (e != cudaSuccess) {
             c->queue_cap = 0;
             return cuda_fail(c, e, "mqi_transport: queue allocation");
@@ -1127,6 +1133,80 @@ mqi_eval_physics(mqi_ctx* c, const float* energies, uint64_t n, float* out) {
     cudaFree(de);
     cudaFree(dout);
     if (e != cudaSuccess) return cuda_fail(c, e, "mqi_eval_physics");
+    return MQI_OK;
+}
+
+int
+mqi_eval_hits(mqi_ctx* c, int child_id, int scorer_type, const float* steps, const uint32_t* cnb,
+              const int32_t* primary, uint64_t n, double* out) {
+    if (!valid_ctx(c) || (n && (!steps || !cnb || !primary || !out)))
+        return fail(c, MQI_ERR_INVALID, "mqi_eval_hits: bad argument");
+    if (child_id < 0 || child_id >= (int) c->children.size() || !c->children[child_id].has_rho)
+        return fail(c, MQI_ERR_INVALID, "mqi_eval_hits: no such child with a density");
+    if (scorer_type < MQI_SCORER_EDEP || scorer_type > MQI_SCORER_DIJ)
+        return fail(c, MQI_ERR_UNSUPPORTED, "mqi_eval_hits: unknown scorer type");
+    const ChildHost& h = c->children[child_id];
+    const uint64_t   nvox = (uint64_t) h.nx * h.ny * h.nz;
+    for (uint64_t i = 0; i < n; ++i)
+        if (cnb[i] >= nvox) return fail(c, MQI_ERR_INVALID, "mqi_eval_hits: a voxel index is outside the grid");
+    ChildDev d{};
+    d.nx = h.nx; d.ny = h.ny; d.nz = h.nz;
+    d.xe = h.xe; d.ye = h.ye; d.ze = h.ze; d.rho = h.rho;
+    std::memcpy(d.rf, h.rf, sizeof(d.rf));
+    std::memcpy(d.ri, h.ri, sizeof(d.ri));
+    std::memcpy(d.tr, h.tr, sizeof(d.tr));
+    d.identity = h.identity;
+    DeviceGuard g(c->device);
+    float*    ds = nullptr;
+    uint32_t* dc = nullptr;
+    int32_t*  dp = nullptr;
+    double*   dout = nullptr;
+    cudaError_t e = cudaMalloc(&ds, n * 9 * sizeof(float) + 16);
+    if (e == cudaSuccess) e = cudaMalloc(&dc, n * sizeof(uint32_t) + 16);
+    if (e == cudaSuccess) e = cudaMalloc(&dp, n * sizeof(int32_t) + 16);
+    if (e == cudaSuccess) e = cudaMalloc(&dout, n * sizeof(double) + 16);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(ds, steps, n * 9 * sizeof(float), cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dc, cnb, n * sizeof(uint32_t), cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dp, primary, n * sizeof(int32_t), cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = launch_eval_hits(d, c->calib, c->physics_debug, scorer_type, ds, dc, dp, n, dout, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(out, dout, n * sizeof(double), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaFree(ds);
+    cudaFree(dc);
+    cudaFree(dp);
+    cudaFree(dout);
+    if (e != cudaSuccess) return cuda_fail(c, e, "mqi_eval_hits");
+    return MQI_OK;
+}
+
+int
+mqi_eval_roi(mqi_ctx* c, int scorer_id, const uint32_t* voxels, uint64_t n, int32_t* idx, int32_t* mask_idx) {
+    if (!valid_ctx(c) || (n && (!voxels || !idx || !mask_idx))) return fail(c, MQI_ERR_INVALID, "mqi_eval_roi: bad argument");
+    if (scorer_id < 0 || scorer_id >= (int) c->scorers.size()) return fail(c, MQI_ERR_INVALID, "mqi_eval_roi: no such scorer");
+    const ScorerHost& s = c->scorers[scorer_id];
+    const ChildHost&  h = c->children[s.child];
+    const uint64_t    nvox = (uint64_t) h.nx * h.ny * h.nz;
+    for (uint64_t i = 0; i < n; ++i)
+        if (voxels[i] >= nvox) return fail(c, MQI_ERR_INVALID, "mqi_eval_roi: a voxel index is outside the grid");
+    ScorerDev d{};
+    d.type = s.type; d.roi_method = s.roi_method; d.stat_mode = s.stat_mode;
+    d.roi_len = s.roi_len; d.start = s.start; d.stride = s.stride; d.acc = s.acc;
+    DeviceGuard g(c->device);
+    uint32_t* dv = nullptr;
+    int32_t*  di = nullptr;
+    int32_t*  dm = nullptr;
+    cudaError_t e = cudaMalloc(&dv, n * sizeof(uint32_t) + 16);
+    if (e == cudaSuccess) e = cudaMalloc(&di, n * sizeof(int32_t) + 16);
+    if (e == cudaSuccess) e = cudaMalloc(&dm, n * sizeof(int32_t) + 16);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dv, voxels, n * sizeof(uint32_t), cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = launch_eval_roi(d, dv, n, di, dm, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(idx, di, n * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(mask_idx, dm, n * sizeof(int32_t), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    cudaFree(dv);
+    cudaFree(di);
+    cudaFree(dm);
+    if (e != cudaSuccess) return cuda_fail(c, e, "mqi_eval_roi");
     return MQI_OK;
 }
 

@@ -127,7 +127,8 @@ struct mqi_ctx {
     bool                    has_spots = false;
     mqi_gpu::QueueBuf       qa, qb;
     uint32_t                queue_cap = 0;
-    uint32_t*               counters = nullptr;     // [0,1] queue sizes, [2] head, [3] error flag
+    mqi_gpu::Deferred*      def = nullptr;          // tracks a wave stopped at nuclear interactions (queue_cap)
+    uint32_t*               counters = nullptr;     // [0,1] queue sizes, [2] head, [3] error flag, [4] deferred
     unsigned long long*     stats = nullptr;        // 8 x u64
     uint32_t*               host_counts = nullptr;  // pinned: 4 x u32
     float*                  tables = nullptr;       // 6*600 physics + 3996 HU correction

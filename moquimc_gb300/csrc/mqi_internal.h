@@ -100,6 +100,23 @@ struct Queue {
     uint32_t  capacity;
 };
 
+/// A track stopped by the wave kernel at a nuclear interaction (p-p elastic, p-O elastic or p-O
+/// inelastic), after its along-step and the draw that chose the process: the post-step kernel runs
+/// the process, scores the step, moves the track and queues it (and its daughters) for the next
+/// wave.  These processes end ~0.2% of the steps, but their code is most of the step loop's
+/// instructions and registers; taking it out of the loop shrinks what every step carries.
+struct Deferred {
+    float    ke0, ke1;
+    float    p0[3], d0[3], p1[3];
+    float    dE;
+    float    spr0;     // SPR the step computed
+    uint32_t cnb;      // voxel of the step
+    uint32_t uid_lo, uid_hi, hist, spot;
+    uint32_t meta;     // below | primary | child | npush, as the queue's meta word
+    uint32_t ctr;      // Philox counter after the step's process draw
+    uint32_t proc;     // 1 p-p elastic, 2 p-O elastic, 3 p-O inelastic
+};
+
 /// A tabulated calibration (mqi_set_calibration); mode 0 = the default curves.
 struct CalibDev {
     int          mode;
@@ -135,6 +152,8 @@ struct WaveParams {
     unsigned long long* stats;  // device: mqi_stats fields (8 x u64)
     const uint32_t* spot_ids;   // per history (may be null)
     uint32_t*       error_flag; // device: 1 a bounded loop gave up, 2 queue overflow, 4 Dij table full
+    Deferred*       def;        // device: tracks stopped at a nuclear interaction (capacity in.capacity)
+    uint32_t*       n_def;      // device: entries in def (zeroed before each wave)
     int             smem_edge_floats; // shared-memory floats for staged child edges
     const float*    tables;     // device: the six physics tables, 6 x 600 floats in Tables order
                                 // (followed by the 3996 HU density-correction factors)
@@ -223,5 +242,9 @@ cudaError_t launch_scale(double* a, uint32_t stride, uint64_t n, double w, int s
 cudaError_t launch_copy_strided(const double* a, uint32_t stride, double* out, uint64_t n, int sms, cudaStream_t s);
 cudaError_t launch_copy_scaled(const double* a, double* out, uint64_t n, double w, int sms, cudaStream_t s);
 cudaError_t launch_eval_physics(const float* tables, const float* e, uint64_t n, float* out, cudaStream_t s);
+cudaError_t launch_eval_hits(const ChildDev& c, const CalibDev& cal, int dbg, int type, const float* steps,
+                             const uint32_t* cnb, const int32_t* prim, uint64_t n, double* out, cudaStream_t s);
+cudaError_t launch_eval_roi(const ScorerDev& sc, const uint32_t* vox, uint64_t n, int32_t* idx, int32_t* mask,
+                            cudaStream_t s);
 
 }   // namespace mqi_gpu

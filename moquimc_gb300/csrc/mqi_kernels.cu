@@ -684,42 +684,19 @@ post_poi(Ctx& C, Trk& t, Rng& rng) {
     t.stopped = true;
 }
 
-/// What a discrete interaction reads and changes.
-struct PostState {
-    Trk      t;
-    Rng      rng;
-    uint32_t n_sec, n_local, n_drop, n_err;
-};
-
-/// The post-step process of an interaction step (mqi_fippel_physics.hpp:178-196).  It stays
-/// inline (an out-of-line call passing the track by value measured 25% slower); what it calls
-/// that is large and rare -- extra Philox blocks, the post-step rotations -- is out of line.
-__device__ __forceinline__ PostState
-post_interaction(const WaveParams* P, const Tables* T, Grid g, int child, bool dbg, float tcut, int proc,
-                 PostState s) {
-    Ctx C;
-    C.P = P; C.T = T; C.g = g; C.child = child; C.dbg = dbg; C.tcut = tcut;
-    C.spot = s.t.spot;
-    C.n_sec = C.n_local = C.n_drop = C.n_err = 0;
-    if (proc == 0) post_delta(C, s.t, s.rng);
-    else if (proc == 1) post_pp(C, s.t, s.rng);
-    else if (proc == 2) post_poe(C, s.t, s.rng);
-    else post_poi(C, s.t, s.rng);
-    s.n_sec = C.n_sec; s.n_local = C.n_local; s.n_drop = C.n_drop; s.n_err = C.n_err;
-    return s;
-}
-
-/// fippel_physics::stepping (mqi_fippel_physics.hpp:67-216).
-__device__ inline void
+/// fippel_physics::stepping (mqi_fippel_physics.hpp:67-216).  Returns 0, or the nuclear process
+/// (1 p-p elastic, 2 p-O elastic, 3 p-O inelastic) the step ended in: its post-step runs in the
+/// post-step kernel (k_post), after the wave; a delta ray is produced here.
+__device__ inline int
 stepping(Ctx& C, Trk& t, Rng& rng, float rho, float d2b) {
     t.spr0 = -1.0f;
     if (rho < 1.0e-7f) {
         t.p1 = advance(t.p0, t.d0, d2b);
-        return;
+        return 0;
     }
     if (rho > 99.9f) {
         t.stopped = true;
-        return;
+        return 0;
     }
     if (t.ke0 <= kTpCut) {
         if (t.ke0 < 0.0f) t.ke0 = 0.0f;
@@ -727,7 +704,7 @@ stepping(Ctx& C, Trk& t, Rng& rng, float rho, float d2b) {
         t.ke1 -= t.ke0;
         t.p1      = last_step_pos(C.T, &C.P->calib, C.dbg, t.p0, t.d0, t.ke0, t.dE, rho);
         t.stopped = true;
-        return;
+        return 0;
     }
     const Tables& T = *C.T;
     rng.begin_step();
@@ -771,19 +748,10 @@ stepping(Ctx& C, Trk& t, Rng& rng, float rho, float d2b) {
         const float u = cs_sum * rng.uniform();
         t.d1          = t.d0;
         const int proc = (u < c0) ? 0 : (u < c0 + c1) ? 1 : (u < c0 + c1 + c2) ? 2 : (u < c0 + c1 + c2 + c3) ? 3 : -1;
-        if (proc >= 0) {
-            PostState ps;
-            ps.t   = t;
-            ps.rng = rng;
-            ps     = post_interaction(C.P, C.T, C.g, C.child, C.dbg, C.tcut, proc, ps);
-            t      = ps.t;
-            rng    = ps.rng;
-            C.n_sec += ps.n_sec;
-            C.n_local += ps.n_local;
-            C.n_drop += ps.n_drop;
-            C.n_err += ps.n_err;
-        }
+        if (proc == 0) post_delta(C, t, rng);   // ~15% of the steps
+        else if (proc > 0) return proc;          // ~0.2% of the steps
     }
+    return 0;
 }
 
 // ------------------------------------------------------------------------------------------
@@ -821,6 +789,66 @@ load_track(const Queue& q, uint32_t i, Trk& t, Rng& rng, bool& step_phase, uint3
     rng.has2   = false;
 }
 
+/// The queue's meta word of a track (without the phase bit).
+__device__ inline uint32_t
+track_meta(const Trk& t) {
+    return (t.below & kMetaBelowMask) | (t.primary ? kMetaPrimary : 0u) | (t.ke1 != t.ke0 ? kMetaKe1Zero : 0u) |
+           ((uint32_t) t.child << kMetaChildShift) | ((t.npush & 1023u) << kMetaNpushShift);
+}
+
+/// Queue a track that left a child grid for the entry into child t.child (world frame).
+__device__ inline void
+requeue_entry(Ctx& C, const Trk& t, const Rng& rng) {
+    const Queue& q   = C.P->out;
+    const uint32_t i = atomicAdd(C.P->n_out, 1u);
+    if (i >= q.capacity) {
+        atomicOr(C.P->error_flag, 2u);
+        ++C.n_err;
+        return;
+    }
+    q.ke[i] = t.ke0;
+    q.px[i] = t.p0.x; q.py[i] = t.p0.y; q.pz[i] = t.p0.z;
+    q.dx[i] = t.d0.x; q.dy[i] = t.d0.y; q.dz[i] = t.d0.z;
+    q.dE0[i] = 0.0f;
+    q.hist[i] = t.hist;
+    q.uid_lo[i] = (uint32_t) t.uid;
+    q.uid_hi[i] = (uint32_t) (t.uid >> 32);
+    q.ctr[i] = rng.ctr;
+    q.meta[i] = track_meta(t);
+    q.cell[i] = 0;
+    q.spot[i] = t.spot;
+}
+
+/// Hand a track whose step ended in nuclear process `proc` to the post-step kernel.  A track is
+/// handed over at most once per wave and every handed-over track was fetched from the wave's
+/// input, so the record array (sized like the input queue) cannot run out.
+__device__ inline void
+defer_track(Ctx& C, const Trk& t, const Rng& rng, uint32_t cnb, int proc) {
+    const uint32_t i = atomicAdd(C.P->n_def, 1u);
+    if (i >= C.P->in.capacity) {
+        atomicOr(C.P->error_flag, 2u);
+        ++C.n_err;
+        return;
+    }
+    Deferred& d = C.P->def[i];
+    d.ke0 = t.ke0;
+    d.ke1 = t.ke1;
+    d.p0[0] = t.p0.x; d.p0[1] = t.p0.y; d.p0[2] = t.p0.z;
+    d.d0[0] = t.d0.x; d.d0[1] = t.d0.y; d.d0[2] = t.d0.z;
+    d.p1[0] = t.p1.x; d.p1[1] = t.p1.y; d.p1[2] = t.p1.z;
+    d.dE     = t.dE;
+    d.spr0   = t.spr0;
+    d.cnb    = cnb;
+    d.uid_lo = (uint32_t) t.uid;
+    d.uid_hi = (uint32_t) (t.uid >> 32);
+    d.hist   = t.hist;
+    d.spot   = t.spot;
+    d.meta   = (t.below & kMetaBelowMask) | (t.primary ? kMetaPrimary : 0u) | ((uint32_t) t.child << kMetaChildShift) |
+             ((t.npush & 1023u) << kMetaNpushShift);
+    d.ctr  = rng.ctr;
+    d.proc = (uint32_t) proc;
+}
+
 /// Write a track that used up its step budget back to the next queue, mid-grid.
 __device__ inline void
 requeue_track(Ctx& C, const Trk& t, const Rng& rng) {
@@ -839,9 +867,7 @@ requeue_track(Ctx& C, const Trk& t, const Rng& rng) {
     q.uid_lo[i] = (uint32_t) t.uid;
     q.uid_hi[i] = (uint32_t) (t.uid >> 32);
     q.ctr[i] = rng.ctr;
-    q.meta[i] = (t.below & kMetaBelowMask) | (t.primary ? kMetaPrimary : 0u) |
-                (t.ke1 != t.ke0 ? kMetaKe1Zero : 0u) | kMetaPhaseStep |
-                ((uint32_t) t.child << kMetaChildShift) | ((t.npush & 1023u) << kMetaNpushShift);
+    q.meta[i] = track_meta(t) | kMetaPhaseStep;
     q.cell[i] = grid_cnb(C.g, t.cell);
     q.spot[i] = t.spot;
 }
@@ -983,8 +1009,14 @@ wave_body(const WaveParams& P) {
         const uint32_t cnb = grid_cnb(C.g, t.cell);
         const float    rho = voxel_rho(C.g, cnb);
         const float    d2b = grid_exit(C.g, t.p0, t.d0, t.cell);
-        stepping(C, t, rng, rho, d2b);
+        const int      nuclear = stepping(C, t, rng, rho, d2b);
         ++n_steps;
+        if (nuclear) {   // the post-step kernel finishes this step and queues the track
+            defer_track(C, t, rng, cnb, nuclear);
+            have    = false;
+            in_grid = false;
+            continue;
+        }
         if (++track_steps > kMaxTrackSteps) {   // no physical track comes near this; never hang
             t.stopped = true;
             ++C.n_err;
@@ -1024,6 +1056,97 @@ wave_body(const WaveParams& P) {
     if (threadIdx.x < 8) sstat[threadIdx.x] = 0ull;
     __syncthreads();
     const unsigned long long v[8] = { n_hist, n_tracks, n_steps, C.n_sec, C.n_local, C.n_drop, 0ull, C.n_err };
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+        if (v[k]) atomicAdd(&sstat[k], v[k]);
+    __syncthreads();
+    if (threadIdx.x < 8 && sstat[threadIdx.x]) atomicAdd(&P.stats[threadIdx.x], sstat[threadIdx.x]);
+    if (C.n_err) atomicOr(P.error_flag, 1u);
+}
+
+/// The post-step kernel's body: for each track the wave stopped at a nuclear interaction, the rest
+/// of its step as the wave would have run it -- the process's post_step (mqi_pp_elastic.hpp:119-219,
+/// mqi_po_elastic.hpp:96-217, mqi_po_inelastic.hpp:158-288), the step's scoring, the cell update
+/// and move() (mqi_transport.hpp:204-233) -- then the track goes to the next wave's queue: mid-grid,
+/// at the entry of the next child, or nowhere when it stopped or left the world.  The random
+/// stream resumes where the step left it (the process draw was the first word of the block at
+/// counter ctr - 1), so the track draws the same numbers as if the wave had run the process.
+template<int kMode>
+__device__ __forceinline__ void
+post_body(const WaveParams& P) {
+    Ctx C;
+    C.P     = &P;
+    C.T     = reinterpret_cast<const Tables*>(P.tables);
+    C.dbg   = P.physics_debug != 0;
+    C.tcut  = P.t_cut;
+    C.n_sec = C.n_local = C.n_drop = C.n_err = 0;
+    uint32_t       n_hist = 0;
+    const uint32_t n_raw  = *P.n_def;
+    const uint32_t n      = n_raw > P.in.capacity ? P.in.capacity : n_raw;   // past it: flagged, not written
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const Deferred& d = P.def[i];
+        Trk t;
+        t.ke0 = d.ke0;
+        t.ke1 = d.ke1;
+        t.p0  = make_float3(d.p0[0], d.p0[1], d.p0[2]);
+        t.d0  = make_float3(d.d0[0], d.d0[1], d.d0[2]);
+        t.p1  = make_float3(d.p1[0], d.p1[1], d.p1[2]);
+        t.d1  = t.d0;
+        t.dE  = d.dE;
+        t.ldE = 0.0f;
+        t.spr0 = d.spr0;
+        t.uid  = (uint64_t) d.uid_lo | ((uint64_t) d.uid_hi << 32);
+        t.hist = d.hist;
+        t.spot = d.spot;
+        t.below   = d.meta & kMetaBelowMask;
+        t.primary = (d.meta & kMetaPrimary) != 0;
+        t.child   = (int) ((d.meta >> kMetaChildShift) & 7u);
+        t.npush   = (d.meta >> kMetaNpushShift) & 1023u;
+        t.stopped = false;
+        Rng rng;
+        rng.k0     = P.k0;
+        rng.k1     = P.k1;
+        rng.hist   = d.hist;
+        rng.uid_lo = d.uid_lo;
+        rng.uid_hi = d.uid_hi;
+        rng.ctr    = d.ctr;
+        rng.blk    = philox_block(d.ctr - 1u, d.hist, d.uid_lo, d.uid_hi, P.k0, P.k1);
+        rng.pos    = 1;
+        rng.has2   = false;
+        C.child = t.child;
+        C.spot  = t.spot;
+        C.g     = make_grid(P.child[t.child], nullptr, nullptr, nullptr);
+        apply_scenario(P, C.g, t.child, t.spot);
+        const uint32_t nxy = (uint32_t) C.g.nx * (uint32_t) C.g.ny;
+        const uint32_t rem = d.cnb % nxy;
+        t.cell = make_int3((int) (rem % (uint32_t) C.g.nx), (int) (rem / (uint32_t) C.g.nx), (int) (d.cnb / nxy));
+        if (d.proc == 1) post_pp(C, t, rng);
+        else if (d.proc == 2) post_poe(C, t, rng);
+        else post_poi(C, t, rng);
+        score_step<kMode>(C, t, d.cnb, voxel_rho(C.g, d.cnb), grid_volume(C.g, t.cell));
+        if (!t.stopped) {
+            grid_step_index(C.g, t.p1, t.d1, t.cell);
+            t.p0  = t.p1;
+            t.d0  = t.d1;
+            t.ke0 = t.ke1;
+            t.dE = t.ldE = 0.0f;
+        }
+        if (!t.stopped && grid_valid(C.g, t.cell)) {
+            requeue_track(C, t, rng);
+            continue;
+        }
+        to_world(C.g, t.p0, t.d0);
+        ++t.child;
+        if (t.stopped || t.child >= P.n_children) {
+            if (t.primary) ++n_hist;
+            continue;
+        }
+        requeue_entry(C, t, rng);
+    }
+    __shared__ unsigned long long sstat[8];
+    if (threadIdx.x < 8) sstat[threadIdx.x] = 0ull;
+    __syncthreads();
+    const unsigned long long v[8] = { n_hist, 0ull, 0ull, C.n_sec, C.n_local, C.n_drop, 0ull, C.n_err };
 #pragma unroll
     for (int k = 0; k < 8; ++k)
         if (v[k]) atomicAdd(&sstat[k], v[k]);
@@ -1117,6 +1240,14 @@ k_wave(const __grid_constant__ WaveParams P) {
     wave_body<kMode>(P);
 }
 
+constexpr int kPostBlock = 128;
+
+template<int kMode>
+__global__ void __launch_bounds__(kPostBlock)
+k_post(const __grid_constant__ WaveParams P) {
+    post_body<kMode>(P);
+}
+
 int
 wave_smem_bytes(const WaveParams& p) {
     return (int) sizeof(Tables) + p.smem_edge_floats * (int) sizeof(float);
@@ -1133,13 +1264,18 @@ wave_edge_floats(const ChildDev* c, int n) {
     return (f + 3) & ~3;
 }
 
+/// One wave: the record count of the post-step kernel cleared, the wave kernel, then the
+/// post-step kernel over the tracks the wave stopped at nuclear interactions (a grid-stride loop
+/// over a count it reads on the device).
 template<int B, int M, int K = 0>
 static cudaError_t
 launch_variant(const WaveParams& p, int grid, cudaStream_t s) {
     const int   smem = wave_smem_bytes(p);
     cudaError_t e    = cudaFuncSetAttribute(k_wave<B, M, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e == cudaSuccess) e = cudaMemsetAsync(p.n_def, 0, sizeof(uint32_t), s);
     if (e != cudaSuccess) return e;
     k_wave<B, M, K><<<grid, B, smem, s>>>(p);
+    k_post<K><<<grid, kPostBlock, 0, s>>>(p);
     return cudaGetLastError();
 }
 
@@ -1281,6 +1417,61 @@ k_eval_physics(const float* __restrict__ tables, const float* __restrict__ e, ui
         o[6] = rel.Te_max;
         o[7] = rel.momentum();
     }
+}
+
+// ------------------------------------------------------------------------------------------
+// Scorer-callback and ROI probes for parity tests: the transport's own device functions on given
+// step states and voxels.
+// ------------------------------------------------------------------------------------------
+__global__ void
+k_eval_hits(const __grid_constant__ ChildDev c, const __grid_constant__ CalibDev cal, int dbg, int type,
+            const float* __restrict__ steps, const uint32_t* __restrict__ cnb, const int32_t* __restrict__ prim,
+            uint64_t n, double* __restrict__ out) {
+    const Grid g = make_grid(c, nullptr, nullptr, nullptr);
+    for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n; i += (uint64_t) gridDim.x * blockDim.x) {
+        const float* st = steps + 9 * i;
+        Trk t;
+        t.ke0 = st[0];
+        t.dE  = st[1];
+        t.ldE = st[2];
+        t.p0  = make_float3(st[3], st[4], st[5]);
+        t.p1  = make_float3(st[6], st[7], st[8]);
+        t.primary = prim[i] != 0;
+        const uint32_t v   = cnb[i];
+        const uint32_t nxy = (uint32_t) g.nx * (uint32_t) g.ny;
+        const int3     cell = make_int3((int) (v % nxy % (uint32_t) g.nx), (int) (v % nxy / (uint32_t) g.nx), (int) (v / nxy));
+        const float rho = g.rho[v];
+        const float vol = grid_volume(g, cell);
+        // dose_to_water of the step exactly as score_step forms it
+        const float spr    = spr_of(cal, rho, t.ke0, dbg != 0);
+        const float dose_w = (rho < 1.0e-7f) ? 0.0f : (t.dE + t.ldE) * 1.60218e-10f / (vol * rho * spr);
+        out[i]             = compute_hit(type, t, rho, vol, dose_w);
+    }
+}
+
+__global__ void
+k_eval_roi(const __grid_constant__ ScorerDev s, const uint32_t* __restrict__ vox, uint64_t n, int32_t* __restrict__ idx,
+           int32_t* __restrict__ mask) {
+    for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n; i += (uint64_t) gridDim.x * blockDim.x) {
+        idx[i]  = roi_idx(s, vox[i]);
+        mask[i] = roi_mask_idx(s, vox[i]);
+    }
+}
+
+cudaError_t
+launch_eval_hits(const ChildDev& c, const CalibDev& cal, int dbg, int type, const float* steps, const uint32_t* cnb,
+                 const int32_t* prim, uint64_t n, double* out, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_eval_hits<<<(unsigned) ((n + 127) / 128 < 4096 ? (n + 127) / 128 : 4096), 128, 0, s>>>(c, cal, dbg, type, steps, cnb,
+                                                                                            prim, n, out);
+    return cudaGetLastError();
+}
+
+cudaError_t
+launch_eval_roi(const ScorerDev& sc, const uint32_t* vox, uint64_t n, int32_t* idx, int32_t* mask, cudaStream_t s) {
+    if (n == 0) return cudaSuccess;
+    k_eval_roi<<<(unsigned) ((n + 127) / 128 < 4096 ? (n + 127) / 128 : 4096), 128, 0, s>>>(sc, vox, n, idx, mask);
+    return cudaGetLastError();
 }
 
 cudaError_t

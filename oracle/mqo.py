@@ -218,6 +218,36 @@ def ref_dij(voxel, spot, value, capacity: int, n_spots: int, nxyz, out_dir: str,
     return os.path.join(out_dir, name + ".npz")
 
 
+HIT_FUNCTIONS = ("energy_deposit", "energy_deposit_primary", "energy_deposit_secondary", "dose_to_water",
+                 "dose_to_water_square", "dose_to_medium", "LETd_weight1", "LETd_weight2", "LETt_weight1",
+                 "LETt_weight2")
+
+
+def ref_hits(nxyz, xe, ye, ze, rho, steps, cnb, primary, debug: bool = False) -> dict:
+    """The reference's scorer callbacks on step states (driver mode `hits`): {name: float64 array}."""
+    with tempfile.TemporaryDirectory() as td:
+        i, o = os.path.join(td, "in.bin"), os.path.join(td, "out.bin")
+        write_vecs(i, [np.asarray(nxyz, np.int32), np.asarray(xe, np.float32), np.asarray(ye, np.float32),
+                       np.asarray(ze, np.float32), np.asarray(rho, np.float32).reshape(-1),
+                       np.asarray(steps, np.float32).reshape(-1), np.asarray(cnb, np.uint32),
+                       np.asarray(primary, np.int32)])
+        subprocess.run([ref_binary(debug), "hits", i, o], check=True, capture_output=True)
+        vecs = read_vecs(o, [np.float64] * len(HIT_FUNCTIONS))
+    return dict(zip(HIT_FUNCTIONS, vecs))
+
+
+def ref_roi(method: int, original_length: int, start, stride, acc, voxels):
+    """roi_t::idx and get_mask_idx from the reference's own roi_t (driver mode `roi`)."""
+    with tempfile.TemporaryDirectory() as td:
+        i, o = os.path.join(td, "in.bin"), os.path.join(td, "out.bin")
+        write_vecs(i, [np.asarray([method, original_length], np.int32), np.asarray(start, np.uint32),
+                       np.asarray(stride if stride is not None else [], np.uint32),
+                       np.asarray(acc if acc is not None else [], np.uint32), np.asarray(voxels, np.uint32)])
+        subprocess.run([ref_binary(False), "roi", i, o], check=True, capture_output=True)
+        idx, mask = read_vecs(o, [np.int32, np.int32])
+    return idx, mask
+
+
 def write_rays(path, grid_bounds, nxyz, max_steps, rays):
     with open(path, "wb") as f:
         f.write(np.asarray(grid_bounds, np.float32).tobytes())

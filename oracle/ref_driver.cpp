@@ -31,6 +31,10 @@
 //       Samples phantom_env's beam source with the reference's own distribution classes.
 //   dij <hits.bin> <capacity> <n_spots> <nx> <ny> <nz> <scale> <out_dir> <name>
 //       Replays recorded Dij insertions through insert_hashtable and writes save_to_npz's file.
+//   hits <in.bin> <out.bin>
+//       Evaluates the scorer callbacks (dose, LET weights, ...) on given step states.
+//   roi <in.bin> <out.bin>
+//       Evaluates roi_t::idx and get_mask_idx on given voxels.
 #include <moqui/base/environments/mqi_phantom_env.hpp>
 #include <moqui/kernel_functions/mqi_transport.hpp>
 
@@ -618,6 +622,82 @@ run_dij(int argc, char** argv) {
     return 0;
 }
 
+/// Scorer callbacks on given step states: the reference's own fp_compute_hit functions
+/// (moqui/base/scorers/mqi_scorer_energy_deposit.hpp:12-177) over a grid3d of the given edges and
+/// densities with the patient material's stopping-power ratio.  Input: vec<i32> {nx, ny, nz},
+/// vec<f32> xe, ye, ze, rho, vec<f32> steps (9 per step: vtx0.ke, dE, local_dE, vtx0.pos, vtx1.pos),
+/// vec<u32> cnb, vec<i32> primary.  Output: ten vec<f64>, in the order energy_deposit,
+/// energy_deposit_primary, energy_deposit_secondary, dose_to_water, dose_to_water_square,
+/// dose_to_medium, LETd_weight1, LETd_weight2, LETt_weight1, LETt_weight2.
+int
+run_hits(const char* in_path, const char* out_path) {
+    std::ifstream fin(in_path, std::ios::binary);
+    const auto dims  = read_vec<int32_t>(fin);
+    const auto xe    = read_vec<float>(fin);
+    const auto ye    = read_vec<float>(fin);
+    const auto ze    = read_vec<float>(fin);
+    auto       rho   = read_vec<float>(fin);
+    const auto steps = read_vec<float>(fin);
+    const auto cnb   = read_vec<uint32_t>(fin);
+    const auto prim  = read_vec<int32_t>(fin);
+    if (!fin || dims.size() != 3) return 3;
+    mqi::grid3d<mqi::density_t, float> geo(xe.data(), dims[0] + 1, ye.data(), dims[1] + 1, ze.data(), dims[2] + 1);
+    geo.set_data(rho.data());
+    mqi::patient_material_t<float> pm;
+    mqi::material_t<float>*        mat = &pm;
+    using fn_t = double (*)(const mqi::track_t<float>&, const mqi::cnb_t&, mqi::grid3d<mqi::density_t, float>&,
+                            mqi::material_t<float>*&);
+    const fn_t fns[10] = { mqi::energy_deposit<float>, mqi::energy_deposit_primary<float>,
+                           mqi::energy_deposit_secondary<float>, mqi::dose_to_water<float>,
+                           mqi::dose_to_water_square<float>, mqi::dose_to_medium<float>, mqi::LETd_weight1<float>,
+                           mqi::LETd_weight2<float>, mqi::LETt_weight1<float>, mqi::LETt_weight2<float> };
+    std::ofstream fout(out_path, std::ios::binary);
+    for (const fn_t f : fns) {
+        std::vector<double> out(cnb.size());
+        for (size_t i = 0; i < cnb.size(); ++i) {
+            const float*        st = &steps[9 * i];
+            mqi::track_t<float> t;
+            t.vtx0.ke  = st[0];
+            t.dE       = st[1];
+            t.local_dE = st[2];
+            t.vtx0.pos = mqi::vec3<float>(st[3], st[4], st[5]);
+            t.vtx1.pos = mqi::vec3<float>(st[6], st[7], st[8]);
+            t.primary  = prim[i] != 0;
+            const mqi::cnb_t c = cnb[i];
+            out[i]             = f(t, c, geo, mat);
+        }
+        write_vec(fout, out);
+    }
+    return 0;
+}
+
+/// roi_t::idx and roi_t::get_mask_idx (moqui/base/mqi_roi.hpp:47-71, 87-160) of given voxels.
+/// Input: vec<i32> {method, original length}, vec<u32> start, stride, acc, voxels.  Output:
+/// vec<i32> idx, vec<i32> mask_idx.
+int
+run_roi(const char* in_path, const char* out_path) {
+    std::ifstream fin(in_path, std::ios::binary);
+    const auto hdr    = read_vec<int32_t>(fin);
+    auto       start  = read_vec<uint32_t>(fin);
+    auto       stride = read_vec<uint32_t>(fin);
+    auto       acc    = read_vec<uint32_t>(fin);
+    const auto vox    = read_vec<uint32_t>(fin);
+    if (!fin || hdr.size() != 2) return 3;
+    const auto method = static_cast<mqi::roi_mapping_t>(hdr[0]);
+    const int32_t len = static_cast<int32_t>(start.size());
+    mqi::roi_t roi(method, static_cast<uint32_t>(hdr[1]), len, start.data(), stride.empty() ? nullptr : stride.data(),
+                   acc.empty() ? nullptr : acc.data());
+    std::vector<int32_t> idx(vox.size()), mask(vox.size());
+    for (size_t i = 0; i < vox.size(); ++i) {
+        idx[i]  = roi.idx(vox[i]);
+        mask[i] = roi.get_mask_idx(vox[i]);
+    }
+    std::ofstream fout(out_path, std::ios::binary);
+    write_vec(fout, idx);
+    write_vec(fout, mask);
+    return 0;
+}
+
 }   // namespace
 
 void
@@ -645,6 +725,8 @@ main(int argc, char** argv) {
     if (mode == "physics" && argc >= 3) return run_physics(argv[2]);
     if (mode == "vertices") return run_vertices(argc, argv);
     if (mode == "dij") return run_dij(argc, argv);
+    if (mode == "hits" && argc >= 4) return run_hits(argv[2], argv[3]);
+    if (mode == "roi" && argc >= 4) return run_roi(argv[2], argv[3]);
     if (mode == "sample" && argc >= 5)
         return run_sample(argv[2], std::atol(argv[3]), static_cast<unsigned>(std::atol(argv[4])));
     std::fprintf(stderr, "bad arguments\n");

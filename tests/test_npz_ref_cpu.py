@@ -121,3 +121,51 @@ int main(int, char** argv) {
     assert len(la[1]) - len(hdr) == 96                 # the reference's sizeof(std::string) x 3 bytes
     m = np.load(ours)
     assert m["format"] == b"csr" and (m["data"] == z["data"]).all()
+
+
+def test_volume_writers_match_the_reference_writers_byte_for_byte(ref, tmp_path):
+    """mqi_host::write_outputs (the host drivers' raw / mhd / mha) against the reference's own
+    save_to_bin / save_to_mhd / save_to_mha (moqui/base/mqi_io.hpp:166-183, 493-583) on the same
+    volume, grid and scale: identical files."""
+    src = tmp_path / "vol.cpp"
+    src.write_text(r'''
+#include <fstream>
+#include <moqui/base/mqi_node.hpp>
+#include <moqui/base/mqi_io.hpp>
+#include "mqi_host.hpp"
+#include <random>
+int main(int, char** argv) {
+    const std::string ref = argv[1], ours = argv[2];
+    const int nx = 7, ny = 5, nz = 9;
+    std::vector<float> xe(nx + 1), ye(ny + 1), ze(nz + 1);
+    for (int i = 0; i <= nx; ++i) xe[i] = -12.25f + 0.98f * i;
+    for (int i = 0; i <= ny; ++i) ye[i] = 3.5f + 1.5f * i;
+    for (int i = 0; i <= nz; ++i) ze[i] = -200.0f + 2.0f * i;
+    std::mt19937_64 g(5);
+    std::uniform_real_distribution<double> u(0.0, 1e-3);
+    std::vector<double> d(nx * ny * nz);
+    for (double& x : d) x = u(g);
+    mqi::node_t<float> node;
+    node.geo = new mqi::grid3d<mqi::density_t, float>(xe.data(), nx + 1, ye.data(), ny + 1, ze.data(), nz + 1);
+    const float scale = 2.5f;
+    mqi::io::save_to_bin<double>(d.data(), scale, ref, "v_bin", (uint32_t) d.size());
+    mqi::io::save_to_mhd<float>(&node, d.data(), scale, ref, "v_mhd", (uint32_t) d.size());
+    mqi::io::save_to_mha<float>(&node, d.data(), scale, ref, "v_mha", (uint32_t) d.size());
+    mqi_host::write_outputs(ours, "v_bin", "raw", d, scale, xe, ye, ze);
+    mqi_host::write_outputs(ours, "v_mhd", "mhd", d, scale, xe, ye, ze);
+    mqi_host::write_outputs(ours, "v_mha", "mha", d, scale, xe, ye, ze);
+    return 0;
+}
+''')
+    exe = tmp_path / "vol"
+    r = subprocess.run(["g++", "-std=c++17", "-O2", "-w", f"-I{ROOT}/oracle/_ref/src", f"-I{ROOT}/include",
+                        f"-I{ROOT}/moquimc_gb300/host", str(src), "-o", str(exe), "-lz"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    a, b = tmp_path / "ref", tmp_path / "ours"
+    a.mkdir()
+    b.mkdir()
+    subprocess.run([str(exe), str(a), str(b)], check=True, capture_output=True)
+    names = ["v_bin.raw", "v_mhd.mhd", "v_mhd.raw", "v_mha.mha"]
+    assert sorted(os.listdir(a)) == sorted(os.listdir(b)) == sorted(names)
+    for n in names:
+        assert (a / n).read_bytes() == (b / n).read_bytes(), n
