@@ -13,7 +13,8 @@ The line also carries plan-level sections measured on rank 0 (skip with --no-pla
 synthetic CT with 2000 spots, one batched call vs one call per spot, and the time to the
 reference's 1% criterion in the >50% dose region; "robust" -- 21 setup/density scenarios in one
 queue drain; "dij" -- the Dij of the plan, its products and 100 optimisation iterations with a
-finite-difference check of the gradient.
+finite-difference check of the gradient.  "robust_full" (only with --sections robust_full) -- the
+whole c4 configuration, 2000 spots x 21 scenarios, autotuned, to the 1% criterion.
 
 --impl reference times the reference's own CPU implementation (the staged reference build in
 oracle/_ref) on the host cores for the same workload and metric.
@@ -234,14 +235,22 @@ def plan_section(torch, capi, workloads, args) -> dict:
     est1, nv = c.stat_uncertainty(d1, d2, N, 0.5)
     st = c.stats()
     c.reset()
+    # the plain path: one mqi_transport_plan call per spot over the whole plan, in its best launch
+    # mode (queue generations: no graph is captured per call); the streamed mode, which captures
+    # and instantiates a graph on every call, is timed on a sample of spots beside it
     sub = list(range(0, len(wl.spots), args.plain_stride))
     h_sub = int(sum(int(cum[s + 1] - cum[s]) for s in sub))
 
-    def plain():
-        for s in sub:
+    def plain(spots):
+        for s in spots:
             c.transport_plan(int(cum[s]), int(cum[s + 1]), 2)
 
-    t_p, _ = _cuda_time(torch, plain)
+    t_ps, _ = _cuda_time(torch, lambda: plain(sub))
+    c.set_launch_mode(streamed=0)
+    plain(sub[:20])                                                 # warm-up in this mode
+    c.reset()
+    t_p, _ = _cuda_time(torch, lambda: plain(range(len(wl.spots))))
+    c.set_launch_mode(streamed=1)
     c.reset()
     t_s, (passes, achieved) = _cuda_time(
         torch, lambda: c.run_plan_until_stat(d1, d2, 0.01, 0.5, args.max_passes, 0x5EED))
@@ -252,18 +261,25 @@ def plan_section(torch, capi, workloads, args) -> dict:
         c.batch_accumulate(sid)
     batch_est, batch_vox, n_batches = c.batch_uncertainty(sid, 0.5) if passes >= 2 else (float("nan"), 0, passes)
     batched = N / t_b
-    plain_rate = h_sub / t_p
+    plain_rate = N / t_p
     out = {
         "workload": wl.name, "voxels": list(wl.nxyz), "voxel_mm": [0.98, 0.98, 2.0], "spots": len(wl.spots),
         "histories_per_pass": N, "physics_debug": False,
         "batched": {"primaries_per_s": batched, "seconds_per_pass": t_b, "steps_per_primary": st["steps"] / N,
                     "waves": st["waves"], "estimate_after_one_pass": est1, "voxels_above_50pct": nv},
-        "plain_per_spot": {"primaries_per_s": plain_rate, "spots_timed": len(sub), "histories_timed": h_sub,
-                           "sample": f"every {args.plain_stride}th spot, one mqi_transport_plan call per spot"},
+        "plain_per_spot": {"primaries_per_s": plain_rate, "seconds_per_pass": t_p, "spots_timed": len(wl.spots),
+                           "histories_timed": N, "launch_mode": "queue generations",
+                           "sample": "the whole plan, one mqi_transport_plan call per spot",
+                           "streamed_with_graph_per_call": {"primaries_per_s": h_sub / t_ps, "spots": len(sub),
+                                                            "sample": f"every {args.plain_stride}th spot"}},
         "batched_over_plain": batched / plain_rate,
         "time_to_1pct_sigma": {"criterion": "reference estimator <= 1% over voxels > 50% of max dose",
                                "batched_s": t_s, "passes": passes, "achieved": achieved,
-                               "histories": passes * N, "plain_s_derived": passes * N / plain_rate,
+                               "histories": passes * N,
+                               "plain_s": passes * t_p,
+                               "plain_note": "measured seconds of one full per-spot pass x the passes: the per-spot "
+                                             "calls run the same histories and streams, so the tallies and the "
+                                             "estimate after each pass are the batched run's",
                                "batch_estimator_same_passes": {"mean_rel_sigma": batch_est, "voxels": batch_vox,
                                                                "batches": n_batches}},
     }
@@ -369,6 +385,41 @@ def robust_section(torch, capi, workloads, args) -> dict:
             "sample": f"every {args.robust_stride}th spot of the c3 plan"}
 
 
+def robust_full_section(torch, capi, workloads, args) -> dict:
+    """C4 as specified: the c3 CT and its whole 2000-spot plan x 21 scenarios (setup shifts 0 and
+    +-3 mm on x, y and z, each with DensityScaling 1, 1.035 and 0.965) in one queue drain per pass,
+    tuned by mqi_autotune on a sample of the plan, statistical stopping at 1% (the reference
+    estimator over voxels above 50% of the maximum, the worst scenario) by whole passes."""
+    wl = workloads.c3()
+    scen = workloads.c4_scenarios()
+    c = capi.Context(0)
+    c.set_physics(False)
+    cid = c.add_child(*wl.edges())
+    c.set_density(cid, c.hu_to_density(wl.hu.ravel()))
+    sid = c.add_scorer(cid, capi.DOSE_W)
+    N = c.set_spot_plan(wl.spots)
+    t_tune, tune = _cuda_time(torch, lambda: c.autotune(0, min(N, 2_000_000), 11, plan=True))
+    best = tune[np.argmax(tune["histories_per_s"])]
+    d1, d2 = c.add_stat_scorers(cid)
+    es = [workloads.scenario_edges(wl, sh) for sh, _ in scen]
+    c.set_scenarios(cid, [e[0] for e in es], [e[1] for e in es], [e[2] for e in es], [k for _, k in scen])
+    c.transport_plan(0, min(N, 50_000), 1)
+    c.reset()
+    t, (passes, achieved) = _cuda_time(
+        torch, lambda: c.run_plan_until_stat(d1, d2, 0.01, 0.5, args.max_passes, 0xC4))
+    st = c.stats()
+    c.close()
+    return {"workload": "c4: the c3 CT and 2000-spot plan x 21 scenarios", "scenarios": len(scen),
+            "spots": len(wl.spots), "histories_per_pass": N, "passes": passes, "seconds": t,
+            "worst_scenario_estimate": achieved,
+            "instance_primaries_per_s": passes * N * len(scen) / t,
+            "criterion": "reference estimator <= 1% over voxels > 50% of max dose, worst scenario",
+            "tuning": {"seconds": t_tune, "candidates": int(len(tune)),
+                       "chosen": {"block": int(best["block"]), "blocks_per_sm": int(best["blocks_per_sm"]),
+                                  "streamed": int(best["streamed"]), "primary_chunk": int(best["primary_chunk"])}},
+            "waves": st["waves"]}
+
+
 # ------------------------------------------------------------------------------------------
 # GPU arm
 # ------------------------------------------------------------------------------------------
@@ -405,6 +456,7 @@ def run_gpu(args, wl):
     cid = ctx.add_child(xe, ye, ze)
     ctx.set_hu(cid, wl.hu)
     sid = ctx.add_scorer(cid, capi.DOSE_W)
+    ctx.set_post_step_mode(args.post_step_mode)
     from moquimc_gb300 import replicas
 
     vseed, seed_base = replicas.replica_seeds(rank)
@@ -460,7 +512,9 @@ def run_gpu(args, wl):
         "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
         "frac": achieved / peaks["hbm_gbs"], "peak_source": f"{peaks['source']} hbm_gbs",
         "traffic": (tps * steps / max(launches, 1)) if tps else None,
-        "kernel": "k_wave", "algorithmic_bytes_per_launch": bytes_per_launch,
+        "kernel": "k_wave (timed with its post-step kernel k_post, which finishes the ~0.2% of steps that end "
+                  "in a nuclear interaction)",
+        "algorithmic_bytes_per_launch": bytes_per_launch,
         "avg_launch_ms": wave_ms / max(launches, 1), "transport_steps_per_s": steps / (wave_ms / 1e3) if wave_ms else 0,
         "wave_share_of_step": wave_ms / ms if ms > 0 else None,
     }
@@ -537,6 +591,7 @@ def run_gpu(args, wl):
 
             for key, fn in (("plan", lambda: plan_section(torch, capi, workloads, args)),
                             ("robust", lambda: robust_section(torch, capi, workloads, args)),
+                            ("robust_full", lambda: robust_full_section(torch, capi, workloads, args)),
                             ("dij", lambda: dij_section(torch, capi, workloads, optimize, args.dij_stride))):
                 if key not in args.sections.split(","):
                     continue
@@ -562,11 +617,15 @@ def main():
     ap.add_argument("--ref-histories", type=int, default=3000, help="histories per CPU process per sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-plan", action="store_true", help="skip the plan, robust and Dij sections")
-    ap.add_argument("--sections", default="plan,robust,dij", help="plan-level sections to run (comma-separated)")
+    ap.add_argument("--sections", default="plan,robust,dij",
+                    help="plan-level sections to run (comma-separated; robust_full -- the whole c4 configuration to 1%% "
+                         "sigma, several minutes -- only when named)")
     ap.add_argument("--dij-stride", type=int, default=1, help="Dij section on every n-th spot of the plan")
     ap.add_argument("--plain-stride", type=int, default=10, help="time every n-th spot for the plain per-spot rate")
     ap.add_argument("--robust-stride", type=int, default=20, help="spots of the plan in the robust sample")
     ap.add_argument("--max-passes", type=int, default=30, help="plan passes allowed for the 1%% criterion")
+    ap.add_argument("--post-step-mode", type=int, default=-1, choices=(-1, 0, 1),
+                    help="nuclear post-steps: -1 by run size, 0 inside the wave, 1 in the post-step kernel")
     ap.add_argument("--tune-histories", type=int, default=0,
                     help="tuner sample (0: the step's histories; -1: no tuning)")
     args = ap.parse_args()

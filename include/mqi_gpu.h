@@ -368,6 +368,14 @@ int mqi_set_tuning(mqi_ctx* ctx, int block, int blocks_per_sm, int slice_steps, 
  * even (default 8); values <= 0 / < 0 keep the current setting.  Results do not depend on it. */
 int mqi_set_launch_mode(mqi_ctx* ctx, int streamed, int graph_waves);
 
+/* Where the post-step of a nuclear interaction (p-p elastic, p-O elastic, p-O inelastic; ~0.2% of
+ * the steps) runs (no counterpart in moqui, which runs it inside the step, mqi_fippel_physics.hpp:
+ * 178-196): 0 inside the wave kernel's step loop; 1 in a post-step kernel after each wave, which
+ * takes that rarely used code out of the step loop (faster per step, one extra wave per
+ * interaction); -1 (default) chooses 1 for runs of at least 2^19 queue entries (histories x
+ * scenarios) and 0 below.  Results do not depend on it. */
+int mqi_set_post_step_mode(mqi_ctx* ctx, int mode);
+
 /* One candidate of mqi_autotune and its measured rate. */
 typedef struct {
     int      block;            /* threads per block of the wave kernel */
@@ -398,7 +406,7 @@ int mqi_autotune(mqi_ctx* ctx, int source_plan, uint64_t h0, uint64_t h1, uint64
  * EDEP, DOSE_W, DOSE_W2, DOSE_M.  Work is issued on `cuda_stream` (NULL = the legacy default
  * stream) and the call returns when it is done.
  *
- * The transport's own scratch (its particle queues) is a 40 MiB static device array in the
+ * The transport's own scratch (its particle queues) is a 24 MiB static device array in the
  * library, held by every GPU that loads it until the process exits.  At most 16777216 histories
  * per call (larger requests return MQI_ERR_INVALID); a queue generation that outgrows the
  * scratch returns MQI_ERR_OVERFLOW.  All calls share the array: calls whose GPU work overlaps

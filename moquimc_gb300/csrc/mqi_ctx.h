@@ -151,6 +151,7 @@ struct mqi_ctx {
     uint64_t                plan_histories = 0;
     std::vector<uint64_t>   plan_cum_host;
     int                     streamed = 1;             // 1: device top-up + graph-captured waves; 0: generations
+    int                     post_step_mode = -1;      // nuclear post-steps: -1 by run size, 0 in the wave, 1 post-step kernel
     int                     graph_waves = 8;          // waves per captured graph (even)
     mqi_gpu::TopUp*         topup = nullptr;          // device: streamed-transport state
     unsigned long long*     host_next = nullptr;      // pinned: TopUp::next after a graph launch
@@ -172,8 +173,11 @@ fail(mqi_ctx* c, int code, const std::string& msg) {
     return code;
 }
 
+/// Report a failed CUDA call.  The runtime keeps a non-sticky error as its "last error" until it
+/// is read; it is read here, so that the next launch's cudaGetLastError reports that launch.
 inline int
 cuda_fail(mqi_ctx* c, cudaError_t e, const char* what) {
+    (void) cudaGetLastError();
     return fail(c, e == cudaErrorMemoryAllocation ? MQI_ERR_NOMEM : MQI_ERR_CUDA,
                 std::string(what) + ": " + cudaGetErrorString(e));
 }

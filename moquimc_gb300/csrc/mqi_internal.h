@@ -152,6 +152,7 @@ struct WaveParams {
     unsigned long long* stats;  // device: mqi_stats fields (8 x u64)
     const uint32_t* spot_ids;   // per history (may be null)
     uint32_t*       error_flag; // device: 1 a bounded loop gave up, 2 queue overflow, 4 Dij table full
+    int             split;      // 1: nuclear post-steps in the post-step kernel; 0: inside the wave
     Deferred*       def;        // device: tracks stopped at a nuclear interaction (capacity in.capacity)
     uint32_t*       n_def;      // device: entries in def (zeroed before each wave)
     int             smem_edge_floats; // shared-memory floats for staged child edges

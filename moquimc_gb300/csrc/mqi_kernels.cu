@@ -684,9 +684,33 @@ post_poi(Ctx& C, Trk& t, Rng& rng) {
     t.stopped = true;
 }
 
-/// fippel_physics::stepping (mqi_fippel_physics.hpp:67-216).  Returns 0, or the nuclear process
-/// (1 p-p elastic, 2 p-O elastic, 3 p-O inelastic) the step ended in: its post-step runs in the
-/// post-step kernel (k_post), after the wave; a delta ray is produced here.
+/// The post-step of a nuclear interaction run inside the step loop (kernel instances that do not
+/// hand them to the post-step kernel): the track and its stream go in and out by value, which
+/// keeps the rarely-taken processes from pinning registers across the loop.
+struct PostState {
+    Trk      t;
+    Rng      rng;
+    uint32_t n_sec, n_local, n_drop, n_err;
+};
+
+__device__ __forceinline__ PostState
+post_nuclear(const WaveParams* P, const Tables* T, Grid g, int child, bool dbg, float tcut, int proc, PostState s) {
+    Ctx C;
+    C.P = P; C.T = T; C.g = g; C.child = child; C.dbg = dbg; C.tcut = tcut;
+    C.spot = s.t.spot;
+    C.n_sec = C.n_local = C.n_drop = C.n_err = 0;
+    if (proc == 1) post_pp(C, s.t, s.rng);
+    else if (proc == 2) post_poe(C, s.t, s.rng);
+    else post_poi(C, s.t, s.rng);
+    s.n_sec = C.n_sec; s.n_local = C.n_local; s.n_drop = C.n_drop; s.n_err = C.n_err;
+    return s;
+}
+
+/// fippel_physics::stepping (mqi_fippel_physics.hpp:67-216).  A delta ray is produced here.  A
+/// nuclear interaction (1 p-p elastic, 2 p-O elastic, 3 p-O inelastic) either runs here too
+/// (kSplit false) or ends the step early: stepping returns the process and the post-step kernel
+/// (k_post) finishes the step after the wave (kSplit true).
+template<bool kSplit>
 __device__ inline int
 stepping(Ctx& C, Trk& t, Rng& rng, float rho, float d2b) {
     t.spr0 = -1.0f;
@@ -748,8 +772,24 @@ stepping(Ctx& C, Trk& t, Rng& rng, float rho, float d2b) {
         const float u = cs_sum * rng.uniform();
         t.d1          = t.d0;
         const int proc = (u < c0) ? 0 : (u < c0 + c1) ? 1 : (u < c0 + c1 + c2) ? 2 : (u < c0 + c1 + c2 + c3) ? 3 : -1;
-        if (proc == 0) post_delta(C, t, rng);   // ~15% of the steps
-        else if (proc > 0) return proc;          // ~0.2% of the steps
+        if (proc == 0) {
+            post_delta(C, t, rng);   // ~15% of the steps
+        } else if (proc > 0) {       // ~0.2% of the steps
+            if constexpr (kSplit) {
+                return proc;
+            } else {
+                PostState ps;
+                ps.t   = t;
+                ps.rng = rng;
+                ps     = post_nuclear(C.P, C.T, C.g, C.child, C.dbg, C.tcut, proc, ps);
+                t      = ps.t;
+                rng    = ps.rng;
+                C.n_sec += ps.n_sec;
+                C.n_local += ps.n_local;
+                C.n_drop += ps.n_drop;
+                C.n_err += ps.n_err;
+            }
+        }
     }
     return 0;
 }
@@ -872,7 +912,7 @@ requeue_track(Ctx& C, const Trk& t, const Rng& rng) {
     q.spot[i] = t.spot;
 }
 
-template<int kMode>
+template<int kMode, bool kSplit>
 __device__ __forceinline__ void
 wave_body(const WaveParams& P) {
     extern __shared__ __align__(16) unsigned char smem[];
@@ -1009,9 +1049,9 @@ wave_body(const WaveParams& P) {
         const uint32_t cnb = grid_cnb(C.g, t.cell);
         const float    rho = voxel_rho(C.g, cnb);
         const float    d2b = grid_exit(C.g, t.p0, t.d0, t.cell);
-        const int      nuclear = stepping(C, t, rng, rho, d2b);
+        const int      nuclear = stepping<kSplit>(C, t, rng, rho, d2b);
         ++n_steps;
-        if (nuclear) {   // the post-step kernel finishes this step and queues the track
+        if (kSplit && nuclear) {   // the post-step kernel finishes this step and queues the track
             defer_track(C, t, rng, cnb, nuclear);
             have    = false;
             in_grid = false;
@@ -1234,10 +1274,10 @@ launch_load_primaries(const Queue& q, const mqi_vertex* v, const uint32_t* spot_
 /// The wave kernel in the launch shapes the tuner chooses from: (threads per block, minimum
 /// resident blocks per SM).  The register budget each shape implies is what differs.  Mode 0
 /// (DIRECT ROIs, simple scorer callbacks) comes in every shape; the other modes in 128 x 5.
-template<int kBlock, int kMinBlocks, int kMode>
+template<int kBlock, int kMinBlocks, int kMode, bool kSplit>
 __global__ void __launch_bounds__(kBlock, kMinBlocks)
 k_wave(const __grid_constant__ WaveParams P) {
-    wave_body<kMode>(P);
+    wave_body<kMode, kSplit>(P);
 }
 
 constexpr int kPostBlock = 128;
@@ -1264,44 +1304,62 @@ wave_edge_floats(const ChildDev* c, int n) {
     return (f + 3) & ~3;
 }
 
-/// One wave: the record count of the post-step kernel cleared, the wave kernel, then the
-/// post-step kernel over the tracks the wave stopped at nuclear interactions (a grid-stride loop
-/// over a count it reads on the device).
-template<int B, int M, int K = 0>
+/// One wave.  With kSplit: the record count of the post-step kernel cleared, the wave kernel, then
+/// the post-step kernel over the tracks the wave stopped at nuclear interactions (a grid-stride
+/// loop over a count it reads on the device).  Without: the wave kernel alone.
+template<int B, int M, int K, bool S>
 static cudaError_t
 launch_variant(const WaveParams& p, int grid, cudaStream_t s) {
     const int   smem = wave_smem_bytes(p);
-    cudaError_t e    = cudaFuncSetAttribute(k_wave<B, M, K>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e == cudaSuccess) e = cudaMemsetAsync(p.n_def, 0, sizeof(uint32_t), s);
-    if (e != cudaSuccess) return e;
-    k_wave<B, M, K><<<grid, B, smem, s>>>(p);
-    k_post<K><<<grid, kPostBlock, 0, s>>>(p);
+    cudaError_t e    = cudaFuncSetAttribute(k_wave<B, M, K, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if constexpr (S) {
+        if (e == cudaSuccess) e = cudaMemsetAsync(p.n_def, 0, sizeof(uint32_t), s);
+    }
+    if (e != cudaSuccess) {
+        (void) cudaGetLastError();   // the failed call's error is returned here, not left for the next launch
+        return e;
+    }
+    k_wave<B, M, K, S><<<grid, B, smem, s>>>(p);
+    if constexpr (S) k_post<K><<<grid, kPostBlock, 0, s>>>(p);
     return cudaGetLastError();
 }
 
+/// Instances: the split form in every launch shape and scoring mode; the inline form in the two
+/// leading shapes of the common modes (one dose-like scorer, DIRECT ROIs) and in 128 x 5 for the
+/// FP64 callbacks (dose to medium, LET).  A request for an inline instance that is not compiled
+/// runs the split one (the results are the same) when the caller gave a record array.
 cudaError_t
 launch_wave(const WaveParams& p, int grid, int block, int blocks_per_sm, cudaStream_t s) {
     const int grid5 = grid / (blocks_per_sm > 0 ? blocks_per_sm : 1) * 5;
+    if (!p.split && (p.kernel_mode == 0 || p.kernel_mode == kModeSingle)) {
+        const bool wide = block != 128;
+        if (p.kernel_mode == kModeSingle)
+            return wide ? launch_variant<256, 2, kModeSingle, false>(p, grid, s)
+                        : launch_variant<128, 5, kModeSingle, false>(p, grid5, s);
+        return wide ? launch_variant<256, 2, 0, false>(p, grid, s) : launch_variant<128, 5, 0, false>(p, grid5, s);
+    }
+    if (!p.split && p.kernel_mode == kModeFull) return launch_variant<128, 5, kModeFull, false>(p, grid5, s);
+    if (!p.def || !p.n_def) return cudaErrorInvalidValue;   // the split form needs its record array
     switch (p.kernel_mode) {
     case 0: break;
     case kModeSingle:
         if (block == 128) {
-            if (blocks_per_sm >= 6) return launch_variant<128, 6, kModeSingle>(p, grid, s);
-            if (blocks_per_sm == 5) return launch_variant<128, 5, kModeSingle>(p, grid, s);
-            return launch_variant<128, 4, kModeSingle>(p, grid, s);
+            if (blocks_per_sm >= 6) return launch_variant<128, 6, kModeSingle, true>(p, grid, s);
+            if (blocks_per_sm == 5) return launch_variant<128, 5, kModeSingle, true>(p, grid, s);
+            return launch_variant<128, 4, kModeSingle, true>(p, grid, s);
         }
-        return launch_variant<256, 2, kModeSingle>(p, grid, s);
-    case kModeFull: return launch_variant<128, 5, kModeFull>(p, grid5, s);
-    case kModeRoi: return launch_variant<128, 5, kModeRoi>(p, grid5, s);
-    case kModeFull | kModeRoi: return launch_variant<128, 5, kModeFull | kModeRoi>(p, grid5, s);
-    default: return launch_variant<128, 5, kModeAll>(p, grid5, s);   // any mode with Dij
+        return launch_variant<256, 2, kModeSingle, true>(p, grid, s);
+    case kModeFull: return launch_variant<128, 5, kModeFull, true>(p, grid5, s);
+    case kModeRoi: return launch_variant<128, 5, kModeRoi, true>(p, grid5, s);
+    case kModeFull | kModeRoi: return launch_variant<128, 5, kModeFull | kModeRoi, true>(p, grid5, s);
+    default: return launch_variant<128, 5, kModeAll, true>(p, grid5, s);   // any mode with Dij
     }
     if (block == 128) {
-        if (blocks_per_sm >= 6) return launch_variant<128, 6>(p, grid, s);
-        if (blocks_per_sm == 5) return launch_variant<128, 5>(p, grid, s);
-        return launch_variant<128, 4>(p, grid, s);
+        if (blocks_per_sm >= 6) return launch_variant<128, 6, 0, true>(p, grid, s);
+        if (blocks_per_sm == 5) return launch_variant<128, 5, 0, true>(p, grid, s);
+        return launch_variant<128, 4, 0, true>(p, grid, s);
     }
-    return launch_variant<256, 2>(p, grid, s);
+    return launch_variant<256, 2, 0, true>(p, grid, s);
 }
 
 // ------------------------------------------------------------------------------------------

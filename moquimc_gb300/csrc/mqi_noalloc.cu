@@ -5,12 +5,11 @@
 // allocator, a plug-in host that forbids allocation after start-up, or a latency-bound loop that
 // cannot afford cudaMalloc's implicit device synchronisation.  For them this entry point
 // transports histories with every buffer supplied by the caller except the transport's own
-// scratch -- the two particle queues, the records of tracks waiting for a nuclear post-step, and
-// their counters -- which lives in a file-scope static device array that each GPU loading the
-// library holds until the process exits.
+// scratch -- the two particle queues and their counters -- which lives in a file-scope static
+// device array that each GPU loading the library holds until the process exits.
 //
 // Limits and sharing, stated once for users:
-//   * the scratch is kNoallocScratchBytes (40 MiB): queues of kNoallocQueueCap entries, i.e. at
+//   * the scratch is kNoallocScratchBytes (24 MiB): queues of kNoallocQueueCap entries, i.e. at
 //     most kNoallocChunk primaries per queue generation; a call processes its histories in such
 //     chunks and accepts at most kNoallocMaxHistories histories;
 //   * every call shares the one array and leaves its contents behind; the counters a call needs
@@ -44,14 +43,12 @@ constexpr uint32_t kNoallocQueueCap     = 3u * kNoallocChunk;  // entries per qu
 constexpr size_t   kNoallocCol          = (size_t) kNoallocQueueCap * 4;   // bytes per queue column
 constexpr int      kNoallocCols         = 15;
 constexpr size_t   kNoallocQueueBytes   = kNoallocCol * kNoallocCols;
-constexpr size_t   kNoallocDeferBytes   = ((size_t) kNoallocQueueCap * sizeof(Deferred) + 255) & ~(size_t) 255;
 constexpr size_t   kNoallocCounterBytes = 256;                 // 8 x u32 counters, 8 x u64 stats
-constexpr size_t   kNoallocScratchBytes = 40u << 20;
+constexpr size_t   kNoallocScratchBytes = 24u << 20;
 constexpr uint64_t kNoallocMaxHistories = 1ull << 24;
 constexpr int      kNoallocTableFloats  = 6 * MQI_TABLE_N + MQI_DENSITY_CORRECTION_N;
 
-static_assert(2 * kNoallocQueueBytes + kNoallocDeferBytes + kNoallocCounterBytes <= kNoallocScratchBytes,
-              "scratch too small");
+static_assert(2 * kNoallocQueueBytes + kNoallocCounterBytes <= kNoallocScratchBytes, "scratch too small");
 static_assert(kNoallocCol % 256 == 0, "queue columns must stay 256-byte aligned");
 
 // The scratch: two SoA particle queues followed by the wave counters and run statistics.
@@ -81,6 +78,7 @@ static __device__ __align__(256) NoallocTables g_noalloc_tables = noalloc_tables
 
 int
 noalloc_fail(int code, const std::string& msg) {
+    if (code == MQI_ERR_CUDA) (void) cudaGetLastError();   // read a failed call's error so the next launch reports its own
     set_thread_error(msg.c_str());
     return code;
 }
@@ -145,9 +143,8 @@ mqi_transport_noalloc(int nx, int ny, int nz, const float* d_xe, const float* d_
     if (e != cudaSuccess) return noalloc_fail(MQI_ERR_CUDA, std::string("mqi_transport_noalloc: device query: ") + cudaGetErrorString(e));
     cudaStream_t   stream   = static_cast<cudaStream_t>(cuda_stream);
     unsigned char* base     = static_cast<unsigned char*>(scratch);
-    Deferred*      deferred = reinterpret_cast<Deferred*>(base + 2 * kNoallocQueueBytes);
-    uint32_t*      counters = reinterpret_cast<uint32_t*>(base + 2 * kNoallocQueueBytes + kNoallocDeferBytes);
-    auto*          stats    = reinterpret_cast<unsigned long long*>(base + 2 * kNoallocQueueBytes + kNoallocDeferBytes + 64);
+    uint32_t*      counters = reinterpret_cast<uint32_t*>(base + 2 * kNoallocQueueBytes);
+    auto*          stats    = reinterpret_cast<unsigned long long*>(base + 2 * kNoallocQueueBytes + 64);
     Queue          qa       = carve_queue(base);
     Queue          qb       = carve_queue(base + kNoallocQueueBytes);
 
@@ -181,8 +178,7 @@ mqi_transport_noalloc(int nx, int ny, int nz, const float* d_xe, const float* d_
     P.inline_local     = 1;
     P.head             = counters + 2;
     P.error_flag       = counters + 3;
-    P.def              = deferred;
-    P.n_def            = counters + 4;
+    P.split            = 0;   // nuclear post-steps inside the wave: no post-step records to hold
     P.stats            = stats;
     P.spot_ids         = nullptr;
     P.tables           = tables;

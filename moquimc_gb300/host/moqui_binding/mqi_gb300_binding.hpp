@@ -83,12 +83,16 @@ scorer_type_of(const mqi::scorer<R>* sc, const callbacks<R>& cb = callbacks<R>()
     return MQI_ERR_UNSUPPORTED;
 }
 
-/// Add `node` (a child of moqui's world) to the context with its densities and dense scorers;
-/// returns the child id and appends one scorer id per node scorer to `scorer_ids`.  The roi_t
-/// arrays are passed as they are (DIRECT needs none).
+/// Add `node` (a child of moqui's world) to the context with its densities and scorers; returns
+/// the child id and appends one scorer id per node scorer to `scorer_ids`, in the node's order.
+/// The roi_t arrays are passed as they are (DIRECT needs none).  tps_env's statistics pair
+/// ("Dose_stat", "DoseSquare_stat", mqi_tps_env.hpp:936-960) becomes mqi_add_stat_scorers; with
+/// `dij` set (tps_env's DOSE_Dij run, whose scorer carries the dose_to_water callback) a dose
+/// scorer becomes a Dij scorer of `dij_capacity` slots.
 template<typename R>
 int
-add_node(mqi_ctx* ctx, mqi::node_t<R>* node, std::vector<int>& scorer_ids) {
+add_node(mqi_ctx* ctx, mqi::node_t<R>* node, std::vector<int>& scorer_ids, bool dij = false,
+         uint64_t dij_capacity = 0) {
     auto*       geo = node->geo;
     const auto  n   = geo->get_nxyz();
     const auto& f   = geo->rotation_matrix_fwd;
@@ -103,15 +107,30 @@ add_node(mqi_ctx* ctx, mqi::node_t<R>* node, std::vector<int>& scorer_ids) {
     check(mqi_set_density(ctx, cid, geo->get_data(), 0), ctx, "mqi_set_density");
     const callbacks<R> cb;
     for (int s = 0; s < node->n_scorers; ++s) {
-        const mqi::scorer<R>* sc   = node->scorers[s];
-        const int             type = scorer_type_of(sc, cb);
+        const mqi::scorer<R>* sc     = node->scorers[s];
+        const mqi::roi_t*     roi    = sc->roi_;
+        const int             method = roi ? (int) roi->method_ : MQI_ROI_DIRECT;
+        const uint32_t        len    = roi ? (uint32_t) roi->length_ : 0;
+        const uint32_t*       start  = roi ? roi->start_ : nullptr;
+        const uint32_t*       stride = roi ? roi->stride_ : nullptr;
+        const uint32_t*       acc    = roi ? roi->acc_stride_ : nullptr;
+        if (std::string(sc->name_) == "Dose_stat" && s + 1 < node->n_scorers &&
+            std::string(node->scorers[s + 1]->name_) == "DoseSquare_stat") {
+            int d1 = -1, d2 = -1;
+            check(mqi_add_stat_scorers(ctx, cid, method, len, start, stride, acc, &d1, &d2), ctx, "mqi_add_stat_scorers");
+            scorer_ids.push_back(d1);
+            scorer_ids.push_back(d2);
+            ++s;
+            continue;
+        }
+        const int type = scorer_type_of(sc, cb);
         if (type < 0) throw std::runtime_error(std::string("scorer ") + sc->name_ + ": a callback without an enum");
-        const mqi::roi_t* roi = sc->roi_;
-        int               sid = -1;
-        check(mqi_add_scorer(ctx, cid, type, roi ? (int) roi->method_ : MQI_ROI_DIRECT, roi ? (uint32_t) roi->length_ : 0,
-                             roi ? roi->start_ : nullptr, roi ? roi->stride_ : nullptr, roi ? roi->acc_stride_ : nullptr,
-                             &sid),
-              ctx, "mqi_add_scorer");
+        int sid = -1;
+        if (dij && type == MQI_SCORER_DOSE_W)
+            check(mqi_add_dij_scorer(ctx, cid, method, len, start, stride, acc, dij_capacity, &sid), ctx,
+                  "mqi_add_dij_scorer");
+        else
+            check(mqi_add_scorer(ctx, cid, type, method, len, start, stride, acc, &sid), ctx, "mqi_add_scorer");
         scorer_ids.push_back(sid);
     }
     return cid;

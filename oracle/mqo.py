@@ -355,6 +355,28 @@ def ref_phantom_parallel(debug: bool, lxyz, pxyz, nxyz, energy, position, size, 
     return np.sum(doses, axis=0), recs, doses
 
 
+def ref_phantom_voxel_stats(debug: bool, lxyz, pxyz, nxyz, energy, position, size, histories_each, n_batches,
+                            hu, seed0, beam="uniform", n_parallel: Optional[int] = None):
+    """Per-voxel batch statistics of the reference CPU build: n_batches processes of
+    histories_each histories with distinct seeds, run n_parallel at a time; returns the per-voxel
+    sums of the batch doses and of their squares (float64 volumes, x fastest)."""
+    n = int(np.prod(nxyz))
+    s1 = np.zeros(n)
+    s2 = np.zeros(n)
+    n_parallel = n_parallel or max(os.cpu_count() or 1, 1)
+    done = 0
+    while done < n_batches:
+        k = min(n_parallel, n_batches - done)
+        with tempfile.TemporaryDirectory(prefix="mqi_refvox_") as td:
+            _, _, doses = ref_phantom_parallel(debug, lxyz, pxyz, nxyz, energy, position, size, histories_each, k, hu,
+                                               seed0 + done, beam, workdir=td)
+            for d in doses:
+                s1 += d
+                s2 += d * d
+        done += k
+    return s1, s2
+
+
 def ref_gpu_available(debug: bool = True) -> bool:
     """True when the reference GPU driver builds here (staged copy and nvcc present)."""
     return bool(_build().build_reference_gpu(debug))

@@ -1,9 +1,10 @@
 """The moqui-side binding on the GPU: moqui's phantom example run through phantom_env_gb300 (moqui's
 own phantom_env class, host beam source and save_reshaped_files, with run()/finalize() on the C
-ABI) writes the same 0_water_dE_total.raw and .mhd as this repository's C++ host driver on the same
-command line: the vertices are the reference's in both, the transport the same kernels and random
-streams, so the doses agree to FP64 summation order; the reference's raw and mhd writers and the
-host driver's produce the same files."""
+ABI) writes the same 0_water_dE_total.raw as this repository's C++ host driver on the same command
+line: the vertices are the reference's in both, the transport the same kernels and random streams,
+so the doses agree to FP64 summation order.  (moqui's phantom_env always writes raw; the host
+driver's --output_format is its own addition, and the writers are compared byte for byte on the
+CPU.)"""
 import os
 import subprocess
 
@@ -19,8 +20,7 @@ ARGS = ["--lxyz", "100", "100", "350", "--pxyz", "0", "0", "-175", "--nxyz", "10
         "--random_seed", "7"]
 
 
-@pytest.mark.parametrize("fmt", ["raw", "mhd"])
-def test_binding_matches_the_host_driver(tmp_path, fmt):
+def test_binding_matches_the_host_driver(tmp_path):
     if not os.path.isdir(os.path.join(REF_SRC, "moqui")):
         pytest.skip("the reference's staged sources are not present")
     from moquimc_gb300 import build
@@ -33,7 +33,7 @@ def test_binding_matches_the_host_driver(tmp_path, fmt):
     for name, prog in (("binding", exe), ("host", os.path.join(build.LIB_DIR, "phantom_env"))):
         d = tmp_path / name
         d.mkdir()
-        r = subprocess.run([prog, *ARGS, "--phantom_path", str(ph), "--output_prefix", str(d), "--output_format", fmt],
+        r = subprocess.run([prog, *ARGS, "--phantom_path", str(ph), "--output_prefix", str(d)],
                            capture_output=True, text=True)
         assert r.returncode == 0, (name, r.stderr[-2000:])
         outs[name] = d
@@ -41,5 +41,3 @@ def test_binding_matches_the_host_driver(tmp_path, fmt):
     b = np.fromfile(outs["host"] / "0_water_dE_total.raw", np.float64)
     assert a.size == b.size == 100 * 100 * 175 and a.sum() > 0
     np.testing.assert_allclose(a, b, rtol=1e-9, atol=1e-300)
-    if fmt == "mhd":
-        assert (outs["binding"] / "0_water_dE_total.mhd").read_bytes() == (outs["host"] / "0_water_dE_total.mhd").read_bytes()

@@ -10,9 +10,11 @@ Fixtures are computed by the reference's CPU build (driver modes `hits` and `roi
 CPU tests check the reference's numbers against the formulas written out here (FP32 operands,
 FP64 accumulation where the reference forms doubles), so the fixture means what the kernels assume.
 GPU tests evaluate the transport's own device functions (mqi_eval_hits, mqi_eval_roi) on the same
-inputs: ROI indices and every callback but dose_to_water bit-exact; dose_to_water (and its square,
-and the Dij value) within one FP32 rounding, because the kernel forms the per-step dose in FP32
-where the reference forms it in double.
+inputs: ROI indices and every callback but dose_to_water bit-exact; dose_to_water (and the Dij
+value) within 4e-7 relative, its square within 8e-7: the kernel forms the per-step dose in FP32
+(the constant 1.60218e-10 rounded to FP32, a product and a quotient rounded to FP32: three roundings
+of 2^-24 at most) where the reference forms it in double, and CUDA's powf in the stopping-power
+ratio is within 2 ulp of the host's.
 """
 import numpy as np
 import pytest
@@ -102,11 +104,11 @@ def test_device_callbacks_match_the_reference(hits, gpu_ctx_factory):
     for name, t in TYPES.items():
         got = c.eval_hits(cid, t, steps, cnb, primary)
         if name == "dose_to_water":
-            np.testing.assert_allclose(got, ref[name], rtol=2.0 ** -23, atol=0, err_msg=name)
-            np.testing.assert_allclose(c.eval_hits(cid, capi.DIJ, steps, cnb, primary), ref[name], rtol=2.0 ** -23,
-                                       atol=0)
+            np.testing.assert_allclose(got, ref[name], rtol=4e-7, atol=0, err_msg=name)
+            np.testing.assert_allclose(c.eval_hits(cid, capi.DIJ, steps, cnb, primary), ref[name], rtol=4e-7, atol=0)
+            assert np.mean(got == ref[name]) < 1.0   # formed in FP32: not the double result
         elif name == "dose_to_water_square":
-            np.testing.assert_allclose(got, ref[name], rtol=2.0 ** -22, atol=0, err_msg=name)
+            np.testing.assert_allclose(got, ref[name], rtol=8e-7, atol=0, err_msg=name)
         else:
             np.testing.assert_array_equal(got, ref[name], err_msg=name)
 
