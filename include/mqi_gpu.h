@@ -376,6 +376,14 @@ int mqi_set_launch_mode(mqi_ctx* ctx, int streamed, int graph_waves);
  * scenarios) and 0 below.  Results do not depend on it. */
 int mqi_set_post_step_mode(mqi_ctx* ctx, int mode);
 
+/* Sort the particle queue by energy before each wave that holds at least min_entries entries
+ * (0: never; default 262144): a counting sort on 1 MeV kinetic-energy bins, highest first, so the
+ * lanes of a warp step tracks of similar energy; primaries that have not taken a step yet follow,
+ * in the order they were loaded (no counterpart in moqui, whose threads each pop their own
+ * stack).  Protons are the only transported particle, so there is no type key.  Results do not
+ * depend on it. */
+int mqi_set_queue_sort(mqi_ctx* ctx, uint32_t min_entries);
+
 /* One candidate of mqi_autotune and its measured rate. */
 typedef struct {
     int      block;            /* threads per block of the wave kernel */

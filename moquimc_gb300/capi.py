@@ -42,7 +42,7 @@ EXPORTS = (
     "mqi_sample_plan", "mqi_add_dij_scorer", "mqi_dij_build", "mqi_dij_get_csr", "mqi_dij_info",
     "mqi_dij_matvec", "mqi_dij_rmatvec", "mqi_set_scenarios", "mqi_run_plan_until_stat", "mqi_set_launch_mode",
     "mqi_autotune", "mqi_set_calibration", "mqi_philox4x32_10", "mqi_dij_record_hits", "mqi_dij_get_hits",
-    "mqi_eval_hits", "mqi_eval_roi", "mqi_set_post_step_mode",
+    "mqi_eval_hits", "mqi_eval_roi", "mqi_set_post_step_mode", "mqi_set_queue_sort",
 )
 
 VERTEX_DTYPE = np.dtype([("ke", "<f4"), ("pos", "<f4", (3,)), ("dir", "<f4", (3,))])
@@ -137,6 +137,7 @@ def load(path: Optional[str] = None) -> C.CDLL:
         "mqi_dij_record_hits": (i32, [vp, i32, u64]),
         "mqi_eval_hits": (i32, [vp, i32, i32, vp, vp, vp, u64, vp]),
         "mqi_set_post_step_mode": (i32, [vp, i32]),
+        "mqi_set_queue_sort": (i32, [vp, u32]),
         "mqi_eval_roi": (i32, [vp, i32, vp, u64, vp, vp]),
         "mqi_dij_get_hits": (i32, [vp, i32, vp, vp, vp, P(u64)]),
         "mqi_add_stat_scorers": (i32, [vp, i32, i32, u32, vp, vp, vp, P(i32), P(i32)]),
@@ -249,6 +250,10 @@ class Context:
     def set_post_step_mode(self, mode: int) -> None:
         """Nuclear post-steps: 0 inside the wave, 1 in the post-step kernel, -1 by run size."""
         self._check(self.lib.mqi_set_post_step_mode(self.h, mode), self.h)
+
+    def set_queue_sort(self, min_entries: int) -> None:
+        """Sort the queue by energy bin before waves of at least min_entries entries (0: never)."""
+        self._check(self.lib.mqi_set_queue_sort(self.h, min_entries), self.h)
 
     def set_launch_mode(self, streamed: int = -1, graph_waves: int = 0) -> None:
         self._check(self.lib.mqi_set_launch_mode(self.h, streamed, graph_waves), self.h)

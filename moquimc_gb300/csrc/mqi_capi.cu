@@ -85,6 +85,13 @@ mqi_set_post_step_mode(mqi_ctx* c, int mode) {
 }
 
 int
+mqi_set_queue_sort(mqi_ctx* c, uint32_t min_entries) {
+    if (!valid_ctx(c)) return fail(c, MQI_ERR_INVALID, "mqi_set_queue_sort: ctx is NULL");
+    c->sort_min = min_entries;
+    return MQI_OK;
+}
+
+int
 mqi_philox4x32_10(const uint32_t* counter, const uint32_t* key, uint32_t* out) {
     if (!counter || !key || !out) {
         set_thread_error("mqi_philox4x32_10: a pointer is NULL");
@@ -175,6 +182,8 @@ mqi_destroy(mqi_ctx* c) {
     cudaFree(c->spot_ids);
     free_queue(c->qa);
     free_queue(c->qb);
+    free_queue(c->qsort);
+    cudaFree(c->sort_bins);
     cudaFree(c->def);
     cudaFree(c->counters);
     cudaFree(c->stats);
@@ -598,7 +607,8 @@ run_generations(mqi_ctx* c, WaveParams P, uint64_t h0, uint64_t h1, bool plan) {
                      "mqi_transport");
             MQI_CUDA(c, cudaStreamSynchronize(c->stream), "mqi_transport: wave");
             ++c->waves;
-            c->kernel_launches += P.split ? 2 : 1;   // the wave and, split, its post-step kernel
+            // the wave, its post-step kernel when split, the four sort kernels when sorting is on
+            c->kernel_launches += (P.split ? 2 : 1) + (P.sort_bins ? 4 : 0);
             ++c->wave_launches;
             float ms = 0.0f;
             if (cudaEventElapsedTime(&ms, c->ev0, c->ev1) == cudaSuccess) c->wave_ms += ms;
@@ -679,7 +689,8 @@ run_streamed(mqi_ctx* c, WaveParams P, uint64_t h0, uint64_t h1, bool plan) {
         }
         c->waves += K;
         c->wave_launches += K;
-        c->kernel_launches += (P.split ? 4 : 3) * (uint64_t) K;   // per wave: top-up, load, wave(, post-step)
+        // per wave: top-up, load, wave (+ post-step when split, + 4 sort kernels when sorting is on)
+        c->kernel_launches += (3 + (P.split ? 1 : 0) + (P.sort_bins ? 4 : 0)) * (uint64_t) K;
         float ms = 0.0f;
         if (cudaEventElapsedTime(&ms, c->ev0, c->ev1) == cudaSuccess) c->wave_ms += ms;
         if (c->host_counts[3] & 2u) {
@@ -703,6 +714,9 @@ run_transport(mqi_ctx* c, uint64_t h0, uint64_t h1, uint64_t seed, bool plan) {
         cudaError_t e = alloc_queue(c->qa, need);
         if (e == cudaSuccess) e = alloc_queue(c->qb, need);
         if (e == cudaSuccess) e = cudaMalloc(&c->def, (size_t) need * sizeof(Deferred));
+        if (e == cudaSuccess) e = alloc_queue(c->qsort, need);
+        if (e == cudaSuccess && !c->sort_bins) e = cudaMalloc(&c->sort_bins, 2 * kSortBins * sizeof(uint32_t));
+        if (e == cudaSuccess) e = cudaMemsetAsync(c->sort_bins, 0, 2 * kSortBins * sizeof(uint32_t), c->stream);
         if (e != cudaSuccess) {
             c->queue_cap = 0;
             return cuda_fail(c, e, "mqi_transport: queue allocation");
@@ -717,6 +731,11 @@ run_transport(mqi_ctx* c, uint64_t h0, uint64_t h1, uint64_t seed, bool plan) {
     // phantom example); runs below kSplitMinEntries queue entries keep them inside the wave.
     P.split = c->post_step_mode >= 0 ? c->post_step_mode
                                      : ((h1 - h0) * (uint64_t) c->n_scen >= kSplitMinEntries ? 1 : 0);
+    if (c->sort_min > 0) {
+        P.sort_tmp  = c->qsort.q;
+        P.sort_bins = c->sort_bins;
+        P.sort_min  = c->sort_min;
+    }
     MQI_CUDA(c, cudaMemsetAsync(c->counters + 3, 0, sizeof(uint32_t), c->stream), "mqi_transport");
     const int rc = c->streamed ? run_streamed(c, P, h0, h1, plan) : run_generations(c, P, h0, h1, plan);
     if (rc != MQI_OK) return rc;

@@ -128,6 +128,9 @@ struct mqi_ctx {
     mqi_gpu::QueueBuf       qa, qb;
     uint32_t                queue_cap = 0;
     mqi_gpu::Deferred*      def = nullptr;          // tracks a wave stopped at nuclear interactions (queue_cap)
+    mqi_gpu::QueueBuf       qsort;                  // scratch of the energy-bin queue sort (queue_cap)
+    uint32_t*               sort_bins = nullptr;    // 2 x kSortBins counters of the sort
+    uint32_t                sort_min = 1u << 18;    // sort waves of at least this many entries (0: never)
     uint32_t*               counters = nullptr;     // [0,1] queue sizes, [2] head, [3] error flag, [4] deferred
     unsigned long long*     stats = nullptr;        // 8 x u64
     uint32_t*               host_counts = nullptr;  // pinned: 4 x u32

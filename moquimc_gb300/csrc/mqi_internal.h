@@ -153,6 +153,9 @@ struct WaveParams {
     const uint32_t* spot_ids;   // per history (may be null)
     uint32_t*       error_flag; // device: 1 a bounded loop gave up, 2 queue overflow, 4 Dij table full
     int             split;      // 1: nuclear post-steps in the post-step kernel; 0: inside the wave
+    Queue           sort_tmp;   // queue-sized scratch of the energy-bin sort (sort_bins null: no sort)
+    uint32_t*       sort_bins;  // device: kSortBins counts (zero between sorts) then kSortBins cursors
+    uint32_t        sort_min;   // sort a wave's input only when it holds at least this many entries
     Deferred*       def;        // device: tracks stopped at a nuclear interaction (capacity in.capacity)
     uint32_t*       n_def;      // device: entries in def (zeroed before each wave)
     int             smem_edge_floats; // shared-memory floats for staged child edges
@@ -174,6 +177,10 @@ struct TopUp {
     uint32_t count;            // entries appended by the current top-up
     uint32_t dst;              // first appended entry
 };
+
+/// Classes of the queue sort: 1 MeV energy bins, the last one open (tracks above 319 MeV), and
+/// one more class for primaries that have not taken a step yet.
+constexpr int kSortBins = 321;
 
 /// Record the calling thread's last error message (returned by mqi_last_error(NULL)).
 void set_thread_error(const char* msg);

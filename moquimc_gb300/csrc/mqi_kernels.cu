@@ -1324,6 +1324,104 @@ launch_variant(const WaveParams& p, int grid, cudaStream_t s) {
     return cudaGetLastError();
 }
 
+// ------------------------------------------------------------------------------------------
+// The queue sorted by energy bin before a wave: a counting sort on 1 MeV bins of the entries'
+// kinetic energy, highest first, through a queue-sized scratch and back.  Primaries that have not
+// taken a step yet form a class of their own, placed after the sorted tracks: they arrive grouped
+// (one spot's histories, one energy, neighbouring voxels) and keep that grouping, which
+// interleaving them with other spots of the same energy would break.  Protons are the only
+// transported particle type (moqui stacks only protons), so the type key is constant.  Each
+// kernel reads the entry count on the device and returns at once below sort_min, so the sort can
+// sit in a captured graph.  A warp claims one range per distinct class (one atomic each), so
+// entries of one class keep their order within a warp.
+// ------------------------------------------------------------------------------------------
+constexpr int kFreshPrimaryClass = kSortBins - 1;
+
+__device__ inline int
+sort_class(const Queue& q, uint32_t i) {
+    if ((q.meta[i] & kMetaPrimary) && q.ctr[i] == 0u) return kFreshPrimaryClass;
+    const int b = (int) q.ke[i];
+    return b < 0 ? 0 : (b >= kFreshPrimaryClass ? kFreshPrimaryClass - 1 : b);
+}
+
+__global__ void
+k_sort_count(Queue q, const uint32_t* __restrict__ n_in, uint32_t sort_min, uint32_t* __restrict__ bins) {
+    __shared__ uint32_t h[kSortBins];
+    const uint32_t n = min(*n_in, q.capacity);
+    if (n < sort_min) return;
+    for (int i = threadIdx.x; i < kSortBins; i += blockDim.x) h[i] = 0;
+    __syncthreads();
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        atomicAdd(&h[sort_class(q, i)], 1u);
+    __syncthreads();
+    for (int i = threadIdx.x; i < kSortBins; i += blockDim.x)
+        if (h[i]) atomicAdd(&bins[i], h[i]);
+}
+
+/// Counts -> cursors (highest energy bin first, fresh primaries last), and the counts zeroed for
+/// the next sort.
+__global__ void
+k_sort_scan(const uint32_t* __restrict__ n_in, uint32_t capacity, uint32_t sort_min, uint32_t* __restrict__ bins) {
+    __shared__ uint32_t c[kSortBins];
+    if (min(*n_in, capacity) < sort_min) return;
+    for (int i = threadIdx.x; i < kSortBins; i += blockDim.x) {
+        c[i]    = bins[i];
+        bins[i] = 0;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t acc = 0;
+        for (int i = kFreshPrimaryClass - 1; i >= 0; --i) {
+            bins[kSortBins + i] = acc;
+            acc += c[i];
+        }
+        bins[kSortBins + kFreshPrimaryClass] = acc;
+    }
+}
+
+__device__ inline void
+copy_entry(const Queue& from, uint32_t i, const Queue& to, uint32_t j) {
+    to.ke[j] = from.ke[i]; to.px[j] = from.px[i]; to.py[j] = from.py[i]; to.pz[j] = from.pz[i];
+    to.dx[j] = from.dx[i]; to.dy[j] = from.dy[i]; to.dz[j] = from.dz[i]; to.dE0[j] = from.dE0[i];
+    to.hist[j] = from.hist[i]; to.uid_lo[j] = from.uid_lo[i]; to.uid_hi[j] = from.uid_hi[i];
+    to.ctr[j] = from.ctr[i]; to.meta[j] = from.meta[i]; to.cell[j] = from.cell[i]; to.spot[j] = from.spot[i];
+}
+
+__global__ void
+k_sort_scatter(Queue q, Queue t, const uint32_t* __restrict__ n_in, uint32_t sort_min, uint32_t* __restrict__ bins) {
+    const uint32_t n = min(*n_in, q.capacity);
+    if (n < sort_min) return;
+    const int lane = threadIdx.x & 31;
+    // the loop bound is the same for every thread of a block, so whole warps take each iteration
+    for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += gridDim.x * blockDim.x) {
+        const uint32_t i     = base + threadIdx.x;
+        const bool     valid = i < n;
+        const int      b     = valid ? sort_class(q, i) : -1;
+        const unsigned peers = __match_any_sync(0xFFFFFFFFu, b);
+        const int      lead  = __ffs(peers) - 1;
+        uint32_t       pos   = 0;
+        if (valid && lane == lead) pos = atomicAdd(&bins[kSortBins + b], (uint32_t) __popc(peers));
+        pos = __shfl_sync(0xFFFFFFFFu, pos, lead);
+        if (valid) copy_entry(q, i, t, pos + (uint32_t) __popc(peers & ((1u << lane) - 1u)));
+    }
+}
+
+__global__ void
+k_sort_copy_back(Queue q, Queue t, const uint32_t* __restrict__ n_in, uint32_t sort_min) {
+    const uint32_t n = min(*n_in, q.capacity);
+    if (n < sort_min) return;
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) copy_entry(t, j, q, j);
+}
+
+static cudaError_t
+launch_sort(const WaveParams& p, int grid, cudaStream_t s) {
+    k_sort_count<<<grid, 256, 0, s>>>(p.in, p.n_in, p.sort_min, p.sort_bins);
+    k_sort_scan<<<1, 256, 0, s>>>(p.n_in, p.in.capacity, p.sort_min, p.sort_bins);
+    k_sort_scatter<<<grid, 256, 0, s>>>(p.in, p.sort_tmp, p.n_in, p.sort_min, p.sort_bins);
+    k_sort_copy_back<<<grid, 256, 0, s>>>(p.in, p.sort_tmp, p.n_in, p.sort_min);
+    return cudaGetLastError();
+}
+
 /// Instances: the split form in every launch shape and scoring mode; the inline form in the two
 /// leading shapes of the common modes (one dose-like scorer, DIRECT ROIs) and in 128 x 5 for the
 /// FP64 callbacks (dose to medium, LET).  A request for an inline instance that is not compiled
@@ -1331,6 +1429,10 @@ launch_variant(const WaveParams& p, int grid, cudaStream_t s) {
 cudaError_t
 launch_wave(const WaveParams& p, int grid, int block, int blocks_per_sm, cudaStream_t s) {
     const int grid5 = grid / (blocks_per_sm > 0 ? blocks_per_sm : 1) * 5;
+    if (p.sort_bins) {
+        const cudaError_t e = launch_sort(p, grid5, s);
+        if (e != cudaSuccess) return e;
+    }
     if (!p.split && (p.kernel_mode == 0 || p.kernel_mode == kModeSingle)) {
         const bool wide = block != 128;
         if (p.kernel_mode == kModeSingle)

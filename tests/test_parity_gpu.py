@@ -307,27 +307,29 @@ def test_slicing_and_launch_shape_do_not_change_results(gpu_ctx_factory):
 
 
 @pytest.mark.parametrize("wname,dbg", [("c1", True), ("c2", False)])
-def test_post_step_modes_give_the_same_tracks(gpu_ctx_factory, wname, dbg):
-    """Nuclear post-steps inside the wave (mode 0) or in the post-step kernel (mode 1) run the same
-    tracks on the same random numbers: identical step counts and tallies to FP64 summation order,
-    in both physics builds; the automatic mode follows the run size."""
+def test_post_step_modes_and_queue_sort_give_the_same_tracks(gpu_ctx_factory, wname, dbg):
+    """Nuclear post-steps inside the wave (mode 0) or in the post-step kernel (mode 1), with the
+    queue sorted by energy bin before every wave or never, run the same tracks on the same random
+    numbers: identical step counts and tallies to FP64 summation order, in both physics builds."""
     wl = workloads.WORKLOADS[wname]()
     wl.physics_debug = dbg
     n = 20_000
     v = wl.vertices(n, 21)
     res = []
-    for mode in (0, 1):
+    for mode, sort_min in ((0, 0), (1, 0), (1, 1), (0, 1)):
         c, cid, sid = _ctx_for(wl, gpu_ctx_factory)
         c.set_post_step_mode(mode)
+        c.set_queue_sort(sort_min)
         c.set_launch_mode(streamed=0)          # queue generations: the wave count is the waves run
         c.set_vertices(v)
         c.transport(0, n, 77)
         res.append((c.tally(sid), c.stats()))
-    (d0, st0), (d1, st1) = res
-    np.testing.assert_allclose(d1, d0, rtol=1e-9, atol=1e-300)
-    for k in ("steps", "histories", "secondaries", "local_daughters", "dropped"):
-        assert st1[k] == st0[k], k
-    assert st1["waves"] > st0["waves"]   # each nuclear interaction ends its track's wave
+    d0, st0 = res[0]
+    for d1, st1 in res[1:]:
+        np.testing.assert_allclose(d1, d0, rtol=1e-9, atol=1e-300)
+        for k in ("steps", "histories", "secondaries", "local_daughters", "dropped"):
+            assert st1[k] == st0[k], k
+    assert res[1][1]["waves"] > st0["waves"]   # each nuclear interaction ends its track's wave
 
 
 def test_slicing_on_a_deep_grid(gpu_ctx_factory):
