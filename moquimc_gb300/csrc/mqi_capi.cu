@@ -545,6 +545,17 @@ make_wave_params(mqi_ctx* c, uint64_t seed, WaveParams& P) {
         if (!s0.stat_mode && s0.tstride == 1 && (s0.type == MQI_SCORER_EDEP || s0.type == MQI_SCORER_DOSE_W))
             P.kernel_mode = kModeSingle;
     }
+    if (P.kernel_mode == 0 && c->scorers.size() == 3) {
+        // a dose scorer followed by the statistics pair, all DIRECT, on one child
+        const ScorerHost& a = c->scorers[0];
+        const ScorerHost& b = c->scorers[1];
+        const ScorerHost& d = c->scorers[2];
+        if (a.type == MQI_SCORER_DOSE_W && !a.stat_mode && a.tstride == 1 && a.roi_method == MQI_ROI_DIRECT &&
+            b.type == MQI_SCORER_DOSE_W && b.stat_mode && b.tstride == 2 && b.roi_method == MQI_ROI_DIRECT &&
+            d.type == MQI_SCORER_DOSE_W2 && d.stat_mode && d.tally == b.tally + 1 && a.child == b.child &&
+            b.child == d.child && a.tally_len == b.tally_len)
+            P.kernel_mode = kModeStat;
+    }
     P.physics_debug   = c->physics_debug;
     P.score_local     = c->score_local;
     P.stack_limit     = c->physics_debug ? 200 : 10;

@@ -44,6 +44,9 @@ constexpr int kModeRoi  = 4;   // INDIRECT or CONTOUR ROI mappings
 constexpr int kModeAll  = kModeDij | kModeFull | kModeRoi;
 constexpr int kModeSingle = 8; // exactly one energy-deposit or dose-to-water scorer, DIRECT ROI,
                                // one child, no statistics pair, no scenarios (the phantom example)
+constexpr int kModeStat = 16;  // one dose-to-water scorer and the statistics pair, DIRECT ROIs, on one
+                               // child (any number of children and scenarios): tps_env's Dose with
+                               // StoppingStatistics
 
 /// Flat device description of one scorer (scorer<R> + roi_t, mqi_scorer.hpp:39-79,
 /// mqi_roi.hpp:18-194).

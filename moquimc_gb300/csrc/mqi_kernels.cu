@@ -333,6 +333,24 @@ score_step(Ctx& C, const Trk& t, uint32_t cnb, float rho, float vol) {
         tally_add(s.tally, cnb, (double) vf, cnb > 0 && vf > 0.0f);
         return;
     }
+    if constexpr (kMode == kModeStat) {
+        // dose_to_water, then the statistics pair of the same value (dose and dose^2 side by side):
+        // the generic loop's per-scorer dispatch and addressing fold away
+        const ChildDev& ch = C.P->child[C.child];
+        if (ch.n_scorers == 0) return;
+        const ScorerDev& sd  = C.P->scorer[ch.scorer_begin];
+        const ScorerDev& sp  = C.P->scorer[ch.scorer_begin + 1];
+        const float      spr = t.spr0 >= 0.0f ? t.spr0 : spr_of(C.P->calib, rho, t.ke0, C.dbg);
+        const float dose_w = (rho < 1.0e-7f) ? 0.0f : (t.dE + t.ldE) * 1.60218e-10f / (vol * rho * spr);
+        if (!(dose_w > 0.0f)) return;
+        const double   v  = (double) dose_w;
+        const uint64_t sc = (uint64_t) (C.spot >> kScenShift);
+        tally_add(sd.tally, sc * sd.tally_len + cnb, v, cnb > 0);   // DIRECT: idx(cnb) = cnb > 0
+        double* pair = sp.tally + (sc * sp.tally_len + cnb) * 2;    // DIRECT: get_mask_idx(cnb) = cnb
+        atomicAdd(pair, v);
+        atomicAdd(pair + 1, v * v);
+        return;
+    }
     const WaveParams& P   = *C.P;
     const ChildDev&   ch  = P.child[C.child];
     const float       spr = t.spr0 >= 0.0f ? t.spr0 : spr_of(P.calib, rho, t.ke0, C.dbg);
@@ -1422,10 +1440,13 @@ launch_sort(const WaveParams& p, int grid, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-/// Instances: the split form in every launch shape and scoring mode; the inline form in the two
-/// leading shapes of the common modes (one dose-like scorer, DIRECT ROIs) and in 128 x 5 for the
-/// FP64 callbacks (dose to medium, LET).  A request for an inline instance that is not compiled
-/// runs the split one (the results are the same) when the caller gave a record array.
+/// Instances: the split form in every launch shape of the common modes and in 128 x 5 for the
+/// others; the inline form in the two leading shapes of the common modes (one dose-like scorer,
+/// DIRECT ROIs) and in 128 x 5 for the FP64 callbacks (dose to medium, LET) and for Dij runs with
+/// DIRECT ROIs (tps_env's Dij runs are one spot per call: small runs) and for the dose scorer with the
+/// statistics pair (per-spot runs with statistical stopping).  A request for an inline
+/// instance that is not compiled runs the split one (the results are the same) when the caller
+/// gave a record array.
 cudaError_t
 launch_wave(const WaveParams& p, int grid, int block, int blocks_per_sm, cudaStream_t s) {
     const int grid5 = grid / (blocks_per_sm > 0 ? blocks_per_sm : 1) * 5;
@@ -1441,6 +1462,9 @@ launch_wave(const WaveParams& p, int grid, int block, int blocks_per_sm, cudaStr
         return wide ? launch_variant<256, 2, 0, false>(p, grid, s) : launch_variant<128, 5, 0, false>(p, grid5, s);
     }
     if (!p.split && p.kernel_mode == kModeFull) return launch_variant<128, 5, kModeFull, false>(p, grid5, s);
+    if (!p.split && p.kernel_mode == kModeDij) return launch_variant<128, 5, kModeDij, false>(p, grid5, s);
+    if (!p.split && p.kernel_mode == kModeStat) return launch_variant<128, 5, kModeStat, false>(p, grid5, s);
+    if (p.kernel_mode == kModeStat && p.def && p.n_def) return launch_variant<128, 5, kModeStat, true>(p, grid5, s);
     if (!p.def || !p.n_def) return cudaErrorInvalidValue;   // the split form needs its record array
     switch (p.kernel_mode) {
     case 0: break;
@@ -1453,6 +1477,7 @@ launch_wave(const WaveParams& p, int grid, int block, int blocks_per_sm, cudaStr
         return launch_variant<256, 2, kModeSingle, true>(p, grid, s);
     case kModeFull: return launch_variant<128, 5, kModeFull, true>(p, grid5, s);
     case kModeRoi: return launch_variant<128, 5, kModeRoi, true>(p, grid5, s);
+    case kModeDij: return launch_variant<128, 5, kModeDij, true>(p, grid5, s);   // Dij (+ dose-like), DIRECT ROIs
     case kModeFull | kModeRoi: return launch_variant<128, 5, kModeFull | kModeRoi, true>(p, grid5, s);
     default: return launch_variant<128, 5, kModeAll, true>(p, grid5, s);   // any mode with Dij
     }

@@ -496,6 +496,15 @@ def test_scorer_plugins_match_the_oracle(oracle, gpu_ctx_factory, stype):
                                per_history=True)
     assert o.sum() > 0
     rel = np.abs(g - o) / np.maximum(np.abs(o), 1e-30)
-    assert (rel <= 1e-4).mean() >= 0.8, ((rel <= 1e-4).mean(), np.flatnonzero(rel > 1e-4)[:10])
-    assert (rel <= 5e-2).mean() >= 0.97, np.sort(rel)[-6:]
+    # a flip that moves a deposit between voxels leaves an energy sum alone, changes the scorers
+    # that depend on the voxel or the step a little, and the squared or LET-cut ones most
+    if stype in (capi.EDEP, capi.EDEP_PRIMARY, capi.EDEP_SECONDARY):
+        share = 0.99
+    elif stype in (capi.DOSE_W2, capi.LETD_NUM):
+        share = 0.8
+    else:
+        share = 0.95
+    print(f"scorer {int(stype)}: {(rel <= 1e-4).mean():.3f} of histories within 1e-4, {(rel <= 5e-2).mean():.3f} within 5e-2")
+    assert (rel <= 1e-4).mean() >= share, ((rel <= 1e-4).mean(), np.flatnonzero(rel > 1e-4)[:10])
+    assert (rel <= 5e-2).mean() >= 0.99, np.sort(rel)[-6:]
     assert abs(g.sum() - o.sum()) <= 1e-2 * abs(o.sum())

@@ -50,6 +50,31 @@ def test_reference_estimator_matches_numpy(gpu_ctx_factory):
     assert plain[0] == 0.0
 
 
+@pytest.mark.parametrize("mode", [0, 1])
+def test_dose_and_stat_pair_mode_matches_the_generic_scoring(gpu_ctx_factory, mode):
+    """A dose scorer followed by the statistics pair runs a kernel instance of its own (the generic
+    per-scorer loop folded away); with a fourth scorer added the same run takes the generic loop.
+    The dose, dose and dose^2 tallies agree to FP64 summation order, inline and split."""
+    wl = workloads.c2()
+    n = 30_000
+    v = wl.vertices(n, 31)
+    out = []
+    for extra in (False, True):
+        c, cid = _ctx(wl, gpu_ctx_factory)
+        c.set_post_step_mode(mode)
+        dose = c.add_scorer(cid, capi.DOSE_W)
+        d1, d2 = c.add_stat_scorers(cid)
+        if extra:
+            c.add_scorer(cid, capi.EDEP)
+        c.set_vertices(v)
+        c.transport(0, n, 1234)
+        out.append((c.tally(dose), c.tally(d1), c.tally(d2), c.stats()["steps"]))
+    for a, b in zip(out[0][:3], out[1][:3]):
+        assert a.sum() > 0
+        np.testing.assert_allclose(a, b, rtol=1e-9, atol=1e-300)
+    assert out[0][3] == out[1][3]
+
+
 def test_estimate_falls_like_one_over_sqrt_n(gpu_ctx_factory):
     wl = workloads.c2()
     c, cid = _ctx(wl, gpu_ctx_factory)
