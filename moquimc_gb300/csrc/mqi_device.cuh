@@ -373,6 +373,18 @@ index_axis(const float* e, int n, float p, float dir) {
     return -1;
 }
 
+/// index_axis when p may lie in interval k: if p is strictly inside [e[k], e[k+1]] and at least the
+/// tolerance away from both edges, index_axis returns k (the bisection lands on k and neither edge
+/// ties), so k is returned without the search; otherwise the search runs.
+__device__ inline int
+index_axis_hint(const float* e, int n, float p, float dir, int k) {
+    if (k >= 0 && k < n) {
+        const float a = fsub(e[k], p), b = fsub(e[k + 1], p);
+        if (a < 0.0f && b > 0.0f && fabsf(a) >= kGeoTol && fabsf(b) >= kGeoTol) return k;
+    }
+    return index_axis(e, n, p, dir);
+}
+
 __device__ inline int3
 grid_index(const Grid& g, float3 p, float3 d) {
     return make_int3(index_axis(g.xe, g.nx, p.x, d.x), index_axis(g.ye, g.ny, p.y, d.y),

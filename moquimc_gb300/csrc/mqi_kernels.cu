@@ -432,12 +432,20 @@ to_world(const Grid& g, float3& p, float3& d) {
 
 /// track_t::update_post_vertex_position with the last_step length
 /// (p_ionization_tabulated::last_step, mqi_p_ionization.hpp:481-490).
-__device__ __noinline__ float3
-last_step_pos(const Tables* T, const CalibDev* cal, bool dbg, float3 p0, float3 d0, float ke0, float dE, float rho) {
+/// The last-step position with the stopping-power ratio at (rho, ke0) given.
+__device__ inline float3
+last_step_pos_spr(const Tables* T, float3 p0, float3 d0, float ke0, float dE, float rho, float spr) {
     float lw = 0.0f;
     if (dE > 0.0f) lw = -dE / dedx_lookup(*T, ke0);
-    const float sl = lw * kWaterDensity / (spr_of(*cal, rho, ke0, dbg) * rho);
+    const float sl = lw * kWaterDensity / (spr * rho);
     return make_float3(p0.x + d0.x * sl, p0.y + d0.y * sl, p0.z + d0.z * sl);
+}
+
+/// The same, out of line and with the ratio computed here (the step loop's cut branch, which ends
+/// each track once).
+__device__ __noinline__ float3
+last_step_pos(const Tables* T, const CalibDev* cal, bool dbg, float3 p0, float3 d0, float ke0, float dE, float rho) {
+    return last_step_pos_spr(T, p0, d0, ke0, dE, rho, spr_of(*cal, rho, ke0, dbg));
 }
 
 /// What the reference does when it pops a deposit-only daughter (kinetic energy at or below
@@ -445,11 +453,17 @@ last_step_pos(const Tables* T, const CalibDev* cal, bool dbg, float3 p0, float3 
 /// cut branch (mqi_fippel_physics.hpp:86-94) and score once.  Returns false when the daughter
 /// needs the general path (outside the grid or in a vacuum voxel).
 __device__ inline bool
-score_local_daughter(Ctx& C, float3 pw, float3 dw, float ke0, float dE0) {
+score_local_daughter(Ctx& C, float3 pw, float3 dw, float ke0, float dE0, uint32_t hint_cnb) {
     float3 p = pw, d = dw;
     to_child(C.g, p, d);
     Trk t;
-    t.cell = grid_index(C.g, p, d);
+    const uint32_t nxy  = (uint32_t) C.g.nx * (uint32_t) C.g.ny;
+    const int3     hint = make_int3((int) (hint_cnb % nxy % (uint32_t) C.g.nx), (int) (hint_cnb % nxy / (uint32_t) C.g.nx),
+                                    (int) (hint_cnb / nxy));
+    // the daughter sits where its parent's step started, nearly always well inside the parent's
+    // voxel: grid3d::index's answer is then that voxel, and the three edge searches are skipped
+    t.cell = make_int3(index_axis_hint(C.g.xe, C.g.nx, p.x, d.x, hint.x), index_axis_hint(C.g.ye, C.g.ny, p.y, d.y, hint.y),
+                       index_axis_hint(C.g.ze, C.g.nz, p.z, d.z, hint.z));
     if (!grid_valid(C.g, t.cell)) return false;
     const uint32_t cnb = grid_cnb(C.g, t.cell);
     const float    rho = voxel_rho(C.g, cnb);
@@ -463,7 +477,8 @@ score_local_daughter(Ctx& C, float3 pw, float3 dw, float ke0, float dE0) {
     t.primary = false;
     if (rho <= 99.9f) {
         t.dE += t.ke0;
-        t.p1 = last_step_pos(C.T, &C.P->calib, C.dbg, p, d, t.ke0, t.dE, rho);
+        t.spr0 = spr_of(C.P->calib, rho, t.ke0, C.dbg);   // computed once for the position and the score
+        t.p1   = last_step_pos_spr(C.T, p, d, t.ke0, t.dE, rho, t.spr0);
     }
     score_step(C, t, cnb, rho, grid_volume(C.g, t.cell));
     return true;
@@ -475,7 +490,7 @@ score_local_daughter(Ctx& C, float3 pw, float3 dw, float ke0, float dE0) {
 /// body would otherwise be inlined at every push site of the four processes.
 /// Returns 0 queued, 1 scored locally, 2 queue overflow.
 static __device__ __noinline__ int
-emit_daughter(const WaveParams* P, const Tables* T, int child, const float* xe, const float* ye, const float* ze,
+emit_daughter(const WaveParams* P, const Tables* T, int child, uint32_t hint, const float* xe, const float* ye, const float* ze,
               bool dbg, uint32_t below, uint64_t uid, uint32_t hist, uint32_t spot, float ke0, bool ke1_zero, float3 p,
               float3 d, float dE0) {
     Ctx C;
@@ -484,7 +499,7 @@ emit_daughter(const WaveParams* P, const Tables* T, int child, const float* xe, 
     apply_scenario(*P, C.g, child, spot);
     C.n_sec = C.n_local = C.n_drop = C.n_err = 0;
     daughter_to_world(C.g, p, d);
-    if (P->inline_local && ke0 <= kTpCut && score_local_daughter(C, p, d, ke0, dE0)) return 1;
+    if (P->inline_local && ke0 <= kTpCut && score_local_daughter(C, p, d, ke0, dE0, hint)) return 1;
     const Queue&   q = P->out;
     const uint32_t i = atomicAdd(P->n_out, 1u);
     if (i >= q.capacity) {
@@ -517,7 +532,8 @@ push_daughter(Ctx& C, Trk& t, float ke0, bool ke1_zero, float3 p, float3 d, floa
     const uint32_t below = t.below + t.npush;
     const uint64_t uid   = daughter_uid(t.uid, t.npush);
     ++t.npush;
-    const int r = emit_daughter(C.P, C.T, C.child, C.g.xe, C.g.ye, C.g.ze, C.dbg, below, uid, t.hist, t.spot, ke0, ke1_zero,
+    const int r = emit_daughter(C.P, C.T, C.child, grid_cnb(C.g, t.cell), C.g.xe, C.g.ye, C.g.ze, C.dbg, below, uid, t.hist,
+                                t.spot, ke0, ke1_zero,
                                 p, d, dE0);
     if (r == 0) ++C.n_sec;
     else if (r == 1) ++C.n_local;
