@@ -452,6 +452,7 @@ last_step_pos(const Tables* T, const CalibDev* cal, bool dbg, float3 p0, float3 
 /// the 0.5 MeV tracking cut) in a single-child world: enter the grid, take the stepping()
 /// cut branch (mqi_fippel_physics.hpp:86-94) and score once.  Returns false when the daughter
 /// needs the general path (outside the grid or in a vacuum voxel).
+template<int kMode>
 __device__ inline bool
 score_local_daughter(Ctx& C, float3 pw, float3 dw, float ke0, float dE0, uint32_t hint_cnb) {
     float3 p = pw, d = dw;
@@ -480,7 +481,7 @@ score_local_daughter(Ctx& C, float3 pw, float3 dw, float ke0, float dE0, uint32_
         t.spr0 = spr_of(C.P->calib, rho, t.ke0, C.dbg);   // computed once for the position and the score
         t.p1   = last_step_pos_spr(C.T, p, d, t.ke0, t.dE, rho, t.spr0);
     }
-    score_step(C, t, cnb, rho, grid_volume(C.g, t.cell));
+    score_step<kMode>(C, t, cnb, rho, grid_volume(C.g, t.cell));
     return true;
 }
 
@@ -489,6 +490,7 @@ score_local_daughter(Ctx& C, float3 pw, float3 dw, float ke0, float dE0, uint32_
 /// the next queue.  Out of line and by value: it runs on a few percent of the steps and its
 /// body would otherwise be inlined at every push site of the four processes.
 /// Returns 0 queued, 1 scored locally, 2 queue overflow.
+template<int kMode>
 static __device__ __noinline__ int
 emit_daughter(const WaveParams* P, const Tables* T, int child, uint32_t hint, const float* xe, const float* ye, const float* ze,
               bool dbg, uint32_t below, uint64_t uid, uint32_t hist, uint32_t spot, float ke0, bool ke1_zero, float3 p,
@@ -499,7 +501,7 @@ emit_daughter(const WaveParams* P, const Tables* T, int child, uint32_t hint, co
     apply_scenario(*P, C.g, child, spot);
     C.n_sec = C.n_local = C.n_drop = C.n_err = 0;
     daughter_to_world(C.g, p, d);
-    if (P->inline_local && ke0 <= kTpCut && score_local_daughter(C, p, d, ke0, dE0, hint)) return 1;
+    if (P->inline_local && ke0 <= kTpCut && score_local_daughter<kMode>(C, p, d, ke0, dE0, hint)) return 1;
     const Queue&   q = P->out;
     const uint32_t i = atomicAdd(P->n_out, 1u);
     if (i >= q.capacity) {
@@ -523,6 +525,7 @@ emit_daughter(const WaveParams* P, const Tables* T, int child, uint32_t hint, co
 /// track_stack_t::push_secondary (mqi_track_stack.hpp:36-41) with the stack depth emulated:
 /// a track popped with `below` entries under it pushes its i-th daughter at depth below + i,
 /// and the push is dropped when that reaches the limit (200 with debug physics, else 10).
+template<int kMode>
 __device__ inline void
 push_daughter(Ctx& C, Trk& t, float ke0, bool ke1_zero, float3 p, float3 d, float dE0) {
     if (t.below + t.npush >= (uint32_t) C.P->stack_limit) {
@@ -532,7 +535,7 @@ push_daughter(Ctx& C, Trk& t, float ke0, bool ke1_zero, float3 p, float3 d, floa
     const uint32_t below = t.below + t.npush;
     const uint64_t uid   = daughter_uid(t.uid, t.npush);
     ++t.npush;
-    const int r = emit_daughter(C.P, C.T, C.child, grid_cnb(C.g, t.cell), C.g.xe, C.g.ye, C.g.ze, C.dbg, below, uid, t.hist,
+    const int r = emit_daughter<kMode>(C.P, C.T, C.child, grid_cnb(C.g, t.cell), C.g.xe, C.g.ye, C.g.ze, C.dbg, below, uid, t.hist,
                                 t.spot, ke0, ke1_zero,
                                 p, d, dE0);
     if (r == 0) ++C.n_sec;
@@ -598,6 +601,7 @@ along_step(Ctx& C, Trk& t, const Rel& rel, float len, float rho, float spr, floa
 }
 
 /// Delta-ray production (p_ionization_tabulated::post_step, mqi_p_ionization.hpp:425-477).
+template<int kMode>
 __device__ inline void
 post_delta(Ctx& C, Trk& t, Rng& rng) {
     const Rel rel(t.ke1);
@@ -612,12 +616,13 @@ post_delta(Ctx& C, Trk& t, Rng& rng) {
             break;
         }
     }
-    if (C.dbg) push_daughter(C, t, 0.0f, true, t.p0, t.d0, Te);
+    if (C.dbg) push_daughter<kMode>(C, t, 0.0f, true, t.p0, t.d0, Te);
     else t.dE += Te;
     t.ke1 -= Te;
 }
 
 /// p-p elastic (pp_elastic_tabulated::post_step, mqi_pp_elastic.hpp:119-219).
+template<int kMode>
 __device__ inline void
 post_pp(Ctx& C, Trk& t, Rng& rng) {
     const Rel   rel(t.ke1);
@@ -643,19 +648,20 @@ post_pp(Ctx& C, Trk& t, Rng& rng) {
     t.ke1 -= dE;
     t.d1 = rotate_dir(t.d1, th3, phi);
     const float3 dd = rotate_dir(t.d1, th4, phi);
-    push_daughter(C, t, dE, false, t.p1, dd, 0.0f);
+    push_daughter<kMode>(C, t, dE, false, t.p1, dd, 0.0f);
 }
 
 /// p-O elastic (po_elastic::post_step, mqi_po_elastic.hpp:96-217).  The energy given to the
 /// oxygen is a truncated exponential of mean Tp_avg on [0, Tp_max]; it is drawn by inverting
 /// its CDF, which has the same law as the reference's redraw-until-below-Tp_max loop
 /// (mqi_math.hpp:298-307) without the loop.
+template<int kMode>
 __device__ inline void
 post_poe(Ctx& C, Trk& t, Rng& rng) {
     const Rel rel(t.ke1);
     if (rel.Ek <= 5.5f) {
         const float dE = rel.Ek;
-        if (C.dbg) push_daughter(C, t, dE, true, t.p1, t.d1, dE);
+        if (C.dbg) push_daughter<kMode>(C, t, dE, true, t.p1, t.d1, dE);
         else t.ldE += dE;
         t.ke1 -= dE;
         t.stopped = true;
@@ -675,13 +681,14 @@ post_poe(Ctx& C, Trk& t, Rng& rng) {
     c3              = fminf(fmaxf(c3, -1.0f), 1.0f);
     const float th3 = acosf(c3);
     const float phi = 2.0f * kPi * rng.uniform();
-    if (C.dbg) push_daughter(C, t, dE, true, t.p0, t.d0, dE);
+    if (C.dbg) push_daughter<kMode>(C, t, dE, true, t.p0, t.d0, dE);
     else t.ldE += dE;
     t.ke1 -= dE;
     t.d1 = rotate_dir(t.d1, th3, phi);
 }
 
 /// p-O inelastic cascade (po_inelastic_tabulated::post_step, mqi_po_inelastic.hpp:158-288).
+template<int kMode>
 __device__ inline void
 post_poi(Ctx& C, Trk& t, Rng& rng) {
     const float Ek = t.ke1;
@@ -705,11 +712,11 @@ post_poi(Ctx& C, Trk& t, Rng& rng) {
             const float th  = acosf(c);
             const float phi = 2.0f * kPi * rng.uniform();
             const float3 dd = rotate_dir(t.d1, th, phi);
-            push_daughter(C, t, dE, false, t.p1, dd, 0.0f);
+            push_daughter<kMode>(C, t, dE, false, t.p1, dd, 0.0f);
         } else if (zeta < PL) {
             // long-range energy (neutrons, photons) leaves the system
         } else if (C.dbg) {
-            push_daughter(C, t, dE, true, t.p0, t.d0, dE);
+            push_daughter<kMode>(C, t, dE, true, t.p0, t.d0, dE);
         }
         Eb *= 0.65f;
     }
@@ -727,15 +734,16 @@ struct PostState {
     uint32_t n_sec, n_local, n_drop, n_err;
 };
 
+template<int kMode>
 __device__ __forceinline__ PostState
 post_nuclear(const WaveParams* P, const Tables* T, Grid g, int child, bool dbg, float tcut, int proc, PostState s) {
     Ctx C;
     C.P = P; C.T = T; C.g = g; C.child = child; C.dbg = dbg; C.tcut = tcut;
     C.spot = s.t.spot;
     C.n_sec = C.n_local = C.n_drop = C.n_err = 0;
-    if (proc == 1) post_pp(C, s.t, s.rng);
-    else if (proc == 2) post_poe(C, s.t, s.rng);
-    else post_poi(C, s.t, s.rng);
+    if (proc == 1) post_pp<kMode>(C, s.t, s.rng);
+    else if (proc == 2) post_poe<kMode>(C, s.t, s.rng);
+    else post_poi<kMode>(C, s.t, s.rng);
     s.n_sec = C.n_sec; s.n_local = C.n_local; s.n_drop = C.n_drop; s.n_err = C.n_err;
     return s;
 }
@@ -744,7 +752,7 @@ post_nuclear(const WaveParams* P, const Tables* T, Grid g, int child, bool dbg, 
 /// nuclear interaction (1 p-p elastic, 2 p-O elastic, 3 p-O inelastic) either runs here too
 /// (kSplit false) or ends the step early: stepping returns the process and the post-step kernel
 /// (k_post) finishes the step after the wave (kSplit true).
-template<bool kSplit>
+template<int kMode, bool kSplit>
 __device__ inline int
 stepping(Ctx& C, Trk& t, Rng& rng, float rho, float d2b) {
     t.spr0 = -1.0f;
@@ -807,7 +815,7 @@ stepping(Ctx& C, Trk& t, Rng& rng, float rho, float d2b) {
         t.d1          = t.d0;
         const int proc = (u < c0) ? 0 : (u < c0 + c1) ? 1 : (u < c0 + c1 + c2) ? 2 : (u < c0 + c1 + c2 + c3) ? 3 : -1;
         if (proc == 0) {
-            post_delta(C, t, rng);   // ~15% of the steps
+            post_delta<kMode>(C, t, rng);   // ~15% of the steps
         } else if (proc > 0) {       // ~0.2% of the steps
             if constexpr (kSplit) {
                 return proc;
@@ -815,7 +823,7 @@ stepping(Ctx& C, Trk& t, Rng& rng, float rho, float d2b) {
                 PostState ps;
                 ps.t   = t;
                 ps.rng = rng;
-                ps     = post_nuclear(C.P, C.T, C.g, C.child, C.dbg, C.tcut, proc, ps);
+                ps     = post_nuclear<kMode>(C.P, C.T, C.g, C.child, C.dbg, C.tcut, proc, ps);
                 t      = ps.t;
                 rng    = ps.rng;
                 C.n_sec += ps.n_sec;
@@ -1083,7 +1091,7 @@ wave_body(const WaveParams& P) {
         const uint32_t cnb = grid_cnb(C.g, t.cell);
         const float    rho = voxel_rho(C.g, cnb);
         const float    d2b = grid_exit(C.g, t.p0, t.d0, t.cell);
-        const int      nuclear = stepping<kSplit>(C, t, rng, rho, d2b);
+        const int      nuclear = stepping<kMode, kSplit>(C, t, rng, rho, d2b);
         ++n_steps;
         if (kSplit && nuclear) {   // the post-step kernel finishes this step and queues the track
             defer_track(C, t, rng, cnb, nuclear);
@@ -1194,9 +1202,9 @@ post_body(const WaveParams& P) {
         const uint32_t nxy = (uint32_t) C.g.nx * (uint32_t) C.g.ny;
         const uint32_t rem = d.cnb % nxy;
         t.cell = make_int3((int) (rem % (uint32_t) C.g.nx), (int) (rem / (uint32_t) C.g.nx), (int) (d.cnb / nxy));
-        if (d.proc == 1) post_pp(C, t, rng);
-        else if (d.proc == 2) post_poe(C, t, rng);
-        else post_poi(C, t, rng);
+        if (d.proc == 1) post_pp<kMode>(C, t, rng);
+        else if (d.proc == 2) post_poe<kMode>(C, t, rng);
+        else post_poi<kMode>(C, t, rng);
         score_step<kMode>(C, t, d.cnb, voxel_rho(C.g, d.cnb), grid_volume(C.g, t.cell));
         if (!t.stopped) {
             grid_step_index(C.g, t.p1, t.d1, t.cell);
