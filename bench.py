@@ -341,8 +341,11 @@ def dij_section(torch, capi, workloads, optimize, stride: int = 1) -> dict:
         torch.cuda.synchronize()
         times[name] = ev0.elapsed_time(ev1) / 10
     vr = c.dij_info(sid)["voxel_rows"]
+    # algorithmic bytes: what each product must move at least.  D.w: spot + value per entry, row
+    # voxel + indptr per voxel row, the dose zeroed and written.  D^T.g: voxel + value per entry,
+    # g read once per voxel that has an entry, the gradient and its FP64 partials per spot.
     fwd_bytes = op.nnz * 8 + vr * 12 + op.n_voxels * 8
-    bwd_bytes = op.nnz * 12 + op.n_spots * 16
+    bwd_bytes = op.nnz * 8 + vr * 4 + op.n_spots * 16
     hbm = measured_peaks()["hbm_gbs"]
     out = {
         "workload": "c3 Dij + c5 objective" + (f" (every {stride}th spot)" if stride > 1 else ""),
@@ -457,6 +460,8 @@ def run_gpu(args, wl):
     ctx.set_hu(cid, wl.hu)
     sid = ctx.add_scorer(cid, capi.DOSE_W)
     ctx.set_post_step_mode(args.post_step_mode)
+    if args.queue_sort >= 0:
+        ctx.set_queue_sort(args.queue_sort)
     from moquimc_gb300 import replicas
 
     vseed, seed_base = replicas.replica_seeds(rank)
@@ -626,6 +631,9 @@ def main():
     ap.add_argument("--max-passes", type=int, default=30, help="plan passes allowed for the 1%% criterion")
     ap.add_argument("--post-step-mode", type=int, default=-1, choices=(-1, 0, 1),
                     help="nuclear post-steps: -1 by run size, 0 inside the wave, 1 in the post-step kernel")
+    ap.add_argument("--queue-sort", type=int, default=-1,
+                    help="sort the queue by energy bin before waves of at least this many entries (0: never; "
+                         "-1: the library default)")
     ap.add_argument("--tune-histories", type=int, default=0,
                     help="tuner sample (0: the step's histories; -1: no tuning)")
     args = ap.parse_args()

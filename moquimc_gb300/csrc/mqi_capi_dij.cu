@@ -27,7 +27,8 @@ void
 free_csr(DijCsr& m) {
     cudaFree(m.s_indptr); cudaFree(m.s_voxel); cudaFree(m.s_value);
     cudaFree(m.v_row); cudaFree(m.v_indptr); cudaFree(m.v_spot); cudaFree(m.v_value);
-    cudaFree(m.seg_start); cudaFree(m.row_seg); cudaFree(m.partial); cudaFree(m.fwd_row_first);
+    cudaFree(m.seg_start); cudaFree(m.row_seg); cudaFree(m.seg_order); cudaFree(m.bwd_cursor);
+    cudaFree(m.partial); cudaFree(m.fwd_row_first); cudaFree(m.fwd_run_k);
     m = DijCsr{};
 }
 
@@ -253,7 +254,8 @@ mqi_dij_build(mqi_ctx* c, int id, uint32_t n_spots, double scale, uint64_t* nnz_
              "mqi_dij_build");
     MQI_CUDA(c, cudaStreamSynchronize(st), "mqi_dij_build");
     if (indptr[n_spots] != n) return fail(c, MQI_ERR_INVALID, "mqi_dij_build: the table holds a spot index >= n_spots");
-    // backward segments: each row cut into runs of at most kDijSegment entries
+    // backward segments: each row cut into runs of at most kDijSegment entries, and their work
+    // order: by the voxel of their first entry (the free sort buffers are reused below)
     {
         std::vector<uint64_t> seg;
         std::vector<uint32_t> row_seg(n_spots + 1);
@@ -266,11 +268,26 @@ mqi_dij_build(mqi_ctx* c, int id, uint32_t n_spots, double scale, uint64_t* nnz_
         seg.push_back(n);
         MQI_CUDA(c, sc.alloc(m.seg_start, seg.size()), "mqi_dij_build: allocation");
         MQI_CUDA(c, sc.alloc(m.row_seg, row_seg.size()), "mqi_dij_build: allocation");
+        MQI_CUDA(c, sc.alloc(m.seg_order, m.n_seg), "mqi_dij_build: allocation");
         MQI_CUDA(c, sc.alloc(m.partial, m.n_seg), "mqi_dij_build: allocation");
-        MQI_CUDA(c, cudaMemcpy(m.seg_start, seg.data(), seg.size() * sizeof(uint64_t), cudaMemcpyHostToDevice),
+        MQI_CUDA(c, sc.alloc(m.bwd_cursor, 1), "mqi_dij_build: allocation");
+        MQI_CUDA(c, cudaMemsetAsync(m.bwd_cursor, 0, sizeof(uint32_t), st), "mqi_dij_build");
+        MQI_CUDA(c, cudaMemcpyAsync(m.seg_start, seg.data(), seg.size() * sizeof(uint64_t), cudaMemcpyHostToDevice, st),
                  "mqi_dij_build");
-        MQI_CUDA(c, cudaMemcpy(m.row_seg, row_seg.data(), row_seg.size() * sizeof(uint32_t), cudaMemcpyHostToDevice),
-                 "mqi_dij_build");
+        MQI_CUDA(c, cudaMemcpyAsync(m.row_seg, row_seg.data(), row_seg.size() * sizeof(uint32_t), cudaMemcpyHostToDevice,
+                                    st), "mqi_dij_build");
+        if (m.n_seg) {
+            unsigned long long* okeys = (skeys == ka) ? kb : ka;
+            unsigned long long* okalt = kc;
+            uint32_t*           oval  = (sslot == ia) ? ib : ia;
+            uint32_t*           ovalt = ic;
+            MQI_CUDA(c, dij_seg_order_keys(m.seg_start, (uint32_t) m.n_seg, skeys, nvox, okeys, oval, st), "mqi_dij_build");
+            MQI_CUDA(c, radix_sort_pairs(okeys, oval, okalt, ovalt, m.n_seg, bit_length(nvox - 1), hist, offs, scan, st),
+                     "mqi_dij_build: sort");
+            MQI_CUDA(c, cudaMemcpyAsync(m.seg_order, oval, m.n_seg * sizeof(uint32_t), cudaMemcpyDeviceToDevice, st),
+                     "mqi_dij_build");
+        }
+        MQI_CUDA(c, cudaStreamSynchronize(st), "mqi_dij_build");   // the host vectors are copied from
     }
 
     // 3. spot-row entries, and (voxel, position) pairs for the voxel-row layout
@@ -300,11 +317,13 @@ mqi_dij_build(mqi_ctx* c, int id, uint32_t n_spots, double scale, uint64_t* nnz_
                                m.v_value, st), "mqi_dij_build");
     // 5. the forward blocks' first rows
     MQI_CUDA(c, sc.alloc(m.fwd_row_first, (n + kFwdEntries - 1) / kFwdEntries + 1), "mqi_dij_build: allocation");
-    MQI_CUDA(c, dij_forward_blocks(m.v_indptr, m.n_vrows, n, m.fwd_row_first, &m.n_fwd_blocks, st), "mqi_dij_build");
+    MQI_CUDA(c, sc.alloc(m.fwd_run_k, (n + kFwdEntries - 1) / kFwdEntries + 1), "mqi_dij_build: allocation");
+    MQI_CUDA(c, dij_forward_blocks(m.v_indptr, m.n_vrows, n, m.fwd_row_first, m.fwd_run_k, &m.n_fwd_blocks, st),
+             "mqi_dij_build");
     MQI_CUDA(c, cudaStreamSynchronize(st), "mqi_dij_build");
     for (void* p : { (void*) m.s_indptr, (void*) m.s_voxel, (void*) m.s_value, (void*) m.v_row, (void*) m.v_indptr,
-                     (void*) m.v_spot, (void*) m.v_value, (void*) m.seg_start, (void*) m.row_seg, (void*) m.partial,
-                     (void*) m.fwd_row_first })
+                     (void*) m.v_spot, (void*) m.v_value, (void*) m.seg_start, (void*) m.row_seg, (void*) m.seg_order,
+                     (void*) m.bwd_cursor, (void*) m.partial, (void*) m.fwd_row_first, (void*) m.fwd_run_k })
         sc.release(p);
     m.built = true;
     s.csr   = m;
@@ -363,8 +382,8 @@ mqi_dij_matvec(mqi_ctx* c, int id, const void* w, void* dose, int fp64, int on_d
         dd = td;
     }
     MQI_CUDA(c, cudaMemsetAsync(dd, 0, m.n_voxels * es, c->stream), "mqi_dij_matvec");
-    MQI_CUDA(c, dij_forward(m.v_row, m.v_indptr, m.fwd_row_first, m.n_fwd_blocks, m.v_spot, m.v_value, dw, dd, fp64,
-                            c->counters + 3, c->stream), "mqi_dij_matvec");
+    MQI_CUDA(c, dij_forward(m.v_row, m.v_indptr, m.fwd_row_first, m.fwd_run_k, m.n_fwd_blocks, m.v_spot, m.v_value,
+                            dw, dd, fp64, c->counters + 3, c->num_sms, c->stream), "mqi_dij_matvec");
     if (!on_device) {
         uint32_t flag = 0;
         MQI_CUDA(c, cudaMemcpyAsync(dose, dd, m.n_voxels * es, cudaMemcpyDeviceToHost, c->stream), "mqi_dij_matvec");
@@ -396,8 +415,8 @@ mqi_dij_rmatvec(mqi_ctx* c, int id, const void* gin, void* grad, int fp64, int o
         dg = tg;
         dr = tr;
     }
-    MQI_CUDA(c, dij_backward(m.seg_start, m.n_seg, m.row_seg, m.n_spots, m.s_voxel, m.s_value, m.partial, dg, dr, fp64,
-                             c->num_sms, c->stream), "mqi_dij_rmatvec");
+    MQI_CUDA(c, dij_backward(m.seg_order, m.seg_start, (uint32_t) m.n_seg, m.row_seg, m.n_spots, m.s_voxel, m.s_value,
+                             m.partial, m.bwd_cursor, dg, dr, fp64, c->num_sms, c->stream), "mqi_dij_rmatvec");
     if (!on_device) {
         MQI_CUDA(c, cudaMemcpyAsync(grad, dr, m.n_spots * es, cudaMemcpyDeviceToHost, c->stream), "mqi_dij_rmatvec");
         MQI_CUDA(c, cudaStreamSynchronize(c->stream), "mqi_dij_rmatvec");

@@ -48,9 +48,12 @@ struct DijCsr {
     uint64_t  n_seg = 0;            // backward segments: contiguous runs of one row's entries
     uint64_t* seg_start = nullptr;  // n_seg + 1
     uint32_t* row_seg = nullptr;    // n_spots + 1: first segment of each row
+    uint32_t* seg_order = nullptr;  // n_seg: segments by first voxel (the backward's work order)
+    uint32_t* bwd_cursor = nullptr; // the backward's work cursor (zero between calls)
     double*   partial = nullptr;    // n_seg
     uint64_t  n_fwd_blocks = 0;     // forward blocks: kFwdEntries entries' worth of voxel rows each
     uint32_t* fwd_row_first = nullptr;   // n_fwd_blocks + 1: first voxel row of each forward block
+    uint64_t* fwd_run_k = nullptr;       // n_fwd_blocks + 1: first entry of each forward block's rows
 };
 
 struct ScorerHost {

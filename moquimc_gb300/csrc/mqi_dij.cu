@@ -10,6 +10,7 @@
 //   voxel rows (only voxels with an entry, "doubly compressed"): row voxel / indptr / spot /
 //              value, spots ascending in a row -- read by D.w.
 // Both products are gathers with a fixed reduction order: no atomics, reproducible results.
+#include <algorithm>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -260,13 +261,28 @@ k_voxel_rows(const unsigned long long* __restrict__ vkeys, const uint32_t* __res
     if (j == n - 1) indptr[rowid[j] + flags[j]] = n;
 }
 
+// ---- backward segments: their work order ---------------------------------------------------
+
+/// Sort keys of the backward's work order: the voxel of each segment's first entry (the keys are
+/// the sorted spot * n_voxels + voxel pairs).
+__global__ void
+k_seg_keys(const uint64_t* __restrict__ seg_start, uint32_t n_seg, const unsigned long long* __restrict__ keys,
+           uint64_t n_voxels, unsigned long long* __restrict__ okeys, uint32_t* __restrict__ oval) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_seg) return;
+    okeys[i] = keys[seg_start[i]] % n_voxels;
+    oval[i]  = i;
+}
+
 // ---- products -------------------------------------------------------------------------------
 
 /// Block b of the staged forward owns the voxel rows that start in entries [b * kFwdEntries,
-/// (b + 1) * kFwdEntries): row_first[b] = the first row r with indptr[r] >= b * kFwdEntries.  One
-/// thread per block boundary, a binary search over indptr (once per Dij build).
+/// (b + 1) * kFwdEntries): row_first[b] = the first row r with indptr[r] >= b * kFwdEntries, and
+/// run_k[b] = indptr[row_first[b]], the run's first entry.  One thread per block boundary, a binary
+/// search over indptr (once per Dij build).
 __global__ void
-k_fwd_blocks(const uint64_t* __restrict__ indptr, uint64_t n_rows, uint64_t n_blocks, uint32_t* __restrict__ row_first) {
+k_fwd_blocks(const uint64_t* __restrict__ indptr, uint64_t n_rows, uint64_t n_blocks, uint32_t* __restrict__ row_first,
+             uint64_t* __restrict__ run_k) {
     const uint64_t b = (uint64_t) blockIdx.x * blockDim.x + threadIdx.x;
     if (b > n_blocks) return;
     const uint64_t target = b * kFwdEntries;
@@ -275,7 +291,9 @@ k_fwd_blocks(const uint64_t* __restrict__ indptr, uint64_t n_rows, uint64_t n_bl
         const uint64_t mid = (lo + hi) >> 1;
         if (indptr[mid] < target) lo = mid + 1; else hi = mid;
     }
-    row_first[b] = (uint32_t) (b == n_blocks ? n_rows : lo);
+    const uint64_t r = b == n_blocks ? n_rows : lo;
+    row_first[b]     = (uint32_t) r;
+    run_k[b]         = indptr[r];
 }
 
 /// dose[row_voxel[r]] = sum_k val[k] * w[spot[k]] over voxel rows (D.w).  A block stages the
@@ -376,78 +394,160 @@ mbar_try_wait(uint64_t* bar, uint32_t parity) {
     return ok != 0;
 }
 
-/// D.w in FP32 with the staging done by the copy engine: one thread issues two bulk copies (the
-/// run's spots and values, rounded out to whole 16-byte groups; the arrays are padded) completing
-/// on a shared-memory mbarrier, the block forms the products in place and sums each row from
-/// there, one thread per row, in entry order (the order of k_dij_forward).  The wait on the
-/// barrier is bounded: a block whose copies have not landed after ~1 s of polling sets bit 8 of
-/// `err` and returns without writing.  A run longer than kFwdBulk entries is summed from global
-/// memory.
-__global__ void __launch_bounds__(256)
-k_dij_forward_bulk(const uint32_t* __restrict__ row_voxel, const uint64_t* __restrict__ indptr,
-                   const uint32_t* __restrict__ row_first, const uint32_t* __restrict__ spot,
-                   const float* __restrict__ val, const float* __restrict__ w, float* __restrict__ dose,
-                   uint32_t* __restrict__ err) {
+/// The rows and entries of one run of the persistent forward, as thread 0 found them.
+struct FwdRun {
+    unsigned long long k0, k1, a0;   // entries [k0, k1); staged from a0 (k0 rounded down to a group of four)
+    uint32_t           r0, r1;       // voxel rows [r0, r1)
+    uint32_t           staged, pad;
+};
+static_assert(sizeof(FwdRun) == 40, "FwdRun layout");
+
+constexpr uint32_t kFwdPipeHeader     = 256;                                  // kFwdStages mbarriers + FwdRuns
+constexpr uint32_t kFwdPipeStageBytes = (uint32_t) kFwdPipeStageEntries * 8;  // spots then values
+static_assert(kFwdStages * (8 + sizeof(FwdRun)) <= kFwdPipeHeader, "forward header");
+
+/// D.w in FP32, persistent, through a ring of kFwdStages shared-memory stages.  Each CTA walks the
+/// runs b = blockIdx.x, blockIdx.x + gridDim.x, ... (run b: the voxel rows that start in entries
+/// [b * kFwdEntries, (b + 1) * kFwdEntries), row_first[b] to row_first[b + 1], first entry
+/// run_k[b]).  While the block forms and sums run i from one stage, the copy engine fills the
+/// others with runs i + 1 .. i + kFwdStages - 1: thread 0 issues two untiled bulk copies per run
+/// (its spots and values, rounded out to whole 16-byte groups; the arrays are padded) completing
+/// on that stage's mbarrier, so each CTA keeps kFwdStages - 1 runs' bytes in flight while it
+/// computes.  In a run the block multiplies each value by w[spot] in place, then each thread sums
+/// whole rows from there in entry order (as k_dij_forward does): the result does not depend on
+/// the grid.  Waits are bounded: a block whose copies have not landed after ~1 s of polling sets
+/// bit 8 of `err`, waits (bounded) for its other stages' copies and returns.  A run longer than a
+/// stage (kFwdPipeStageEntries entries: a row of more than ~2000 spots) is summed from global memory.
+__global__ void __launch_bounds__(kFwdPipeThreads)
+k_dij_forward_pipe(const uint32_t* __restrict__ row_voxel, const uint64_t* __restrict__ indptr,
+                   const uint32_t* __restrict__ row_first, const uint64_t* __restrict__ run_k, uint64_t n_blocks,
+                   const uint32_t* __restrict__ spot, const float* __restrict__ val, const float* __restrict__ w,
+                   float* __restrict__ dose, uint32_t* __restrict__ err) {
     extern __shared__ __align__(16) unsigned char fwd_smem[];
-    uint64_t* bar    = reinterpret_cast<uint64_t*>(fwd_smem);
-    uint32_t* s_spot = reinterpret_cast<uint32_t*>(fwd_smem + 16);
-    float*    s_val  = reinterpret_cast<float*>(fwd_smem + 16 + kFwdBulk * sizeof(uint32_t));
-    const uint32_t r0 = row_first[blockIdx.x], r1 = row_first[blockIdx.x + 1];
-    if (r0 >= r1) return;
-    const uint64_t k0 = indptr[r0], k1 = indptr[r1];
-    const uint64_t a0 = k0 & ~3ull, a1 = (k1 + 3) & ~3ull;
-    const bool     staged = a1 - a0 <= kFwdBulk;
-    uint32_t r  = r0 + threadIdx.x;
-    uint64_t rb = 0, re = 0;
-    uint32_t rv = 0;
-    if (r < r1) {
-        rb = indptr[r];
-        re = indptr[r + 1];
-        rv = row_voxel[r];
+    uint64_t*      bar  = reinterpret_cast<uint64_t*>(fwd_smem);
+    FwdRun*        runs = reinterpret_cast<FwdRun*>(fwd_smem + 8 * kFwdStages);
+    unsigned char* data = fwd_smem + kFwdPipeHeader;
+    const int      tid  = threadIdx.x;
+    const uint64_t step = gridDim.x;
+
+    // Thread 0 reads a run's bounds one run before it starts that run's copies, so the loads'
+    // latency passes while the block computes.
+    uint32_t           pf_r0 = 0, pf_r1 = 0;
+    unsigned long long pf_k0 = 0, pf_k1 = 0;
+    auto fetch = [&](uint64_t b) {
+        pf_r0 = row_first[b];
+        pf_r1 = row_first[b + 1];
+        pf_k0 = run_k[b];
+        pf_k1 = run_k[b + 1];
+    };
+    // thread 0: describe the fetched run in stage s and start its copies
+    auto issue = [&](int s) {
+        FwdRun R;
+        R.r0  = pf_r0;
+        R.r1  = pf_r1;
+        R.k0  = pf_k0;
+        R.k1  = pf_k1;
+        R.a0  = R.k0 & ~3ull;
+        R.pad = 0;
+        const unsigned long long a1 = (R.k1 + 3ull) & ~3ull;
+        R.staged = (R.r0 < R.r1 && a1 - R.a0 <= kFwdPipeStageEntries) ? 1u : 0u;
+        if (R.staged) {
+            const uint32_t bytes = (uint32_t) ((a1 - R.a0) * sizeof(uint32_t));
+            unsigned char* st    = data + (size_t) s * kFwdPipeStageBytes;
+            mbar_expect_tx(&bar[s], 2 * bytes);
+            bulk_load(st, spot + R.a0, bytes, &bar[s]);
+            bulk_load(st + kFwdPipeStageEntries * sizeof(uint32_t), val + R.a0, bytes, &bar[s]);
+        }
+        runs[s] = R;
+    };
+
+    if (tid == 0) {
+        for (int s = 0; s < kFwdStages; ++s) mbar_init(&bar[s], 1);
+        // the first kFwdStages - 1 runs start at once
+        uint64_t b = blockIdx.x;
+        for (int s = 0; s < kFwdStages - 1 && b < n_blocks; ++s, b += step) {
+            fetch(b);
+            issue(s);
+        }
+        if (b < n_blocks) fetch(b);
     }
-    if (staged) {
-        const uint32_t bytes = (uint32_t) ((a1 - a0) * sizeof(uint32_t));
-        if (threadIdx.x == 0) mbar_init(bar, 1);
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            mbar_expect_tx(bar, 2 * bytes);
-            bulk_load(s_spot, spot + a0, bytes, bar);
-            bulk_load(s_val, val + a0, bytes, bar);
+    __syncthreads();
+    uint32_t parity = 0;   // bit s: the phase of stage s's barrier to wait for next
+    bool     failed = false;
+    int      s      = 0;   // the stage of run i
+    uint64_t b      = blockIdx.x;
+    for (; b < n_blocks; b += step) {
+        const uint64_t ahead = b + (kFwdStages - 1) * step;     // the run that goes into the stage freed last
+        const int      sf    = s == 0 ? kFwdStages - 1 : s - 1;
+        if (tid == 0 && ahead < n_blocks) {
+            issue(sf);
+            if (ahead + step < n_blocks) fetch(ahead + step);
         }
-        bool     done  = false;
-        uint32_t spins = 0;
-        while (!(done = mbar_try_wait(bar, 0)) && ++spins < kBulkSpinLimit) {
+        const FwdRun R = runs[s];
+        if (R.r0 < R.r1) {
+            uint32_t r  = R.r0 + tid;
+            uint64_t rb = 0, re = 0;
+            uint32_t rv = 0;
+            if (r < R.r1) {
+                rb = indptr[r];
+                re = indptr[r + 1];
+                rv = row_voxel[r];
+            }
+            uint32_t* s_spot = reinterpret_cast<uint32_t*>(data + (size_t) s * kFwdPipeStageBytes);
+            float*    s_val  = reinterpret_cast<float*>(data + (size_t) s * kFwdPipeStageBytes +
+                                                       kFwdPipeStageEntries * sizeof(uint32_t));
+            if (R.staged) {
+                bool     done  = false;
+                uint32_t spins = 0;
+                while (!(done = mbar_try_wait(&bar[s], (parity >> s) & 1u)) && ++spins < kBulkSpinLimit) {
+                }
+                parity ^= 1u << s;
+                if (__syncthreads_or(!done)) {
+                    failed = true;
+                    break;
+                }
+                for (uint64_t k = R.k0 + tid; k < R.k1; k += blockDim.x) s_val[k - R.a0] *= w[s_spot[k - R.a0]];
+                __syncthreads();
+            }
+            while (r < R.r1) {
+                float acc = 0.0f;
+                if (R.staged)
+                    for (uint64_t k = rb; k < re; ++k) acc += s_val[k - R.a0];
+                else
+                    for (uint64_t k = rb; k < re; ++k) acc += val[k] * w[spot[k]];
+                dose[rv] = acc;
+                r += blockDim.x;
+                if (r < R.r1) {
+                    rb = indptr[r];
+                    re = indptr[r + 1];
+                    rv = row_voxel[r];
+                }
+            }
         }
-        if (__syncthreads_or(!done)) {
-            if (threadIdx.x == 0) atomicOr(err, 8u);
-            return;
-        }
-        for (uint64_t k = k0 + threadIdx.x; k < k1; k += blockDim.x) s_val[k - a0] *= w[s_spot[k - a0]];
-        __syncthreads();
+        __syncthreads();   // stage s is free: the next iteration refills it
+        s = s + 1 == kFwdStages ? 0 : s + 1;
     }
-    while (r < r1) {
-        float acc = 0.0f;
-        if (staged)
-            for (uint64_t k = rb; k < re; ++k) acc += s_val[k - a0];
-        else
-            for (uint64_t k = rb; k < re; ++k) acc += val[k] * w[spot[k]];
-        dose[rv] = acc;
-        r += blockDim.x;
-        if (r < r1) {
-            rb = indptr[r];
-            re = indptr[r + 1];
-            rv = row_voxel[r];
+    if (failed && tid == 0) {
+        atomicOr(err, 8u);
+        // copies started for the other stages may still be landing: wait for them (bounded) before
+        // the block's shared memory is released
+        for (int k = 1; k < kFwdStages; ++k) {
+            const int      so = (s + k) % kFwdStages;
+            const uint64_t bo = b + (uint64_t) k * step;
+            if (bo < n_blocks && runs[so].staged)
+                for (uint32_t spins = 0; !mbar_try_wait(&bar[so], (parity >> so) & 1u) && spins < kBulkSpinLimit; ++spins) {
+                }
         }
     }
 }
 
 /// grad[s] = sum_k val[k] * g[voxel[k]] over spot rows (the transposed operator), in two passes
-/// with a fixed order.  Pass 1: the entries are cut into segments of at most kDijSegment entries
-/// that never cross a row; one block per segment sums its products (signed terms of a gradient
-/// cancel, so plain FP32 partials lose digits: a double-float accumulator per thread for FP32 g,
-/// FP64 for FP64 g; FP64 across the block) and writes one partial.  Pass 2: one thread per
-/// row adds its segments' partials in order.  Rows of very different lengths (1e4 to 3e6 entries
-/// at 2000 spots) thereby spread over every SM.
+/// with a fixed order.  Pass 1 (k_dij_backward_segments): the entries are cut into segments of at
+/// most kDijSegment entries that never cross a row; one block sums a segment's products (signed
+/// terms of a gradient cancel, so plain FP32 sums lose digits: a double-float accumulator per
+/// thread for FP32 g, FP64 for FP64 g; FP64 across the block) into one FP64 partial.  Pass 2
+/// (k_dij_backward_rows): one thread per row adds its segments' partials in order.  Rows of very
+/// different lengths (1e4 to 3e6 entries at 2000 spots) thereby spread over every SM.
 /// s + c += a * b with no rounding error in the product (TwoProd: one FMA gives the product's
 /// rounding error) and Knuth's TwoSum for the addition: a double-float accumulator of about 48
 /// significant bits on the FP32 pipes.  GB300's FP64 pipe is far narrower than its FP32 pipes,
@@ -463,17 +563,18 @@ df_fma(float& s, float& c, float a, float b) {
     s               = t;
 }
 
+/// A block's share of the products of entries [b, e) of a spot row, per thread, in a fixed order:
+/// thread t takes the groups of four q = (b >> 2) + t, + blockDim.x, ... (16-byte loads of voxels
+/// and values, four independent gathers of g per group; the arrays are padded to whole groups).
 template<typename T>
 __device__ __forceinline__ double
 segment_sum(uint64_t b, uint64_t e, const uint32_t* __restrict__ vox, const float* __restrict__ val,
             const T* __restrict__ g) {
+    const uint4*   v4 = reinterpret_cast<const uint4*>(vox);
+    const float4*  a4 = reinterpret_cast<const float4*>(val);
+    const uint64_t q1 = (e + 3) >> 2;
     if constexpr (sizeof(T) == sizeof(float)) {
-        // groups of four entries with 16-byte loads (the arrays are padded to whole groups) and four
-        // independent gathers of g in flight per group; entries outside [b, e) are skipped
-        const uint4*   v4 = reinterpret_cast<const uint4*>(vox);
-        const float4*  a4 = reinterpret_cast<const float4*>(val);
-        const uint64_t q1 = (e + 3) >> 2;
-        float          s = 0.0f, c = 0.0f;
+        float s = 0.0f, c = 0.0f;
 #pragma unroll 4
         for (uint64_t q = (b >> 2) + threadIdx.x; q < q1; q += blockDim.x) {
             const uint4    vv = v4[q];
@@ -491,19 +592,43 @@ segment_sum(uint64_t b, uint64_t e, const uint32_t* __restrict__ vox, const floa
         return (double) s + (double) c;
     } else {
         double d = 0.0;
-        for (uint64_t k = b + threadIdx.x; k < e; k += blockDim.x) d += (double) val[k] * g[vox[k]];
+#pragma unroll 2
+        for (uint64_t q = (b >> 2) + threadIdx.x; q < q1; q += blockDim.x) {
+            const uint4    vv = v4[q];
+            const float4   aa = a4[q];
+            const uint64_t k  = q << 2;
+            if (k >= b && k < e) d += (double) aa.x * g[vv.x];
+            if (k + 1 >= b && k + 1 < e) d += (double) aa.y * g[vv.y];
+            if (k + 2 >= b && k + 2 < e) d += (double) aa.z * g[vv.z];
+            if (k + 3 >= b && k + 3 < e) d += (double) aa.w * g[vv.w];
+        }
         return d;
     }
 }
 
+/// Pass 1 of D^T.g.  The blocks take segments from a shared cursor in the order of their first
+/// voxel (`order`), so the segments in flight at any moment -- of every spot -- cover a narrow
+/// band of depth, and their gathers of g come from a few megabytes that stay in L2 instead of each
+/// spot's row sweeping the whole dose-gradient vector (a 4-byte gather then costs a 32-byte DRAM
+/// sector).  Each segment's partial is written at its spot-major index; which block computes it
+/// does not change it, so the result is reproducible.  The cursor is returned to zero by
+/// k_dij_backward_rows, which runs after this kernel on the same stream.
 template<typename T>
-__global__ void
-k_dij_backward_segments(const uint64_t* __restrict__ seg_start, uint64_t n_seg, const uint32_t* __restrict__ vox,
-                        const float* __restrict__ val, const T* __restrict__ g, double* __restrict__ partial) {
-    __shared__ double part[32];
-    for (uint64_t sg = blockIdx.x; sg < n_seg; sg += gridDim.x) {
-        const uint64_t b = seg_start[sg], e = seg_start[sg + 1];
-        double         d = segment_sum<T>(b, e, vox, val, g);
+__global__ void __launch_bounds__(256, 8)
+k_dij_backward_segments(const uint32_t* __restrict__ order, uint32_t n_seg, const uint64_t* __restrict__ seg_start,
+                        const uint32_t* __restrict__ vox, const float* __restrict__ val, const T* __restrict__ g,
+                        double* __restrict__ partial, uint32_t* __restrict__ cursor) {
+    __shared__ double   part[32];
+    __shared__ uint32_t s_next;
+    if (threadIdx.x == 0) s_next = atomicAdd(cursor, 1u);
+    __syncthreads();
+    uint32_t i = s_next;
+    while (i < n_seg) {
+        __syncthreads();   // everyone has read s_next
+        // the next segment is claimed before this one is summed, so the claim's latency overlaps it
+        if (threadIdx.x == 0) s_next = atomicAdd(cursor, 1u);
+        const uint32_t sg = order[i];
+        double         d  = segment_sum<T>(seg_start[sg], seg_start[sg + 1], vox, val, g);
         for (int o = 16; o > 0; o >>= 1) d += __shfl_down_sync(0xFFFFFFFFu, d, o);
         if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = d;
         __syncthreads();
@@ -512,15 +637,17 @@ k_dij_backward_segments(const uint64_t* __restrict__ seg_start, uint64_t n_seg, 
             for (int o = 16; o > 0; o >>= 1) d += __shfl_down_sync(0xFFFFFFFFu, d, o);
             if (threadIdx.x == 0) partial[sg] = d;
         }
-        __syncthreads();
+        __syncthreads();   // part[] is free again; s_next holds the next claim
+        i = s_next;
     }
 }
 
 template<typename T>
 __global__ void
 k_dij_backward_rows(const uint32_t* __restrict__ row_seg, uint32_t n_rows, const double* __restrict__ partial,
-                    T* __restrict__ grad) {
+                    T* __restrict__ grad, uint32_t* __restrict__ cursor) {
     const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r == 0 && cursor) *cursor = 0u;
     if (r >= n_rows) return;
     double d = 0.0;
     for (uint32_t k = row_seg[r]; k < row_seg[r + 1]; ++k) d += partial[k];
@@ -633,17 +760,26 @@ dij_voxel_rows(const unsigned long long* vkeys, const uint32_t* vpos, uint64_t n
 }
 
 cudaError_t
-dij_forward_blocks(const uint64_t* indptr, uint64_t n_rows, uint64_t nnz, uint32_t* row_first, uint64_t* n_blocks,
-                   cudaStream_t s) {
+dij_forward_blocks(const uint64_t* indptr, uint64_t n_rows, uint64_t nnz, uint32_t* row_first, uint64_t* run_k,
+                   uint64_t* n_blocks, cudaStream_t s) {
     const uint64_t nb = (nnz + kFwdEntries - 1) / kFwdEntries;
     *n_blocks         = nb;
-    k_fwd_blocks<<<blocks_for(nb + 1, 256), 256, 0, s>>>(indptr, n_rows, nb, row_first);
+    k_fwd_blocks<<<blocks_for(nb + 1, 256), 256, 0, s>>>(indptr, n_rows, nb, row_first, run_k);
     return cudaGetLastError();
 }
 
 cudaError_t
-dij_forward(const uint32_t* row_voxel, const uint64_t* indptr, const uint32_t* row_first, uint64_t n_blocks,
-            const uint32_t* spot, const float* val, const void* w, void* dose, int fp64, uint32_t* err, cudaStream_t s) {
+dij_seg_order_keys(const uint64_t* seg_start, uint32_t n_seg, const unsigned long long* keys, uint64_t n_voxels,
+                   unsigned long long* okeys, uint32_t* oval, cudaStream_t s) {
+    if (n_seg == 0) return cudaSuccess;
+    k_seg_keys<<<blocks_for(n_seg, 256), 256, 0, s>>>(seg_start, n_seg, keys, n_voxels, okeys, oval);
+    return cudaGetLastError();
+}
+
+cudaError_t
+dij_forward(const uint32_t* row_voxel, const uint64_t* indptr, const uint32_t* row_first, const uint64_t* run_k,
+            uint64_t n_blocks, const uint32_t* spot, const float* val, const void* w, void* dose, int fp64, uint32_t* err,
+            int sms, cudaStream_t s) {
     if (n_blocks == 0) return cudaSuccess;
     static_assert(kFwdStage * sizeof(double) <= 227 * 1024, "staging buffer exceeds shared memory");
     if (fp64) {
@@ -653,29 +789,36 @@ dij_forward(const uint32_t* row_voxel, const uint64_t* indptr, const uint32_t* r
         k_dij_forward<double><<<(unsigned) n_blocks, 256, sm, s>>>(row_voxel, indptr, row_first, spot, val,
                                                                   (const double*) w, (double*) dose);
     } else {
-        const size_t sm = 16 + kFwdBulk * (sizeof(uint32_t) + sizeof(float));
-        cudaError_t  e  = cudaFuncSetAttribute(k_dij_forward_bulk, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) sm);
+        constexpr size_t sm = kFwdPipeHeader + kFwdStages * (size_t) kFwdPipeStageBytes;
+        static_assert(kFwdPipeBlocksPerSm * (sm + 1024) <= 228 * 1024, "the persistent forward blocks must fit one SM");
+        cudaError_t e = cudaFuncSetAttribute(k_dij_forward_pipe, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) sm);
         if (e != cudaSuccess) return e;
-        k_dij_forward_bulk<<<(unsigned) n_blocks, 256, sm, s>>>(row_voxel, indptr, row_first, spot, val,
-                                                               (const float*) w, (float*) dose, err);
+        const uint64_t cap  = (uint64_t) sms * kFwdPipeBlocksPerSm;
+        const unsigned grid = (unsigned) (n_blocks < cap ? n_blocks : cap);
+        k_dij_forward_pipe<<<grid, kFwdPipeThreads, sm, s>>>(row_voxel, indptr, row_first, run_k, n_blocks, spot, val,
+                                                            (const float*) w, (float*) dose, err);
     }
     return cudaGetLastError();
 }
 
 cudaError_t
-dij_backward(const uint64_t* seg_start, uint64_t n_seg, const uint32_t* row_seg, uint32_t n_rows, const uint32_t* vox,
-             const float* val, double* partial, const void* g, void* grad, int fp64, int sms, cudaStream_t s) {
+dij_backward(const uint32_t* order, const uint64_t* seg_start, uint32_t n_seg, const uint32_t* row_seg, uint32_t n_rows,
+             const uint32_t* vox, const float* val, double* partial, uint32_t* cursor, const void* g, void* grad,
+             int fp64, int sms, cudaStream_t s) {
     if (n_rows == 0) return cudaSuccess;
     if (n_seg) {
-        const unsigned grid = (unsigned) (n_seg < (uint64_t) sms * 64 ? n_seg : (uint64_t) sms * 64);
+        const uint64_t cap  = (uint64_t) sms * 8;   // 8 blocks of 256 threads per SM
+        const unsigned grid = (unsigned) std::min<uint64_t>(n_seg, cap);
         if (fp64)
-            k_dij_backward_segments<double><<<grid, 256, 0, s>>>(seg_start, n_seg, vox, val, (const double*) g, partial);
+            k_dij_backward_segments<double><<<grid, 256, 0, s>>>(order, n_seg, seg_start, vox, val, (const double*) g,
+                                                                 partial, cursor);
         else
-            k_dij_backward_segments<float><<<grid, 256, 0, s>>>(seg_start, n_seg, vox, val, (const float*) g, partial);
+            k_dij_backward_segments<float><<<grid, 256, 0, s>>>(order, n_seg, seg_start, vox, val, (const float*) g,
+                                                                partial, cursor);
     }
     const unsigned rb = (n_rows + 255) / 256;
-    if (fp64) k_dij_backward_rows<double><<<rb, 256, 0, s>>>(row_seg, n_rows, partial, (double*) grad);
-    else k_dij_backward_rows<float><<<rb, 256, 0, s>>>(row_seg, n_rows, partial, (float*) grad);
+    if (fp64) k_dij_backward_rows<double><<<rb, 256, 0, s>>>(row_seg, n_rows, partial, (double*) grad, cursor);
+    else k_dij_backward_rows<float><<<rb, 256, 0, s>>>(row_seg, n_rows, partial, (float*) grad, cursor);
     return cudaGetLastError();
 }
 

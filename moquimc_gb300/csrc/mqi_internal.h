@@ -211,16 +211,21 @@ cudaError_t dij_voxel_rows(const unsigned long long* vkeys, const uint32_t* vpos
 constexpr uint64_t kFwdEntries = 4096;    // entries whose rows one forward block owns
 constexpr uint64_t kFwdStage   = 8192;    // staged products per forward block (rows up to 4096 entries)
 cudaError_t dij_forward_blocks(const uint64_t* indptr, uint64_t n_rows, uint64_t nnz, uint32_t* row_first,
-                               uint64_t* n_blocks, cudaStream_t s);
-constexpr uint64_t kFwdBulk    = 6144;    // entries a bulk-copy forward block stages (spots and values)
+                               uint64_t* run_k, uint64_t* n_blocks, cudaStream_t s);
+constexpr uint64_t kFwdPipeStageEntries = 6144;   // entries one stage of the persistent forward holds
+constexpr int      kFwdStages           = 2;      // its ring of stages (one run in flight while one is summed)
+constexpr int      kFwdPipeThreads      = 512;    // persistent forward block
+constexpr int      kFwdPipeBlocksPerSm  = 2;      // two 96 KB blocks per SM
 constexpr uint32_t kBulkSpinLimit = 1u << 20;   // bounded polls of a bulk-copy mbarrier
-cudaError_t dij_forward(const uint32_t* row_voxel, const uint64_t* indptr, const uint32_t* row_first, uint64_t n_blocks,
-                        const uint32_t* spot, const float* val, const void* w, void* dose, int fp64, uint32_t* err,
-                        cudaStream_t s);
-constexpr uint64_t kDijSegment = 16384;   // entries per backward segment
-cudaError_t dij_backward(const uint64_t* seg_start, uint64_t n_seg, const uint32_t* row_seg, uint32_t n_rows,
-                         const uint32_t* vox, const float* val, double* partial, const void* g, void* grad, int fp64,
-                         int sms, cudaStream_t s);
+cudaError_t dij_forward(const uint32_t* row_voxel, const uint64_t* indptr, const uint32_t* row_first,
+                        const uint64_t* run_k, uint64_t n_blocks, const uint32_t* spot, const float* val, const void* w,
+                        void* dose, int fp64, uint32_t* err, int sms, cudaStream_t s);
+constexpr uint64_t kDijSegment = 16384;   // entries per backward segment (segments never cross a row)
+cudaError_t dij_seg_order_keys(const uint64_t* seg_start, uint32_t n_seg, const unsigned long long* keys,
+                               uint64_t n_voxels, unsigned long long* okeys, uint32_t* oval, cudaStream_t s);
+cudaError_t dij_backward(const uint32_t* order, const uint64_t* seg_start, uint32_t n_seg, const uint32_t* row_seg,
+                         uint32_t n_rows, const uint32_t* vox, const float* val, double* partial, uint32_t* cursor,
+                         const void* g, void* grad, int fp64, int sms, cudaStream_t s);
 
 // ---- launchers (mqi_kernels.cu) ----
 // Loaders: n histories from h0, each once per scenario (n_scen >= 1), scenario-interleaved:

@@ -135,6 +135,12 @@ def test_dij_products_match_dense_references(gpu_ctx_factory, wl):
     np.testing.assert_allclose(g64, ref_g, rtol=1e-11, atol=1e-11 * np.abs(ref_g).max())
     g32 = c.dij_rmatvec(dij, g.astype(np.float32), op.n_spots)
     np.testing.assert_allclose(g32, ref_g, rtol=1e-4, atol=1e-5 * np.abs(ref_g).max())
+    # fixed reduction orders: repeated products give identical bits (the backward's warps take its
+    # segments from a shared cursor, in whatever order they get there)
+    for _ in range(3):
+        np.testing.assert_array_equal(c.dij_rmatvec(dij, g.astype(np.float32), op.n_spots), g32)
+        np.testing.assert_array_equal(c.dij_rmatvec(dij, g.astype(np.float64), op.n_spots), g64)
+        np.testing.assert_array_equal(c.dij_matvec(dij, w.astype(np.float32), op.n_voxels), d32)
     # unit weights reproduce the dense dose of the same run (FP32 matrix entries)
     e, eid = _ctx(gpu_ctx_factory, wl)
     dose = e.add_scorer(eid, capi.DOSE_W)

@@ -172,13 +172,14 @@ def test_calibration_arguments_are_checked(gpu_ctx_factory):
 
 
 def test_gpu_matches_oracle_in_aggregate(oracle, gpu_ctx_factory):
-    """Full-resolution phantom example, 4 x 1000 histories on each side: the depth-dose curves of
-    the GPU and of the C restatement agree within 2% or 3 sigma.  (Voxel-for-voxel equality on the
+    """Full-resolution phantom example, 4 x 3000 histories on each side: the depth-dose curves of
+    the GPU and of the C restatement agree within 2% or 3 sigma, and R80 within 0.2 mm (the
+    standard error of each side's R80 is about 0.03 mm at 12 000 histories).  (Voxel-for-voxel equality on the
     same streams does not hold: a 1-ulp difference between CUDA's and libm's powf in the stopping
     power ratio flips near-ties such as a 1.0 mm boundary distance against a 1.0 mm step limit,
     and the extra step shifts the track's Philox block counter.)"""
     wl = workloads.c1()
-    each, seed = 1000, 0xBEEF
+    each, seed = 3000, 0xBEEF
     c, cid, sid = _ctx_for(wl, gpu_ctx_factory, capi.DOSE_W)
     grid = _oracle_grid(oracle, wl)
     g_b, o_b = [], []
@@ -197,7 +198,7 @@ def test_gpu_matches_oracle_in_aggregate(oracle, gpu_ctx_factory):
     sel = om > 0.1 * om.max()
     ok = (np.abs(gm - om) <= 0.02 * om) | (np.abs(gm - om) <= 3 * np.sqrt(gs ** 2 + os_ ** 2))
     assert ok[sel].mean() >= 0.95
-    assert abs(ph.r80(gm, 1.0) - ph.r80(om, 1.0)) <= 0.3
+    assert abs(ph.r80(gm, 1.0) - ph.r80(om, 1.0)) <= 0.2, (ph.r80(gm, 1.0), ph.r80(om, 1.0))
 
 
 def test_gpu_fp32_matches_the_fp64_oracle(oracle, gpu_ctx_factory):
