@@ -401,11 +401,13 @@ def robust_full_section(torch, capi, workloads, args) -> dict:
     c.set_density(cid, c.hu_to_density(wl.hu.ravel()))
     sid = c.add_scorer(cid, capi.DOSE_W)
     N = c.set_spot_plan(wl.spots)
-    t_tune, tune = _cuda_time(torch, lambda: c.autotune(0, min(N, 2_000_000), 11, plan=True))
-    best = tune[np.argmax(tune["histories_per_s"])]
     d1, d2 = c.add_stat_scorers(cid)
     es = [workloads.scenario_edges(wl, sh) for sh, _ in scen]
     c.set_scenarios(cid, [e[0] for e in es], [e[1] for e in es], [e[2] for e in es], [k for _, k in scen])
+    # tuned on the scenario workload itself (500 000 histories x 21 scenarios per candidate): with 21
+    # instances per history the launch mode that wins differs from the single-scenario plan's
+    t_tune, tune = _cuda_time(torch, lambda: c.autotune(0, min(N, 500_000), 11, plan=True))
+    best = tune[np.argmax(tune["histories_per_s"])]
     c.transport_plan(0, min(N, 50_000), 1)
     c.reset()
     t, (passes, achieved) = _cuda_time(
