@@ -229,6 +229,10 @@ def plan_section(torch, capi, workloads, args) -> dict:
     d1, d2 = c.add_stat_scorers(cid)
     N = c.set_spot_plan(wl.spots)
     cum = c.plan_cum
+    # the batched form runs with the launch shape, queue size and launch mode the tuner picks on a
+    # sample of the plan (2e6 histories per candidate, the dose and statistics scorers as timed)
+    t_tune, tune = _cuda_time(torch, lambda: c.autotune(0, min(N, 2_000_000), 11, plan=True))
+    best = tune[np.argmax(tune["histories_per_s"])]
     c.transport_plan(0, min(N, 200_000), 1)                       # warm-up
     c.reset()
     t_b, _ = _cuda_time(torch, lambda: c.transport_plan(0, N, 2))
@@ -250,7 +254,7 @@ def plan_section(torch, capi, workloads, args) -> dict:
     plain(sub[:20])                                                 # warm-up in this mode
     c.reset()
     t_p, _ = _cuda_time(torch, lambda: plain(range(len(wl.spots))))
-    c.set_launch_mode(streamed=1)
+    c.set_launch_mode(streamed=int(best["streamed"]))               # back to the tuned batched form
     c.reset()
     t_s, (passes, achieved) = _cuda_time(
         torch, lambda: c.run_plan_until_stat(d1, d2, 0.01, 0.5, args.max_passes, 0x5EED))
@@ -266,7 +270,11 @@ def plan_section(torch, capi, workloads, args) -> dict:
         "workload": wl.name, "voxels": list(wl.nxyz), "voxel_mm": [0.98, 0.98, 2.0], "spots": len(wl.spots),
         "histories_per_pass": N, "physics_debug": False,
         "batched": {"primaries_per_s": batched, "seconds_per_pass": t_b, "steps_per_primary": st["steps"] / N,
-                    "waves": st["waves"], "estimate_after_one_pass": est1, "voxels_above_50pct": nv},
+                    "waves": st["waves"], "estimate_after_one_pass": est1, "voxels_above_50pct": nv,
+                    "tuning": {"seconds": t_tune, "candidates": int(len(tune)),
+                               "chosen": {"block": int(best["block"]), "blocks_per_sm": int(best["blocks_per_sm"]),
+                                          "streamed": int(best["streamed"]),
+                                          "primary_chunk": int(best["primary_chunk"])}}},
         "plain_per_spot": {"primaries_per_s": plain_rate, "seconds_per_pass": t_p, "spots_timed": len(wl.spots),
                            "histories_timed": N, "launch_mode": "queue generations",
                            "sample": "the whole plan, one mqi_transport_plan call per spot",
@@ -378,6 +386,8 @@ def robust_section(torch, capi, workloads, args) -> dict:
     es = [workloads.scenario_edges(wl, sh) for sh, _ in scen]
     c.set_scenarios(cid, [e[0] for e in es], [e[1] for e in es], [e[2] for e in es], [k for _, k in scen])
     N = c.set_spot_plan(sub)
+    tune = c.autotune(0, min(N, 300_000), 11, plan=True)        # on the scenario workload itself
+    best = tune[np.argmax(tune["histories_per_s"])]
     c.transport_plan(0, min(N, 50_000), 1)
     c.reset()
     t, _ = _cuda_time(torch, lambda: c.transport_plan(0, N, 2))
@@ -385,7 +395,9 @@ def robust_section(torch, capi, workloads, args) -> dict:
     c.close()
     return {"scenarios": len(scen), "spots": len(sub), "histories": N, "instances": N * len(scen),
             "instance_primaries_per_s": N * len(scen) / t, "seconds": t, "worst_scenario_estimate": est,
-            "sample": f"every {args.robust_stride}th spot of the c3 plan"}
+            "sample": f"every {args.robust_stride}th spot of the c3 plan",
+            "tuned": {"block": int(best["block"]), "blocks_per_sm": int(best["blocks_per_sm"]),
+                      "streamed": int(best["streamed"]), "primary_chunk": int(best["primary_chunk"])}}
 
 
 def robust_full_section(torch, capi, workloads, args) -> dict:
