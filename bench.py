@@ -230,8 +230,9 @@ def plan_section(torch, capi, workloads, args) -> dict:
     N = c.set_spot_plan(wl.spots)
     cum = c.plan_cum
     # the batched form runs with the launch shape, queue size and launch mode the tuner picks on a
-    # sample of the plan (2e6 histories per candidate, the dose and statistics scorers as timed)
-    t_tune, tune = _cuda_time(torch, lambda: c.autotune(0, min(N, 2_000_000), 11, plan=True))
+    # sample of the plan (8e6 histories per candidate -- several queue loads, so that the launch
+    # modes' behaviour at load boundaries shows -- with the dose and statistics scorers as timed)
+    t_tune, tune = _cuda_time(torch, lambda: c.autotune(0, min(N, 8_000_000), 11, plan=True))
     best = tune[np.argmax(tune["histories_per_s"])]
     c.transport_plan(0, min(N, 200_000), 1)                       # warm-up
     c.reset()
@@ -386,7 +387,7 @@ def robust_section(torch, capi, workloads, args) -> dict:
     es = [workloads.scenario_edges(wl, sh) for sh, _ in scen]
     c.set_scenarios(cid, [e[0] for e in es], [e[1] for e in es], [e[2] for e in es], [k for _, k in scen])
     N = c.set_spot_plan(sub)
-    tune = c.autotune(0, min(N, 300_000), 11, plan=True)        # on the scenario workload itself
+    tune = c.autotune(0, min(N, 500_000), 11, plan=True)        # on the scenario workload itself
     best = tune[np.argmax(tune["histories_per_s"])]
     c.transport_plan(0, min(N, 50_000), 1)
     c.reset()

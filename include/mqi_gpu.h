@@ -397,7 +397,10 @@ typedef struct {
 /* Tuner (no counterpart in moqui): transport the sample [h0, h1) of the current source (vertices,
  * or the spot plan when source_plan = 1) once per candidate launch shape, queue size and launch
  * mode, into scratch tallies (the caller's tallies and counters are kept), and keep the fastest
- * candidate as the context's setting.  Up to max_results measurements go to `results`;
+ * candidate as the context's setting.  A sample of several queue loads (several times the queue
+ * size, 2^21 entries by default, counting each history once per scenario) lets the launch modes'
+ * behaviour at load boundaries show; on a single load they time alike.  Up to max_results
+ * measurements go to `results`;
  * n_results receives the number of candidates run.  Results of later runs do not depend on the
  * choice.  Not with a Dij scorer present (add it after tuning). */
 int mqi_autotune(mqi_ctx* ctx, int source_plan, uint64_t h0, uint64_t h1, uint64_t seed,

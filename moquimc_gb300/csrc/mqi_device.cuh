@@ -178,6 +178,20 @@ intpl1d(float x, float x0, float x1, float y0, float y1) {
     return (x1 == x0) ? y0 : y0 + (x - x0) * (y1 - y0) / (x1 - x0);
 }
 
+/// intpl1d at a node of the 0.1 MeV + 0.5 MeV * i energy grid: there x1 - x0 is exactly 0.5 in FP32
+/// except at the four nodes whose interval crosses 2, 8, 32 or 128 MeV (checked exhaustively), and
+/// dividing by exactly 0.5 is multiplying by 2, so the division runs only at those four.  The
+/// result is intpl1d's, bit for bit.
+__host__ __device__ inline float
+intpl1d_grid(float x, float x0, float x1, float y0, float y1) {
+    const float w   = x1 - x0;
+    const float num = (x - x0) * (y1 - y0);
+    float       q;
+    if (w == 0.5f) q = num * 2.0f;
+    else q = num / w;
+    return y0 + q;
+}
+
 /// relativistic_quantities (mqi_relativistic_quantities.hpp:24-40), FP32.
 struct Rel {
     float Ek, Et, Et_sq, gamma, gamma_sq, beta_sq, Te_max;
@@ -215,7 +229,7 @@ cs_lookup(const float* tab, float Ek, float e_min, float e_max, float rho) {
         const int i1 = min(i0 + 1, MQI_TABLE_N - 1);
         const float x0 = e_min + (float) i0 * 0.5f;
         const float x1 = x0 + 0.5f;
-        cs             = intpl1d(Ek, x0, x1, tab[i0], tab[i1]);
+        cs             = intpl1d_grid(Ek, x0, x1, tab[i0], tab[i1]);
     }
     return cs * rho;
 }
@@ -261,7 +275,7 @@ dedx_lookup(const Tables& T, float Ek) {
         const int i1 = min(i0 + 1, MQI_TABLE_N - 1);
         const float x0 = 0.1f + (float) i0 * 0.5f;
         const float x1 = x0 + 0.5f;
-        pw             = intpl1d(Ek, x0, x1, T.dedx[i0], T.dedx[i1]);
+        pw             = intpl1d_grid(Ek, x0, x1, T.dedx[i0], T.dedx[i1]);
     } else if (Ek < 0.1f && Ek > 0.0f) {
         pw = T.dedx[0];
     }

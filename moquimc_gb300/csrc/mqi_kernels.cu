@@ -559,7 +559,7 @@ energy_loss(const Tables& T, const Rel& rel, float rho, float len, float spr, fl
     float x1 = x0 + 0.5f;
     if (x0 > rel.Ek && n > 0) n -= 1;
     if (x1 < rel.Ek && n < MQI_TABLE_N - 2) n += 1;
-    float r = intpl1d(rel.Ek, x0, x1, T.range[n], T.range[n + 1]);
+    float r = intpl1d_grid(rel.Ek, x0, x1, T.range[n], T.range[n + 1]);
     if (r < lw) return rel.Ek;
     r -= lw;
     while (n > 0 && r < T.range[n]) --n;
