@@ -517,7 +517,7 @@ make_wave_params(mqi_ctx* c, uint64_t seed, WaveParams& P) {
         d.type = s.type; d.roi_method = s.roi_method; d.stat_mode = s.stat_mode;
         d.roi_len = s.roi_len; d.start = s.start; d.stride = s.stride; d.acc = s.acc;
         d.tally = s.tally; d.tally_len = s.tally_len; d.tstride = s.tstride;
-        d.dij = s.dij; d.dij_mask = s.dij_cap ? s.dij_cap - 1 : 0; d.dij_count = s.dij_count;
+        d.dij = s.dij; d.dij_mask = s.dij_cap ? s.dij_cap - 1 : 0;
         d.hit_log = s.hit_log; d.hit_count = s.hit_count; d.hit_cap = s.hit_cap;
         if (s.dij) {
             c->scorers[i].csr.built = false;   // new entries invalidate a built matrix

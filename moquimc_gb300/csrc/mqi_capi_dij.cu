@@ -204,6 +204,7 @@ mqi_dij_build(mqi_ctx* c, int id, uint32_t n_spots, double scale, uint64_t* nnz_
     cudaStream_t st = c->stream;
     free_csr(s.csr);
     unsigned long long count = 0;
+    MQI_CUDA(c, dij_count(s.dij, s.dij_cap, s.dij_count, c->num_sms, st), "mqi_dij_build: count");
     MQI_CUDA(c, cudaMemcpyAsync(&count, s.dij_count, sizeof(count), cudaMemcpyDeviceToHost, st), "mqi_dij_build");
     MQI_CUDA(c, cudaStreamSynchronize(st), "mqi_dij_build");
     const uint64_t n = count;
@@ -352,6 +353,7 @@ mqi_dij_info(mqi_ctx* c, int id, uint64_t* table_slots, uint64_t* occupied, uint
     if (!sp) return MQI_ERR_INVALID;
     DeviceGuard g(c->device);
     unsigned long long occ = 0;
+    MQI_CUDA(c, dij_count(sp->dij, sp->dij_cap, sp->dij_count, c->num_sms, c->stream), "mqi_dij_info");
     MQI_CUDA(c, cudaMemcpyAsync(&occ, sp->dij_count, sizeof(occ), cudaMemcpyDeviceToHost, c->stream), "mqi_dij_info");
     MQI_CUDA(c, cudaStreamSynchronize(c->stream), "mqi_dij_info");
     if (table_slots) *table_slots = sp->dij_cap;

@@ -76,7 +76,7 @@ struct ScorerHost {
     uint64_t  n_batches = 0;
     DijSlot*  dij = nullptr;        // MQI_SCORER_DIJ: hash table of dij_cap slots (power of two)
     uint64_t  dij_cap = 0;
-    unsigned long long* dij_count = nullptr;
+    unsigned long long* dij_count = nullptr;   // device: occupied slots, counted on demand (dij_count())
     DijHit*   hit_log = nullptr;    // mqi_dij_record_hits: recorded insertions
     unsigned long long* hit_count = nullptr;
     uint64_t  hit_cap = 0;

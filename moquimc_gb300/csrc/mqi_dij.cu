@@ -63,6 +63,17 @@ k_dij_compact(const DijSlot* __restrict__ tab, uint64_t cap, uint64_t n_voxels, 
     }
 }
 
+/// *out += the number of occupied slots (nonzero keys) of the table: a grid-stride count, one
+/// atomic per warp.
+__global__ void
+k_dij_count(const DijSlot* __restrict__ tab, uint64_t cap, unsigned long long* __restrict__ out) {
+    const uint64_t     stride = (uint64_t) gridDim.x * blockDim.x;
+    unsigned long long n      = 0;
+    for (uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < cap; i += stride) n += tab[i].key != 0ull;
+    for (int o = 16; o > 0; o >>= 1) n += __shfl_down_sync(0xFFFFFFFFu, n, o);
+    if ((threadIdx.x & 31) == 0 && n) atomicAdd(out, n);
+}
+
 // ---- exclusive scan of u32 ------------------------------------------------------------------
 
 __device__ inline uint32_t
@@ -673,6 +684,14 @@ blocks_for(uint64_t n, int per_block) {
 cudaError_t
 dij_clear(DijSlot* tab, uint64_t cap, int sms, cudaStream_t s) {
     k_dij_clear<<<sms * 8, 256, 0, s>>>(tab, cap);
+    return cudaGetLastError();
+}
+
+cudaError_t
+dij_count(const DijSlot* tab, uint64_t cap, unsigned long long* out, int sms, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(out, 0, sizeof(unsigned long long), s);
+    if (e != cudaSuccess || cap == 0) return e;
+    k_dij_count<<<(unsigned) std::min<uint64_t>((cap + 255) / 256, (uint64_t) sms * 8), 256, 0, s>>>(tab, cap, out);
     return cudaGetLastError();
 }
 

@@ -64,7 +64,6 @@ struct ScorerDev {
     uint32_t        tstride;       // 1, or 2 for the interleaved statistics pair (dose, dose^2)
     DijSlot*        dij;           // MQI_SCORER_DIJ: open-addressing table of dij_mask + 1 slots
     uint64_t        dij_mask;
-    unsigned long long* dij_count; // device: occupied slots
     DijHit*         hit_log;       // optional: every insertion, appended (null: not recorded)
     unsigned long long* hit_count; // device: insertions recorded (counts on past hit_cap)
     uint64_t        hit_cap;
@@ -190,6 +189,8 @@ void set_thread_error(const char* msg);
 
 // ---- Dij (mqi_dij.cu) ----
 cudaError_t dij_clear(DijSlot* tab, uint64_t cap, int sms, cudaStream_t s);
+// Occupied slots of a Dij table into *out (cleared first).
+cudaError_t dij_count(const DijSlot* tab, uint64_t cap, unsigned long long* out, int sms, cudaStream_t s);
 cudaError_t dij_compact(const DijSlot* tab, uint64_t cap, uint64_t n_voxels, unsigned long long* keys, uint32_t* idx,
                         uint64_t n_max, unsigned long long* cursor, int sms, cudaStream_t s);
 uint64_t    scan_scratch_words(uint64_t n);
