@@ -236,7 +236,8 @@ int mqi_dij_build(mqi_ctx* ctx, int scorer_id, uint32_t n_spots, double scale, u
 int mqi_dij_get_csr(mqi_ctx* ctx, int scorer_id, uint64_t* indptr, uint32_t* indices, float* data,
                     int on_device);
 
-/* Table slots, occupied slots, and (after a build) entries and voxel rows of the matrix. */
+/* Table slots, occupied slots (counted by one pass over the table on the context's stream; the
+ * call waits for it), and (after a build) entries and voxel rows of the matrix. */
 int mqi_dij_info(mqi_ctx* ctx, int scorer_id, uint64_t* table_slots, uint64_t* occupied,
                  uint64_t* nnz, uint64_t* n_voxel_rows);
 
@@ -256,6 +257,8 @@ int mqi_dij_get_hits(mqi_ctx* ctx, int scorer_id, uint32_t* voxel, uint32_t* spo
 /* dose = D.w (n_voxels outputs from n_spots weights) and grad = D^T.g (n_spots outputs from
  * n_voxels inputs); fp64 selects double buffers (the matrix stays FP32).  With on_device = 1 the
  * buffers are device pointers and the work is queued on the context's stream without a sync.
+ * Both use fixed reduction orders: repeated calls give identical bits.  Calls on one matrix share
+ * its work buffers and must not overlap on the GPU (the context's stream orders them).
  * No reference counterpart: moqui stops at writing the matrix. */
 int mqi_dij_matvec(mqi_ctx* ctx, int scorer_id, const void* w, void* dose, int fp64, int on_device);
 int mqi_dij_rmatvec(mqi_ctx* ctx, int scorer_id, const void* g, void* grad, int fp64, int on_device);
