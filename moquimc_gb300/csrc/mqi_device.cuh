@@ -325,10 +325,6 @@ struct Grid {
     const float* ye;
     const float* ze;
     const float* rho;  // g/mm^3, x fastest
-    const float* rf;   // rotation fwd (row-major 3x3), kernel-parameter space
-    const float* ri;   // rotation inverse
-    const float* tr;   // translation
-    int          identity;   // rf == I and tr == 0
     float        rho_scale;  // density scale of the track's scenario (1: none)
 };
 

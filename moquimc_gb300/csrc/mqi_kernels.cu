@@ -54,8 +54,18 @@ struct Ctx {
     uint32_t          spot;
     bool              dbg;
     float             tcut;
-    uint32_t          n_sec, n_local, n_drop, n_err;
 };
+
+/// A block's event counters (indices of mqi_stats: histories, tracks, steps, secondaries queued,
+/// secondaries scored in place, secondaries dropped, -, errors), kept in shared memory so that the
+/// step loop does not carry them in registers; flushed once per block.
+enum { kCntHist = 0, kCntTracks = 1, kCntSteps = 2, kCntSec = 3, kCntLocal = 4, kCntDrop = 5, kCntErr = 7 };
+static __shared__ unsigned int s_cnt[8];
+
+__device__ __forceinline__ void
+count_event(int k) {
+    atomicAdd(&s_cnt[k], 1u);
+}
 
 // ------------------------------------------------------------------------------------------
 // Calibration plug-in (material_t::compute_rsp_ / compute_rl_, materials/mqi_material.hpp:10-25):
@@ -120,10 +130,6 @@ make_grid(const ChildDev& c, const float* sxe, const float* sye, const float* sz
     g.ye = sye ? sye : c.ye;
     g.ze = sze ? sze : c.ze;
     g.rho = c.rho;
-    g.rf  = c.rf;
-    g.ri  = c.ri;
-    g.tr  = c.tr;
-    g.identity = c.identity;
     g.rho_scale = 1.0f;
     return g;
 }
@@ -402,7 +408,7 @@ score_step(Ctx& C, const Trk& t, uint32_t cnb, float rho, float vol) {
 /// Child-frame -> world-frame transform the reference applies to a daughter's vertex before
 /// pushing it (e.g. mqi_pp_elastic.hpp:188-195): R_fwd * (p - T) + T and R_fwd * d.
 __device__ inline void
-daughter_to_world(const Grid& g, float3& p, float3& d) {
+daughter_to_world(const ChildDev& g, float3& p, float3& d) {
     if (g.identity) return;
     const float3 q = make_float3(p.x - g.tr[0], p.y - g.tr[1], p.z - g.tr[2]);
     const float3 r = matvec(g.rf, q);
@@ -412,7 +418,7 @@ daughter_to_world(const Grid& g, float3& p, float3& d) {
 
 /// World -> child frame on entry (mqi_transport.hpp:165-168).
 __device__ inline void
-to_child(const Grid& g, float3& p, float3& d) {
+to_child(const ChildDev& g, float3& p, float3& d) {
     if (!g.identity) {
         p = matvec(g.ri, make_float3(fsub(p.x, g.tr[0]), fsub(p.y, g.tr[1]), fsub(p.z, g.tr[2])));
         d = matvec(g.ri, d);
@@ -422,7 +428,7 @@ to_child(const Grid& g, float3& p, float3& d) {
 
 /// Child -> world frame on exit (mqi_transport.hpp:234-237).
 __device__ inline void
-to_world(const Grid& g, float3& p, float3& d) {
+to_world(const ChildDev& g, float3& p, float3& d) {
     if (g.identity) return;
     const float3 r = matvec(g.rf, p);
     p              = make_float3(fadd(r.x, g.tr[0]), fadd(r.y, g.tr[1]), fadd(r.z, g.tr[2]));
@@ -455,7 +461,7 @@ template<int kMode>
 __device__ inline bool
 score_local_daughter(Ctx& C, float3 pw, float3 dw, float ke0, float dE0, uint32_t hint_cnb) {
     float3 p = pw, d = dw;
-    to_child(C.g, p, d);
+    to_child(C.P->child[C.child], p, d);
     Trk t;
     const uint32_t nxy  = (uint32_t) C.g.nx * (uint32_t) C.g.ny;
     const int3     hint = make_int3((int) (hint_cnb % nxy % (uint32_t) C.g.nx), (int) (hint_cnb % nxy / (uint32_t) C.g.nx),
@@ -498,8 +504,7 @@ emit_daughter(const WaveParams* P, const Tables* T, int child, uint32_t hint, co
     C.P = P; C.T = T; C.child = child; C.dbg = dbg; C.tcut = 0.0f; C.spot = spot;
     C.g = make_grid(P->child[child], xe, ye, ze);
     apply_scenario(*P, C.g, child, spot);
-    C.n_sec = C.n_local = C.n_drop = C.n_err = 0;
-    daughter_to_world(C.g, p, d);
+    daughter_to_world(P->child[child], p, d);
     if (P->inline_local && ke0 <= kTpCut && score_local_daughter<kMode>(C, p, d, ke0, dE0, hint)) return 1;
     const Queue&   q = P->out;
     const uint32_t i = atomicAdd(P->n_out, 1u);
@@ -528,7 +533,7 @@ template<int kMode>
 __device__ inline void
 push_daughter(Ctx& C, Trk& t, float ke0, bool ke1_zero, float3 p, float3 d, float dE0) {
     if (t.below + t.npush >= (uint32_t) C.P->stack_limit) {
-        ++C.n_drop;
+        count_event(kCntDrop);
         return;
     }
     const uint32_t below = t.below + t.npush;
@@ -537,9 +542,7 @@ push_daughter(Ctx& C, Trk& t, float ke0, bool ke1_zero, float3 p, float3 d, floa
     const int r = emit_daughter<kMode>(C.P, C.T, C.child, grid_cnb(C.g, t.cell), C.g.xe, C.g.ye, C.g.ze, C.dbg, below, uid, t.hist,
                                 t.spot, ke0, ke1_zero,
                                 p, d, dE0);
-    if (r == 0) ++C.n_sec;
-    else if (r == 1) ++C.n_local;
-    else ++C.n_err;
+    count_event(r == 0 ? kCntSec : (r == 1 ? kCntLocal : kCntErr));
 }
 
 // ------------------------------------------------------------------------------------------
@@ -611,7 +614,7 @@ post_delta(Ctx& C, Trk& t, Rng& rng) {
         Te /= ((1.0f - n) * rel.Te_max + n * C.tcut);
         if (rng.uniform() < 1.0f - rel.beta_sq * Te / rel.Te_max + Te * Te / (2.0f * rel.Et_sq)) break;
         if (it >= 63) {   // acceptance >= 1 - beta^2 > 0: unreachable in practice, bounded anyway
-            ++C.n_err;
+            count_event(kCntErr);
             break;
         }
     }
@@ -698,7 +701,7 @@ post_poi(Ctx& C, Trk& t, Rng& rng) {
     else if (Ek > 150.0f)            { P2 = 0.72f; PL = P2 + (1.0f - P2) * 0.83f; pw = 0.45f; }
     else                             { P2 = 0.7f;  PL = P2 + (1.0f - P2) * 0.83f; pw = 0.52f; }
     for (int round = 0; (Er - Eb) > 2.0f; ++round) {
-        if (round >= 64) { ++C.n_err; break; }   // Eb shrinks by 0.65 and Er by >= 2 MeV per round
+        if (round >= 64) { count_event(kCntErr); break; }   // Eb shrinks by 0.65 and Er by >= 2 MeV per round
         Er -= Eb;
         float dE = powf(rng.uniform(), pw) * (Er - 2.0f) + 2.0f;
         if (dE >= Er) dE = Er;
@@ -728,9 +731,8 @@ post_poi(Ctx& C, Trk& t, Rng& rng) {
 /// hand them to the post-step kernel): the track and its stream go in and out by value, which
 /// keeps the rarely-taken processes from pinning registers across the loop.
 struct PostState {
-    Trk      t;
-    Rng      rng;
-    uint32_t n_sec, n_local, n_drop, n_err;
+    Trk t;
+    Rng rng;
 };
 
 template<int kMode>
@@ -739,11 +741,9 @@ post_nuclear(const WaveParams* P, const Tables* T, Grid g, int child, bool dbg, 
     Ctx C;
     C.P = P; C.T = T; C.g = g; C.child = child; C.dbg = dbg; C.tcut = tcut;
     C.spot = s.t.spot;
-    C.n_sec = C.n_local = C.n_drop = C.n_err = 0;
     if (proc == 1) post_pp<kMode>(C, s.t, s.rng);
     else if (proc == 2) post_poe<kMode>(C, s.t, s.rng);
     else post_poi<kMode>(C, s.t, s.rng);
-    s.n_sec = C.n_sec; s.n_local = C.n_local; s.n_drop = C.n_drop; s.n_err = C.n_err;
     return s;
 }
 
@@ -825,10 +825,6 @@ stepping(Ctx& C, Trk& t, Rng& rng, float rho, float d2b) {
                 ps     = post_nuclear<kMode>(C.P, C.T, C.g, C.child, C.dbg, C.tcut, proc, ps);
                 t      = ps.t;
                 rng    = ps.rng;
-                C.n_sec += ps.n_sec;
-                C.n_local += ps.n_local;
-                C.n_drop += ps.n_drop;
-                C.n_err += ps.n_err;
             }
         }
     }
@@ -884,7 +880,7 @@ requeue_entry(Ctx& C, const Trk& t, const Rng& rng) {
     const uint32_t i = atomicAdd(C.P->n_out, 1u);
     if (i >= q.capacity) {
         atomicOr(C.P->error_flag, 2u);
-        ++C.n_err;
+        count_event(kCntErr);
         return;
     }
     q.ke[i] = t.ke0;
@@ -908,7 +904,7 @@ defer_track(Ctx& C, const Trk& t, const Rng& rng, uint32_t cnb, int proc) {
     const uint32_t i = atomicAdd(C.P->n_def, 1u);
     if (i >= C.P->in.capacity) {
         atomicOr(C.P->error_flag, 2u);
-        ++C.n_err;
+        count_event(kCntErr);
         return;
     }
     Deferred& d = C.P->def[i];
@@ -937,7 +933,7 @@ requeue_track(Ctx& C, const Trk& t, const Rng& rng) {
     const uint32_t i = atomicAdd(C.P->n_out, 1u);
     if (i >= q.capacity) {
         atomicOr(C.P->error_flag, 2u);
-        ++C.n_err;
+        count_event(kCntErr);
         return;
     }
     q.ke[i] = t.ke0;
@@ -967,6 +963,7 @@ wave_body(const WaveParams& P) {
     float* sedges     = reinterpret_cast<float*>(smem + sizeof(Tables));
     __shared__ const float* s_edges[kMaxChildren][3];   // staged edge arrays per child (null: global)
     if (threadIdx.x < kMaxChildren * 3) s_edges[threadIdx.x / 3][threadIdx.x % 3] = nullptr;
+    if (threadIdx.x < 8) s_cnt[threadIdx.x] = 0u;
     __syncthreads();
     {
         int off = 0;
@@ -994,8 +991,7 @@ wave_body(const WaveParams& P) {
     C.T      = T;
     C.dbg    = P.physics_debug != 0;
     C.tcut   = P.t_cut;
-    C.n_sec = C.n_local = C.n_drop = C.n_err = 0;
-    uint32_t n_tracks = 0, n_steps = 0, n_hist = 0;
+    uint32_t n_steps = 0;
 
     Rng rng;
     rng.k0 = P.k0;
@@ -1031,7 +1027,7 @@ wave_body(const WaveParams& P) {
                 in_grid = step_phase;
                 slice   = 0;
                 track_steps = 0;
-                ++n_tracks;
+                count_event(kCntTracks);
                 if (step_phase) {
                     C.child = t.child;
                     C.g     = make_grid(P.child[t.child], s_edges[t.child][0], s_edges[t.child][1], s_edges[t.child][2]);
@@ -1045,7 +1041,7 @@ wave_body(const WaveParams& P) {
         if (!in_grid) {
             // ---- child entry (mqi_transport.hpp:161-190) ----
             if (t.stopped || t.child >= P.n_children) {
-                if (t.primary) ++n_hist;
+                if (t.primary) count_event(kCntHist);
                 have = false;
                 continue;
             }
@@ -1053,14 +1049,14 @@ wave_body(const WaveParams& P) {
             C.g     = make_grid(P.child[t.child], s_edges[t.child][0], s_edges[t.child][1], s_edges[t.child][2]);
             apply_scenario(P, C.g, t.child, t.spot);
             C.spot  = t.spot;
-            to_child(C.g, t.p0, t.d0);
+            to_child(P.child[t.child], t.p0, t.d0);
             t.p1 = t.p0;
             t.d1 = t.d0;
             int3 c = grid_index(C.g, t.p0, t.d0);
             if (!grid_valid(C.g, c)) {
                 const float dist = grid_entry(C.g, t.p0, t.d0);
                 if (dist < 0.0f) {
-                    to_world(C.g, t.p0, t.d0);
+                    to_world(P.child[t.child], t.p0, t.d0);
                     t.p1 = t.p0;
                     t.d1 = t.d0;
                     ++t.child;
@@ -1076,7 +1072,7 @@ wave_body(const WaveParams& P) {
             }
             t.cell = c;
             if (!grid_valid(C.g, c)) {
-                to_world(C.g, t.p0, t.d0);
+                to_world(P.child[t.child], t.p0, t.d0);
                 t.p1 = t.p0;
                 t.d1 = t.d0;
                 ++t.child;
@@ -1100,7 +1096,7 @@ wave_body(const WaveParams& P) {
         }
         if (++track_steps > kMaxTrackSteps) {   // no physical track comes near this; never hang
             t.stopped = true;
-            ++C.n_err;
+            count_event(kCntErr);
         }
         bool leave = false;
         if (d2b < 0.0f) {
@@ -1117,7 +1113,7 @@ wave_body(const WaveParams& P) {
             leave = t.stopped || !grid_valid(C.g, t.cell);
         }
         if (leave) {
-            to_world(C.g, t.p0, t.d0);
+            to_world(P.child[C.child], t.p0, t.d0);
             t.p1 = t.p0;
             t.d1 = t.d0;
             ++t.child;
@@ -1131,18 +1127,11 @@ wave_body(const WaveParams& P) {
         }
     }
 
-    // ---- counters: shared-memory reduction, one global atomic per block and field ----
+    // ---- counters: one global atomic per block and field ----
+    if (n_steps) atomicAdd(&s_cnt[kCntSteps], n_steps);
     __syncthreads();
-    __shared__ unsigned long long sstat[8];
-    if (threadIdx.x < 8) sstat[threadIdx.x] = 0ull;
-    __syncthreads();
-    const unsigned long long v[8] = { n_hist, n_tracks, n_steps, C.n_sec, C.n_local, C.n_drop, 0ull, C.n_err };
-#pragma unroll
-    for (int k = 0; k < 8; ++k)
-        if (v[k]) atomicAdd(&sstat[k], v[k]);
-    __syncthreads();
-    if (threadIdx.x < 8 && sstat[threadIdx.x]) atomicAdd(&P.stats[threadIdx.x], sstat[threadIdx.x]);
-    if (C.n_err) atomicOr(P.error_flag, 1u);
+    if (threadIdx.x < 8 && s_cnt[threadIdx.x]) atomicAdd(&P.stats[threadIdx.x], (unsigned long long) s_cnt[threadIdx.x]);
+    if (threadIdx.x == 0 && s_cnt[kCntErr]) atomicOr(P.error_flag, 1u);
 }
 
 /// The post-step kernel's body: for each track the wave stopped at a nuclear interaction, the rest
@@ -1160,8 +1149,8 @@ post_body(const WaveParams& P) {
     C.T     = reinterpret_cast<const Tables*>(P.tables);
     C.dbg   = P.physics_debug != 0;
     C.tcut  = P.t_cut;
-    C.n_sec = C.n_local = C.n_drop = C.n_err = 0;
-    uint32_t       n_hist = 0;
+    if (threadIdx.x < 8) s_cnt[threadIdx.x] = 0u;
+    __syncthreads();
     const uint32_t n_raw  = *P.n_def;
     const uint32_t n      = n_raw > P.in.capacity ? P.in.capacity : n_raw;   // past it: flagged, not written
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -1216,24 +1205,17 @@ post_body(const WaveParams& P) {
             requeue_track(C, t, rng);
             continue;
         }
-        to_world(C.g, t.p0, t.d0);
+        to_world(P.child[C.child], t.p0, t.d0);
         ++t.child;
         if (t.stopped || t.child >= P.n_children) {
-            if (t.primary) ++n_hist;
+            if (t.primary) count_event(kCntHist);
             continue;
         }
         requeue_entry(C, t, rng);
     }
-    __shared__ unsigned long long sstat[8];
-    if (threadIdx.x < 8) sstat[threadIdx.x] = 0ull;
     __syncthreads();
-    const unsigned long long v[8] = { n_hist, 0ull, 0ull, C.n_sec, C.n_local, C.n_drop, 0ull, C.n_err };
-#pragma unroll
-    for (int k = 0; k < 8; ++k)
-        if (v[k]) atomicAdd(&sstat[k], v[k]);
-    __syncthreads();
-    if (threadIdx.x < 8 && sstat[threadIdx.x]) atomicAdd(&P.stats[threadIdx.x], sstat[threadIdx.x]);
-    if (C.n_err) atomicOr(P.error_flag, 1u);
+    if (threadIdx.x < 8 && s_cnt[threadIdx.x]) atomicAdd(&P.stats[threadIdx.x], (unsigned long long) s_cnt[threadIdx.x]);
+    if (threadIdx.x == 0 && s_cnt[kCntErr]) atomicOr(P.error_flag, 1u);
 }
 
 }   // namespace mqi_gpu
@@ -1563,7 +1545,7 @@ k_trace_rays(const __grid_constant__ ChildDev c, const float* __restrict__ rays,
     const Grid g = make_grid(c, nullptr, nullptr, nullptr);
     float3 p0 = make_float3(rays[6 * r + 0], rays[6 * r + 1], rays[6 * r + 2]);
     float3 d0 = make_float3(rays[6 * r + 3], rays[6 * r + 4], rays[6 * r + 5]);
-    to_child(g, p0, d0);
+    to_child(c, p0, d0);
     float3 d1 = d0;
     int3   cell = grid_index(g, p0, d0);
     uint32_t k = 0;
