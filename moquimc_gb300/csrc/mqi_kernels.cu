@@ -406,33 +406,35 @@ score_step(Ctx& C, const Trk& t, uint32_t cnb, float rho, float vol) {
 // ------------------------------------------------------------------------------------------
 
 /// Child-frame -> world-frame transform the reference applies to a daughter's vertex before
-/// pushing it (e.g. mqi_pp_elastic.hpp:188-195): R_fwd * (p - T) + T and R_fwd * d.
+/// pushing it (e.g. mqi_pp_elastic.hpp:188-195): R_fwd * (p - T) + T and R_fwd * d.  The child's
+/// rotation and translation are read from the kernel parameters (the per-lane grid does not carry
+/// them: they are used only at child entry and exit and for daughters).
 __device__ inline void
-daughter_to_world(const ChildDev& g, float3& p, float3& d) {
-    if (g.identity) return;
-    const float3 q = make_float3(p.x - g.tr[0], p.y - g.tr[1], p.z - g.tr[2]);
-    const float3 r = matvec(g.rf, q);
-    p              = make_float3(r.x + g.tr[0], r.y + g.tr[1], r.z + g.tr[2]);
-    d              = matvec(g.rf, d);
+daughter_to_world(const ChildDev& ch, float3& p, float3& d) {
+    if (ch.identity) return;
+    const float3 q = make_float3(p.x - ch.tr[0], p.y - ch.tr[1], p.z - ch.tr[2]);
+    const float3 r = matvec(ch.rf, q);
+    p              = make_float3(r.x + ch.tr[0], r.y + ch.tr[1], r.z + ch.tr[2]);
+    d              = matvec(ch.rf, d);
 }
 
 /// World -> child frame on entry (mqi_transport.hpp:165-168).
 __device__ inline void
-to_child(const ChildDev& g, float3& p, float3& d) {
-    if (!g.identity) {
-        p = matvec(g.ri, make_float3(fsub(p.x, g.tr[0]), fsub(p.y, g.tr[1]), fsub(p.z, g.tr[2])));
-        d = matvec(g.ri, d);
+to_child(const ChildDev& ch, float3& p, float3& d) {
+    if (!ch.identity) {
+        p = matvec(ch.ri, make_float3(fsub(p.x, ch.tr[0]), fsub(p.y, ch.tr[1]), fsub(p.z, ch.tr[2])));
+        d = matvec(ch.ri, d);
     }
     d = normalize3(d);
 }
 
 /// Child -> world frame on exit (mqi_transport.hpp:234-237).
 __device__ inline void
-to_world(const ChildDev& g, float3& p, float3& d) {
-    if (g.identity) return;
-    const float3 r = matvec(g.rf, p);
-    p              = make_float3(fadd(r.x, g.tr[0]), fadd(r.y, g.tr[1]), fadd(r.z, g.tr[2]));
-    d              = matvec(g.rf, d);
+to_world(const ChildDev& ch, float3& p, float3& d) {
+    if (ch.identity) return;
+    const float3 r = matvec(ch.rf, p);
+    p              = make_float3(fadd(r.x, ch.tr[0]), fadd(r.y, ch.tr[1]), fadd(r.z, ch.tr[2]));
+    d              = matvec(ch.rf, d);
 }
 
 /// track_t::update_post_vertex_position with the last_step length
