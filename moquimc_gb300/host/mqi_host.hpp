@@ -1,21 +1,88 @@
 // Host pieces shared by the C++ drivers over the C ABI (phantom_env_main.cpp, tps_env_main.cpp):
-// moqui's command-line reader, the coordinate-transform rotations, grid edges, the volume writers.
+// moqui's input-file and command-line readers, the coordinate-transform rotations, grid edges, the
+// volume writers.
 #pragma once
 
 #include <array>
 #include <cmath>
 #include <cstdlib>
+#include <cstring>
 #include <fstream>
 #include <iomanip>
 #include <map>
+#include <sstream>
 #include <stdexcept>
 #include <string>
 #include <vector>
+#include <strings.h>
 
 #include "mqi_gpu.h"
 
 namespace mqi_host
 {
+
+/// White space trimmed as moqui's trim_copy trims it (moqui/base/mqi_utils.hpp:22-36): space,
+/// \f, \n, \r, \t, \v (its delimiter literal ends at an embedded NUL).  moqui throws on a string
+/// of white space only; here it trims to "".
+inline std::string
+trim(const std::string& s) {
+    const char*  ws = " \f\n\r\t\v";
+    const size_t a = s.find_first_not_of(ws), b = s.find_last_not_of(ws);
+    return a == std::string::npos ? "" : s.substr(a, b - a + 1);
+}
+
+/// mqi::file_parser (moqui/base/mqi_file_handler.hpp:220-420): "Key value" lines; '#' starts a
+/// comment line or ends a line; a key is the text before the line's first space and matches
+/// case-insensitively; the first matching line wins; numbers are read with atof / atoi, a
+/// missing key's default is written with std::to_string first (so a float default keeps six
+/// decimals).  moqui's reader throws on a line of white space only, on a value of white space
+/// only and on an empty item of a list; here the line is skipped, the value reads as "" and the
+/// item is left out.
+class InputFile
+{
+public:
+    explicit InputFile(const std::string& path) {
+        std::ifstream f(path);
+        if (!f) throw std::runtime_error("Cannot open input parameter file.");
+        std::string line;
+        while (std::getline(f, line)) {
+            if (line.empty()) continue;
+            line = trim(line);
+            if (line.empty() || line[0] == '#') continue;
+            const size_t c = line.find('#');
+            if (c != std::string::npos) line = line.substr(0, c);
+            lines_.push_back(line);
+        }
+    }
+    std::string
+    get_string(const std::string& key, const std::string& dflt) const {
+        for (const auto& l : lines_) {
+            const size_t pos = l.find(' ');
+            if (pos != std::string::npos && strcasecmp(trim(l.substr(0, pos)).c_str(), key.c_str()) == 0)
+                return trim(l.substr(pos + 1));
+        }
+        return dflt;
+    }
+    std::vector<std::string>
+    get_vector(const std::string& key, char sep) const {
+        std::vector<std::string> out;
+        std::stringstream ss(get_string(key, ""));
+        std::string t;
+        while (std::getline(ss, t, sep))
+            if (!trim(t).empty()) out.push_back(trim(t));
+        return out;
+    }
+    float get_float(const std::string& k, float d) const { return std::atof(get_string(k, std::to_string(d)).c_str()); }
+    int get_int(const std::string& k, int d) const { return std::atoi(get_string(k, std::to_string(d)).c_str()); }
+    bool
+    get_bool(const std::string& k, bool d) const {
+        const std::string t = get_string(k, std::to_string(d));
+        return strcasecmp(t.c_str(), "true") == 0 || std::atoi(t.c_str()) != 0;
+    }
+
+private:
+    std::vector<std::string> lines_;
+};
 
 /// moqui's cli: "--name v1 v2 ..." (moqui/base/mqi_cli.hpp).
 class Cli

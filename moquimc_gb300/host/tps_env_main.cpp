@@ -46,59 +46,6 @@ namespace
 
 using namespace mqi_host;
 
-std::string
-trim(const std::string& s) {
-    const size_t a = s.find_first_not_of(" \t\r\n"), b = s.find_last_not_of(" \t\r\n");
-    return a == std::string::npos ? "" : s.substr(a, b - a + 1);
-}
-
-/// mqi::file_parser: "Key value" lines; '#' starts a comment line or ends a line; keys match
-/// case-insensitively; the first matching line wins.
-class InputFile
-{
-public:
-    explicit InputFile(const std::string& path) {
-        std::ifstream f(path);
-        if (!f) throw std::runtime_error("Cannot open input parameter file.");
-        std::string line;
-        while (std::getline(f, line)) {
-            if (line.empty()) continue;
-            line = trim(line);
-            if (line.empty() || line[0] == '#') continue;
-            const size_t c = line.find('#');
-            if (c != std::string::npos) line = line.substr(0, c);
-            lines_.push_back(line);
-        }
-    }
-    std::string
-    get_string(const std::string& key, const std::string& dflt) const {
-        for (const auto& l : lines_) {
-            const size_t pos = l.find(' ');
-            if (pos != std::string::npos && strcasecmp(trim(l.substr(0, pos)).c_str(), key.c_str()) == 0)
-                return trim(l.substr(pos + 1));
-        }
-        return dflt;
-    }
-    std::vector<std::string>
-    get_vector(const std::string& key, char sep) const {
-        std::vector<std::string> out;
-        std::stringstream ss(get_string(key, ""));
-        std::string t;
-        while (std::getline(ss, t, sep))
-            if (!trim(t).empty()) out.push_back(trim(t));
-        return out;
-    }
-    float get_float(const std::string& k, float d) const { return std::atof(get_string(k, std::to_string(d)).c_str()); }
-    int get_int(const std::string& k, int d) const { return std::atoi(get_string(k, std::to_string(d)).c_str()); }
-    bool
-    get_bool(const std::string& k, bool d) const {
-        const std::string t = get_string(k, std::to_string(d));
-        return strcasecmp(t.c_str(), "true") == 0 || std::atoi(t.c_str()) != 0;
-    }
-
-private:
-    std::vector<std::string> lines_;
-};
 
 /// The generic PBS beam model (mqi_treatment_machine_pbs.hpp): load_beamdata's geometry and spot
 /// sections, and characterize_beamlet / characterize_history for MODULATED spots, in FP32.

@@ -26,53 +26,72 @@ from . import capi
 from .machine import PBSMachine, coordinate_rotation
 
 
+_WS = " \f\n\r\t\v"   # what moqui's trim_copy trims (its delimiter literal ends at an embedded NUL)
+_LIBC = None
+
+
+def _libc():
+    global _LIBC
+    if _LIBC is None:
+        import ctypes
+        import ctypes.util
+
+        _LIBC = ctypes.CDLL(ctypes.util.find_library("c"))
+        _LIBC.atof.restype = ctypes.c_double
+        _LIBC.atof.argtypes = [ctypes.c_char_p]
+        _LIBC.atoi.restype = ctypes.c_int
+        _LIBC.atoi.argtypes = [ctypes.c_char_p]
+    return _LIBC
+
+
 class InputFile:
-    """mqi::file_parser: lines are "Key value"; blank lines and lines starting with '#' are skipped
-    and a '#' ends a line; a key matches case-insensitively and the first matching line wins."""
+    """mqi::file_parser (moqui/base/mqi_file_handler.hpp:220-420): lines are "Key value"; blank
+    lines and lines starting with '#' are skipped and a '#' ends a line; the key is the text before
+    the line's first space and matches case-insensitively; the first matching line wins.  Numbers
+    are read with the C library's atof / atoi, floats rounded to FP32 (get_float returns a float),
+    and a missing key's default is written as std::to_string writes it first ("%f" for floats, so
+    a default below 5e-7 reads back as 0).  moqui's reader throws on a line of white space only, on
+    a value of white space only and on an empty item of a list; here the line is skipped, the value
+    reads as "" and the item is left out."""
 
     def __init__(self, text: str, delimiter: str = " "):
         self.lines: List[str] = []
         self.delimiter = delimiter
-        for raw in text.splitlines():
+        for raw in text.split("\n"):
             if not raw:
                 continue
-            line = raw.strip()
+            line = raw.strip(_WS)
             if not line or line[0] == "#":
                 continue
             self.lines.append(line.split("#", 1)[0])
 
     @classmethod
     def load(cls, path: str) -> "InputFile":
-        with open(path) as f:
+        with open(path, newline="") as f:
             return cls(f.read())
 
     def get_string(self, key: str, default: str) -> str:
         for line in self.lines:
             pos = line.find(self.delimiter)
-            if pos >= 0 and line[:pos].strip().lower() == key.lower():
-                return line[pos + 1:].strip()
+            if pos >= 0 and line[:pos].strip(_WS).lower() == key.lower():
+                return line[pos + 1:].strip(_WS)
         return default
 
     def get_string_vector(self, key: str, sep: str) -> List[str]:
         v = self.get_string(key, "")
-        return [t.strip() for t in v.split(sep) if t.strip()] if v else []
+        return [t.strip(_WS) for t in v.split(sep) if t.strip(_WS)] if v else []
 
     @staticmethod
     def _atof(s: str) -> float:
-        import re
-
-        m = re.match(r"\s*[+-]?(\d+\.?\d*|\.\d+)([eE][+-]?\d+)?", s)
-        return float(m.group(0)) if m else 0.0
+        return float(_libc().atof(s.encode()))
 
     @staticmethod
     def _atoi(s: str) -> int:
-        import re
-
-        m = re.match(r"\s*[+-]?\d+", s)
-        return int(m.group(0)) if m else 0
+        return int(_libc().atoi(s.encode()))
 
     def get_float(self, key: str, default: float) -> float:
-        return self._atof(self.get_string(key, repr(float(default))))
+        with np.errstate(over="ignore"):   # beyond the float range: inf, as the C++ conversion gives
+            return float(np.float32(self._atof(self.get_string(key, "%f" % float(np.float32(default))))))
 
     def get_int(self, key: str, default: int) -> int:
         return self._atoi(self.get_string(key, str(int(default))))
@@ -380,7 +399,8 @@ class TpsEnv:
                     if h1 > h0:
                         c.transport_plan(h0, h1, seed)
             pph = 1.0 if cfg.unit_weights > 0 else cfg.particles_per_history
-            scale = pph * cfg.rbe * self.n_fractions
+            # in FP32, as tps_env forms it (float particles_per_history * float rbe * int n_fractions)
+            scale = float(np.float32(np.float32(pph) * np.float32(cfg.rbe)) * np.float32(self.n_fractions))
             child_index = len(beam.devices)
             for name, sid in names:
                 fname = f"{beam.name}_{child_index}_{name}"

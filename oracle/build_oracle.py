@@ -5,6 +5,8 @@
   ``dbg`` is built with ``-D__PHYSICS_DEBUG__`` (moqui's phantom example build), ``rel`` without.
   When the reference checkout is present the copy is re-staged first; elsewhere the copy that
   travelled with the repository is compiled as is.
+* ``oracle/_ref/bin/ref_parser``: moqui's input-file reader (``mqi::file_parser``) from the staged
+  copy of its header without the DICOM includes, driven by ``oracle/ref_parser.cpp``.
 * ``oracle/_ref/bin/ref_gpu_{dbg,rel}``: the reference's own CUDA kernel for sm_103a, compiled with
   nvcc from the same staged copy and ``oracle/ref_gpu_driver.cu`` with the phantom example's flags
   (``--use_fast_math``, and ``-D__PHYSICS_DEBUG__`` for ``dbg``) plus ``-maxrregcount=128``: uncapped, ptxas gives the
@@ -50,6 +52,10 @@ def ref_binary(debug: bool) -> str:
     return os.path.join(REF_BIN, "ref_oracle_dbg" if debug else "ref_oracle_rel")
 
 
+def ref_parser_binary() -> str:
+    return os.path.join(REF_BIN, "ref_parser")
+
+
 def build_reference(force: bool = False) -> bool:
     """Stage (when possible) and compile the reference CPU oracle.  Returns False when no staged
     copy exists (the reference was never available to this checkout)."""
@@ -60,6 +66,8 @@ def build_reference(force: bool = False) -> bool:
 
         if force or not os.path.isdir(os.path.join(REF_SRC, "moqui")):
             stage_ref.stage(root)
+        elif not os.path.exists(os.path.join(REF_SRC, "moqui", "base", "mqi_file_handler_parser.hpp")):
+            stage_ref.stage_parser(root)
     if not os.path.isdir(os.path.join(REF_SRC, "moqui")):
         return False
     os.makedirs(REF_BIN, exist_ok=True)
@@ -73,6 +81,11 @@ def build_reference(force: bool = False) -> bool:
             if debug:
                 cmd.insert(4, "-D__PHYSICS_DEBUG__")
             jobs.append(subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True))
+    parser_hdr = os.path.join(REF_SRC, "moqui", "base", "mqi_file_handler_parser.hpp")
+    parser_src = os.path.join(HERE, "ref_parser.cpp")
+    if os.path.exists(parser_hdr) and (force or _stale(ref_parser_binary(), [parser_src, parser_hdr])):
+        jobs.append(subprocess.Popen(["g++", "-std=c++17", "-O1", "-w", f"-I{REF_SRC}", parser_src, "-o",
+                                      ref_parser_binary()], stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True))
     for j in jobs:
         out, err = j.communicate()
         if j.returncode != 0:

@@ -18,6 +18,13 @@ Two problems keep it from running unmodified, and both are handled here or in th
    the loop by the guarded form "step n down while n > 0 and r < r_steps[n]", which produces the same
    index in every case where the original does not wrap.
 
+A third file is staged beside the copy, for the input-file tests: ``mqi_file_handler.hpp`` holds
+moqui's input-file reader (``mqi::file_parser``) but includes the beam-module headers, which need
+the DICOM library (GDCM), absent here.  The reader itself needs none of them.
+``moqui/base/mqi_file_handler_parser.hpp`` is the same file with that one include replaced by the
+three DICOM-free headers the file does use (``mqi_common.hpp``, ``mqi_vec.hpp``,
+``mqi_scorer.hpp``) and ``<cassert>`` added; ``oracle/ref_parser.cpp`` is compiled against it.
+
 Usage: ``python oracle/stage_ref.py --src <reference root>`` (the directory holding ``moqui/``; the
 checkout is only read).  The copy is only (re)written when the source is present, so on a machine
 without the reference the previously staged copy is used as is.
@@ -38,6 +45,25 @@ _LOOP = re.compile(
 _GUARDED = "while (n > 0 && r < r_steps[n]) { --n; } /* oracle: guarded against uint16 wrap */"
 
 
+_BEAM_MODULE_INCLUDE = "#include <moqui/base/mqi_beam_module_ion.hpp>"
+_PARSER_INCLUDES = ("#include <cassert>\n#include <moqui/base/mqi_common.hpp>\n#include <moqui/base/mqi_vec.hpp>\n"
+                    "#include <moqui/base/mqi_scorer.hpp>")
+
+
+def stage_parser(src_root: str) -> str:
+    """Write moqui/base/mqi_file_handler_parser.hpp (see the module docstring) into the staged
+    copy; returns its path."""
+    with open(os.path.join(src_root, "moqui", "base", "mqi_file_handler.hpp")) as f:
+        text = f.read()
+    if text.count(_BEAM_MODULE_INCLUDE) != 1:
+        raise RuntimeError("expected exactly one beam-module include in mqi_file_handler.hpp")
+    out = os.path.join(DEST, "moqui", "base", "mqi_file_handler_parser.hpp")
+    os.makedirs(os.path.dirname(out), exist_ok=True)
+    with open(out, "w") as f:
+        f.write(text.replace(_BEAM_MODULE_INCLUDE, _PARSER_INCLUDES))
+    return out
+
+
 def stage(src_root: str) -> str:
     src = os.path.join(src_root, "moqui")
     if not os.path.isdir(src):
@@ -56,6 +82,7 @@ def stage(src_root: str) -> str:
         raise RuntimeError(f"expected exactly one range-table loop to patch, found {n}")
     with open(target, "w") as f:
         f.write(text)
+    stage_parser(src_root)
     return DEST
 
 
