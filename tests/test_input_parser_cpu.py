@@ -11,7 +11,10 @@ non-zero integer), defaults of missing keys written with std::to_string first (s
 keeps six decimals), and comma-separated lists.
 
 Where moqui's reader throws (a line of white space only; a value of white space only; an empty
-item in a comma-separated list) the drivers read on; those files are checked separately."""
+item in a comma-separated list) the drivers read on; those files are checked separately.
+
+The mask files of ScoringMask / StatROIMaskFilename are checked the same way against moqui's
+mask_reader (read_mask_files, mask_to_roi): the summed mask and its CONTOUR runs."""
 import os
 import subprocess
 
@@ -158,3 +161,69 @@ def test_white_space_moqui_throws_on_is_read_on(text, expect, ref_parser, host_p
     rc, cpp, err = _run(host_parser, path, queries)
     assert rc == 0 and cpp == expect, (cpp, err)
     assert _python(path, queries) == expect
+
+
+# ---- masks: mask_reader::read_mask_files + mask_to_roi (moqui/base/mqi_file_handler.hpp:13-218)
+
+def _write_mha(path, mask, dims, style=0):
+    nx, ny, nz = dims
+    keys = [("ObjectType", "Image"), ("NDims", "3"), ("BinaryData", "True"), ("BinaryDataByteOrderMSB", "False"),
+            ("CompressedData", "False"), ("TransformMatrix", "1 0 0 0 1 0 0 0 1"), ("Offset", "-10 -20 5.5"),
+            ("CenterOfRotation", "0 0 0"), ("AnatomicalOrientation", "RAI"), ("ElementSpacing", "1 1 2"),
+            ("DimSize", f"{nx} {ny} {nz}"), ("ElementType", "MET_UCHAR"), ("ElementDataFile", "LOCAL")]
+    if style == 1:   # other spacing around '=' and other key case, as MHA writers vary
+        lines = [f"{k.lower() if i % 2 else k}={v}" if i % 3 else f"  {k}  =   {v}  " for i, (k, v) in enumerate(keys)]
+    else:
+        lines = [f"{k} = {v}" for k, v in keys]
+    with open(path, "wb") as f:
+        f.write(("\n".join(lines) + "\n").encode() + np.asarray(mask, np.uint8).tobytes())
+
+
+def _ref_runs(exe, dims, files):
+    r = subprocess.run([exe, "--mask", *map(str, dims), *files], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    lines = [ln.split() for ln in r.stdout.splitlines() if ln.startswith(("roi ", "run "))]
+    assert lines[0][0] == "roi" and int(lines[0][1]) == len(lines) - 1
+    return [tuple(x[1:]) for x in lines[1:]]
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_mask_runs_match_moqui(seed, ref_parser, tmp_path):
+    """Two or three random masks (overlaps sum to 2, which continues a run but does not start one),
+    written with varied header formatting: the summed mask and its CONTOUR runs (start, stride,
+    accumulated stride) equal moqui's, run for run."""
+    rng = np.random.default_rng(seed)
+    dims = (30, 20, 10)
+    n = int(np.prod(dims))
+    files, total = [], np.zeros(n, np.int64)
+    for k in range(2 + seed % 2):
+        m = np.zeros(n, np.uint8)
+        for _ in range(40):   # boxes of ones, so that runs of many lengths occur
+            a = rng.integers(0, n - 1)
+            m[a:a + rng.integers(1, 60)] = 1
+        m[-1] = 0             # every run closes inside the volume
+        path = os.path.join(tmp_path, f"m{k}.mha")
+        _write_mha(path, m, dims, style=k % 2)
+        files.append(path)
+        total += m
+    ref = _ref_runs(ref_parser, dims, files)
+    summed = sum(tps.read_mask_mha(f).astype(np.int64) for f in files)
+    np.testing.assert_array_equal(summed, total)
+    start, stride, acc = tps.mask_to_contour(summed)
+    assert [tuple(map(str, t)) for t in zip(start, stride, acc)] == ref
+    assert (summed == 2).any()
+
+
+def test_mask_run_open_at_the_end(ref_parser, tmp_path):
+    """A run that reaches the last voxel: moqui starts it and leaves its stride unset; here it is
+    closed at the end of the volume."""
+    dims = (4, 3, 2)
+    m = np.zeros(24, np.uint8)
+    m[2:5] = 1
+    m[20:] = 1
+    path = os.path.join(tmp_path, "m.mha")
+    _write_mha(path, m, dims)
+    ref = _ref_runs(ref_parser, dims, [path])
+    assert ref == [("2", "3", "3"), ("20", "open")]
+    start, stride, acc = tps.mask_to_contour(tps.read_mask_mha(path))
+    assert list(start) == [2, 20] and list(stride) == [3, 4] and list(acc) == [3, 7]
